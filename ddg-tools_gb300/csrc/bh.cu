@@ -1,0 +1,1150 @@
+// Barnes-Hut tangent-point energy and exact adjoint gradient on the GPU
+// (RS/src/energy/barnes_hut.rs, RS/src/kernel.rs, RS/src/geometry.rs), behind the C ABI
+// rs_bh_* of include/rsgpu.h.
+//
+// Per step:   host BVH build (host_tree.cpp) -> device list build (lists_count/lists_fill,
+//             radix-sorted transposes).
+// Per energy: refit (FP64 face geometry + bottom-up node aggregates, packs FP32 offsets)
+//             -> bh_pair (the pair kernel, warp per target leaf)
+//             -> node_sums -> downward (per-leaf chain walk) -> final (own + partner +
+//             cluster) -> pull_back (per-vertex gather) -> energy reduction (FP64).
+// Every reduction has a fixed order (gathers over the transposed lists, fixed shuffle
+// trees), so results are bitwise reproducible run to run.
+#include <cub/device/device_radix_sort.cuh>
+
+#include <algorithm>
+#include <cmath>
+#include <memory>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "bh_kernels.cuh"
+#include "common.hpp"
+#include "host_tree.hpp"
+#include "profile.hpp"
+
+namespace rsg {
+
+constexpr int kMaxDepth = 96;  // DFS stack bound of the list traversal (checked on the host)
+
+// ------------------------------------------------------------------ refit
+
+// L2-coherent load of a node record written by another thread of the same launch.
+__device__ __forceinline__ double4 ldcg4(const double4 *p) {
+  const double2 *q = reinterpret_cast<const double2 *>(p);
+  double2 a = __ldcg(q), b = __ldcg(q + 1);
+  return make_double4(a.x, a.y, b.x, b.y);
+}
+
+// One thread per leaf: FP64 face geometry of the leaf's faces (face_quantities,
+// RS/src/geometry.rs:33-39), the leaf's area and moment (Bvh::refit order, bvh.rs:226-260),
+// the packed FP32 face records relative to the leaf centroid, then the parents bottom-up: the
+// second child to arrive at a parent computes it (left + right), so every node is written once
+// with the crate's summation order.
+__global__ void refit_kernel(BhDev d, const double *__restrict__ pos) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.n_leaves) return;
+  uint32_t leaf = d.leaves[k];
+  uint32_t s0 = d.node_start[leaf], s1 = d.node_end[leaf];
+  double A = 0.0, M0 = 0.0, M1 = 0.0, M2 = 0.0;
+  double xb[8][3], ar[8];
+  float nr[8][3];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    uint32_t p = s0 + i;
+    if (p >= s1) break;
+    uint32_t f = d.order[p];
+    const double *p0 = pos + 3 * (size_t)d.faces[3 * f];
+    const double *p1 = pos + 3 * (size_t)d.faces[3 * f + 1];
+    const double *p2 = pos + 3 * (size_t)d.faces[3 * f + 2];
+    double u0 = __dsub_rn(p1[0], p0[0]), u1 = __dsub_rn(p1[1], p0[1]), u2 = __dsub_rn(p1[2], p0[2]);
+    double w0 = __dsub_rn(p2[0], p0[0]), w1 = __dsub_rn(p2[1], p0[1]), w2 = __dsub_rn(p2[2], p0[2]);
+    double c0 = __dsub_rn(__dmul_rn(u1, w2), __dmul_rn(u2, w1));
+    double c1 = __dsub_rn(__dmul_rn(u2, w0), __dmul_rn(u0, w2));
+    double c2 = __dsub_rn(__dmul_rn(u0, w1), __dmul_rn(u1, w0));
+    double len = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(c0, c0), __dmul_rn(c1, c1)), __dmul_rn(c2, c2)));
+    const double third = 1.0 / 3.0;
+    double x0 = __dmul_rn(__dadd_rn(__dadd_rn(p0[0], p1[0]), p2[0]), third);
+    double x1 = __dmul_rn(__dadd_rn(__dadd_rn(p0[1], p1[1]), p2[1]), third);
+    double x2 = __dmul_rn(__dadd_rn(__dadd_rn(p0[2], p1[2]), p2[2]), third);
+    double a = __dmul_rn(0.5, len);
+    double il = __drcp_rn(len);
+    nr[i][0] = (float)__dmul_rn(c0, il);
+    nr[i][1] = (float)__dmul_rn(c1, il);
+    nr[i][2] = (float)__dmul_rn(c2, il);
+    xb[i][0] = x0, xb[i][1] = x1, xb[i][2] = x2, ar[i] = a;
+    A = __dadd_rn(A, a);
+    M0 = __dadd_rn(M0, __dmul_rn(a, x0));
+    M1 = __dadd_rn(M1, __dmul_rn(a, x1));
+    M2 = __dadd_rn(M2, __dmul_rn(a, x2));
+  }
+  double cx = __ddiv_rn(M0, A), cy = __ddiv_rn(M1, A), cz = __ddiv_rn(M2, A);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    uint32_t p = s0 + i;
+    if (p >= s1) break;
+    d.fxa[p] = make_float4((float)(xb[i][0] - cx), (float)(xb[i][1] - cy), (float)(xb[i][2] - cz),
+                           (float)ar[i]);
+    d.fnn[p] = make_float4(nr[i][0], nr[i][1], nr[i][2], 0.f);
+  }
+  d.nmom[leaf] = make_double4(M0, M1, M2, A);
+  d.ncA[leaf] = make_double4(cx, cy, cz, A);
+  uint32_t n = leaf;
+  while (n != 0) {
+    uint32_t par = d.node_parent[n];
+    __threadfence();
+    unsigned old = atomicAdd(&d.refit_count[par], 1u);
+    if ((old & 1u) == 0u) return;  // first child here: the sibling completes the parent
+    __threadfence();
+    double4 l = ldcg4(&d.nmom[par + 1]);
+    double4 r = ldcg4(&d.nmom[d.node_right[par]]);
+    double4 m = make_double4(__dadd_rn(l.x, r.x), __dadd_rn(l.y, r.y), __dadd_rn(l.z, r.z),
+                             __dadd_rn(l.w, r.w));
+    d.nmom[par] = m;
+    d.ncA[par] = make_double4(__ddiv_rn(m.x, m.w), __ddiv_rn(m.y, m.w), __ddiv_rn(m.z, m.w), m.w);
+    n = par;
+  }
+}
+
+// ------------------------------------------------------------------ interaction lists
+
+struct ListsDev {
+  const double *box;     // 6 per node (build positions)
+  const double *radius;  // per node
+  double theta2;
+};
+
+// bh_admissible (RS/src/spatial/mod.rs:131-163): max(r_l, r_c)^2 < theta^2 d_box^2, in FP64
+// without contraction so the lists match the crate's bit for bit.
+__device__ __forceinline__ bool admissible(const ListsDev &L, const double *lb, double lr,
+                                           uint32_t c) {
+  const double *cb = L.box + 6 * (size_t)c;
+  double d2 = 0.0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    double dd = fmax(__dsub_rn(fmax(lb[k], cb[k]), fmin(lb[3 + k], cb[3 + k])), 0.0);
+    d2 = __dadd_rn(d2, __dmul_rn(dd, dd));
+  }
+  double h = fmax(lr, L.radius[c]);
+  return __dmul_rn(h, h) < __dmul_rn(L.theta2, d2);
+}
+
+// Depth-first traversal from the root, left child first (barnes_hut.rs:752-766). FILL=false
+// counts, FILL=true writes the entries at the offsets computed from the counts.
+template <bool FILL>
+__global__ void lists_kernel(BhDev d, ListsDev L, uint32_t *cnt_lum, uint32_t *cnt_ex,
+                             uint32_t *cnt_partner, unsigned long long *pairs,
+                             unsigned long long *lum_inter, uint32_t *lumped, uint32_t *exact,
+                             uint32_t *partner_off, const uint32_t *partner_base,
+                             unsigned int *overflow) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.n_leaves) return;
+  uint32_t leaf = d.leaves[k];
+  double lb[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) lb[i] = L.box[6 * (size_t)leaf + i];
+  double lr = L.radius[leaf];
+  uint32_t ns = d.node_end[leaf] - d.node_start[leaf];
+  uint32_t stack[kMaxDepth];
+  int sp = 0;
+  stack[sp++] = 0;
+  uint32_t nl = 0, ne = 0, np = 0;
+  unsigned long long pr = 0;
+  uint32_t lo = FILL ? d.lumped_off[k] : 0, eo = FILL ? d.exact_off[k] : 0;
+  uint32_t pb = FILL ? partner_base[k] : 0;
+  while (sp > 0) {
+    uint32_t c = stack[--sp];
+    if (admissible(L, lb, lr, c)) {
+      if (FILL) lumped[lo + nl] = c;
+      ++nl;
+    } else if (d.node_right[c] == 0) {
+      uint32_t nc = d.node_end[c] - d.node_start[c];
+      if (FILL) {
+        exact[eo + ne] = c;
+        partner_off[eo + ne] = pb + np;
+      }
+      ++ne;
+      np += nc;
+      pr += (c == leaf) ? (unsigned long long)ns * (ns - 1) : (unsigned long long)ns * nc;
+    } else {
+      if (sp + 2 > kMaxDepth) {
+        atomicExch(overflow, 1u);
+        break;
+      }
+      stack[sp++] = d.node_right[c];
+      stack[sp++] = c + 1;
+    }
+  }
+  if (!FILL) {
+    cnt_lum[k] = nl;
+    cnt_ex[k] = ne;
+    cnt_partner[k] = np;
+    pairs[k] = pr;
+    lum_inter[k] = (unsigned long long)nl * ns;
+  }
+}
+
+__global__ void iota_kernel(uint32_t *v, uint32_t n) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = i;
+}
+
+__global__ void leaf_key_kernel(const uint32_t *exact, const uint32_t *leaf_ordinal_of_node,
+                                uint32_t *key, uint32_t n) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) key[i] = leaf_ordinal_of_node[exact[i]];
+}
+
+// Group boundaries of sorted keys -> CSR offsets (off[k] = first index with key >= k).
+__global__ void offsets_from_sorted(const uint32_t *key, uint32_t n, uint32_t m, uint32_t *off) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > n) return;
+  uint32_t prev = (i == 0) ? 0 : key[i - 1] + 1;
+  uint32_t cur = (i == n) ? m : key[i];
+  for (uint32_t k = prev; k <= cur; ++k) off[k] = i;
+}
+
+// ------------------------------------------------------------------ the pair kernel
+
+// Transposing reduce of a per-lane 8 x 4 array P over the 8 lanes of a lane group (lane bits
+// 0..2): afterwards lane s holds the group sum of row s. 28 shuffles, fixed order.
+__device__ __forceinline__ float4 group_transpose_reduce(float (&P)[32], int s) {
+  float Q[16];
+  const bool b2 = (s >> 2) & 1;
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    float send = b2 ? P[i] : P[16 + i];
+    float keep = b2 ? P[16 + i] : P[i];
+    Q[i] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+  }
+  float R[8];
+  const bool b1 = (s >> 1) & 1;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    float send = b1 ? Q[i] : Q[8 + i];
+    float keep = b1 ? Q[8 + i] : Q[i];
+    R[i] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
+  }
+  float T[4];
+  const bool b0 = s & 1;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    float send = b0 ? R[i] : R[4 + i];
+    float keep = b0 ? R[4 + i] : R[i];
+    T[i] = keep + __shfl_xor_sync(0xffffffffu, send, 1);
+  }
+  return make_float4(T[0], T[1], T[2], T[3]);
+}
+
+// One warp per target leaf (leaf size <= 8). Lane = s + 8 j: s is the target face of the
+// leaf, j one of four entry groups. Lumped entries are taken in batches of 8 per group (the
+// node terms b = sum_S a_S K, u = -sum_S a_S dK/dv reduced over s by one transposing reduce),
+// exact entries one leaf block per group (the partner terms reduced the same way). Own
+// partials and the energy go through Kahan accumulators (leaf_with_gradient,
+// barnes_hut.rs:627-689; value only: leaf_energy, barnes_hut.rs:583-614).
+template <bool GRAD, bool FAST>
+__global__ void __launch_bounds__(256) bh_pair_kernel(BhDev d, Pow pw) {
+  const int lane = threadIdx.x & 31;
+  const int s = lane & 7;
+  const int j = lane >> 3;
+  for (;;) {
+    unsigned int w = 0;
+    if (lane == 0) w = atomicAdd(d.ticket, 1u);
+    w = __shfl_sync(0xffffffffu, w, 0);
+    if (w >= (unsigned)d.n_leaves) return;
+    const uint32_t k = d.schedule[w];
+    const uint32_t leaf = d.leaves[k];
+    const uint32_t s0 = d.node_start[leaf];
+    const uint32_t ns = d.node_end[leaf] - s0;
+    const bool act = (uint32_t)s < ns;
+    const float4 xs = act ? d.fxa[s0 + s] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 nS = act ? d.fnn[s0 + s] : make_float4(0.f, 0.f, 1.f, 0.f);
+    const double4 cL = d.ncA[leaf];
+    const float a_s = xs.w;
+    Kahan e_acc, da_acc, dx0, dx1, dx2, dn0, dn1, dn2;
+
+    // ---- lumped nodes, 8 per group per batch
+    const uint32_t llo = d.lumped_off[k], lhi = d.lumped_off[k + 1];
+    for (uint32_t base = llo; base < lhi; base += 32) {
+      float P[32];
+      float bda = 0.f, be = 0.f, bx0 = 0.f, bx1 = 0.f, bx2 = 0.f, bn0 = 0.f, bn1 = 0.f, bn2 = 0.f;
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const uint32_t q = base + 8 * j + i;
+        const bool ok = act && q < lhi;
+        float K = 0.f, cn = 0.f, g = 0.f;
+        float v0 = 0.f, v1 = 0.f, v2 = 0.f, Ac = 0.f;
+        if (q < lhi) {
+          const uint32_t c = d.lumped[q];
+          const double4 cC = d.ncA[c];
+          v0 = (float)(cL.x - cC.x) + xs.x;
+          v1 = (float)(cL.y - cC.y) + xs.y;
+          v2 = (float)(cL.z - cC.z) + xs.z;
+          Ac = (float)cC.w;
+        }
+        if (ok) {
+          float r2 = v0 * v0 + v1 * v1 + v2 * v2;
+          float ir2 = 1.f / r2;
+          float nu = nS.x * v0 + nS.y * v1 + nS.z * v2;
+          kernel_k<FAST>(pw, nu, r2, ir2, K, cn);
+          g = pw.beta * K * ir2;
+        }
+        be += a_s * K * Ac;
+        if (GRAD) {
+          // dK/dv = c_n N - beta K v / r2 ; dK/dN = c_n v
+          float dv0 = cn * nS.x - g * v0, dv1 = cn * nS.y - g * v1, dv2 = cn * nS.z - g * v2;
+          bda += K * Ac;
+          float aa = a_s * Ac;
+          bx0 += aa * dv0, bx1 += aa * dv1, bx2 += aa * dv2;
+          bn0 += aa * cn * v0, bn1 += aa * cn * v1, bn2 += aa * cn * v2;
+          P[4 * i + 0] = a_s * K;
+          P[4 * i + 1] = -a_s * dv0;
+          P[4 * i + 2] = -a_s * dv1;
+          P[4 * i + 3] = -a_s * dv2;
+        }
+      }
+      e_acc.add(be);
+      if (GRAD) {
+        da_acc.add(bda);
+        dx0.add(bx0), dx1.add(bx1), dx2.add(bx2);
+        dn0.add(bn0), dn1.add(bn1), dn2.add(bn2);
+        float4 t = group_transpose_reduce(P, s);
+        const uint32_t q = base + 8 * j + s;
+        if (q < lhi) d.node_term[q] = t;
+      }
+    }
+
+    // ---- exact leaves, one block per group
+    const uint32_t elo = d.exact_off[k], ehi = d.exact_off[k + 1];
+    for (uint32_t base = elo; base < ehi; base += 4) {
+      const uint32_t q = base + j;
+      const bool qok = q < ehi;
+      uint32_t c = 0, cs = 0, nc = 0;
+      float d0 = 0.f, d1 = 0.f, d2 = 0.f;
+      if (qok) {
+        c = d.exact[q];
+        cs = d.node_start[c];
+        nc = d.node_end[c] - cs;
+        const double4 cC = d.ncA[c];
+        d0 = (float)(cL.x - cC.x);
+        d1 = (float)(cL.y - cC.y);
+        d2 = (float)(cL.z - cC.z);
+      }
+      float P[32];
+      float row = 0.f, rx0 = 0.f, rx1 = 0.f, rx2 = 0.f, rn0 = 0.f, rn1 = 0.f, rn2 = 0.f;
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        float K = 0.f, cn = 0.f, g = 0.f, v0 = 0.f, v1 = 0.f, v2 = 0.f, a_t = 0.f;
+        if ((uint32_t)t < nc) {
+          const float4 xt = d.fxa[cs + t];
+          a_t = xt.w;
+          const bool self = (c == leaf) && (t == s);
+          if (act && !self) {
+            v0 = (xs.x - xt.x) + d0;
+            v1 = (xs.y - xt.y) + d1;
+            v2 = (xs.z - xt.z) + d2;
+            float r2 = v0 * v0 + v1 * v1 + v2 * v2;
+            float ir2 = 1.f / r2;
+            float nu = nS.x * v0 + nS.y * v1 + nS.z * v2;
+            kernel_k<FAST>(pw, nu, r2, ir2, K, cn);
+            g = pw.beta * K * ir2;
+          }
+        }
+        row += a_t * K;
+        if (GRAD) {
+          float dv0 = cn * nS.x - g * v0, dv1 = cn * nS.y - g * v1, dv2 = cn * nS.z - g * v2;
+          rx0 += a_t * dv0, rx1 += a_t * dv1, rx2 += a_t * dv2;
+          rn0 += a_t * cn * v0, rn1 += a_t * cn * v1, rn2 += a_t * cn * v2;
+          float aa = -a_s * a_t;
+          P[4 * t + 0] = a_s * K;
+          P[4 * t + 1] = aa * dv0;
+          P[4 * t + 2] = aa * dv1;
+          P[4 * t + 3] = aa * dv2;
+        }
+      }
+      e_acc.add(a_s * row);
+      if (GRAD) {
+        da_acc.add(row);
+        dx0.add(a_s * rx0), dx1.add(a_s * rx1), dx2.add(a_s * rx2);
+        dn0.add(a_s * rn0), dn1.add(a_s * rn1), dn2.add(a_s * rn2);
+        float4 t4 = group_transpose_reduce(P, s);
+        if (qok && (uint32_t)s < nc) d.partner[d.partner_off[q] + s] = t4;
+      }
+    }
+
+    // ---- reduce over the four groups; lanes 0..7 write their face's own partials
+    if (GRAD) {
+      float o[7] = {da_acc.value(), dx0.value(), dx1.value(), dx2.value(),
+                    dn0.value(),    dn1.value(), dn2.value()};
+#pragma unroll
+      for (int i = 0; i < 7; ++i) {
+        o[i] += __shfl_xor_sync(0xffffffffu, o[i], 8);
+        o[i] += __shfl_xor_sync(0xffffffffu, o[i], 16);
+      }
+      if (j == 0 && act) {
+        d.own[2 * (s0 + s)] = make_float4(o[0], o[1], o[2], o[3]);
+        d.own[2 * (s0 + s) + 1] = make_float4(o[4], o[5], o[6], 0.f);
+      }
+    }
+    double e = (double)e_acc.s - (double)e_acc.c;
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) e += __shfl_xor_sync(0xffffffffu, e, m);
+    if (lane == 0) d.leaf_energy[k] = e;
+  }
+}
+
+// b_C, u_C per node over the transposed lumped lists, increasing entry (barnes_hut.rs:505-520).
+__global__ void node_sums_kernel(BhDev d) {
+  int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= d.n_nodes) return;
+  Kahan b, u0, u1, u2;
+  for (uint32_t e = d.lumped_t_off[n]; e < d.lumped_t_off[n + 1]; ++e) {
+    float4 t = d.node_term[d.lumped_t[e]];
+    b.add(t.x), u0.add(t.y), u1.add(t.z), u2.add(t.w);
+  }
+  d.node_sum[n] = make_float4(b.value(), u0.value(), u1.value(), u2.value());
+}
+
+// Downward pass per leaf along its root -> leaf chain (barnes_hut.rs:521-538):
+// beta_c = beta_p + U_p.(X_c - X_p) + b_c, U_c = U_p + u_c.
+__global__ void downward_kernel(BhDev d) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.n_leaves) return;
+  uint32_t c0 = d.chain_off[k], c1 = d.chain_off[k + 1];
+  uint32_t p = d.chain[c0];
+  float4 s = d.node_sum[p];
+  float beta = s.x, U0 = s.y, U1 = s.z, U2 = s.w;
+  double4 xp = d.ncA[p];
+  for (uint32_t i = c0 + 1; i < c1; ++i) {
+    uint32_t c = d.chain[i];
+    double4 xc = d.ncA[c];
+    float4 sc = d.node_sum[c];
+    float sh0 = (float)(xc.x - xp.x), sh1 = (float)(xc.y - xp.y), sh2 = (float)(xc.z - xp.z);
+    beta = beta + (U0 * sh0 + U1 * sh1 + U2 * sh2) + sc.x;
+    U0 += sc.y, U1 += sc.z, U2 += sc.w;
+    xp = xc;
+  }
+  d.leaf_bu[k] = make_float4(beta, U0, U1, U2);
+}
+
+// Per face: own + partner (transposed exact lists) + cluster part (barnes_hut.rs:539-567),
+// written by face id.
+__global__ void final_kernel(BhDev d) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= d.n_faces) return;
+  uint32_t k = d.leaf_of_pos[p];
+  uint32_t leaf = d.leaves[k];
+  uint32_t t = p - d.node_start[leaf];
+  float4 o0 = d.own[2 * p], o1 = d.own[2 * p + 1];
+  Kahan a, x0, x1, x2;
+  a.add(o0.x), x0.add(o0.y), x1.add(o0.z), x2.add(o0.w);
+  for (uint32_t e = d.exact_t_off[k]; e < d.exact_t_off[k + 1]; ++e) {
+    float4 pp = d.partner[d.partner_off[d.exact_t[e]] + t];
+    a.add(pp.x), x0.add(pp.y), x1.add(pp.z), x2.add(pp.w);
+  }
+  float4 bu = d.leaf_bu[k];
+  float4 xa = d.fxa[p];  // offset X_T - X_leaf and a_T
+  a.add(bu.x + (bu.y * xa.x + bu.z * xa.y + bu.w * xa.z));
+  x0.add(xa.w * bu.y), x1.add(xa.w * bu.z), x2.add(xa.w * bu.w);
+  uint32_t f = d.order[p];
+  d.partials[2 * f] = make_float4(a.value(), x0.value(), x1.value(), x2.value());
+  d.partials[2 * f + 1] = o1;
+}
+
+// Pull-back to the vertices (face_pull_back, RS/src/geometry.rs:87-110, summed over the
+// incident faces in increasing face order, geometry.rs:172-188).
+__global__ void pull_back_kernel(BhDev d, const double *__restrict__ pos, double *__restrict__ dE) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= d.n_vertices) return;
+  float g0 = 0.f, g1 = 0.f, g2 = 0.f;
+  for (uint32_t e = d.inc_off[v]; e < d.inc_off[v + 1]; ++e) {
+    uint32_t fc = d.inc[e];
+    uint32_t f = fc >> 2, c = fc & 3;
+    const uint32_t *t = d.faces + 3 * (size_t)f;
+    const double *p0 = pos + 3 * (size_t)t[0];
+    const double *p1 = pos + 3 * (size_t)t[1];
+    const double *p2 = pos + 3 * (size_t)t[2];
+    float u0 = (float)(p1[0] - p0[0]), u1 = (float)(p1[1] - p0[1]), u2 = (float)(p1[2] - p0[2]);
+    float w0 = (float)(p2[0] - p0[0]), w1 = (float)(p2[1] - p0[1]), w2 = (float)(p2[2] - p0[2]);
+    float n0 = u1 * w2 - u2 * w1, n1 = u2 * w0 - u0 * w2, n2 = u0 * w1 - u1 * w0;
+    float len = sqrtf(n0 * n0 + n1 * n1 + n2 * n2);
+    float il = 1.f / len;
+    n0 *= il, n1 *= il, n2 *= il;
+    // edge opposite corner c: e_jk = p2 - p1, e_ki = p0 - p2, e_ij = p1 - p0
+    const double *pa = c == 0 ? p1 : (c == 1 ? p2 : p0);
+    const double *pb = c == 0 ? p2 : (c == 1 ? p0 : p1);
+    float e0 = (float)(pb[0] - pa[0]), e1 = (float)(pb[1] - pa[1]), e2 = (float)(pb[2] - pa[2]);
+    float4 q0 = d.partials[2 * f], q1 = d.partials[2 * f + 1];
+    float ha = 0.5f * q0.x;
+    // N x e, e x N
+    float c0 = n1 * e2 - n2 * e1, c1 = n2 * e0 - n0 * e2, c2 = n0 * e1 - n1 * e0;
+    float dotn = -(c0 * q1.x + c1 * q1.y + c2 * q1.z) * il;
+    const float third = 1.f / 3.f;
+    g0 += ha * c0 + q0.y * third + n0 * dotn;
+    g1 += ha * c1 + q0.z * third + n1 * dotn;
+    g2 += ha * c2 + q0.w * third + n2 * dotn;
+  }
+  dE[3 * v] = g0, dE[3 * v + 1] = g1, dE[3 * v + 2] = g2;
+}
+
+// Energy over the leaves in FP64: fixed strided partial sums, then a fixed tree.
+__global__ void energy_reduce_kernel(const double *leaf_energy, int n, double *out) {
+  __shared__ double sh[1024];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += leaf_energy[i];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int m = blockDim.x / 2; m > 0; m >>= 1) {
+    if ((int)threadIdx.x < m) sh[threadIdx.x] += sh[threadIdx.x + m];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
+// First exact pair in leaf, list, s, t order whose FP32 term is non-finite (culprit_pair,
+// barnes_hut.rs:693-724): the smallest (entry << 8 | s << 4 | t) rank.
+template <bool FAST>
+__global__ void culprit_kernel(BhDev d, Pow pw, unsigned long long *best) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.n_leaves) return;
+  uint32_t leaf = d.leaves[k];
+  uint32_t s0 = d.node_start[leaf], s1 = d.node_end[leaf];
+  double4 cL = d.ncA[leaf];
+  for (uint32_t q = d.exact_off[k]; q < d.exact_off[k + 1]; ++q) {
+    uint32_t c = d.exact[q], cs = d.node_start[c], ce = d.node_end[c];
+    double4 cC = d.ncA[c];
+    float d0 = (float)(cL.x - cC.x), d1 = (float)(cL.y - cC.y), d2 = (float)(cL.z - cC.z);
+    for (uint32_t ps = s0; ps < s1; ++ps)
+      for (uint32_t pt = cs; pt < ce; ++pt) {
+        if (ps == pt) continue;
+        float4 xs = d.fxa[ps], xt = d.fxa[pt], n = d.fnn[ps];
+        float v0 = (xs.x - xt.x) + d0, v1 = (xs.y - xt.y) + d1, v2 = (xs.z - xt.z) + d2;
+        float r2 = v0 * v0 + v1 * v1 + v2 * v2, ir2 = 1.f / r2, K, cn;
+        kernel_k<FAST>(pw, n.x * v0 + n.y * v1 + n.z * v2, r2, ir2, K, cn);
+        float term = K * xs.w * xt.w;
+        if (!isfinite(term) || !isfinite(cn) || !isfinite(ir2)) {
+          unsigned long long rank =
+              ((unsigned long long)q << 8) | ((ps - s0) << 4) | (unsigned long long)(pt - cs);
+          atomicMin(best, rank);
+          return;
+        }
+      }
+  }
+}
+
+}  // namespace rsg
+
+// ====================================================================== host driver
+
+using namespace rsg;
+
+struct rs_bh {
+  rs_ctx *ctx = nullptr;
+  int nv = 0, nf = 0, leaf_size = 8;
+  double theta = 0.5;
+  Tree tree;
+  std::vector<uint32_t> faces_h;
+  uint64_t pairs_exact = 0, lumped_inter = 0;
+  size_t n_lumped = 0, n_exact = 0, n_partner = 0;
+  int64_t culprit[2] = {-1, -1};
+  // device topology
+  DevBuf<uint32_t> faces, order, node_start, node_end, node_right, node_parent, leaves,
+      leaf_of_pos, schedule, chain_off, chain, inc_off, inc, leaf_ordinal;
+  DevBuf<double> box, radius;
+  DevBuf<uint32_t> lumped_off, lumped, exact_off, exact, partner_off, lumped_t_off, lumped_t,
+      exact_t_off, exact_t;
+  // per evaluation
+  DevBuf<double> pos;
+  DevBuf<float4> fxa, fnn, own, node_term, partner, node_sum, leaf_bu, partials;
+  DevBuf<double4> ncA, nmom;
+  DevBuf<uint32_t> refit_count;
+  DevBuf<double> leaf_energy, energy, dE;
+  DevBuf<unsigned int> ticket;
+  DevBuf<unsigned long long> culprit_key;
+  bool positions_current = false;
+  Profiler prof;
+
+  BhDev dev() const {
+    BhDev d;
+    d.faces = faces.p, d.order = order.p, d.node_start = node_start.p, d.node_end = node_end.p;
+    d.node_right = node_right.p, d.node_parent = node_parent.p, d.leaves = leaves.p;
+    d.leaf_of_pos = leaf_of_pos.p, d.schedule = schedule.p, d.chain_off = chain_off.p;
+    d.chain = chain.p, d.inc_off = inc_off.p, d.inc = inc.p;
+    d.lumped_off = lumped_off.p, d.lumped = lumped.p, d.exact_off = exact_off.p, d.exact = exact.p;
+    d.partner_off = partner_off.p, d.lumped_t_off = lumped_t_off.p, d.lumped_t = lumped_t.p;
+    d.exact_t_off = exact_t_off.p, d.exact_t = exact_t.p;
+    d.n_vertices = nv, d.n_faces = nf, d.n_nodes = (int)tree.n_nodes();
+    d.n_leaves = (int)tree.leaves.size();
+    d.fxa = fxa.p, d.fnn = fnn.p, d.ncA = ncA.p, d.nmom = nmom.p, d.refit_count = refit_count.p;
+    d.own = own.p, d.node_term = node_term.p, d.partner = partner.p, d.node_sum = node_sum.p;
+    d.leaf_bu = leaf_bu.p, d.partials = partials.p, d.leaf_energy = leaf_energy.p;
+    d.ticket = ticket.p;
+    return d;
+  }
+  cudaStream_t st() const { return ctx->stream; }
+};
+
+namespace {
+
+inline unsigned blocks(size_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
+
+template <class T>
+void upload_vec(DevBuf<T> &b, const std::vector<T> &v, cudaStream_t s) {
+  b.alloc(v.size());
+  b.upload(v.data(), v.size(), s);
+}
+
+Pow make_pow(double alpha, double beta) {
+  // Exponents::new (RS/src/kernel.rs:50-76)
+  if (!std::isfinite(alpha) || !std::isfinite(beta))
+    fail(RS_INVALID_EXPONENTS, "InvalidExponents", "energy", "both exponents must be finite");
+  if (alpha <= 1.0) fail(RS_INVALID_EXPONENTS, "InvalidExponents", "energy", "alpha must be greater than 1");
+  if (beta <= alpha + 2.0)
+    fail(RS_INVALID_EXPONENTS, "InvalidExponents", "energy",
+         "beta must be greater than alpha + 2 (s = (beta - 2)/alpha > 1)");
+  if (beta >= 2.0 * alpha + 2.0)
+    fail(RS_INVALID_EXPONENTS, "InvalidExponents", "energy",
+         "beta must be smaller than 2 alpha + 2 (s = (beta - 2)/alpha < 2)");
+  Pow p;
+  p.alpha = (float)alpha;
+  p.beta = (float)beta;
+  p.a_int = (alpha == std::trunc(alpha) && alpha >= 2 && alpha <= 64) ? (int)alpha : -1;
+  double ab = beta - alpha;
+  p.ab_int = (ab == std::trunc(ab) && ab >= 0 && ab <= 128) ? (int)ab : -1;
+  return p;
+}
+
+bool is_fast(double alpha, double beta) { return alpha == 6.0 && beta == 12.0; }
+
+// Topology arrays common to rs_bh_build and rs_bh_attach: parents, leaf chains, leaf of
+// every position, vertex incidence.
+void upload_topology(rs_bh *h) {
+  cudaStream_t s = h->st();
+  const Tree &T = h->tree;
+  size_t nn = T.n_nodes(), nl = T.leaves.size();
+  std::vector<uint32_t> parent(nn, 0);
+  for (size_t i = 0; i < nn; ++i)
+    if (T.right[i]) parent[i + 1] = (uint32_t)i, parent[T.right[i]] = (uint32_t)i;
+  std::vector<uint32_t> leaf_of_pos(h->nf), coff(nl + 1, 0), chain;
+  size_t max_depth = 0;
+  for (size_t k = 0; k < nl; ++k) {
+    uint32_t l = T.leaves[k];
+    for (uint32_t p = T.start[l]; p < T.end[l]; ++p) leaf_of_pos[p] = (uint32_t)k;
+    size_t b = chain.size();
+    uint32_t a = l;
+    for (;;) {
+      chain.push_back(a);
+      if (a == 0) break;
+      a = parent[a];
+    }
+    std::reverse(chain.begin() + b, chain.end());
+    max_depth = std::max(max_depth, chain.size() - b);
+    coff[k + 1] = (uint32_t)chain.size();
+  }
+  if (max_depth + 2 >= (size_t)kMaxDepth)
+    fail(RS_INVALID_OPTION, "InvalidOption", "upload",
+         "tree depth " + std::to_string(max_depth) + " exceeds the traversal stack");
+  if (h->leaf_size > 8)
+    fail(RS_INVALID_OPTION, "InvalidOption", "upload", "the GPU path needs leaf_size <= 8");
+  for (size_t k = 0; k < nl; ++k) {
+    uint32_t l = T.leaves[k];
+    if (T.end[l] - T.start[l] > 8)
+      fail(RS_INVALID_OPTION, "InvalidOption", "upload", "a leaf holds more than 8 faces");
+  }
+  // vertex -> (face, corner), faces ascending
+  std::vector<uint32_t> ioff((size_t)h->nv + 1, 0), inc(3 * (size_t)h->nf);
+  for (int f = 0; f < h->nf; ++f)
+    for (int c = 0; c < 3; ++c) ioff[h->faces_h[3 * f + c] + 1]++;
+  for (int v = 0; v < h->nv; ++v) ioff[v + 1] += ioff[v];
+  {
+    std::vector<uint32_t> fill(ioff.begin(), ioff.end() - 1);
+    for (int f = 0; f < h->nf; ++f)
+      for (int c = 0; c < 3; ++c) inc[fill[h->faces_h[3 * f + c]]++] = ((uint32_t)f << 2) | c;
+  }
+  upload_vec(h->faces, h->faces_h, s);
+  upload_vec(h->order, T.order, s);
+  upload_vec(h->node_start, T.start, s);
+  upload_vec(h->node_end, T.end, s);
+  upload_vec(h->node_right, T.right, s);
+  upload_vec(h->node_parent, parent, s);
+  upload_vec(h->leaves, T.leaves, s);
+  upload_vec(h->leaf_of_pos, leaf_of_pos, s);
+  upload_vec(h->chain_off, coff, s);
+  upload_vec(h->chain, chain, s);
+  upload_vec(h->inc_off, ioff, s);
+  upload_vec(h->inc, inc, s);
+  upload_vec(h->leaf_ordinal, T.leaf_ordinal, s);
+  h->fxa.alloc(h->nf);
+  h->fnn.alloc(h->nf);
+  h->own.alloc(2 * (size_t)h->nf);
+  h->partials.alloc(2 * (size_t)h->nf);
+  h->ncA.alloc(nn);
+  h->nmom.alloc(nn);
+  h->node_sum.alloc(nn);
+  h->refit_count.alloc(nn);
+  RSG_CUDA("upload", cudaMemsetAsync(h->refit_count.p, 0, nn * sizeof(uint32_t), s));
+  h->leaf_bu.alloc(nl);
+  h->leaf_energy.alloc(nl);
+  h->energy.alloc(1);
+  h->dE.alloc(3 * (size_t)h->nv);
+  h->pos.alloc(3 * (size_t)h->nv);
+  h->ticket.alloc(1);
+  h->culprit_key.alloc(1);
+}
+
+// Transposes of the lists (barnes_hut.rs:798-806, 811-827) by a stable radix sort of
+// (key, entry) pairs, and the processing schedule.
+void finish_lists(rs_bh *h, const std::vector<uint32_t> &work_per_leaf) {
+  cudaStream_t s = h->st();
+  size_t nn = h->tree.n_nodes(), nl = h->tree.leaves.size();
+  auto transpose = [&](const uint32_t *keys_in, size_t n, size_t m, DevBuf<uint32_t> &off,
+                       DevBuf<uint32_t> &idx, const char *what) {
+    off.alloc(m + 1);
+    idx.alloc(std::max<size_t>(n, 1));
+    if (n == 0) {
+      RSG_CUDA("upload", cudaMemsetAsync(off.p, 0, (m + 1) * sizeof(uint32_t), s));
+      return;
+    }
+    DevBuf<uint32_t> vals(n), keys_out(n);
+    iota_kernel<<<blocks(n, 256), 256, 0, s>>>(vals.p, (uint32_t)n);
+    RSG_LAUNCHED(h->ctx, "iota");
+    size_t tmp_bytes = 0;
+    int bits = 1;
+    while ((size_t(1) << bits) < m + 1) ++bits;
+    RSG_CUDA("upload", cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys_in, keys_out.p, vals.p,
+                                                  idx.p, (int)n, 0, bits, s));
+    DevBuf<unsigned char> tmp(tmp_bytes);
+    RSG_CUDA("upload", cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, keys_in, keys_out.p, vals.p,
+                                                  idx.p, (int)n, 0, bits, s));
+    offsets_from_sorted<<<blocks(n + 1, 256), 256, 0, s>>>(keys_out.p, (uint32_t)n, (uint32_t)m, off.p);
+    RSG_LAUNCHED(h->ctx, what);
+    RSG_CUDA("upload", cudaStreamSynchronize(s));
+  };
+  transpose(h->lumped.p, h->n_lumped, nn, h->lumped_t_off, h->lumped_t, "lumped_t");
+  {
+    DevBuf<uint32_t> key(std::max<size_t>(h->n_exact, 1));
+    if (h->n_exact) {
+      leaf_key_kernel<<<blocks(h->n_exact, 256), 256, 0, s>>>(h->exact.p, h->leaf_ordinal.p, key.p,
+                                                             (uint32_t)h->n_exact);
+      RSG_LAUNCHED(h->ctx, "leaf_key");
+    }
+    transpose(key.p, h->n_exact, nl, h->exact_t_off, h->exact_t, "exact_t");
+  }
+  // Longest work first: warps take leaves from an atomic ticket in this order.
+  std::vector<uint32_t> sched(nl);
+  std::iota(sched.begin(), sched.end(), 0u);
+  std::stable_sort(sched.begin(), sched.end(),
+                   [&](uint32_t a, uint32_t b) { return work_per_leaf[a] > work_per_leaf[b]; });
+  upload_vec(h->schedule, sched, s);
+  h->node_term.alloc(std::max<size_t>(h->n_lumped, 1));
+  h->partner.alloc(std::max<size_t>(h->n_partner, 1));
+  RSG_CUDA("upload", cudaStreamSynchronize(s));
+}
+
+void build_lists_device(rs_bh *h) {
+  cudaStream_t s = h->st();
+  const Tree &T = h->tree;
+  size_t nl = T.leaves.size();
+  upload_vec(h->box, T.box, s);
+  upload_vec(h->radius, T.radius, s);
+  ListsDev L{h->box.p, h->radius.p, h->theta * h->theta};
+  DevBuf<uint32_t> c_lum(nl), c_ex(nl), c_par(nl);
+  DevBuf<unsigned long long> pairs(nl), linter(nl);
+  DevBuf<unsigned int> overflow(1);
+  RSG_CUDA("upload", cudaMemsetAsync(overflow.p, 0, sizeof(unsigned), s));
+  BhDev d = h->dev();
+  lists_kernel<false><<<blocks(nl, 128), 128, 0, s>>>(d, L, c_lum.p, c_ex.p, c_par.p, pairs.p,
+                                                       linter.p, nullptr, nullptr, nullptr, nullptr,
+                                                       overflow.p);
+  RSG_LAUNCHED(h->ctx, "lists_count");
+  std::vector<uint32_t> hl(nl), he(nl), hp(nl);
+  std::vector<unsigned long long> hpr(nl), hli(nl);
+  unsigned ovf = 0;
+  c_lum.download(hl.data(), nl, s);
+  c_ex.download(he.data(), nl, s);
+  c_par.download(hp.data(), nl, s);
+  pairs.download(hpr.data(), nl, s);
+  linter.download(hli.data(), nl, s);
+  overflow.download(&ovf, 1, s);
+  RSG_CUDA("upload", cudaStreamSynchronize(s));
+  if (ovf) fail(RS_INTERNAL, "Internal", "upload", "traversal stack overflow");
+  std::vector<uint32_t> lo(nl + 1, 0), eo(nl + 1, 0), pb(nl, 0), work(nl);
+  uint64_t tl = 0, te = 0, tp = 0;
+  h->pairs_exact = 0;
+  h->lumped_inter = 0;
+  for (size_t k = 0; k < nl; ++k) {
+    pb[k] = (uint32_t)tp;
+    tl += hl[k], te += he[k], tp += hp[k];
+    if (tl > 0xffffffffull || tp > 0xffffffffull)
+      fail(RS_INVALID_OPTION, "InvalidOption", "upload", "interaction lists exceed 2^32 entries");
+    lo[k + 1] = (uint32_t)tl, eo[k + 1] = (uint32_t)te;
+    h->pairs_exact += hpr[k];
+    h->lumped_inter += hli[k];
+    work[k] = (uint32_t)std::min<unsigned long long>(hpr[k] + hli[k], 0xffffffffull);
+  }
+  h->n_lumped = tl, h->n_exact = te, h->n_partner = tp;
+  upload_vec(h->lumped_off, lo, s);
+  upload_vec(h->exact_off, eo, s);
+  DevBuf<uint32_t> pbase;
+  upload_vec(pbase, pb, s);
+  h->lumped.alloc(std::max<size_t>(tl, 1));
+  h->exact.alloc(std::max<size_t>(te, 1));
+  h->partner_off.alloc(te + 1);
+  d = h->dev();
+  lists_kernel<true><<<blocks(nl, 128), 128, 0, s>>>(d, L, nullptr, nullptr, nullptr, nullptr,
+                                                      nullptr, h->lumped.p, h->exact.p,
+                                                      h->partner_off.p, pbase.p, overflow.p);
+  RSG_LAUNCHED(h->ctx, "lists_fill");
+  uint32_t tp32 = (uint32_t)tp;
+  RSG_CUDA("upload", cudaMemcpyAsync(h->partner_off.p + te, &tp32, sizeof(uint32_t),
+                                     cudaMemcpyHostToDevice, s));
+  RSG_CUDA("upload", cudaStreamSynchronize(s));
+  finish_lists(h, work);
+}
+
+void refit_device(rs_bh *h) {
+  BhDev d = h->dev();
+  size_t nl = h->tree.leaves.size();
+  refit_kernel<<<blocks(nl, 128), 128, 0, h->st()>>>(d, h->pos.p);
+  RSG_LAUNCHED(h->ctx, "refit");
+  h->positions_current = true;
+}
+
+void check_positions_host(rs_bh *h, const double *pos) {
+  // BhTree::refit (barnes_hut.rs:204-229): counts and finiteness; degenerate faces make the
+  // energy non-finite instead.
+  for (int v = 0; v < h->nv; ++v)
+    for (int k = 0; k < 3; ++k)
+      if (!std::isfinite(pos[3 * v + k]))
+        fail(RS_NONFINITE_POSITION, "NonFinitePosition", "energy", "vertex " + std::to_string(v));
+}
+
+// Resident 256-thread blocks per SM of the pair kernel (a persistent grid: one wave).
+int pair_blocks_per_sm(bool grad, bool fast) {
+  static int cache[4] = {0, 0, 0, 0};
+  int &c = cache[(grad ? 2 : 0) + (fast ? 1 : 0)];
+  if (c == 0) {
+    const void *fn = grad ? (fast ? (const void *)bh_pair_kernel<true, true> : (const void *)bh_pair_kernel<true, false>)
+                          : (fast ? (const void *)bh_pair_kernel<false, true> : (const void *)bh_pair_kernel<false, false>);
+    int b = 0;
+    RSG_CUDA("launch", cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, 256, 0));
+    c = b > 0 ? b : 1;
+  }
+  return c;
+}
+
+// The pair kernel and the gradient passes on the context stream (no synchronisation).
+void evaluate(rs_bh *h, const Pow &pw, bool fast, bool grad, double *energy_dev, double *dE_dev) {
+  if (!h->positions_current) fail(RS_INVALID_OPTION, "InvalidOption", "energy", "no positions");
+  cudaStream_t s = h->st();
+  BhDev d = h->dev();
+  size_t nl = h->tree.leaves.size(), nn = h->tree.n_nodes();
+  Profiler &P = h->prof;
+  RSG_CUDA("launch", cudaMemsetAsync(h->ticket.p, 0, sizeof(unsigned), s));
+  unsigned grid = (unsigned)std::min<size_t>((size_t)h->ctx->sm_count * pair_blocks_per_sm(grad, fast),
+                                             blocks(nl, 8));
+  P.begin(s, grad ? "bh_pair_grad" : "bh_pair_value");
+  if (grad) {
+    if (fast) bh_pair_kernel<true, true><<<grid, 256, 0, s>>>(d, pw);
+    else bh_pair_kernel<true, false><<<grid, 256, 0, s>>>(d, pw);
+  } else {
+    if (fast) bh_pair_kernel<false, true><<<grid, 256, 0, s>>>(d, pw);
+    else bh_pair_kernel<false, false><<<grid, 256, 0, s>>>(d, pw);
+  }
+  RSG_LAUNCHED(h->ctx, "bh_pair");
+  P.end(s);
+  if (grad) {
+    P.begin(s, "node_sums");
+    node_sums_kernel<<<blocks(nn, 256), 256, 0, s>>>(d);
+    RSG_LAUNCHED(h->ctx, "node_sums");
+    P.end(s);
+    P.begin(s, "downward");
+    downward_kernel<<<blocks(nl, 128), 128, 0, s>>>(d);
+    RSG_LAUNCHED(h->ctx, "downward");
+    P.end(s);
+    P.begin(s, "final");
+    final_kernel<<<blocks(h->nf, 256), 256, 0, s>>>(d);
+    RSG_LAUNCHED(h->ctx, "final");
+    P.end(s);
+    if (dE_dev) {
+      P.begin(s, "pull_back");
+      pull_back_kernel<<<blocks(h->nv, 256), 256, 0, s>>>(d, h->pos.p, dE_dev);
+      RSG_LAUNCHED(h->ctx, "pull_back");
+      P.end(s);
+    }
+  }
+  P.begin(s, "energy_reduce");
+  energy_reduce_kernel<<<1, 1024, 0, s>>>(h->leaf_energy.p, (int)nl, energy_dev);
+  RSG_LAUNCHED(h->ctx, "energy_reduce");
+  P.end(s);
+}
+
+void find_culprit(rs_bh *h, const Pow &pw, bool fast) {
+  cudaStream_t s = h->st();
+  unsigned long long init = ~0ull, rank = ~0ull;
+  RSG_CUDA("product", cudaMemcpyAsync(h->culprit_key.p, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+  size_t nl = h->tree.leaves.size();
+  if (fast) culprit_kernel<true><<<blocks(nl, 128), 128, 0, s>>>(h->dev(), pw, h->culprit_key.p);
+  else culprit_kernel<false><<<blocks(nl, 128), 128, 0, s>>>(h->dev(), pw, h->culprit_key.p);
+  RSG_LAUNCHED(h->ctx, "culprit");
+  h->culprit_key.download(&rank, 1, s);
+  RSG_CUDA("product", cudaStreamSynchronize(s));
+  h->culprit[0] = h->culprit[1] = -1;
+  if (rank == ~0ull) return;
+  uint32_t q = (uint32_t)(rank >> 8), ds = (rank >> 4) & 15, dt = rank & 15;
+  std::vector<uint32_t> eo(nl + 1);
+  uint32_t c = 0;
+  h->exact_off.download(eo.data(), nl + 1, s);
+  RSG_CUDA("product", cudaMemcpyAsync(&c, h->exact.p + q, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  RSG_CUDA("product", cudaStreamSynchronize(s));
+  size_t k = (size_t)(std::upper_bound(eo.begin(), eo.end(), q) - eo.begin()) - 1;
+  const Tree &T = h->tree;
+  uint32_t leaf = T.leaves[k];
+  uint32_t fs = T.order[T.start[leaf] + ds], ft = T.order[T.start[c] + dt];
+  h->culprit[0] = std::min(fs, ft);
+  h->culprit[1] = std::max(fs, ft);
+}
+
+}  // namespace
+
+extern "C" {
+
+int rs_bh_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const double *positions_host,
+                double theta, int leaf_size, rs_bh **out) {
+  *out = nullptr;
+  return guard([&] {
+    if (!(std::isfinite(theta) && theta >= 0.0))
+      fail(RS_INVALID_OPTION, "InvalidOption", "energy", "theta must be finite and non-negative");
+    if (leaf_size < 1) fail(RS_INVALID_OPTION, "InvalidOption", "energy", "leaf_size must be at least 1");
+    validate_topology(nv, nf, faces);
+    validate_positions(nv, nf, faces, positions_host);
+    ctx->use();
+    auto h = std::make_unique<rs_bh>();
+    h->ctx = ctx;
+    h->nv = nv, h->nf = nf, h->theta = theta, h->leaf_size = leaf_size;
+    h->faces_h.assign(faces, faces + 3 * (size_t)nf);
+    FaceGeom g = face_geometry(nf, faces, positions_host);
+    h->tree = build_face_tree(nf, faces, positions_host, g, leaf_size);
+    upload_topology(h.get());
+    build_lists_device(h.get());
+    h->pos.upload(positions_host, 3 * (size_t)nv, h->st());
+    refit_device(h.get());
+    RSG_CUDA("upload", cudaStreamSynchronize(h->st()));
+    *out = h.release();
+  });
+}
+
+int rs_bh_attach(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const double *positions_host,
+                 int n_nodes, const uint32_t *node_start, const uint32_t *node_end,
+                 const uint32_t *node_right, const uint32_t *order, const int64_t *lumped_off,
+                 const uint32_t *lumped, const int64_t *exact_off, const uint32_t *exact,
+                 rs_bh **out) {
+  *out = nullptr;
+  return guard([&] {
+    validate_topology(nv, nf, faces);
+    validate_positions(nv, nf, faces, positions_host);
+    if (n_nodes < 1) fail(RS_INVALID_OPTION, "InvalidOption", "upload", "empty tree");
+    ctx->use();
+    auto h = std::make_unique<rs_bh>();
+    h->ctx = ctx;
+    h->nv = nv, h->nf = nf;
+    h->faces_h.assign(faces, faces + 3 * (size_t)nf);
+    Tree &T = h->tree;
+    T.start.assign(node_start, node_start + n_nodes);
+    T.end.assign(node_end, node_end + n_nodes);
+    T.right.assign(node_right, node_right + n_nodes);
+    T.order.assign(order, order + nf);
+    T.leaf_ordinal.assign(n_nodes, UINT32_MAX);
+    int max_leaf = 0;
+    for (int i = 0; i < n_nodes; ++i) {
+      if (T.right[i] && (T.right[i] <= (uint32_t)i || T.right[i] >= (uint32_t)n_nodes))
+        fail(RS_INVALID_OPTION, "InvalidOption", "upload", "bad right child");
+      if (T.end[i] < T.start[i] || T.end[i] > (uint32_t)nf)
+        fail(RS_INVALID_OPTION, "InvalidOption", "upload", "bad node range");
+      if (T.right[i] == 0) {
+        T.leaf_ordinal[i] = (uint32_t)T.leaves.size();
+        T.leaves.push_back((uint32_t)i);
+        max_leaf = std::max<int>(max_leaf, (int)(T.end[i] - T.start[i]));
+      }
+    }
+    h->leaf_size = max_leaf;
+    size_t nl = T.leaves.size();
+    upload_topology(h.get());
+    // lists from the caller
+    cudaStream_t s = h->st();
+    std::vector<uint32_t> lo(nl + 1), eo(nl + 1), work(nl, 0);
+    for (size_t k = 0; k <= nl; ++k) lo[k] = (uint32_t)lumped_off[k], eo[k] = (uint32_t)exact_off[k];
+    h->n_lumped = lo[nl], h->n_exact = eo[nl];
+    std::vector<uint32_t> poff(h->n_exact + 1, 0);
+    h->pairs_exact = 0, h->lumped_inter = 0;
+    uint64_t p = 0;
+    for (size_t k = 0; k < nl; ++k) {
+      uint32_t l = T.leaves[k];
+      uint64_t ns = T.end[l] - T.start[l];
+      for (uint32_t q = eo[k]; q < eo[k + 1]; ++q) {
+        uint32_t c = exact[q];
+        if (c >= (uint32_t)n_nodes || T.right[c] != 0)
+          fail(RS_INVALID_OPTION, "InvalidOption", "upload", "exact entry is not a leaf");
+        uint64_t nc = T.end[c] - T.start[c];
+        poff[q] = (uint32_t)p;
+        p += nc;
+        h->pairs_exact += (c == l) ? ns * (ns - 1) : ns * nc;
+      }
+      for (uint32_t q = lo[k]; q < lo[k + 1]; ++q)
+        if (lumped[q] >= (uint32_t)n_nodes)
+          fail(RS_INVALID_OPTION, "InvalidOption", "upload", "lumped entry out of range");
+      h->lumped_inter += (uint64_t)(lo[k + 1] - lo[k]) * ns;
+      work[k] = (uint32_t)std::min<uint64_t>((uint64_t)(lo[k + 1] - lo[k]) * ns +
+                                                 (uint64_t)(eo[k + 1] - eo[k]) * ns * 8,
+                                             0xffffffffull);
+    }
+    poff[h->n_exact] = (uint32_t)p;
+    h->n_partner = p;
+    upload_vec(h->lumped_off, lo, s);
+    upload_vec(h->exact_off, eo, s);
+    h->lumped.upload(lumped, std::max<size_t>(h->n_lumped, 1), s);
+    h->exact.upload(exact, std::max<size_t>(h->n_exact, 1), s);
+    upload_vec(h->partner_off, poff, s);
+    finish_lists(h.get(), work);
+    h->pos.upload(positions_host, 3 * (size_t)nv, s);
+    refit_device(h.get());
+    RSG_CUDA("upload", cudaStreamSynchronize(s));
+    *out = h.release();
+  });
+}
+
+void rs_bh_free(rs_bh *bh) {
+  if (!bh) return;
+  cudaSetDevice(bh->ctx->device);
+  cudaStreamSynchronize(bh->ctx->stream);
+  delete bh;
+}
+
+int rs_bh_refit(rs_bh *h, const double *positions_host) {
+  return guard([&] {
+    check_positions_host(h, positions_host);
+    h->ctx->use();
+    h->pos.upload(positions_host, 3 * (size_t)h->nv, h->st());
+    refit_device(h);
+  });
+}
+
+int rs_bh_refit_device(rs_bh *h, const double *positions_dev) {
+  return guard([&] {
+    h->ctx->use();
+    RSG_CUDA("upload", cudaMemcpyAsync(h->pos.p, positions_dev, 3 * (size_t)h->nv * sizeof(double),
+                                       cudaMemcpyDeviceToDevice, h->st()));
+    refit_device(h);
+  });
+}
+
+int rs_bh_energy(rs_bh *h, double alpha, double beta, double *energy) {
+  return guard([&] {
+    Pow pw = make_pow(alpha, beta);
+    h->ctx->use();
+    evaluate(h, pw, is_fast(alpha, beta), false, h->energy.p, nullptr);
+    h->energy.download(energy, 1, h->st());
+    RSG_CUDA("product", cudaStreamSynchronize(h->st()));
+  });
+}
+
+static void eval_host(rs_bh *h, double alpha, double beta, double *energy, double *dE_host,
+                      double *p7_host) {
+  Pow pw = make_pow(alpha, beta);
+  bool fast = is_fast(alpha, beta);
+  h->ctx->use();
+  evaluate(h, pw, fast, true, h->energy.p, h->dE.p);
+  cudaStream_t s = h->st();
+  double E = 0;
+  h->energy.download(&E, 1, s);
+  size_t nd = 3 * (size_t)h->nv;
+  double *stage = (double *)h->ctx->staging(nd * sizeof(double) + 8 * sizeof(float) * (size_t)h->nf);
+  h->dE.download(stage, nd, s);
+  float *p7 = (float *)(stage + nd);
+  if (p7_host) h->partials.download((float4 *)p7, 2 * (size_t)h->nf, s);
+  RSG_CUDA("product", cudaStreamSynchronize(s));
+  bool finite = std::isfinite(E);
+  for (size_t i = 0; i < nd && finite; ++i) finite = std::isfinite(stage[i]);
+  if (!finite) {
+    find_culprit(h, pw, fast);
+    fail(RS_NONFINITE_ENERGY, "NonFiniteEnergy", "energy",
+         "faces (" + std::to_string(h->culprit[0]) + ", " + std::to_string(h->culprit[1]) +
+             ") have the same barycenter or a non-finite term");
+  }
+  *energy = E;
+  if (dE_host) std::memcpy(dE_host, stage, nd * sizeof(double));
+  if (p7_host)
+    for (int f = 0; f < h->nf; ++f)
+      for (int c = 0; c < 7; ++c) p7_host[7 * (size_t)f + c] = (double)p7[8 * (size_t)f + c];
+}
+
+int rs_bh_energy_and_differential(rs_bh *h, double alpha, double beta, double *energy,
+                                  double *differential_host) {
+  return guard([&] { eval_host(h, alpha, beta, energy, differential_host, nullptr); });
+}
+
+int rs_bh_face_partials(rs_bh *h, double alpha, double beta, double *energy, double *p7) {
+  return guard([&] { eval_host(h, alpha, beta, energy, nullptr, p7); });
+}
+
+int rs_bh_energy_and_differential_device(rs_bh *h, double alpha, double beta, double *energy_dev,
+                                         double *differential_dev) {
+  return guard([&] {
+    Pow pw = make_pow(alpha, beta);
+    h->ctx->use();
+    evaluate(h, pw, is_fast(alpha, beta), true, energy_dev, differential_dev);
+  });
+}
+
+int rs_bh_sizes(rs_bh *h, int64_t *o) {
+  return guard([&] {
+    o[0] = (int64_t)h->tree.n_nodes();
+    o[1] = (int64_t)h->tree.leaves.size();
+    o[2] = (int64_t)h->n_lumped;
+    o[3] = (int64_t)h->n_exact;
+    o[4] = (int64_t)h->n_partner;
+    o[5] = (int64_t)h->pairs_exact;
+    o[6] = (int64_t)h->lumped_inter;
+  });
+}
+
+int rs_bh_export(rs_bh *h, uint32_t *node_start, uint32_t *node_end, uint32_t *node_right,
+                 uint32_t *order, int64_t *lumped_off, uint32_t *lumped, int64_t *exact_off,
+                 uint32_t *exact) {
+  return guard([&] {
+    const Tree &T = h->tree;
+    std::copy(T.start.begin(), T.start.end(), node_start);
+    std::copy(T.end.begin(), T.end.end(), node_end);
+    std::copy(T.right.begin(), T.right.end(), node_right);
+    std::copy(T.order.begin(), T.order.end(), order);
+    size_t nl = T.leaves.size();
+    std::vector<uint32_t> lo(nl + 1), eo(nl + 1);
+    cudaStream_t s = h->st();
+    h->lumped_off.download(lo.data(), nl + 1, s);
+    h->exact_off.download(eo.data(), nl + 1, s);
+    if (h->n_lumped) h->lumped.download(lumped, h->n_lumped, s);
+    if (h->n_exact) h->exact.download(exact, h->n_exact, s);
+    RSG_CUDA("product", cudaStreamSynchronize(s));
+    for (size_t k = 0; k <= nl; ++k) lumped_off[k] = lo[k], exact_off[k] = eo[k];
+  });
+}
+
+int rs_bh_culprit(rs_bh *h, int64_t *faces2) {
+  return guard([&] { faces2[0] = h->culprit[0], faces2[1] = h->culprit[1]; });
+}
+
+int rs_bh_profile(rs_bh *h, double alpha, double beta, int reps, char *names, int names_len,
+                  double *ms, int max_kernels, int *n_kernels) {
+  return guard([&] {
+    Pow pw = make_pow(alpha, beta);
+    bool fast = is_fast(alpha, beta);
+    h->ctx->use();
+    h->prof.start();
+    for (int r = 0; r < reps; ++r) evaluate(h, pw, fast, true, h->energy.p, h->dE.p);
+    h->prof.stop(h->st());
+    h->prof.report(names, names_len, ms, max_kernels, n_kernels, reps);
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,127 @@
+// Device code of the Barnes-Hut tangent-point energy and its exact adjoint gradient
+// (RS/src/energy/barnes_hut.rs; kernel RS/src/kernel.rs). See bh.cu for the host driver.
+//
+// Data layout in HBM (per evaluation, BVH order = the order of the tree's `order` array, so a
+// leaf's faces are contiguous):
+//   fxa[p] : float4 (X_S - X_leaf (xyz, FP32 offset from the leaf centroid), a_S)
+//   fnn[p] : float4 (N_S (xyz), 0)
+//   ncA[n] : double4 (X_n (xyz), A_n) cluster centroid and area of every node, FP64
+// Leaf centroids are FP64; a pair's separation is (X_L - X_C) in FP64, rounded once per block,
+// plus the difference of the two FP32 offsets. This keeps v = X_S - X_T at FP32 precision
+// relative to |v| (not to |X|), which the near-field terms (r^-12 nu^6) need.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace rsg {
+
+struct BhDev {
+  // topology (fixed per step)
+  const uint32_t *faces;       // 3F, original face order
+  const uint32_t *order;       // F: BVH position -> face
+  const uint32_t *node_start;  // N
+  const uint32_t *node_end;    // N
+  const uint32_t *node_right;  // N
+  const uint32_t *node_parent; // N (root: 0)
+  const uint32_t *leaves;      // L: node id of each leaf
+  const uint32_t *leaf_of_pos; // F: leaf ordinal of each BVH position
+  const uint32_t *schedule;    // L: leaf ordinals, most work first
+  const uint32_t *chain_off;   // L + 1: root -> leaf chains
+  const uint32_t *chain;
+  const uint32_t *inc_off;     // V + 1: vertex -> incident (face << 2 | corner), faces ascending
+  const uint32_t *inc;
+  // interaction lists (CSR per leaf ordinal) and their transposes
+  const uint32_t *lumped_off, *lumped, *exact_off, *exact, *partner_off;
+  const uint32_t *lumped_t_off, *lumped_t, *exact_t_off, *exact_t;
+  int n_vertices, n_faces, n_nodes, n_leaves;
+  // per-evaluation state
+  float4 *fxa, *fnn;
+  double4 *ncA;     // node centroid (xyz) and area (w)
+  double4 *nmom;    // node first moment (xyz) and area (w), for the bottom-up refit
+  uint32_t *refit_count;
+  // outputs and scratch
+  float4 *own;       // 2 per position: (d_a, d_x), (d_n, 0)
+  float4 *node_term; // per lumped entry: (b, u)
+  float4 *partner;   // per partner slot: (d_a, d_x)
+  float4 *node_sum;  // per node: (b_C, u_C)
+  float4 *leaf_bu;   // per leaf: (beta, U) of the downward pass
+  float4 *partials;  // 2 per face (by face id): (d_a, d_x), (d_n, 0)
+  double *leaf_energy;
+  unsigned int *ticket;
+};
+
+// Exponents of K = |N.v|^alpha |v|^-beta in the forms the kernels evaluate:
+// K = q^(alpha/2) r2^((alpha-beta)/2), q = nu^2 / r2 in [0, 1]; c_n = alpha nu q^(alpha/2-1) r2^((alpha-beta)/2-1).
+struct Pow {
+  float alpha, beta;
+  int a_int;   // alpha as an integer, or -1
+  int ab_int;  // beta - alpha as an integer, or -1
+};
+
+// q^(alpha/2 - 1): (alpha - 2)/2 = h, integer or half-integer for integer alpha.
+__device__ __forceinline__ float pow_q1(const Pow &p, float q) {
+  if (p.a_int >= 2) {
+    int m = p.a_int - 2;  // q^(m/2)
+    float acc = 1.f, x = q;
+    int k = m >> 1;
+    while (k) {
+      if (k & 1) acc *= x;
+      x *= x;
+      k >>= 1;
+    }
+    if (m & 1) acc *= sqrtf(q);
+    return acc;
+  }
+  return q > 0.f ? powf(q, 0.5f * p.alpha - 1.f) : 0.f;
+}
+
+// r2^((alpha-beta)/2) = ir2^((beta-alpha)/2)
+__device__ __forceinline__ float pow_r(const Pow &p, float r2, float ir2) {
+  if (p.ab_int >= 0) {
+    int m = p.ab_int;
+    float acc = 1.f, x = ir2;
+    int k = m >> 1;
+    while (k) {
+      if (k & 1) acc *= x;
+      x *= x;
+      k >>= 1;
+    }
+    if (m & 1) acc *= rsqrtf(r2);
+    return acc;
+  }
+  return powf(r2, 0.5f * (p.alpha - p.beta));
+}
+
+// K and c_n for (alpha, beta) = (6, 12) (FAST) or the general exponents.
+template <bool FAST>
+__device__ __forceinline__ void kernel_k(const Pow &p, float nu, float r2, float ir2, float &K,
+                                         float &cn) {
+  float q = nu * nu * ir2;
+  if (FAST) {
+    float q2 = q * q;
+    float i3 = ir2 * ir2 * ir2;
+    float t = q2 * i3;  // nu^4 r^-10 .. scaled: q^2 ir2^3
+    K = t * q;
+    cn = 6.f * nu * t * ir2;
+  } else {
+    float a1 = pow_q1(p, q);
+    float b = pow_r(p, r2, ir2);
+    float t = a1 * b;
+    K = t * q;
+    cn = (nu == 0.f) ? 0.f : p.alpha * nu * t * ir2;
+  }
+}
+
+// Kahan-compensated FP32 accumulator.
+struct Kahan {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    float y = x - c;
+    float t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+  __device__ __forceinline__ float value() const { return s - c; }
+};
+
+}  // namespace rsg

@@ -1,0 +1,114 @@
+// Shared host-side plumbing of librsgpu: status/error reporting, the context, device buffers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "rsgpu.h"
+
+namespace rsg {
+
+// An error carrying the RsError kind, the operation word and a detail string
+// (RsError::Gpu { operation, detail }, RS/src/gpu/cuda.rs:19-24).
+struct Error : std::runtime_error {
+  int code;
+  std::string kind, operation;
+  Error(int c, std::string k, std::string op, const std::string &detail)
+      : std::runtime_error(detail), code(c), kind(std::move(k)), operation(std::move(op)) {}
+};
+
+[[noreturn]] inline void fail(int code, const char *kind, const char *op, const std::string &d) {
+  throw Error(code, kind, op, d);
+}
+
+inline void cuda_check(cudaError_t e, const char *op, const char *what) {
+  if (e != cudaSuccess)
+    fail(RS_GPU, "Gpu", op, std::string(what) + ": " + cudaGetErrorString(e));
+}
+#define RSG_CUDA(op, call) ::rsg::cuda_check((call), op, #call)
+
+void set_last_error(const Error &e);
+void set_last_error_other(int code, const char *what);
+
+// Runs `f`, converting exceptions into a status and the thread's last error.
+template <class F>
+int guard(F &&f) {
+  try {
+    f();
+    return RS_OK;
+  } catch (const Error &e) {
+    set_last_error(e);
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    set_last_error_other(RS_INTERNAL, "host allocation failed");
+    return RS_INTERNAL;
+  } catch (const std::exception &e) {
+    set_last_error_other(RS_INTERNAL, e.what());
+    return RS_INTERNAL;
+  }
+}
+
+// A typed device allocation owned by one object (freed on destruction).
+template <class T>
+struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  explicit DevBuf(size_t count) { alloc(count); }
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr, o.n = 0; }
+  DevBuf &operator=(DevBuf &&o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p, n = o.n, o.p = nullptr, o.n = 0;
+    }
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  void alloc(size_t count) {
+    release();
+    n = count;
+    if (count) RSG_CUDA("upload", cudaMalloc(&p, count * sizeof(T)));
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr, n = 0;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+  void upload(const T *h, size_t count, cudaStream_t s) {
+    if (count != n) alloc(count);
+    if (count) RSG_CUDA("upload", cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+  void upload(const std::vector<T> &v, cudaStream_t s) { upload(v.data(), v.size(), s); }
+  void download(T *h, size_t count, cudaStream_t s) const {
+    if (count) RSG_CUDA("product", cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, s));
+  }
+};
+
+}  // namespace rsg
+
+struct rs_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int sm_count = 0;
+  int cc_major = 0, cc_minor = 0;
+  std::string name;
+  int64_t launches = 0;
+  // Pinned staging buffer for host <-> device copies of the entry points with host arrays.
+  void *pinned = nullptr;
+  size_t pinned_bytes = 0;
+  void *staging(size_t bytes);
+  void use() const;  // makes the context's device current for the calling thread
+};
+
+// Counts one kernel launch of `ctx` and checks the launch status.
+#define RSG_LAUNCHED(ctx, what)                                   \
+  do {                                                            \
+    (ctx)->launches++;                                            \
+    ::rsg::cuda_check(cudaGetLastError(), "launch", what);        \
+  } while (0)

@@ -1,0 +1,361 @@
+"""rs_gb300 -- the GB300 Repulsive-Surfaces hot path behind the crate's own entry points.
+
+A thin Python host over ``librsgpu.so`` (C ABI in ``include/rsgpu.h``). The names mirror the
+reference crate ``ddg-repulsive-surfaces`` (m1el/ddg-tools):
+
+* ``Exponents`` (RS/src/kernel.rs:26-76), ``BhOptions`` (RS/src/energy/mod.rs:62-102);
+* ``BhTree.build / attach / refit / try_energy / energy_and_differential /
+  try_face_partials`` (RS/src/energy/barnes_hut.rs:156-471);
+* ``energy()`` (RS/src/energy/mod.rs:168-219) returning an ``EnergyReport`` (:130-146);
+* ``RsError`` carrying the crate's error kind (RS/src/error.rs).
+
+There is no CPU fallback: if the library or a CUDA device is missing, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import time
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+
+from . import generators  # noqa: F401
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "librsgpu.so"
+
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_u32p = np.ctypeslib.ndpointer(dtype=np.uint32, flags="C_CONTIGUOUS")
+_i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+_vp = C.c_void_p
+_dp = C.POINTER(C.c_double)
+
+
+class RsError(RuntimeError):
+    """An error of the library: ``kind`` is the crate's RsError variant name, ``operation`` the
+    failing operation word (RsError::Gpu { operation, detail }, RS/src/gpu/cuda.rs:19-24)."""
+
+    def __init__(self, code: int, kind: str, operation: str, detail: str):
+        super().__init__(f"{kind} ({operation}): {detail}")
+        self.code, self.kind, self.operation, self.detail = code, kind, operation, detail
+
+
+_lib = None
+
+
+def load_library(path: str | os.PathLike | None = None):
+    """Loads librsgpu.so from the package directory (built by ``build.build()``)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RsError(10, "Gpu", "context", f"{p} is missing: run rs_gb300.build.build() first")
+    L = C.CDLL(str(p))
+    for name in ("rs_last_error", "rs_last_error_operation", "rs_last_error_kind"):
+        getattr(L, name).restype = C.c_char_p
+    sig = {
+        "rs_device_count": [C.POINTER(C.c_int)],
+        "rs_ctx_create": [C.c_int, C.POINTER(_vp)],
+        "rs_ctx_stream": [_vp, C.POINTER(_vp)],
+        "rs_ctx_synchronize": [_vp],
+        "rs_ctx_info": [_vp, C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                        C.POINTER(C.c_int)],
+        "rs_ctx_launch_count": [_vp, C.POINTER(C.c_int64)],
+        "rs_fp32_peak": [_vp, C.POINTER(C.c_double)],
+        "rs_surface_validate": [C.c_int, C.c_int, _u32p, _f64p],
+        "rs_face_tree_build": [C.c_int, C.c_int, _u32p, _f64p, C.c_int, C.c_int, _u32p, _u32p,
+                               _u32p, _u32p, _f64p, _f64p, C.POINTER(C.c_int)],
+        "rs_bh_build": [_vp, C.c_int, C.c_int, _u32p, _f64p, C.c_double, C.c_int, C.POINTER(_vp)],
+        "rs_bh_attach": [_vp, C.c_int, C.c_int, _u32p, _f64p, C.c_int, _u32p, _u32p, _u32p, _u32p,
+                         _i64p, _u32p, _i64p, _u32p, C.POINTER(_vp)],
+        "rs_bh_refit": [_vp, _f64p],
+        "rs_bh_refit_device": [_vp, _vp],
+        "rs_bh_energy": [_vp, C.c_double, C.c_double, _dp],
+        "rs_bh_energy_and_differential": [_vp, C.c_double, C.c_double, _dp, _f64p],
+        "rs_bh_energy_and_differential_device": [_vp, C.c_double, C.c_double, _vp, _vp],
+        "rs_bh_face_partials": [_vp, C.c_double, C.c_double, _dp, _f64p],
+        "rs_bh_sizes": [_vp, _i64p],
+        "rs_bh_export": [_vp, _u32p, _u32p, _u32p, _u32p, _i64p, _u32p, _i64p, _u32p],
+        "rs_bh_culprit": [_vp, _i64p],
+        "rs_bh_profile": [_vp, C.c_double, C.c_double, C.c_int, C.c_char_p, C.c_int, _f64p,
+                          C.c_int, C.POINTER(C.c_int)],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    L.rs_ctx_free.argtypes = [_vp]
+    L.rs_ctx_free.restype = None
+    L.rs_bh_free.argtypes = [_vp]
+    L.rs_bh_free.restype = None
+    _lib = L
+    return L
+
+
+def _check(code: int) -> None:
+    if code != 0:
+        L = load_library()
+        raise RsError(code, L.rs_last_error_kind().decode(), L.rs_last_error_operation().decode(),
+                      L.rs_last_error().decode())
+
+
+def device_count() -> int:
+    n = C.c_int()
+    _check(load_library().rs_device_count(C.byref(n)))
+    return n.value
+
+
+class Context:
+    """A device and its stream (GpuContext, RS/src/gpu/mod.rs:36-127)."""
+
+    def __init__(self, ordinal: int = 0):
+        L = load_library()
+        h = _vp()
+        _check(L.rs_ctx_create(int(ordinal), C.byref(h)))
+        self._h = h
+        self.ordinal = ordinal
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.rs_ctx_free(self._h)
+            self._h = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def stream(self) -> int:
+        s = _vp()
+        _check(_lib.rs_ctx_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    def synchronize(self) -> None:
+        _check(_lib.rs_ctx_synchronize(self._h))
+
+    def info(self) -> dict:
+        name = C.create_string_buffer(256)
+        sm, ma, mi = C.c_int(), C.c_int(), C.c_int()
+        _check(_lib.rs_ctx_info(self._h, name, 256, C.byref(sm), C.byref(ma), C.byref(mi)))
+        return {"name": name.value.decode(), "sm_count": sm.value, "cc": (ma.value, mi.value)}
+
+    def fp32_peak_tflops(self) -> float:
+        """Measured FP32 FMA throughput of the device (TFLOP/s)."""
+        t = C.c_double()
+        _check(_lib.rs_fp32_peak(self._h, C.byref(t)))
+        return t.value
+
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        _check(_lib.rs_ctx_launch_count(self._h, C.byref(n)))
+        return n.value
+
+
+_default_ctx = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+@dataclass(frozen=True)
+class Exponents:
+    """(alpha, beta) of the tangent-point kernel (RS/src/kernel.rs:26-76)."""
+
+    alpha: float = 6.0
+    beta: float = 12.0
+
+    def __post_init__(self):
+        a, b = self.alpha, self.beta
+        if not (np.isfinite(a) and np.isfinite(b)):
+            raise RsError(1, "InvalidExponents", "energy", "both exponents must be finite")
+        if a <= 1.0:
+            raise RsError(1, "InvalidExponents", "energy", "alpha must be greater than 1")
+        if b <= a + 2.0:
+            raise RsError(1, "InvalidExponents", "energy",
+                          "beta must be greater than alpha + 2 (s = (beta - 2)/alpha > 1)")
+        if b >= 2.0 * a + 2.0:
+            raise RsError(1, "InvalidExponents", "energy",
+                          "beta must be smaller than 2 alpha + 2 (s = (beta - 2)/alpha < 2)")
+
+    @property
+    def s(self) -> float:
+        return (self.beta - 2.0) / self.alpha
+
+
+@dataclass(frozen=True)
+class BhOptions:
+    """Barnes-Hut parameters (RS/src/energy/mod.rs:62-102): theta 0.5, leaf size 8."""
+
+    theta: float = 0.5
+    leaf_size: int = 8
+
+
+def _mesh(faces, positions):
+    faces = np.ascontiguousarray(faces, dtype=np.uint32).reshape(-1, 3)
+    positions = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+    return faces, positions
+
+
+def validate_surface(faces, positions) -> None:
+    """Surface::new + validate_positions (RS/src/surface.rs:132-541); raises RsError."""
+    faces, positions = _mesh(faces, positions)
+    _check(load_library().rs_surface_validate(len(positions), len(faces), faces.ravel(),
+                                              positions.ravel()))
+
+
+def face_tree(faces, positions, leaf_size: int = 8) -> dict:
+    """The face BVH as the library builds it on the host (no device work)."""
+    faces, positions = _mesh(faces, positions)
+    cap = max(2 * len(faces), 1)
+    start, end, right = (np.empty(cap, np.uint32) for _ in range(3))
+    order = np.empty(len(faces), np.uint32)
+    box, radius = np.empty(6 * cap), np.empty(cap)
+    n = C.c_int()
+    _check(load_library().rs_face_tree_build(len(positions), len(faces), faces.ravel(),
+                                             positions.ravel(), int(leaf_size), cap, start, end,
+                                             right, order, box, radius, C.byref(n)))
+    k = n.value
+    return dict(start=start[:k], end=end[:k], right=right[:k], order=order,
+                box=box[: 6 * k].reshape(k, 6), radius=radius[:k])
+
+
+class BhTree:
+    """The Barnes-Hut evaluator of one step on the GPU (BhTree + DeviceBh,
+    RS/src/energy/barnes_hut.rs:114-471). Build once per step, refit for line-search trials."""
+
+    def __init__(self, handle, ctx: Context, n_vertices: int, n_faces: int):
+        self._h, self.ctx, self.n_vertices, self.n_faces = handle, ctx, n_vertices, n_faces
+
+    @classmethod
+    def build(cls, faces, positions, opts: BhOptions = BhOptions(), ctx: Context | None = None):
+        ctx = ctx or default_context()
+        faces, positions = _mesh(faces, positions)
+        h = _vp()
+        _check(_lib.rs_bh_build(ctx.handle, len(positions), len(faces), faces.ravel(),
+                                positions.ravel(), float(opts.theta), int(opts.leaf_size),
+                                C.byref(h)))
+        t = cls(h, ctx, len(positions), len(faces))
+        t.options = opts
+        return t
+
+    @classmethod
+    def attach(cls, faces, positions, tree: dict, lists: dict, ctx: Context | None = None):
+        """attach_gpu with a tree and lists built by the caller (dicts as the oracle exports)."""
+        ctx = ctx or default_context()
+        faces, positions = _mesh(faces, positions)
+        u = lambda a: np.ascontiguousarray(a, dtype=np.uint32)  # noqa: E731
+        i = lambda a: np.ascontiguousarray(a, dtype=np.int64)  # noqa: E731
+        h = _vp()
+        _check(_lib.rs_bh_attach(ctx.handle, len(positions), len(faces), faces.ravel(),
+                                 positions.ravel(), len(tree["start"]), u(tree["start"]),
+                                 u(tree["end"]), u(tree["right"]), u(tree["order"]),
+                                 i(lists["lumped_off"]), u(lists["lumped"]),
+                                 i(lists["exact_off"]), u(lists["exact"]), C.byref(h)))
+        return cls(h, ctx, len(positions), len(faces))
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.rs_bh_free(self._h)
+            self._h = None
+
+    def refit(self, positions) -> None:
+        p = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1)
+        if p.size != 3 * self.n_vertices:
+            raise RsError(3, "PositionCountMismatch", "energy",
+                          f"expected {self.n_vertices} positions, found {p.size // 3}")
+        _check(_lib.rs_bh_refit(self._h, p))
+
+    def refit_device(self, positions_dev_ptr: int) -> None:
+        _check(_lib.rs_bh_refit_device(self._h, _vp(positions_dev_ptr)))
+
+    def try_energy(self, e: Exponents = Exponents()) -> float:
+        out = C.c_double()
+        _check(_lib.rs_bh_energy(self._h, e.alpha, e.beta, C.byref(out)))
+        return out.value
+
+    def energy_and_differential(self, e: Exponents = Exponents()):
+        out = C.c_double()
+        d = np.empty((self.n_vertices, 3))
+        _check(_lib.rs_bh_energy_and_differential(self._h, e.alpha, e.beta, C.byref(out), d.ravel()))
+        return out.value, d
+
+    def energy_and_differential_device(self, e: Exponents, energy_dev_ptr: int, dE_dev_ptr: int):
+        _check(_lib.rs_bh_energy_and_differential_device(self._h, e.alpha, e.beta,
+                                                         _vp(energy_dev_ptr), _vp(dE_dev_ptr)))
+
+    def try_face_partials(self, e: Exponents = Exponents()):
+        out = C.c_double()
+        p = np.empty((self.n_faces, 7))
+        _check(_lib.rs_bh_face_partials(self._h, e.alpha, e.beta, C.byref(out), p.ravel()))
+        return out.value, p
+
+    def sizes(self) -> dict:
+        o = np.zeros(7, np.int64)
+        _check(_lib.rs_bh_sizes(self._h, o))
+        keys = ["n_nodes", "n_leaves", "n_lumped", "n_exact", "n_partner", "pairs_exact",
+                "lumped_interactions"]
+        return dict(zip(keys, (int(x) for x in o)))
+
+    def export(self) -> tuple[dict, dict]:
+        s = self.sizes()
+        nn, nl = s["n_nodes"], s["n_leaves"]
+        start, end, right = (np.empty(nn, np.uint32) for _ in range(3))
+        order = np.empty(self.n_faces, np.uint32)
+        lo, eo = np.empty(nl + 1, np.int64), np.empty(nl + 1, np.int64)
+        lum, ex = np.empty(max(s["n_lumped"], 1), np.uint32), np.empty(max(s["n_exact"], 1), np.uint32)
+        _check(_lib.rs_bh_export(self._h, start, end, right, order, lo, lum, eo, ex))
+        return (dict(start=start, end=end, right=right, order=order),
+                dict(lumped_off=lo, lumped=lum[: s["n_lumped"]], exact_off=eo, exact=ex[: s["n_exact"]]))
+
+    def culprit(self) -> tuple[int, int]:
+        o = np.zeros(2, np.int64)
+        _check(_lib.rs_bh_culprit(self._h, o))
+        return int(o[0]), int(o[1])
+
+    def profile(self, e: Exponents = Exponents(), reps: int = 5) -> dict:
+        """Average ms per kernel of one energy+differential evaluation (CUDA events)."""
+        names = C.create_string_buffer(4096)
+        ms = np.zeros(32)
+        n = C.c_int()
+        _check(_lib.rs_bh_profile(self._h, e.alpha, e.beta, int(reps), names, 4096, ms, 32, C.byref(n)))
+        raw = names.raw.split(b"\0")[: n.value]
+        return {k.decode(): float(v) for k, v in zip(raw, ms[: n.value])}
+
+
+@dataclass
+class EnergyReport:
+    """Result of energy() (RS/src/energy/mod.rs:130-146)."""
+
+    energy: float
+    differential: np.ndarray
+    penalties: list = field(default_factory=list)
+    subcritical: bool = False
+    pairs_exact: int = 0
+    nodes_lumped: int = 0
+    seconds: float = 0.0
+
+    def total(self) -> float:
+        return self.energy + sum(self.penalties)
+
+
+def energy(faces, positions, exponents: Exponents = Exponents(), eval=None,
+           ctx: Context | None = None) -> EnergyReport:
+    """The crate's energy entry (RS/src/energy/mod.rs:168-219) on the GPU.
+
+    ``eval`` is ``"exact"`` (all ordered pairs; on the device this is Barnes-Hut with theta 0,
+    which admits no far field) or a ``BhOptions``. Penalties are not part of this path."""
+    t0 = time.perf_counter()
+    opts = BhOptions(theta=0.0) if eval in (None, "exact") else eval
+    tree = BhTree.build(faces, positions, opts, ctx)
+    E, dE = tree.energy_and_differential(exponents)
+    s = tree.sizes()
+    return EnergyReport(energy=E, differential=dE, subcritical=exponents.beta - exponents.alpha <= 4.0,
+                        pairs_exact=s["pairs_exact"], nodes_lumped=s["n_lumped"],
+                        seconds=time.perf_counter() - t0)

@@ -1,0 +1,162 @@
+/*
+ * librsgpu -- GB300 (sm_103a) implementation of the data-parallel core of the
+ * Repulsive-Surfaces flow (crate `ddg-repulsive-surfaces` of m1el/ddg-tools).
+ *
+ * A plain C ABI: opaque handles, plain pointers and sizes, int status codes. It is the
+ * boundary a host in any language binds (the reference's Rust crate would bind it with
+ * `extern "C"` declarations). Each entry point names the reference
+ * interface it replaces (paths relative to the reference project; RS/ =
+ * crates/ddg-repulsive-surfaces/).
+ *
+ * Conventions
+ *  - Positions are V x 3 doubles (x, y, z per vertex); faces are F x 3 uint32 vertex ids;
+ *    per-vertex vectors are interleaved `3 v + axis`, like the crate's `&[[f64; 3]]`.
+ *  - `*_host` pointers are caller-owned host memory; `*_dev` pointers are device memory of
+ *    the context's device (for example from cudaMalloc or a torch tensor).
+ *  - All work is issued on the context's own CUDA stream (rs_ctx_stream); entry points with
+ *    host outputs synchronise it before returning, `*_device` entry points do not.
+ *  - Every function returns RS_OK (0) or an error status; rs_last_error() describes the last
+ *    failure of the calling thread as the reference's `RsError::Gpu { operation, detail }`
+ *    (RS/src/gpu/cuda.rs:19-24) or the matching `RsError` kind.
+ *  - There is no CPU fallback: without a usable CUDA device every call fails with RS_GPU.
+ */
+#ifndef RSGPU_H
+#define RSGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. Each maps to one `RsError` variant of RS/src/error.rs. */
+enum rs_status {
+  RS_OK = 0,
+  RS_INVALID_EXPONENTS = 1,  /* RsError::InvalidExponents (RS/src/error.rs:110) */
+  RS_INVALID_OPTION = 2,     /* RsError::InvalidOption (:119) */
+  RS_POSITION_COUNT = 3,     /* RsError::PositionCountMismatch (:83) */
+  RS_NONFINITE_POSITION = 4, /* RsError::NonFinitePosition (:90) */
+  RS_DEGENERATE_FACE = 5,    /* RsError::DegenerateFace (:95) */
+  RS_NONFINITE_ENERGY = 6,   /* RsError::NonFiniteEnergy (:104) */
+  RS_TOPOLOGY = 7,           /* NoFaces / VertexOutOfRange / RepeatedVertex / DuplicateFace /
+                                NonManifoldEdge / NonManifoldVertex / UnreferencedVertex */
+  RS_SOLVER_DIVERGED = 8,    /* RsError::SolverDiverged (:174) */
+  RS_SINGULAR = 9,           /* RsError::SingularSaddle (:169) */
+  RS_GPU = 10,               /* RsError::Gpu (:218) */
+  RS_INTERNAL = 99
+};
+
+typedef struct rs_ctx rs_ctx; /* GpuContext (RS/src/gpu/mod.rs:36-127) */
+typedef struct rs_bh rs_bh;   /* BhTree + DeviceBh (RS/src/energy/barnes_hut.rs:114-127) */
+
+/* ---------------------------------------------------------------- errors and devices */
+
+/* The last failure of the calling thread: `operation` is a short word ("context",
+ * "upload", "launch", "product", "surface", "energy", ...), `detail` free text; `kind` is
+ * the RsError variant name ("Gpu", "DegenerateFace", ...). Strings stay valid until the
+ * thread's next failing call. Replaces RsError::Gpu { operation, detail } (cuda.rs:19-24). */
+const char *rs_last_error(void);
+const char *rs_last_error_operation(void);
+const char *rs_last_error_kind(void);
+
+/* Number of CUDA devices (gpu::device_count, RS/src/gpu/mod.rs:89-100). */
+int rs_device_count(int *count);
+
+/* A context on device `ordinal` with its own non-blocking stream
+ * (GpuContext::new, RS/src/gpu/mod.rs:102-127; cuda.rs:100-119). */
+int rs_ctx_create(int ordinal, rs_ctx **out);
+void rs_ctx_free(rs_ctx *ctx);
+/* The context's cudaStream_t, for callers that time or order work around it. */
+int rs_ctx_stream(rs_ctx *ctx, void **stream);
+int rs_ctx_synchronize(rs_ctx *ctx);
+/* Device name and SM count (gpu_info, crates/ddg-py/src/python/repulsive_surfaces.rs:687-691). */
+int rs_ctx_info(rs_ctx *ctx, char *name, int name_len, int *sm_count, int *cc_major,
+                int *cc_minor);
+/* Kernel launches issued by this context since creation (all entry points). */
+int rs_ctx_launch_count(rs_ctx *ctx, int64_t *count);
+
+/* Measured FP32 (non-tensor) FMA throughput of the context's device in TFLOP/s: the
+ * denominator of the pair kernel's roofline. No reference counterpart (a measurement aid). */
+int rs_fp32_peak(rs_ctx *ctx, double *tflops);
+
+/* ---------------------------------------------------------------- surface validation */
+
+/* Surface::new topology checks (RS/src/surface.rs:132-330) followed by
+ * Surface::validate_positions (surface.rs:513-541): no faces, vertex out of range, repeated
+ * vertex, duplicate face, non-manifold edge or vertex, unreferenced vertex, position count,
+ * non-finite position, degenerate face. Host-side, no device work. */
+int rs_surface_validate(int nv, int nf, const uint32_t *faces, const double *positions_host);
+
+/* The face BVH alone, built on the host exactly as rs_bh_build builds it (FaceTree::build,
+ * RS/src/spatial/mod.rs:175-221; split rule RC/src/spatial/bvh.rs:126-220). No device work.
+ * Arrays have room for `capacity` nodes (at most 2 nf - 1 are needed); box6 is lo xyz, hi xyz
+ * per node at the given positions; radius the farthest box corner from the node centroid. */
+int rs_face_tree_build(int nv, int nf, const uint32_t *faces, const double *positions_host,
+                       int leaf_size, int capacity, uint32_t *start, uint32_t *end,
+                       uint32_t *right, uint32_t *order, double *box6, double *radius,
+                       int *n_nodes);
+
+/* ---------------------------------------------------------------- Barnes-Hut energy */
+
+/* BhTree::build + attach_gpu (RS/src/energy/barnes_hut.rs:156-195, 265-307): validates
+ * the surface, builds the face BVH (leaf size `leaf_size`, split rule of
+ * RC/src/spatial/bvh.rs:126-220) at `positions_host`, uploads it, and builds the frozen
+ * interaction lists for the opening angle `theta` ON THE DEVICE (barnes_hut.rs:743-808). */
+int rs_bh_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces,
+                const double *positions_host, double theta, int leaf_size, rs_bh **out);
+
+/* BhTree::attach_gpu with the tree and lists built by the caller (the crate's own host
+ * build): node ranges/right children [n_nodes], the element order [nf], and the CSR
+ * lists per leaf (leaves in increasing node index; offsets have n_leaves+1 entries).
+ * `positions_host` sets the current positions (as rs_bh_refit). */
+int rs_bh_attach(rs_ctx *ctx, int nv, int nf, const uint32_t *faces,
+                 const double *positions_host, int n_nodes, const uint32_t *node_start,
+                 const uint32_t *node_end, const uint32_t *node_right, const uint32_t *order,
+                 const int64_t *lumped_off, const uint32_t *lumped, const int64_t *exact_off,
+                 const uint32_t *exact, rs_bh **out);
+void rs_bh_free(rs_bh *bh);
+
+/* BhTree::refit (barnes_hut.rs:204-229): new positions, same topology, boxes and lists. */
+int rs_bh_refit(rs_bh *bh, const double *positions_host);
+int rs_bh_refit_device(rs_bh *bh, const double *positions_dev);
+
+/* BhTree::try_energy (barnes_hut.rs:350-360): the energy on the frozen lists. */
+int rs_bh_energy(rs_bh *bh, double alpha, double beta, double *energy);
+
+/* BhTree::energy_and_differential (barnes_hut.rs:387-412): energy and dE/df_v, V x 3.
+ * NonFiniteEnergy names the culprit pair (faces[2]) when not finite. */
+int rs_bh_energy_and_differential(rs_bh *bh, double alpha, double beta, double *energy,
+                                  double *differential_host);
+
+/* Device-resident variant: energy (one double) and differential (V x 3 doubles) written to
+ * device memory on the context stream, without synchronising. */
+int rs_bh_energy_and_differential_device(rs_bh *bh, double alpha, double beta,
+                                         double *energy_dev, double *differential_dev);
+
+/* BhTree::try_face_partials (barnes_hut.rs:421-471): per-face (d_area, d_bary[3],
+ * d_normal[3]) by face index, F x 7. */
+int rs_bh_face_partials(rs_bh *bh, double alpha, double beta, double *energy,
+                        double *partials7_host);
+
+/* Counts of InteractionLists (barnes_hut.rs:94-107) and the tree:
+ * out[0..7] = n_nodes, n_leaves, n_lumped, n_exact, n_partner_slots, pairs_exact,
+ *             lumped_interactions (sum over lumped entries of the leaf's face count). */
+int rs_bh_sizes(rs_bh *bh, int64_t *out7);
+/* The tree and lists (for parity checks): arrays sized by rs_bh_sizes. */
+int rs_bh_export(rs_bh *bh, uint32_t *node_start, uint32_t *node_end, uint32_t *node_right,
+                 uint32_t *order, int64_t *lumped_off, uint32_t *lumped, int64_t *exact_off,
+                 uint32_t *exact);
+/* Culprit pair of the last non-finite evaluation (faces[2]), or -1,-1. */
+int rs_bh_culprit(rs_bh *bh, int64_t *faces2);
+
+/* Average device time (ms) of each kernel of the last `rs_bh_profile` run: runs the
+ * energy+differential `reps` times with CUDA events around every launch and returns up to
+ * `max_kernels` (name, ms) pairs; names are NUL-separated in `names` (size names_len). */
+int rs_bh_profile(rs_bh *bh, double alpha, double beta, int reps, char *names, int names_len,
+                  double *ms, int max_kernels, int *n_kernels);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -30,6 +30,15 @@ constexpr int kMaxDepth = 96;  // DFS stack bound of the list traversal (checked
 
 // ------------------------------------------------------------------ refit
 
+// The node centroid in FP64 and as a float pair (hi + lo) for the pair kernel.
+__device__ __forceinline__ void store_centroid(const BhDev &d, uint32_t n, double x, double y,
+                                               double z, double A) {
+  d.ncA[n] = make_double4(x, y, z, A);
+  float hx = (float)x, hy = (float)y, hz = (float)z;
+  d.nch[n] = make_float4(hx, hy, hz, (float)A);
+  d.ncl[n] = make_float4((float)(x - (double)hx), (float)(y - (double)hy), (float)(z - (double)hz), 0.f);
+}
+
 // L2-coherent load of a node record written by another thread of the same launch.
 __device__ __forceinline__ double4 ldcg4(const double4 *p) {
   const double2 *q = reinterpret_cast<const double2 *>(p);
@@ -89,7 +98,7 @@ __global__ void refit_kernel(BhDev d, const double *__restrict__ pos) {
     d.fnn[p] = make_float4(nr[i][0], nr[i][1], nr[i][2], 0.f);
   }
   d.nmom[leaf] = make_double4(M0, M1, M2, A);
-  d.ncA[leaf] = make_double4(cx, cy, cz, A);
+  store_centroid(d, leaf, cx, cy, cz, A);
   uint32_t n = leaf;
   while (n != 0) {
     uint32_t par = d.node_parent[n];
@@ -102,7 +111,7 @@ __global__ void refit_kernel(BhDev d, const double *__restrict__ pos) {
     double4 m = make_double4(__dadd_rn(l.x, r.x), __dadd_rn(l.y, r.y), __dadd_rn(l.z, r.z),
                              __dadd_rn(l.w, r.w));
     d.nmom[par] = m;
-    d.ncA[par] = make_double4(__ddiv_rn(m.x, m.w), __ddiv_rn(m.y, m.w), __ddiv_rn(m.z, m.w), m.w);
+    store_centroid(d, par, __ddiv_rn(m.x, m.w), __ddiv_rn(m.y, m.w), __ddiv_rn(m.z, m.w), m.w);
     n = par;
   }
 }
@@ -260,7 +269,7 @@ __global__ void __launch_bounds__(256) bh_pair_kernel(BhDev d, Pow pw) {
     const bool act = (uint32_t)s < ns;
     const float4 xs = act ? d.fxa[s0 + s] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 nS = act ? d.fnn[s0 + s] : make_float4(0.f, 0.f, 1.f, 0.f);
-    const double4 cL = d.ncA[leaf];
+    const float4 cLh = d.nch[leaf], cLl = d.ncl[leaf];
     const float a_s = xs.w;
     Kahan e_acc, da_acc, dx0, dx1, dx2, dn0, dn1, dn2;
 
@@ -277,11 +286,11 @@ __global__ void __launch_bounds__(256) bh_pair_kernel(BhDev d, Pow pw) {
         float v0 = 0.f, v1 = 0.f, v2 = 0.f, Ac = 0.f;
         if (q < lhi) {
           const uint32_t c = d.lumped[q];
-          const double4 cC = d.ncA[c];
-          v0 = (float)(cL.x - cC.x) + xs.x;
-          v1 = (float)(cL.y - cC.y) + xs.y;
-          v2 = (float)(cL.z - cC.z) + xs.z;
-          Ac = (float)cC.w;
+          const float4 ch = d.nch[c], cl = d.ncl[c];
+          v0 = ((cLh.x - ch.x) + (cLl.x - cl.x)) + xs.x;
+          v1 = ((cLh.y - ch.y) + (cLl.y - cl.y)) + xs.y;
+          v2 = ((cLh.z - ch.z) + (cLl.z - cl.z)) + xs.z;
+          Ac = ch.w;
         }
         if (ok) {
           float r2 = v0 * v0 + v1 * v1 + v2 * v2;
@@ -326,10 +335,10 @@ __global__ void __launch_bounds__(256) bh_pair_kernel(BhDev d, Pow pw) {
         c = d.exact[q];
         cs = d.node_start[c];
         nc = d.node_end[c] - cs;
-        const double4 cC = d.ncA[c];
-        d0 = (float)(cL.x - cC.x);
-        d1 = (float)(cL.y - cC.y);
-        d2 = (float)(cL.z - cC.z);
+        const float4 ch = d.nch[c], cl = d.ncl[c];
+        d0 = (cLh.x - ch.x) + (cLl.x - cl.x);
+        d1 = (cLh.y - ch.y) + (cLl.y - cl.y);
+        d2 = (cLh.z - ch.z) + (cLl.z - cl.z);
       }
       float P[32];
       float row = 0.f, rx0 = 0.f, rx1 = 0.f, rx2 = 0.f, rn0 = 0.f, rn1 = 0.f, rn2 = 0.f;
@@ -394,70 +403,113 @@ __global__ void __launch_bounds__(256) bh_pair_kernel(BhDev d, Pow pw) {
   }
 }
 
-// b_C, u_C per node over the transposed lumped lists, increasing entry (barnes_hut.rs:505-520).
+// b_C, u_C per node over the transposed lumped lists (barnes_hut.rs:505-520): one warp per
+// node, lanes strided over the entries (Kahan), then a fixed shuffle tree.
 __global__ void node_sums_kernel(BhDev d) {
-  int n = blockIdx.x * blockDim.x + threadIdx.x;
+  int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
   if (n >= d.n_nodes) return;
   Kahan b, u0, u1, u2;
-  for (uint32_t e = d.lumped_t_off[n]; e < d.lumped_t_off[n + 1]; ++e) {
+  for (uint32_t e = d.lumped_t_off[n] + lane; e < d.lumped_t_off[n + 1]; e += 32) {
     float4 t = d.node_term[d.lumped_t[e]];
     b.add(t.x), u0.add(t.y), u1.add(t.z), u2.add(t.w);
   }
-  d.node_sum[n] = make_float4(b.value(), u0.value(), u1.value(), u2.value());
+  float r0 = b.value(), r1 = u0.value(), r2 = u1.value(), r3 = u2.value();
+#pragma unroll
+  for (int m = 16; m >= 1; m >>= 1) {
+    r0 += __shfl_xor_sync(0xffffffffu, r0, m);
+    r1 += __shfl_xor_sync(0xffffffffu, r1, m);
+    r2 += __shfl_xor_sync(0xffffffffu, r2, m);
+    r3 += __shfl_xor_sync(0xffffffffu, r3, m);
+  }
+  if (lane == 0) d.node_sum[n] = make_float4(r0, r1, r2, r3);
 }
 
-// Downward pass per leaf along its root -> leaf chain (barnes_hut.rs:521-538):
-// beta_c = beta_p + U_p.(X_c - X_p) + b_c, U_c = U_p + u_c.
+// Downward pass per leaf along its root -> leaf chain (barnes_hut.rs:521-538), in FP64 (about
+// 20 steps per leaf): beta_c = beta_p + U_p.(X_c - X_p) + b_c, U_c = U_p + u_c.
 __global__ void downward_kernel(BhDev d) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= d.n_leaves) return;
   uint32_t c0 = d.chain_off[k], c1 = d.chain_off[k + 1];
   uint32_t p = d.chain[c0];
   float4 s = d.node_sum[p];
-  float beta = s.x, U0 = s.y, U1 = s.z, U2 = s.w;
+  double beta = s.x, U0 = s.y, U1 = s.z, U2 = s.w;
   double4 xp = d.ncA[p];
   for (uint32_t i = c0 + 1; i < c1; ++i) {
     uint32_t c = d.chain[i];
     double4 xc = d.ncA[c];
     float4 sc = d.node_sum[c];
-    float sh0 = (float)(xc.x - xp.x), sh1 = (float)(xc.y - xp.y), sh2 = (float)(xc.z - xp.z);
-    beta = beta + (U0 * sh0 + U1 * sh1 + U2 * sh2) + sc.x;
+    beta = beta + (U0 * (xc.x - xp.x) + U1 * (xc.y - xp.y) + U2 * (xc.z - xp.z)) + (double)sc.x;
     U0 += sc.y, U1 += sc.z, U2 += sc.w;
     xp = xc;
   }
-  d.leaf_bu[k] = make_float4(beta, U0, U1, U2);
+  d.leaf_bu[k] = make_float4((float)beta, (float)U0, (float)U1, (float)U2);
 }
 
-// Per face: own + partner (transposed exact lists) + cluster part (barnes_hut.rs:539-567),
-// written by face id.
+// Per leaf (one warp): own + partner (transposed exact lists) + cluster part
+// (barnes_hut.rs:539-567), written by face id. Lanes stride over the leaf's transposed exact
+// entries, each summing the leaf's (<= 8) partner slots of an entry into 8 x 4 registers; a
+// transposing reduce over the 32 lanes leaves lane 4 t + c with component c of face t.
 __global__ void final_kernel(BhDev d) {
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= d.n_faces) return;
-  uint32_t k = d.leaf_of_pos[p];
-  uint32_t leaf = d.leaves[k];
-  uint32_t t = p - d.node_start[leaf];
-  float4 o0 = d.own[2 * p], o1 = d.own[2 * p + 1];
-  Kahan a, x0, x1, x2;
-  a.add(o0.x), x0.add(o0.y), x1.add(o0.z), x2.add(o0.w);
-  for (uint32_t e = d.exact_t_off[k]; e < d.exact_t_off[k + 1]; ++e) {
-    float4 pp = d.partner[d.partner_off[d.exact_t[e]] + t];
-    a.add(pp.x), x0.add(pp.y), x1.add(pp.z), x2.add(pp.w);
+  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (k >= d.n_leaves) return;
+  const uint32_t leaf = d.leaves[k];
+  const uint32_t s0 = d.node_start[leaf];
+  const uint32_t ns = d.node_end[leaf] - s0;
+  float acc[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) acc[i] = 0.f;
+  for (uint32_t e = d.exact_t_off[k] + lane; e < d.exact_t_off[k + 1]; e += 32) {
+    const float4 *pp = d.partner + d.partner_off[d.exact_t[e]];
+#pragma unroll
+    for (int t = 0; t < 8; ++t)
+      if ((uint32_t)t < ns) {
+        float4 v = pp[t];
+        acc[4 * t] += v.x, acc[4 * t + 1] += v.y, acc[4 * t + 2] += v.z, acc[4 * t + 3] += v.w;
+      }
   }
-  float4 bu = d.leaf_bu[k];
-  float4 xa = d.fxa[p];  // offset X_T - X_leaf and a_T
-  a.add(bu.x + (bu.y * xa.x + bu.z * xa.y + bu.w * xa.z));
-  x0.add(xa.w * bu.y), x1.add(xa.w * bu.z), x2.add(xa.w * bu.w);
-  uint32_t f = d.order[p];
-  d.partials[2 * f] = make_float4(a.value(), x0.value(), x1.value(), x2.value());
-  d.partials[2 * f + 1] = o1;
+  // 32 -> 16 -> 8 -> 4 -> 2 -> 1 values per lane; lane L ends with the sum of acc[L]
+  float r16[16], r8[8], r4[4], r2[2];
+  const bool b4 = (lane >> 4) & 1, b3 = (lane >> 3) & 1, b2 = (lane >> 2) & 1, b1 = (lane >> 1) & 1,
+             b0 = lane & 1;
+#pragma unroll
+  for (int i = 0; i < 16; ++i)
+    r16[i] = (b4 ? acc[16 + i] : acc[i]) + __shfl_xor_sync(0xffffffffu, b4 ? acc[i] : acc[16 + i], 16);
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+    r8[i] = (b3 ? r16[8 + i] : r16[i]) + __shfl_xor_sync(0xffffffffu, b3 ? r16[i] : r16[8 + i], 8);
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    r4[i] = (b2 ? r8[4 + i] : r8[i]) + __shfl_xor_sync(0xffffffffu, b2 ? r8[i] : r8[4 + i], 4);
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+    r2[i] = (b1 ? r4[2 + i] : r4[i]) + __shfl_xor_sync(0xffffffffu, b1 ? r4[i] : r4[2 + i], 2);
+  float part = (b0 ? r2[1] : r2[0]) + __shfl_xor_sync(0xffffffffu, b0 ? r2[0] : r2[1], 1);
+  const uint32_t t = lane >> 2, c = lane & 3;
+  if (t < ns) {
+    const uint32_t p = s0 + t;
+    const float own = reinterpret_cast<const float *>(d.own)[8 * (size_t)p + c];
+    const float4 bu = d.leaf_bu[k];
+    const float4 xa = d.fxa[p];  // offset X_T - X_leaf and a_T
+    float cl;
+    if (c == 0) cl = bu.x + (bu.y * xa.x + bu.z * xa.y + bu.w * xa.z);
+    else cl = xa.w * (c == 1 ? bu.y : (c == 2 ? bu.z : bu.w));
+    const uint32_t f = d.order[p];
+    float *out = reinterpret_cast<float *>(d.partials);
+    out[8 * (size_t)f + c] = (own + part) + cl;
+    if (c == 0) d.partials[2 * f + 1] = d.own[2 * p + 1];
+  }
 }
 
 // Pull-back to the vertices (face_pull_back, RS/src/geometry.rs:87-110, summed over the
-// incident faces in increasing face order, geometry.rs:172-188).
+// incident faces in increasing face order, geometry.rs:172-188), in FP64: the face terms
+// around a vertex cancel to a small differential, so this O(F) step keeps FP64.
 __global__ void pull_back_kernel(BhDev d, const double *__restrict__ pos, double *__restrict__ dE) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= d.n_vertices) return;
-  float g0 = 0.f, g1 = 0.f, g2 = 0.f;
+  double g0 = 0.0, g1 = 0.0, g2 = 0.0;
+  const float *pa_ = reinterpret_cast<const float *>(d.partials);
   for (uint32_t e = d.inc_off[v]; e < d.inc_off[v + 1]; ++e) {
     uint32_t fc = d.inc[e];
     uint32_t f = fc >> 2, c = fc & 3;
@@ -465,25 +517,24 @@ __global__ void pull_back_kernel(BhDev d, const double *__restrict__ pos, double
     const double *p0 = pos + 3 * (size_t)t[0];
     const double *p1 = pos + 3 * (size_t)t[1];
     const double *p2 = pos + 3 * (size_t)t[2];
-    float u0 = (float)(p1[0] - p0[0]), u1 = (float)(p1[1] - p0[1]), u2 = (float)(p1[2] - p0[2]);
-    float w0 = (float)(p2[0] - p0[0]), w1 = (float)(p2[1] - p0[1]), w2 = (float)(p2[2] - p0[2]);
-    float n0 = u1 * w2 - u2 * w1, n1 = u2 * w0 - u0 * w2, n2 = u0 * w1 - u1 * w0;
-    float len = sqrtf(n0 * n0 + n1 * n1 + n2 * n2);
-    float il = 1.f / len;
+    double u0 = p1[0] - p0[0], u1 = p1[1] - p0[1], u2 = p1[2] - p0[2];
+    double w0 = p2[0] - p0[0], w1 = p2[1] - p0[1], w2 = p2[2] - p0[2];
+    double n0 = u1 * w2 - u2 * w1, n1 = u2 * w0 - u0 * w2, n2 = u0 * w1 - u1 * w0;
+    double len = sqrt(n0 * n0 + n1 * n1 + n2 * n2);
+    double il = 1.0 / len;
     n0 *= il, n1 *= il, n2 *= il;
     // edge opposite corner c: e_jk = p2 - p1, e_ki = p0 - p2, e_ij = p1 - p0
     const double *pa = c == 0 ? p1 : (c == 1 ? p2 : p0);
     const double *pb = c == 0 ? p2 : (c == 1 ? p0 : p1);
-    float e0 = (float)(pb[0] - pa[0]), e1 = (float)(pb[1] - pa[1]), e2 = (float)(pb[2] - pa[2]);
-    float4 q0 = d.partials[2 * f], q1 = d.partials[2 * f + 1];
-    float ha = 0.5f * q0.x;
-    // N x e, e x N
-    float c0 = n1 * e2 - n2 * e1, c1 = n2 * e0 - n0 * e2, c2 = n0 * e1 - n1 * e0;
-    float dotn = -(c0 * q1.x + c1 * q1.y + c2 * q1.z) * il;
-    const float third = 1.f / 3.f;
-    g0 += ha * c0 + q0.y * third + n0 * dotn;
-    g1 += ha * c1 + q0.z * third + n1 * dotn;
-    g2 += ha * c2 + q0.w * third + n2 * dotn;
+    double e0 = pb[0] - pa[0], e1 = pb[1] - pa[1], e2 = pb[2] - pa[2];
+    const float *q = pa_ + 8 * (size_t)f;
+    double ha = 0.5 * (double)q[0];
+    double c0 = n1 * e2 - n2 * e1, c1 = n2 * e0 - n0 * e2, c2 = n0 * e1 - n1 * e0;  // N x e
+    double dotn = -(c0 * (double)q[4] + c1 * (double)q[5] + c2 * (double)q[6]) * il;
+    const double third = 1.0 / 3.0;
+    g0 += ha * c0 + (double)q[1] * third + n0 * dotn;
+    g1 += ha * c1 + (double)q[2] * third + n1 * dotn;
+    g2 += ha * c2 + (double)q[3] * third + n2 * dotn;
   }
   dE[3 * v] = g0, dE[3 * v + 1] = g1, dE[3 * v + 2] = g2;
 }
@@ -558,6 +609,7 @@ struct rs_bh {
   DevBuf<double> pos;
   DevBuf<float4> fxa, fnn, own, node_term, partner, node_sum, leaf_bu, partials;
   DevBuf<double4> ncA, nmom;
+  DevBuf<float4> nch, ncl;
   DevBuf<uint32_t> refit_count;
   DevBuf<double> leaf_energy, energy, dE;
   DevBuf<unsigned int> ticket;
@@ -577,6 +629,7 @@ struct rs_bh {
     d.n_vertices = nv, d.n_faces = nf, d.n_nodes = (int)tree.n_nodes();
     d.n_leaves = (int)tree.leaves.size();
     d.fxa = fxa.p, d.fnn = fnn.p, d.ncA = ncA.p, d.nmom = nmom.p, d.refit_count = refit_count.p;
+    d.nch = nch.p, d.ncl = ncl.p;
     d.own = own.p, d.node_term = node_term.p, d.partner = partner.p, d.node_sum = node_sum.p;
     d.leaf_bu = leaf_bu.p, d.partials = partials.p, d.leaf_energy = leaf_energy.p;
     d.ticket = ticket.p;
@@ -681,6 +734,8 @@ void upload_topology(rs_bh *h) {
   h->partials.alloc(2 * (size_t)h->nf);
   h->ncA.alloc(nn);
   h->nmom.alloc(nn);
+  h->nch.alloc(nn);
+  h->ncl.alloc(nn);
   h->node_sum.alloc(nn);
   h->refit_count.alloc(nn);
   RSG_CUDA("upload", cudaMemsetAsync(h->refit_count.p, 0, nn * sizeof(uint32_t), s));
@@ -856,7 +911,7 @@ void evaluate(rs_bh *h, const Pow &pw, bool fast, bool grad, double *energy_dev,
   P.end(s);
   if (grad) {
     P.begin(s, "node_sums");
-    node_sums_kernel<<<blocks(nn, 256), 256, 0, s>>>(d);
+    node_sums_kernel<<<blocks(nn * 32, 256), 256, 0, s>>>(d);
     RSG_LAUNCHED(h->ctx, "node_sums");
     P.end(s);
     P.begin(s, "downward");
@@ -864,7 +919,7 @@ void evaluate(rs_bh *h, const Pow &pw, bool fast, bool grad, double *energy_dev,
     RSG_LAUNCHED(h->ctx, "downward");
     P.end(s);
     P.begin(s, "final");
-    final_kernel<<<blocks(h->nf, 256), 256, 0, s>>>(d);
+    final_kernel<<<blocks(nl * 32, 256), 256, 0, s>>>(d);
     RSG_LAUNCHED(h->ctx, "final");
     P.end(s);
     if (dE_dev) {
@@ -1003,8 +1058,10 @@ int rs_bh_attach(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const doubl
     h->n_partner = p;
     upload_vec(h->lumped_off, lo, s);
     upload_vec(h->exact_off, eo, s);
-    h->lumped.upload(lumped, std::max<size_t>(h->n_lumped, 1), s);
-    h->exact.upload(exact, std::max<size_t>(h->n_exact, 1), s);
+    h->lumped.alloc(std::max<size_t>(h->n_lumped, 1));
+    if (h->n_lumped) h->lumped.upload(lumped, h->n_lumped, s);
+    h->exact.alloc(std::max<size_t>(h->n_exact, 1));
+    if (h->n_exact) h->exact.upload(exact, h->n_exact, s);
     upload_vec(h->partner_off, poff, s);
     finish_lists(h.get(), work);
     h->pos.upload(positions_host, 3 * (size_t)nv, s);

@@ -6,9 +6,11 @@
 //   fxa[p] : float4 (X_S - X_leaf (xyz, FP32 offset from the leaf centroid), a_S)
 //   fnn[p] : float4 (N_S (xyz), 0)
 //   ncA[n] : double4 (X_n (xyz), A_n) cluster centroid and area of every node, FP64
-// Leaf centroids are FP64; a pair's separation is (X_L - X_C) in FP64, rounded once per block,
-// plus the difference of the two FP32 offsets. This keeps v = X_S - X_T at FP32 precision
-// relative to |v| (not to |X|), which the near-field terms (r^-12 nu^6) need.
+//   nch[n], ncl[n] : the same centroid as a float pair (hi + lo) and the area in FP32
+// A pair's separation is (X_L - X_C) formed from the float pairs ((hi_L - hi_C) + (lo_L - lo_C),
+// exact to FP32 rounding of the result), plus the difference of the two FP32 offsets. This
+// keeps v = X_S - X_T at FP32 precision relative to |v| (not to |X|), which the near-field
+// terms (r^-12 nu^6) need, without FP64 work in the pair kernel.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -37,6 +39,8 @@ struct BhDev {
   // per-evaluation state
   float4 *fxa, *fnn;
   double4 *ncA;     // node centroid (xyz) and area (w)
+  float4 *nch;      // node centroid as a float pair: hi (xyz) and area (w) ...
+  float4 *ncl;      // ... and lo (xyz): X = hi + lo to ~48 bits, no FP64 in the pair kernel
   double4 *nmom;    // node first moment (xyz) and area (w), for the bottom-up refit
   uint32_t *refit_count;
   // outputs and scratch

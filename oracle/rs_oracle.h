@@ -98,6 +98,33 @@ int rso_bh_energy_and_differential(const rso_bh *h, double alpha, double beta,
 int rso_pull_back(int nv, const double *pos, int nf, const uint32_t *faces,
                   const double *face_partials7, double *dE);
 
+/* ---- hierarchical metric (RS/src/metric/hierarchical.rs, RS/src/spatial/block_tree.rs) ---- */
+typedef struct rso_metric rso_metric;
+/* FaceMetricTree::build (hierarchical.rs:302-363): face tree (leaf_size), block cluster tree
+ * of h_hi = rho^-2s and h_lo = (nu_S^2 + nu_T^2)/2 rho^-4 rho^-2s (chi, leaf_pairs), H~ a. */
+int rso_metric_build(int nv, const double *pos, int nf, const uint32_t *faces, double alpha,
+                     double beta, double chi, int leaf_size, int leaf_pairs, rso_metric **out);
+void rso_metric_free(rso_metric *h);
+const char *rso_metric_last_error(void);
+/* far blocks, near blocks, near entries, depth, nodes */
+int rso_metric_stats(const rso_metric *h, int64_t *out5);
+int rso_metric_blocks(const rso_metric *h, int64_t *far_ptr, uint32_t *far_col, double *far_coef,
+                      int64_t *near_ptr, uint32_t *near_col);
+int rso_metric_ha(const rso_metric *h, double *ha2);
+/* y = (w_hi B~ + w_lo B~0) x for nb interleaved 3V vectors (hierarchical.rs:521-812). */
+int rso_metric_apply(const rso_metric *h, double w_hi, double w_lo, int nb, const double *xs,
+                     double *ys);
+
+typedef struct rso_vfrac rso_vfrac;
+/* VertexFractionalTree::build (hierarchical.rs:1017-1084): vertex BVH with dual-area masses,
+ * kernel |f_v - f_w|^-(2 tau + 2). */
+int rso_vfrac_build(int nv, const double *pos, const double *mass, double tau, double chi,
+                    int leaf_size, int leaf_pairs, rso_vfrac **out);
+void rso_vfrac_free(rso_vfrac *h);
+int rso_vfrac_stats(const rso_vfrac *h, int64_t *out5);
+/* y = L^V_tau x = 2 (a . H~a . x - a . H~(a . x)) per axis (hierarchical.rs:1313-1345). */
+int rso_vfrac_apply(const rso_vfrac *h, int nb, const double *xs, double *ys);
+
 #ifdef __cplusplus
 }
 #endif

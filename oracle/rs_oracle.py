@@ -191,3 +191,105 @@ class BhTree:
         p7 = np.empty((self.nf, 7)) if partials else None
         _check(lib().rso_bh_energy_and_differential(self._h, alpha, beta, C.byref(e), _ptr(dE), _ptr(p7)))
         return (e.value, dE, p7) if partials else (e.value, dE)
+
+
+def _metric_lib():
+    L = lib()
+    if not getattr(L, "_metric_ready", False):
+        L.rso_metric_build.argtypes = [C.c_int, _f64p, C.c_int, _u32p, C.c_double, C.c_double,
+                                       C.c_double, C.c_int, C.c_int, C.POINTER(C.c_void_p)]
+        L.rso_metric_free.argtypes = [C.c_void_p]
+        L.rso_metric_last_error.restype = C.c_char_p
+        L.rso_metric_stats.argtypes = [C.c_void_p, _i64p]
+        L.rso_metric_blocks.argtypes = [C.c_void_p, _i64p, _u32p, _f64p, _i64p, _u32p]
+        L.rso_metric_ha.argtypes = [C.c_void_p, _f64p]
+        L.rso_metric_apply.argtypes = [C.c_void_p, C.c_double, C.c_double, C.c_int, _f64p, _f64p]
+        L.rso_vfrac_build.argtypes = [C.c_int, _f64p, _f64p, C.c_double, C.c_double, C.c_int, C.c_int,
+                                      C.POINTER(C.c_void_p)]
+        L.rso_vfrac_free.argtypes = [C.c_void_p]
+        L.rso_vfrac_stats.argtypes = [C.c_void_p, _i64p]
+        L.rso_vfrac_apply.argtypes = [C.c_void_p, C.c_int, _f64p, _f64p]
+        L._metric_ready = True
+    return L
+
+
+def _mcheck(code: int) -> None:
+    if code != 0:
+        raise OracleError(code, _metric_lib().rso_metric_last_error().decode())
+
+
+class FaceMetricTree:
+    """The oracle's hierarchical B~ + B~0 (FaceMetricTree, RS/src/metric/hierarchical.rs)."""
+
+    def __init__(self, pos, faces, alpha=6.0, beta=12.0, chi=0.5, leaf_size=8, leaf_pairs=64):
+        pos, faces = _mesh(pos, faces)
+        self.nv, self.nf = len(pos), len(faces)
+        h = C.c_void_p()
+        _mcheck(_metric_lib().rso_metric_build(self.nv, pos.ravel(), self.nf, faces.ravel(), alpha, beta,
+                                               chi, leaf_size, leaf_pairs, C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.rso_metric_free(self._h)
+            self._h = None
+
+    def stats(self) -> dict:
+        o = np.zeros(5, np.int64)
+        _mcheck(_metric_lib().rso_metric_stats(self._h, o))
+        return dict(zip(["far_blocks", "near_blocks", "near_entries", "depth", "nodes"], map(int, o)))
+
+    def blocks(self) -> dict:
+        s = self.stats()
+        nn = s["nodes"]
+        fp, np_ = np.empty(nn + 1, np.int64), np.empty(nn + 1, np.int64)
+        fc = np.empty(max(s["far_blocks"], 1), np.uint32)
+        coef = np.empty(2 * max(s["far_blocks"], 1))
+        nc = np.empty(max(s["near_blocks"], 1), np.uint32)
+        _mcheck(_metric_lib().rso_metric_blocks(self._h, fp, fc, coef, np_, nc))
+        return dict(far_ptr=fp, far_col=fc[: s["far_blocks"]],
+                    far_coef=coef[: 2 * s["far_blocks"]].reshape(-1, 2), near_ptr=np_,
+                    near_col=nc[: s["near_blocks"]])
+
+    def ha(self):
+        out = np.empty((self.nf, 2))
+        _mcheck(_metric_lib().rso_metric_ha(self._h, out.ravel()))
+        return out
+
+    def apply(self, x, w_hi=1.0, w_lo=1.0):
+        """y = (w_hi B~ + w_lo B~0) x for x of shape (3V,) or (nb, 3V)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        xs = x.reshape(-1, 3 * self.nv)
+        ys = np.empty_like(xs)
+        _mcheck(_metric_lib().rso_metric_apply(self._h, w_hi, w_lo, len(xs), xs.ravel(), ys.ravel()))
+        return ys.reshape(x.shape)
+
+
+class VertexFractionalTree:
+    """The oracle's vertex-pair L^V_tau (VertexFractionalTree, RS/src/metric/hierarchical.rs)."""
+
+    def __init__(self, pos, mass, tau, chi=0.5, leaf_size=8, leaf_pairs=64):
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+        mass = np.ascontiguousarray(mass, dtype=np.float64)
+        self.nv = len(pos)
+        h = C.c_void_p()
+        _mcheck(_metric_lib().rso_vfrac_build(self.nv, pos.ravel(), mass, tau, chi, leaf_size, leaf_pairs,
+                                              C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.rso_vfrac_free(self._h)
+            self._h = None
+
+    def stats(self) -> dict:
+        o = np.zeros(5, np.int64)
+        _mcheck(_metric_lib().rso_vfrac_stats(self._h, o))
+        return dict(zip(["far_blocks", "near_blocks", "near_entries", "depth", "nodes"], map(int, o)))
+
+    def apply(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        xs = x.reshape(-1, 3 * self.nv)
+        ys = np.empty_like(xs)
+        _mcheck(_metric_lib().rso_vfrac_apply(self._h, len(xs), xs.ravel(), ys.ravel()))
+        return ys.reshape(x.shape)

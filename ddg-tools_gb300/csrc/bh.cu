@@ -57,8 +57,7 @@ __global__ void refit_kernel(BhDev d, const double *__restrict__ pos) {
   uint32_t leaf = d.leaves[k];
   uint32_t s0 = d.node_start[leaf], s1 = d.node_end[leaf];
   double A = 0.0, M0 = 0.0, M1 = 0.0, M2 = 0.0;
-  double xb[8][3], ar[8];
-  float nr[8][3];
+  double xb[8][3], ar[8], nr[8][3];
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     uint32_t p = s0 + i;
@@ -79,9 +78,9 @@ __global__ void refit_kernel(BhDev d, const double *__restrict__ pos) {
     double x2 = __dmul_rn(__dadd_rn(__dadd_rn(p0[2], p1[2]), p2[2]), third);
     double a = __dmul_rn(0.5, len);
     double il = __drcp_rn(len);
-    nr[i][0] = (float)__dmul_rn(c0, il);
-    nr[i][1] = (float)__dmul_rn(c1, il);
-    nr[i][2] = (float)__dmul_rn(c2, il);
+    nr[i][0] = __dmul_rn(c0, il);
+    nr[i][1] = __dmul_rn(c1, il);
+    nr[i][2] = __dmul_rn(c2, il);
     xb[i][0] = x0, xb[i][1] = x1, xb[i][2] = x2, ar[i] = a;
     A = __dadd_rn(A, a);
     M0 = __dadd_rn(M0, __dmul_rn(a, x0));
@@ -93,9 +92,15 @@ __global__ void refit_kernel(BhDev d, const double *__restrict__ pos) {
   for (int i = 0; i < 8; ++i) {
     uint32_t p = s0 + i;
     if (p >= s1) break;
-    d.fxa[p] = make_float4((float)(xb[i][0] - cx), (float)(xb[i][1] - cy), (float)(xb[i][2] - cz),
-                           (float)ar[i]);
-    d.fnn[p] = make_float4(nr[i][0], nr[i][1], nr[i][2], 0.f);
+    double o0 = xb[i][0] - cx, o1 = xb[i][1] - cy, o2 = xb[i][2] - cz;
+    float h0 = (float)o0, h1 = (float)o1, h2 = (float)o2;
+    d.fxa[p] = make_float4(h0, h1, h2, (float)ar[i]);
+    d.fol[p] = make_float4((float)(o0 - (double)h0), (float)(o1 - (double)h1), (float)(o2 - (double)h2), 0.f);
+    float n0 = (float)nr[i][0], n1 = (float)nr[i][1], n2 = (float)nr[i][2];
+    d.fnn[p] = make_float4(n0, n1, n2, 0.f);
+    double alpha = nr[i][0] * o0 + nr[i][1] * o1 + nr[i][2] * o2;
+    d.fnl[p] = make_float4((float)(nr[i][0] - (double)n0), (float)(nr[i][1] - (double)n1),
+                           (float)(nr[i][2] - (double)n2), (float)alpha);
   }
   d.nmom[leaf] = make_double4(M0, M1, M2, A);
   store_centroid(d, leaf, cx, cy, cz, A);
@@ -246,14 +251,47 @@ __device__ __forceinline__ float4 group_transpose_reduce(float (&P)[32], int s) 
   return make_float4(T[0], T[1], T[2], T[3]);
 }
 
-// One warp per target leaf (leaf size <= 8). Lane = s + 8 j: s is the target face of the
-// leaf, j one of four entry groups. Lumped entries are taken in batches of 8 per group (the
-// node terms b = sum_S a_S K, u = -sum_S a_S dK/dv reduced over s by one transposing reduce),
-// exact entries one leaf block per group (the partner terms reduced the same way). Own
-// partials and the energy go through Kahan accumulators (leaf_with_gradient,
-// barnes_hut.rs:627-689; value only: leaf_energy, barnes_hut.rs:583-614).
+// Error-free product and sum (Dekker/Knuth with FMA): a*b = p + e, a+b = s + t exactly.
+__device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
+  p = a * b;
+  e = fmaf(a, b, -p);
+}
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &t) {
+  s = a + b;
+  float bv = s - a;
+  t = (a - (s - bv)) + (b - bv);
+}
+
+// N . o for a unit normal and an offset both held as float pairs (hi + lo), compensated
+// (the Dot2 scheme of Ogita, Rump and Oishi, 2005): the sum of the three products carries its
+// rounding errors, which matters because it nearly cancels for a smooth surface.
+__device__ __forceinline__ float dot2(float nx, float ny, float nz, float lx, float ly, float lz,
+                                      float ox, float oy, float oz, float px, float py, float pz) {
+  float p0, e0, p1, e1, p2, e2, s, t0, u, t1;
+  two_prod(nx, ox, p0, e0);
+  two_prod(ny, oy, p1, e1);
+  two_prod(nz, oz, p2, e2);
+  two_sum(p0, p1, s, t0);
+  two_sum(s, p2, u, t1);
+  float lo = ((e0 + e1) + (e2 + t0)) + t1;
+  lo += (nx * px + ny * py + nz * pz) + (lx * ox + ly * oy + lz * oz);
+  return u + lo;
+}
+
+// The pair kernel. One warp per work item: a slice of one target leaf's lumped and exact
+// lists (leaf size <= 8; long lists are split so that no warp carries a whole-mesh leaf).
+// Lane = s + 8 j: s is the target face of the leaf, j one of four entry groups. Lumped entries
+// are taken in batches of 8 per group (the node terms b = sum_S a_S K, u = -sum_S a_S dK/dv
+// reduced over s by one transposing reduce), exact entries one leaf block per group (the
+// partner terms reduced the same way). Own partials and the energy go through Kahan
+// accumulators and are written per work item (leaf_with_gradient, barnes_hut.rs:627-689; value
+// only: leaf_energy, barnes_hut.rs:583-614).
+//
+// For exact (near) pairs nu = N_S . (X_S - X_T) is formed as alpha_S + N_S.(X_L - X_C) -
+// N_S.(X_T - X_C) with float-pair normals and offsets and compensated dot products: on a
+// smooth surface nu is ~|v|^2 kappa, far below |v|, and plain FP32 loses it.
 template <bool GRAD, bool FAST>
-__global__ void __launch_bounds__(256) bh_pair_kernel(BhDev d, Pow pw) {
+__global__ void __launch_bounds__(128) bh_pair_kernel(BhDev d, Pow pw) {
   const int lane = threadIdx.x & 31;
   const int s = lane & 7;
   const int j = lane >> 3;
@@ -261,20 +299,23 @@ __global__ void __launch_bounds__(256) bh_pair_kernel(BhDev d, Pow pw) {
     unsigned int w = 0;
     if (lane == 0) w = atomicAdd(d.ticket, 1u);
     w = __shfl_sync(0xffffffffu, w, 0);
-    if (w >= (unsigned)d.n_leaves) return;
-    const uint32_t k = d.schedule[w];
+    if (w >= (unsigned)d.n_items) return;
+    const uint32_t item = d.schedule[w];
+    const uint4 it = d.items[item];  // (leaf ordinal, lumped begin, exact begin, packed ends)
+    const uint32_t k = d.item_leaf[item];
     const uint32_t leaf = d.leaves[k];
     const uint32_t s0 = d.node_start[leaf];
     const uint32_t ns = d.node_end[leaf] - s0;
     const bool act = (uint32_t)s < ns;
     const float4 xs = act ? d.fxa[s0 + s] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 nS = act ? d.fnn[s0 + s] : make_float4(0.f, 0.f, 1.f, 0.f);
+    const float4 nL = act ? d.fnl[s0 + s] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 cLh = d.nch[leaf], cLl = d.ncl[leaf];
     const float a_s = xs.w;
     Kahan e_acc, da_acc, dx0, dx1, dx2, dn0, dn1, dn2;
 
     // ---- lumped nodes, 8 per group per batch
-    const uint32_t llo = d.lumped_off[k], lhi = d.lumped_off[k + 1];
+    const uint32_t llo = it.x, lhi = it.y;
     for (uint32_t base = llo; base < lhi; base += 32) {
       float P[32];
       float bda = 0.f, be = 0.f, bx0 = 0.f, bx1 = 0.f, bx2 = 0.f, bn0 = 0.f, bn1 = 0.f, bn2 = 0.f;
@@ -294,14 +335,13 @@ __global__ void __launch_bounds__(256) bh_pair_kernel(BhDev d, Pow pw) {
         }
         if (ok) {
           float r2 = v0 * v0 + v1 * v1 + v2 * v2;
-          float ir2 = 1.f / r2;
+          float ir2 = __fdividef(1.f, r2);
           float nu = nS.x * v0 + nS.y * v1 + nS.z * v2;
           kernel_k<FAST>(pw, nu, r2, ir2, K, cn);
           g = pw.beta * K * ir2;
         }
         be += a_s * K * Ac;
         if (GRAD) {
-          // dK/dv = c_n N - beta K v / r2 ; dK/dN = c_n v
           float dv0 = cn * nS.x - g * v0, dv1 = cn * nS.y - g * v1, dv2 = cn * nS.z - g * v2;
           bda += K * Ac;
           float aa = a_s * Ac;
@@ -325,20 +365,26 @@ __global__ void __launch_bounds__(256) bh_pair_kernel(BhDev d, Pow pw) {
     }
 
     // ---- exact leaves, one block per group
-    const uint32_t elo = d.exact_off[k], ehi = d.exact_off[k + 1];
+    const uint32_t elo = it.z, ehi = it.w;
     for (uint32_t base = elo; base < ehi; base += 4) {
       const uint32_t q = base + j;
       const bool qok = q < ehi;
       uint32_t c = 0, cs = 0, nc = 0;
-      float d0 = 0.f, d1 = 0.f, d2 = 0.f;
+      float d0 = 0.f, d1 = 0.f, d2 = 0.f, ab = 0.f;
       if (qok) {
         c = d.exact[q];
         cs = d.node_start[c];
         nc = d.node_end[c] - cs;
         const float4 ch = d.nch[c], cl = d.ncl[c];
-        d0 = (cLh.x - ch.x) + (cLl.x - cl.x);
-        d1 = (cLh.y - ch.y) + (cLl.y - cl.y);
-        d2 = (cLh.z - ch.z) + (cLl.z - cl.z);
+        // d = X_L - X_C as a float pair (hi + lo) from the centroids' float pairs
+        float h0, t0, h1, t1, h2, t2;
+        two_sum(cLh.x, -ch.x, h0, t0);
+        two_sum(cLh.y, -ch.y, h1, t1);
+        two_sum(cLh.z, -ch.z, h2, t2);
+        const float l0 = t0 + (cLl.x - cl.x), l1 = t1 + (cLl.y - cl.y), l2 = t2 + (cLl.z - cl.z);
+        d0 = h0 + l0, d1 = h1 + l1, d2 = h2 + l2;
+        // alpha_S + N_S . (X_L - X_C)
+        ab = nL.w + dot2(nS.x, nS.y, nS.z, nL.x, nL.y, nL.z, h0, h1, h2, l0, l1, l2);
       }
       float P[32];
       float row = 0.f, rx0 = 0.f, rx1 = 0.f, rx2 = 0.f, rn0 = 0.f, rn1 = 0.f, rn2 = 0.f;
@@ -350,12 +396,13 @@ __global__ void __launch_bounds__(256) bh_pair_kernel(BhDev d, Pow pw) {
           a_t = xt.w;
           const bool self = (c == leaf) && (t == s);
           if (act && !self) {
+            const float4 xl = d.fol[cs + t];  // offset lo part of T
             v0 = (xs.x - xt.x) + d0;
             v1 = (xs.y - xt.y) + d1;
             v2 = (xs.z - xt.z) + d2;
             float r2 = v0 * v0 + v1 * v1 + v2 * v2;
-            float ir2 = 1.f / r2;
-            float nu = nS.x * v0 + nS.y * v1 + nS.z * v2;
+            float ir2 = __fdividef(1.f, r2);
+            float nu = ab - dot2(nS.x, nS.y, nS.z, nL.x, nL.y, nL.z, xt.x, xt.y, xt.z, xl.x, xl.y, xl.z);
             kernel_k<FAST>(pw, nu, r2, ir2, K, cn);
             g = pw.beta * K * ir2;
           }
@@ -382,7 +429,7 @@ __global__ void __launch_bounds__(256) bh_pair_kernel(BhDev d, Pow pw) {
       }
     }
 
-    // ---- reduce over the four groups; lanes 0..7 write their face's own partials
+    // ---- reduce over the four groups; lanes 0..7 write the item's own partials
     if (GRAD) {
       float o[7] = {da_acc.value(), dx0.value(), dx1.value(), dx2.value(),
                     dn0.value(),    dn1.value(), dn2.value()};
@@ -391,15 +438,15 @@ __global__ void __launch_bounds__(256) bh_pair_kernel(BhDev d, Pow pw) {
         o[i] += __shfl_xor_sync(0xffffffffu, o[i], 8);
         o[i] += __shfl_xor_sync(0xffffffffu, o[i], 16);
       }
-      if (j == 0 && act) {
-        d.own[2 * (s0 + s)] = make_float4(o[0], o[1], o[2], o[3]);
-        d.own[2 * (s0 + s) + 1] = make_float4(o[4], o[5], o[6], 0.f);
+      if (j == 0) {
+        d.own[16 * (size_t)item + 2 * s] = make_float4(o[0], o[1], o[2], o[3]);
+        d.own[16 * (size_t)item + 2 * s + 1] = make_float4(o[4], o[5], o[6], 0.f);
       }
     }
     double e = (double)e_acc.s - (double)e_acc.c;
 #pragma unroll
     for (int m = 16; m >= 1; m >>= 1) e += __shfl_xor_sync(0xffffffffu, e, m);
-    if (lane == 0) d.leaf_energy[k] = e;
+    if (lane == 0) d.item_energy[item] = e;
   }
 }
 
@@ -489,7 +536,12 @@ __global__ void final_kernel(BhDev d) {
   const uint32_t t = lane >> 2, c = lane & 3;
   if (t < ns) {
     const uint32_t p = s0 + t;
-    const float own = reinterpret_cast<const float *>(d.own)[8 * (size_t)p + c];
+    const float *ow = reinterpret_cast<const float *>(d.own);
+    float own = 0.f, ownn = 0.f;
+    for (uint32_t i = d.item_off[k]; i < d.item_off[k + 1]; ++i) {
+      own += ow[128 * (size_t)i + 8 * t + c];
+      ownn += ow[128 * (size_t)i + 8 * t + 4 + c];
+    }
     const float4 bu = d.leaf_bu[k];
     const float4 xa = d.fxa[p];  // offset X_T - X_leaf and a_T
     float cl;
@@ -498,7 +550,7 @@ __global__ void final_kernel(BhDev d) {
     const uint32_t f = d.order[p];
     float *out = reinterpret_cast<float *>(d.partials);
     out[8 * (size_t)f + c] = (own + part) + cl;
-    if (c == 0) d.partials[2 * f + 1] = d.own[2 * p + 1];
+    out[8 * (size_t)f + 4 + c] = ownn;
   }
 }
 
@@ -601,17 +653,19 @@ struct rs_bh {
   int64_t culprit[2] = {-1, -1};
   // device topology
   DevBuf<uint32_t> faces, order, node_start, node_end, node_right, node_parent, leaves,
-      leaf_of_pos, schedule, chain_off, chain, inc_off, inc, leaf_ordinal;
+      leaf_of_pos, schedule, chain_off, chain, inc_off, inc, leaf_ordinal, item_leaf, item_off;
+  DevBuf<uint4> items;
+  size_t n_items = 0;
   DevBuf<double> box, radius;
   DevBuf<uint32_t> lumped_off, lumped, exact_off, exact, partner_off, lumped_t_off, lumped_t,
       exact_t_off, exact_t;
   // per evaluation
   DevBuf<double> pos;
-  DevBuf<float4> fxa, fnn, own, node_term, partner, node_sum, leaf_bu, partials;
+  DevBuf<float4> fxa, fnn, fol, fnl, own, node_term, partner, node_sum, leaf_bu, partials;
   DevBuf<double4> ncA, nmom;
   DevBuf<float4> nch, ncl;
   DevBuf<uint32_t> refit_count;
-  DevBuf<double> leaf_energy, energy, dE;
+  DevBuf<double> item_energy, energy, dE;
   DevBuf<unsigned int> ticket;
   DevBuf<unsigned long long> culprit_key;
   bool positions_current = false;
@@ -622,6 +676,8 @@ struct rs_bh {
     d.faces = faces.p, d.order = order.p, d.node_start = node_start.p, d.node_end = node_end.p;
     d.node_right = node_right.p, d.node_parent = node_parent.p, d.leaves = leaves.p;
     d.leaf_of_pos = leaf_of_pos.p, d.schedule = schedule.p, d.chain_off = chain_off.p;
+    d.items = items.p, d.item_leaf = item_leaf.p, d.item_off = item_off.p, d.n_items = (int)n_items;
+    d.fol = fol.p, d.fnl = fnl.p;
     d.chain = chain.p, d.inc_off = inc_off.p, d.inc = inc.p;
     d.lumped_off = lumped_off.p, d.lumped = lumped.p, d.exact_off = exact_off.p, d.exact = exact.p;
     d.partner_off = partner_off.p, d.lumped_t_off = lumped_t_off.p, d.lumped_t = lumped_t.p;
@@ -631,7 +687,7 @@ struct rs_bh {
     d.fxa = fxa.p, d.fnn = fnn.p, d.ncA = ncA.p, d.nmom = nmom.p, d.refit_count = refit_count.p;
     d.nch = nch.p, d.ncl = ncl.p;
     d.own = own.p, d.node_term = node_term.p, d.partner = partner.p, d.node_sum = node_sum.p;
-    d.leaf_bu = leaf_bu.p, d.partials = partials.p, d.leaf_energy = leaf_energy.p;
+    d.leaf_bu = leaf_bu.p, d.partials = partials.p, d.item_energy = item_energy.p;
     d.ticket = ticket.p;
     return d;
   }
@@ -730,7 +786,8 @@ void upload_topology(rs_bh *h) {
   upload_vec(h->leaf_ordinal, T.leaf_ordinal, s);
   h->fxa.alloc(h->nf);
   h->fnn.alloc(h->nf);
-  h->own.alloc(2 * (size_t)h->nf);
+  h->fol.alloc(h->nf);
+  h->fnl.alloc(h->nf);
   h->partials.alloc(2 * (size_t)h->nf);
   h->ncA.alloc(nn);
   h->nmom.alloc(nn);
@@ -740,7 +797,6 @@ void upload_topology(rs_bh *h) {
   h->refit_count.alloc(nn);
   RSG_CUDA("upload", cudaMemsetAsync(h->refit_count.p, 0, nn * sizeof(uint32_t), s));
   h->leaf_bu.alloc(nl);
-  h->leaf_energy.alloc(nl);
   h->energy.alloc(1);
   h->dE.alloc(3 * (size_t)h->nv);
   h->pos.alloc(3 * (size_t)h->nv);
@@ -750,7 +806,7 @@ void upload_topology(rs_bh *h) {
 
 // Transposes of the lists (barnes_hut.rs:798-806, 811-827) by a stable radix sort of
 // (key, entry) pairs, and the processing schedule.
-void finish_lists(rs_bh *h, const std::vector<uint32_t> &work_per_leaf) {
+void finish_lists(rs_bh *h, const std::vector<uint32_t> &lo, const std::vector<uint32_t> &eo) {
   cudaStream_t s = h->st();
   size_t nn = h->tree.n_nodes(), nl = h->tree.leaves.size();
   auto transpose = [&](const uint32_t *keys_in, size_t n, size_t m, DevBuf<uint32_t> &off,
@@ -786,12 +842,37 @@ void finish_lists(rs_bh *h, const std::vector<uint32_t> &work_per_leaf) {
     }
     transpose(key.p, h->n_exact, nl, h->exact_t_off, h->exact_t, "exact_t");
   }
-  // Longest work first: warps take leaves from an atomic ticket in this order.
-  std::vector<uint32_t> sched(nl);
+  // Work items: every leaf's lumped and exact ranges split into slices of at most ~512
+  // lumped / ~128 exact entries (a few leaves of a degenerate tree open every other leaf);
+  // warps take them from an atomic ticket, most work first.
+  std::vector<uint4> it;
+  std::vector<uint32_t> it_leaf, it_off(nl + 1, 0);
+  std::vector<uint64_t> cost;
+  for (size_t k = 0; k < nl; ++k) {
+    uint32_t l0 = lo[k], l1 = lo[k + 1], e0 = eo[k], e1 = eo[k + 1];
+    uint32_t nl_ = l1 - l0, ne = e1 - e0;
+    uint32_t n = std::max<uint32_t>(1, std::max((nl_ + 511) / 512, (ne + 127) / 128));
+    uint32_t leaf = h->tree.leaves[k];
+    uint64_t ns = h->tree.end[leaf] - h->tree.start[leaf];
+    for (uint32_t i = 0; i < n; ++i) {
+      uint32_t a0 = l0 + (uint32_t)((uint64_t)nl_ * i / n), a1 = l0 + (uint32_t)((uint64_t)nl_ * (i + 1) / n);
+      uint32_t b0 = e0 + (uint32_t)((uint64_t)ne * i / n), b1 = e0 + (uint32_t)((uint64_t)ne * (i + 1) / n);
+      it.push_back(make_uint4(a0, a1, b0, b1));
+      it_leaf.push_back((uint32_t)k);
+      cost.push_back(ns * ((uint64_t)(a1 - a0) + 8ull * (b1 - b0)));
+    }
+    it_off[k + 1] = (uint32_t)it.size();
+  }
+  h->n_items = it.size();
+  std::vector<uint32_t> sched(it.size());
   std::iota(sched.begin(), sched.end(), 0u);
-  std::stable_sort(sched.begin(), sched.end(),
-                   [&](uint32_t a, uint32_t b) { return work_per_leaf[a] > work_per_leaf[b]; });
+  std::stable_sort(sched.begin(), sched.end(), [&](uint32_t a, uint32_t b) { return cost[a] > cost[b]; });
   upload_vec(h->schedule, sched, s);
+  upload_vec(h->items, it, s);
+  upload_vec(h->item_leaf, it_leaf, s);
+  upload_vec(h->item_off, it_off, s);
+  h->own.alloc(16 * it.size());
+  h->item_energy.alloc(it.size());
   h->node_term.alloc(std::max<size_t>(h->n_lumped, 1));
   h->partner.alloc(std::max<size_t>(h->n_partner, 1));
   RSG_CUDA("upload", cudaStreamSynchronize(s));
@@ -824,7 +905,7 @@ void build_lists_device(rs_bh *h) {
   overflow.download(&ovf, 1, s);
   RSG_CUDA("upload", cudaStreamSynchronize(s));
   if (ovf) fail(RS_INTERNAL, "Internal", "upload", "traversal stack overflow");
-  std::vector<uint32_t> lo(nl + 1, 0), eo(nl + 1, 0), pb(nl, 0), work(nl);
+  std::vector<uint32_t> lo(nl + 1, 0), eo(nl + 1, 0), pb(nl, 0);
   uint64_t tl = 0, te = 0, tp = 0;
   h->pairs_exact = 0;
   h->lumped_inter = 0;
@@ -836,7 +917,6 @@ void build_lists_device(rs_bh *h) {
     lo[k + 1] = (uint32_t)tl, eo[k + 1] = (uint32_t)te;
     h->pairs_exact += hpr[k];
     h->lumped_inter += hli[k];
-    work[k] = (uint32_t)std::min<unsigned long long>(hpr[k] + hli[k], 0xffffffffull);
   }
   h->n_lumped = tl, h->n_exact = te, h->n_partner = tp;
   upload_vec(h->lumped_off, lo, s);
@@ -855,7 +935,7 @@ void build_lists_device(rs_bh *h) {
   RSG_CUDA("upload", cudaMemcpyAsync(h->partner_off.p + te, &tp32, sizeof(uint32_t),
                                      cudaMemcpyHostToDevice, s));
   RSG_CUDA("upload", cudaStreamSynchronize(s));
-  finish_lists(h, work);
+  finish_lists(h, lo, eo);
 }
 
 void refit_device(rs_bh *h) {
@@ -883,7 +963,7 @@ int pair_blocks_per_sm(bool grad, bool fast) {
     const void *fn = grad ? (fast ? (const void *)bh_pair_kernel<true, true> : (const void *)bh_pair_kernel<true, false>)
                           : (fast ? (const void *)bh_pair_kernel<false, true> : (const void *)bh_pair_kernel<false, false>);
     int b = 0;
-    RSG_CUDA("launch", cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, 256, 0));
+    RSG_CUDA("launch", cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fn, 128, 0));
     c = b > 0 ? b : 1;
   }
   return c;
@@ -898,14 +978,14 @@ void evaluate(rs_bh *h, const Pow &pw, bool fast, bool grad, double *energy_dev,
   Profiler &P = h->prof;
   RSG_CUDA("launch", cudaMemsetAsync(h->ticket.p, 0, sizeof(unsigned), s));
   unsigned grid = (unsigned)std::min<size_t>((size_t)h->ctx->sm_count * pair_blocks_per_sm(grad, fast),
-                                             blocks(nl, 8));
+                                             blocks(h->n_items, 4));
   P.begin(s, grad ? "bh_pair_grad" : "bh_pair_value");
   if (grad) {
-    if (fast) bh_pair_kernel<true, true><<<grid, 256, 0, s>>>(d, pw);
-    else bh_pair_kernel<true, false><<<grid, 256, 0, s>>>(d, pw);
+    if (fast) bh_pair_kernel<true, true><<<grid, 128, 0, s>>>(d, pw);
+    else bh_pair_kernel<true, false><<<grid, 128, 0, s>>>(d, pw);
   } else {
-    if (fast) bh_pair_kernel<false, true><<<grid, 256, 0, s>>>(d, pw);
-    else bh_pair_kernel<false, false><<<grid, 256, 0, s>>>(d, pw);
+    if (fast) bh_pair_kernel<false, true><<<grid, 128, 0, s>>>(d, pw);
+    else bh_pair_kernel<false, false><<<grid, 128, 0, s>>>(d, pw);
   }
   RSG_LAUNCHED(h->ctx, "bh_pair");
   P.end(s);
@@ -930,7 +1010,7 @@ void evaluate(rs_bh *h, const Pow &pw, bool fast, bool grad, double *energy_dev,
     }
   }
   P.begin(s, "energy_reduce");
-  energy_reduce_kernel<<<1, 1024, 0, s>>>(h->leaf_energy.p, (int)nl, energy_dev);
+  energy_reduce_kernel<<<1, 1024, 0, s>>>(h->item_energy.p, (int)h->n_items, energy_dev);
   RSG_LAUNCHED(h->ctx, "energy_reduce");
   P.end(s);
 }
@@ -1028,7 +1108,7 @@ int rs_bh_attach(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const doubl
     upload_topology(h.get());
     // lists from the caller
     cudaStream_t s = h->st();
-    std::vector<uint32_t> lo(nl + 1), eo(nl + 1), work(nl, 0);
+    std::vector<uint32_t> lo(nl + 1), eo(nl + 1);
     for (size_t k = 0; k <= nl; ++k) lo[k] = (uint32_t)lumped_off[k], eo[k] = (uint32_t)exact_off[k];
     h->n_lumped = lo[nl], h->n_exact = eo[nl];
     std::vector<uint32_t> poff(h->n_exact + 1, 0);
@@ -1050,9 +1130,6 @@ int rs_bh_attach(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const doubl
         if (lumped[q] >= (uint32_t)n_nodes)
           fail(RS_INVALID_OPTION, "InvalidOption", "upload", "lumped entry out of range");
       h->lumped_inter += (uint64_t)(lo[k + 1] - lo[k]) * ns;
-      work[k] = (uint32_t)std::min<uint64_t>((uint64_t)(lo[k + 1] - lo[k]) * ns +
-                                                 (uint64_t)(eo[k + 1] - eo[k]) * ns * 8,
-                                             0xffffffffull);
     }
     poff[h->n_exact] = (uint32_t)p;
     h->n_partner = p;
@@ -1063,7 +1140,7 @@ int rs_bh_attach(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const doubl
     h->exact.alloc(std::max<size_t>(h->n_exact, 1));
     if (h->n_exact) h->exact.upload(exact, h->n_exact, s);
     upload_vec(h->partner_off, poff, s);
-    finish_lists(h.get(), work);
+    finish_lists(h.get(), lo, eo);
     h->pos.upload(positions_host, 3 * (size_t)nv, s);
     refit_device(h.get());
     RSG_CUDA("upload", cudaStreamSynchronize(s));

@@ -27,7 +27,11 @@ struct BhDev {
   const uint32_t *node_parent; // N (root: 0)
   const uint32_t *leaves;      // L: node id of each leaf
   const uint32_t *leaf_of_pos; // F: leaf ordinal of each BVH position
-  const uint32_t *schedule;    // L: leaf ordinals, most work first
+  const uint32_t *schedule;    // work items, most work first
+  const uint4 *items;          // per work item: lumped [x, y), exact [z, w) entry ranges
+  const uint32_t *item_leaf;   // per work item: its leaf ordinal
+  const uint32_t *item_off;    // L + 1: the work items of each leaf (leaf-major numbering)
+  int n_items;
   const uint32_t *chain_off;   // L + 1: root -> leaf chains
   const uint32_t *chain;
   const uint32_t *inc_off;     // V + 1: vertex -> incident (face << 2 | corner), faces ascending
@@ -38,19 +42,21 @@ struct BhDev {
   int n_vertices, n_faces, n_nodes, n_leaves;
   // per-evaluation state
   float4 *fxa, *fnn;
+  float4 *fol;      // per position: lo part of the offset (xyz) -- offset = fxa.xyz + fol.xyz
+  float4 *fnl;      // per position: lo part of the normal (xyz), alpha_S = N_S.(X_S - X_leaf) (w)
   double4 *ncA;     // node centroid (xyz) and area (w)
   float4 *nch;      // node centroid as a float pair: hi (xyz) and area (w) ...
   float4 *ncl;      // ... and lo (xyz): X = hi + lo to ~48 bits, no FP64 in the pair kernel
   double4 *nmom;    // node first moment (xyz) and area (w), for the bottom-up refit
   uint32_t *refit_count;
   // outputs and scratch
-  float4 *own;       // 2 per position: (d_a, d_x), (d_n, 0)
+  float4 *own;       // 16 per work item (2 per leaf face slot): (d_a, d_x), (d_n, 0)
   float4 *node_term; // per lumped entry: (b, u)
   float4 *partner;   // per partner slot: (d_a, d_x)
   float4 *node_sum;  // per node: (b_C, u_C)
   float4 *leaf_bu;   // per leaf: (beta, U) of the downward pass
   float4 *partials;  // 2 per face (by face id): (d_a, d_x), (d_n, 0)
-  double *leaf_energy;
+  double *item_energy;
   unsigned int *ticket;
 };
 

@@ -1,0 +1,26 @@
+// Block cluster tree structure (host C++): the admissible (far) and inadmissible (near) blocks
+// of a BVH, grouped by row node, as BlockTree::build_impl classifies them
+// (RS/src/spatial/block_tree.rs:159-247): level by level from (root, root); a pair of distinct
+// nodes is far when separated (max(r_a, r_b)^2 <= chi^2 d_box^2, d_box > 0;
+// RS/src/metric/hierarchical.rs:116-123), near when both are leaves or |a||b| <= leaf_pairs,
+// else both non-leaf sides are split. The near entries are not stored: the device evaluates
+// them in every product.
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include "host_tree.hpp"
+
+namespace rsg {
+
+struct Blocks {
+  std::vector<uint32_t> far_ptr, far_col;    // CSR by row node (stable: level order)
+  std::vector<uint32_t> near_ptr, near_col;  // CSR by row node
+  uint64_t near_entries = 0;                 // off-diagonal element pairs of the near blocks
+  uint64_t far_pairs = 0;                    // element pairs covered by far blocks
+  size_t depth = 0;
+};
+
+Blocks classify_blocks(const Tree &T, double chi, size_t leaf_pairs, int threads = 0);
+
+}  // namespace rsg

@@ -1,0 +1,791 @@
+// Hierarchical (block cluster tree) products on the GPU: the Hs metric B~ + B~0 over face
+// pairs (FaceMetricTree, RS/src/metric/hierarchical.rs:279-812) and the vertex-pair fractional
+// operator L^V_{2-s} of the preconditioner (VertexFractionalTree, hierarchical.rs:998-1346),
+// behind rs_metric_* / rs_vfrac_* of include/rsgpu.h.
+//
+// Both are kernel-matrix forms L u = 2 M^T diag(a) (diag(H~a) M u - H~(a M u)) with a block
+// cluster tree H~: rank-one far blocks (cluster data) and exact near blocks. The near entries
+// are NOT stored: every product evaluates them from the element records (FP32 offsets from the
+// leaf centroid, normals) while it streams the columns, which costs less than reading a stored
+// near field from HBM (0.3 G entries x 2 kernels at 204,800 faces).
+//
+// Per product (C channels per element: 9 gradient + 3 average per input vector for faces, 3
+// per vector for vertices):
+//   prologue    m = M x per element (FP32), element-major [n][C]
+//   upward      up[node] = sum_{q in node} a_q m_q, bottom-up (the second child to arrive adds)
+//   far         farx[node] = sum_{b in far(node)} h(node, b) up[b]            (warp per node)
+//   rows        per leaf (warp): near sums over the chain's near blocks with H~a accumulated
+//               in the same loop, far sums along the chain, z = H~a m - H~(a m)
+//   epilogue    y = 2 M^T diag(a) W z (faces: per-vertex gather; vertices: y = 2 a z)
+// H~a is formed with the same operations as H~(a m) for m = 1, so L 1 = 0 exactly (the
+// reference's null-space property, hierarchical.rs:13-16).
+#include <algorithm>
+#include <cmath>
+#include <memory>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "block_tree.hpp"
+#include "common.hpp"
+#include "host_tree.hpp"
+#include "profile.hpp"
+
+namespace rsg {
+
+constexpr int FACE = 0, VERTEX = 1;
+
+struct HDev {
+  const uint32_t *start, *end, *right, *parent, *leaves, *chain_off, *chain, *leaf_of_pos;
+  const uint32_t *far_ptr, *far_col, *near_ptr, *near_col;
+  const float2 *far_coef;    // per far block: (k_0, k_1)
+  const float4 *el;          // per BVH position: offset from the leaf centroid (xyz), weight a
+  const float4 *nrm;         // per BVH position: normal (faces only)
+  const float4 *ch, *cl;     // per node: centroid as a float pair (hi xyz + weight w, lo xyz)
+  const float2 *leaf_farA;   // per leaf: the far part of H~a along its chain (k_0, k_1)
+  float *up;                 // per node: C channel sums
+  float *farx;               // per node: C channel far sums
+  uint32_t *count;           // per node: arrival counter of the upward pass
+  const float *m;            // [n][C]
+  float *z;                  // [n][C]
+  int n_nodes, n_leaves, n_el, C;
+  float neg_s;               // kernel exponent applied to r^2
+};
+
+// The near kernel values of an element pair (hierarchical.rs:185-189, 224-231 and 987-991):
+// faces: [r2^-s, (nu_p^2 + nu_q^2)/2 r2^-2 r2^-s]; vertices: [r2^e].
+template <int KIND>
+__device__ __forceinline__ void near_kernel(float d0, float d1, float d2, const float4 &np,
+                                            const float4 &nq, float neg_s, float &k0, float &k1) {
+  float r2 = d0 * d0 + d1 * d1 + d2 * d2;
+  float h = exp2f(neg_s * log2f(r2));
+  k0 = h;
+  if (KIND == FACE) {
+    float a = np.x * d0 + np.y * d1 + np.z * d2;
+    float b = nq.x * d0 + nq.y * d1 + nq.z * d2;
+    float ir2 = 1.f / r2;
+    k1 = 0.5f * (a * a + b * b) * ir2 * ir2 * h;
+  } else {
+    k1 = h;
+  }
+}
+
+// Bottom-up channel sums: one thread per leaf sums its elements, then climbs; at every parent
+// the second child to arrive adds left + right (fixed order, no waiting).
+__global__ void hm_upward_kernel(HDev d) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.n_leaves) return;
+  const int C = d.C;
+  uint32_t leaf = d.leaves[k];
+  float *u = d.up + (size_t)leaf * C;
+  for (int c = 0; c < C; ++c) u[c] = 0.f;
+  for (uint32_t p = d.start[leaf]; p < d.end[leaf]; ++p) {
+    float a = d.el[p].w;
+    const float *mp = d.m + (size_t)p * C;
+    for (int c = 0; c < C; ++c) u[c] += a * mp[c];
+  }
+  uint32_t n = leaf;
+  while (n != 0) {
+    uint32_t par = d.parent[n];
+    __threadfence();
+    unsigned old = atomicAdd(&d.count[par], 1u);
+    if ((old & 1u) == 0u) return;
+    __threadfence();
+    const float *l = d.up + (size_t)(par + 1) * C;
+    const float *r = d.up + (size_t)d.right[par] * C;
+    float *o = d.up + (size_t)par * C;
+    for (int c = 0; c < C; ++c) o[c] = __ldcg(l + c) + __ldcg(r + c);
+    n = par;
+  }
+}
+
+// farx[a][c] = sum over the far blocks (a, b) of h(a, b)[kernel(c)] up[b][c] (block_tree.rs:
+// 564-578); one warp per node, lanes over channels. `split` = first channel of kernel 1.
+__global__ void hm_far_kernel(HDev d, int split) {
+  int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (a >= d.n_nodes) return;
+  const int C = d.C;
+  for (int c0 = 0; c0 < C; c0 += 32) {
+    int c = c0 + lane;
+    float acc = 0.f;
+    if (c < C)
+      for (uint32_t q = d.far_ptr[a]; q < d.far_ptr[a + 1]; ++q) {
+        float2 k = d.far_coef[q];
+        acc += (c < split ? k.x : k.y) * d.up[(size_t)d.far_col[q] * C + c];
+      }
+    if (c < C) d.farx[(size_t)a * C + c] = acc;
+  }
+}
+
+// One warp per leaf; lane = r + 8 j: r the row (element) of the leaf, j one of four column
+// groups. The near blocks of the chain root -> leaf are streamed column by column (group j
+// takes every fourth column), each column's kernel values evaluated once per row and applied to
+// all C channels; H~a's near part is summed in the same loop. CC = C (compile-time).
+template <int KIND, int CC>
+__global__ void __launch_bounds__(128) hm_rows_kernel(HDev d, int split) {
+  const int lane = threadIdx.x & 31;
+  const int r = lane & 7, j = lane >> 3;
+  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (k >= d.n_leaves) return;
+  const uint32_t leaf = d.leaves[k];
+  const uint32_t s0 = d.start[leaf], ns = d.end[leaf] - s0;
+  const bool act = (uint32_t)r < ns;
+  const uint32_t p = s0 + (act ? r : 0);
+  const float4 ep = d.el[p];
+  const float4 np = KIND == FACE ? d.nrm[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 cph = d.ch[leaf], cpl = d.cl[leaf];
+  float acc[CC];
+#pragma unroll
+  for (int c = 0; c < CC; ++c) acc[c] = 0.f;
+  float sw0 = 0.f, sw1 = 0.f;
+  const uint32_t c0 = d.chain_off[k], c1 = d.chain_off[k + 1];
+  for (uint32_t ci = c0; ci < c1; ++ci) {
+    const uint32_t a = d.chain[ci];
+    for (uint32_t qb = d.near_ptr[a]; qb < d.near_ptr[a + 1]; ++qb) {
+      const uint32_t b = d.near_col[qb];
+      const uint32_t cs = d.start[b], ce = d.end[b];
+      for (uint32_t q = cs + j; q < ce; q += 4) {
+        if (!act || q == p) continue;
+        const uint32_t lq = d.leaves[d.leaf_of_pos[q]];
+        const float4 cqh = d.ch[lq], cql = d.cl[lq];
+        const float4 eq = d.el[q];
+        const float d0 = ((cph.x - cqh.x) + (cpl.x - cql.x)) + (ep.x - eq.x);
+        const float d1 = ((cph.y - cqh.y) + (cpl.y - cql.y)) + (ep.y - eq.y);
+        const float d2 = ((cph.z - cqh.z) + (cpl.z - cql.z)) + (ep.z - eq.z);
+        float k0, k1;
+        near_kernel<KIND>(d0, d1, d2, np, KIND == FACE ? d.nrm[q] : np, d.neg_s, k0, k1);
+        const float w0 = k0 * eq.w, w1 = k1 * eq.w;
+        sw0 += w0;
+        sw1 += w1;
+        const float4 *mq = reinterpret_cast<const float4 *>(d.m + (size_t)q * CC);
+#pragma unroll
+        for (int c4 = 0; c4 < CC / 4; ++c4) {
+          const float4 v = mq[c4];
+          const int c = 4 * c4;
+          acc[c] += (c < split ? w0 : w1) * v.x;
+          acc[c + 1] += (c + 1 < split ? w0 : w1) * v.y;
+          acc[c + 2] += (c + 2 < split ? w0 : w1) * v.z;
+          acc[c + 3] += (c + 3 < split ? w0 : w1) * v.w;
+        }
+      }
+    }
+  }
+  // reduce over the four column groups
+#pragma unroll
+  for (int c = 0; c < CC; ++c) {
+    acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 8);
+    acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 16);
+  }
+  sw0 += __shfl_xor_sync(0xffffffffu, sw0, 8);
+  sw0 += __shfl_xor_sync(0xffffffffu, sw0, 16);
+  sw1 += __shfl_xor_sync(0xffffffffu, sw1, 8);
+  sw1 += __shfl_xor_sync(0xffffffffu, sw1, 16);
+  if (j != 0 || !act) return;
+  const float2 fa = d.leaf_farA[k];
+  const float ha0 = sw0 + fa.x, ha1 = sw1 + fa.y;
+  const float *mp = d.m + (size_t)p * CC;
+  float *zp = d.z + (size_t)p * CC;
+#pragma unroll
+  for (int c = 0; c < CC; ++c) {
+    float fx = 0.f;
+    for (uint32_t ci = c0; ci < c1; ++ci) fx += d.farx[(size_t)d.chain[ci] * CC + c];
+    zp[c] = (c < split ? ha0 : ha1) * mp[c] - (acc[c] + fx);
+  }
+}
+
+// Far part of H~a per leaf (the far field of psi = a, pushed down the chain): same kernels as a
+// product, channel count 2.
+__global__ void hm_leaf_farA_kernel(HDev d, float2 *out) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= d.n_leaves) return;
+  float f0 = 0.f, f1 = 0.f;
+  for (uint32_t ci = d.chain_off[k]; ci < d.chain_off[k + 1]; ++ci) {
+    uint32_t a = d.chain[ci];
+    f0 += d.farx[2 * (size_t)a];
+    f1 += d.farx[2 * (size_t)a + 1];
+  }
+  out[k] = make_float2(f0, f1);
+}
+
+// ------------------------------------------------------------------ face prologue / epilogue
+
+struct FaceOps {
+  const uint32_t *faces;   // 3F original order
+  const uint32_t *order;   // BVH position -> face
+  const uint32_t *position;  // face -> BVH position
+  const float *g;          // 9 per face (original order): g_c (df_coefficients, mod.rs:120-131)
+  const float *area;       // per face
+  const uint32_t *inc_off, *inc;  // vertex -> (face << 2 | corner), faces ascending
+  int nv, nf;
+};
+
+// m per face in BVH order (FaceMetricTree::product, hierarchical.rs:711-746): per vector q,
+// 9 gradient channels 9q + 3k + r = sum_c x[3 t_c + k] g_c[r], then 3 average channels
+// 9 nb + 3q + k = (x_0 + x_1 + x_2)/3 for axis k.
+__global__ void face_m_kernel(FaceOps o, const double *__restrict__ xs, int nb, int C, float *m) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= o.nf) return;
+  uint32_t f = o.order[p];
+  const uint32_t *t = o.faces + 3 * (size_t)f;
+  const float *g = o.g + 9 * (size_t)f;
+  float *mp = m + (size_t)p * C;
+  const size_t n3 = 3 * (size_t)o.nv;
+  for (int q = 0; q < nb; ++q) {
+    const double *x = xs + q * n3;
+    for (int k = 0; k < 3; ++k) {
+      float x0 = (float)x[3 * (size_t)t[0] + k], x1 = (float)x[3 * (size_t)t[1] + k],
+            x2 = (float)x[3 * (size_t)t[2] + k];
+      for (int r = 0; r < 3; ++r) mp[9 * q + 3 * k + r] = x0 * g[r] + x1 * g[3 + r] + x2 * g[6 + r];
+      mp[9 * nb + 3 * q + k] = ((x0 + x1) + x2) * (1.f / 3.f);
+    }
+  }
+  for (int c = 12 * nb; c < C; ++c) mp[c] = 0.f;
+}
+
+// y_v = 2 sum_{S ni v} a_S (w_hi g_c . z_hi + w_lo z_lo / 3) in FP64 (hierarchical.rs:779-811).
+__global__ void face_gather_kernel(FaceOps o, const float *__restrict__ z, int nb, int C,
+                                   double w_hi, double w_lo, double *__restrict__ ys) {
+  int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= o.nv) return;
+  const size_t n3 = 3 * (size_t)o.nv;
+  for (int q = 0; q < nb; ++q) {
+    double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0;
+    for (uint32_t e = o.inc_off[v]; e < o.inc_off[v + 1]; ++e) {
+      uint32_t fc = o.inc[e], f = fc >> 2, c = fc & 3;
+      double a = o.area[f];
+      const float *g = o.g + 9 * (size_t)f + 3 * c;
+      const float *zs = z + (size_t)o.position[f] * C;
+      double acc[3];
+      for (int k = 0; k < 3; ++k) {
+        const float *zh = zs + 9 * q + 3 * k;
+        double hi = (double)g[0] * zh[0] + (double)g[1] * zh[1] + (double)g[2] * zh[2];
+        acc[k] = a * (w_hi * hi + w_lo * (1.0 / 3.0) * (double)zs[9 * nb + 3 * q + k]);
+      }
+      acc0 += acc[0], acc1 += acc[1], acc2 += acc[2];
+    }
+    double *y = ys + q * n3 + 3 * (size_t)v;
+    y[0] = 2.0 * acc0, y[1] = 2.0 * acc1, y[2] = 2.0 * acc2;
+  }
+}
+
+// ------------------------------------------------------------------ vertex prologue / epilogue
+
+// psi channels of the vertex operator: m = x per axis (ψ = a x in the upward/near sums).
+__global__ void vertex_m_kernel(const uint32_t *order, const double *__restrict__ xs, int nv,
+                                int nb, int C, float *m) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nv) return;
+  uint32_t v = order[p];
+  float *mp = m + (size_t)p * C;
+  for (int q = 0; q < nb; ++q)
+    for (int k = 0; k < 3; ++k) mp[3 * q + k] = (float)xs[q * 3 * (size_t)nv + 3 * (size_t)v + k];
+  for (int c = 3 * nb; c < C; ++c) mp[c] = 0.f;
+}
+
+// y = 2 a (H~a x - H~(a x)) = 2 a z (hierarchical.rs:1330-1343).
+__global__ void vertex_out_kernel(const uint32_t *order, const float4 *el, const float *z, int nv,
+                                  int nb, int C, double scale, double *__restrict__ ys) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nv) return;
+  uint32_t v = order[p];
+  double a = el[p].w;
+  for (int q = 0; q < nb; ++q)
+    for (int k = 0; k < 3; ++k)
+      ys[q * 3 * (size_t)nv + 3 * (size_t)v + k] = scale * 2.0 * a * (double)z[(size_t)p * C + 3 * q + k];
+}
+
+// Element records relative to the leaf centroids, node centroids as float pairs; FP64 in.
+__global__ void hm_pack_kernel(const double *pts, const double *wt, const double *nrm64,
+                               const uint32_t *order, const uint32_t *leaf_of_pos,
+                               const uint32_t *leaves, const double *cent, int n, float4 *el,
+                               float4 *nrm) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  uint32_t e = order[p];
+  const double *c = cent + 3 * (size_t)leaves[leaf_of_pos[p]];
+  el[p] = make_float4((float)(pts[3 * (size_t)e] - c[0]), (float)(pts[3 * (size_t)e + 1] - c[1]),
+                      (float)(pts[3 * (size_t)e + 2] - c[2]), (float)wt[e]);
+  if (nrm) nrm[p] = make_float4((float)nrm64[3 * (size_t)e], (float)nrm64[3 * (size_t)e + 1],
+                                (float)nrm64[3 * (size_t)e + 2], 0.f);
+}
+
+}  // namespace rsg
+
+// ====================================================================== host side
+
+using namespace rsg;
+
+namespace {
+
+inline unsigned nblk(size_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
+
+template <class T>
+void up_vec(DevBuf<T> &b, const std::vector<T> &v, cudaStream_t s) {
+  b.alloc(std::max<size_t>(v.size(), 1));
+  if (!v.empty()) b.upload(v.data(), v.size(), s);
+}
+
+// The block cluster tree on the device with its per-step data (both operators).
+struct HMat {
+  rs_ctx *ctx = nullptr;
+  int kind = FACE;
+  Tree tree;
+  Blocks blocks;
+  size_t n_el = 0;
+  double neg_s = 0;
+  DevBuf<uint32_t> start, end, right, parent, leaves, chain_off, chain, leaf_of_pos;
+  DevBuf<uint32_t> far_ptr, far_col, near_ptr, near_col, count;
+  DevBuf<float2> far_coef, leaf_farA;
+  DevBuf<float4> el, nrm, ch, cl;
+  DevBuf<float> up, farx, m, z;
+  int C = 0;
+  Profiler prof;
+
+  HDev dev(int C_) const {
+    HDev d;
+    d.start = start.p, d.end = end.p, d.right = right.p, d.parent = parent.p, d.leaves = leaves.p;
+    d.chain_off = chain_off.p, d.chain = chain.p, d.leaf_of_pos = leaf_of_pos.p;
+    d.far_ptr = far_ptr.p, d.far_col = far_col.p, d.near_ptr = near_ptr.p, d.near_col = near_col.p;
+    d.far_coef = far_coef.p, d.el = el.p, d.nrm = nrm.p, d.ch = ch.p, d.cl = cl.p;
+    d.leaf_farA = leaf_farA.p, d.up = up.p, d.farx = farx.p, d.count = count.p;
+    d.m = m.p, d.z = z.p;
+    d.n_nodes = (int)tree.n_nodes(), d.n_leaves = (int)tree.leaves.size(), d.n_el = (int)n_el;
+    d.C = C_;
+    d.neg_s = (float)neg_s;
+    return d;
+  }
+  cudaStream_t st() const { return ctx->stream; }
+
+  // Channel scratch for C channels.
+  void reserve(int C_) {
+    size_t nn = tree.n_nodes();
+    if ((size_t)C_ * nn > up.n) up.alloc((size_t)C_ * nn), farx.alloc((size_t)C_ * nn);
+    if ((size_t)C_ * n_el > m.n) m.alloc((size_t)C_ * n_el), z.alloc((size_t)C_ * n_el);
+  }
+
+  // Uploads the tree, the blocks, the element records and the far coefficients; computes the
+  // far part of H~a. pts/wt/nrm64 are per element (original order), FP64.
+  void setup(const double *pts, const double *wt, const double *nrm64, const double *proj6) {
+    cudaStream_t s = st();
+    const Tree &T = tree;
+    size_t nn = T.n_nodes(), nl = T.leaves.size();
+    std::vector<uint32_t> parent_h(nn, 0), coff(nl + 1, 0), chain_h, lop(n_el);
+    for (size_t i = 0; i < nn; ++i)
+      if (T.right[i]) parent_h[i + 1] = (uint32_t)i, parent_h[T.right[i]] = (uint32_t)i;
+    for (size_t k = 0; k < nl; ++k) {
+      uint32_t l = T.leaves[k];
+      for (uint32_t p = T.start[l]; p < T.end[l]; ++p) lop[p] = (uint32_t)k;
+      if (T.end[l] - T.start[l] > 8)
+        fail(RS_INVALID_OPTION, "InvalidOption", "upload", "the GPU path needs leaf_size <= 8");
+      size_t b = chain_h.size();
+      uint32_t a = l;
+      for (;;) {
+        chain_h.push_back(a);
+        if (a == 0) break;
+        a = parent_h[a];
+      }
+      std::reverse(chain_h.begin() + b, chain_h.end());
+      coff[k + 1] = (uint32_t)chain_h.size();
+    }
+    up_vec(start, T.start, s), up_vec(end, T.end, s), up_vec(right, T.right, s);
+    up_vec(parent, parent_h, s), up_vec(leaves, T.leaves, s), up_vec(chain_off, coff, s);
+    up_vec(chain, chain_h, s), up_vec(leaf_of_pos, lop, s);
+    up_vec(far_ptr, blocks.far_ptr, s), up_vec(far_col, blocks.far_col, s);
+    up_vec(near_ptr, blocks.near_ptr, s), up_vec(near_col, blocks.near_col, s);
+    count.alloc(nn);
+    RSG_CUDA("upload", cudaMemsetAsync(count.p, 0, nn * sizeof(uint32_t), s));
+    // node centroids (float pairs) and far coefficients on the host in FP64 (kernel.far,
+    // hierarchical.rs:210-220 / 980-984), rounded once
+    std::vector<float4> chh(nn), clh(nn);
+    for (size_t i = 0; i < nn; ++i) {
+      const double *c = &T.centroid[3 * i];
+      float hx = (float)c[0], hy = (float)c[1], hz = (float)c[2];
+      chh[i] = make_float4(hx, hy, hz, (float)T.mass[i]);
+      clh[i] = make_float4((float)(c[0] - hx), (float)(c[1] - hy), (float)(c[2] - hz), 0.f);
+    }
+    up_vec(ch, chh, s), up_vec(cl, clh, s);
+    std::vector<float2> coef(blocks.far_col.size());
+    auto qf = [&](size_t n, const double *d) {
+      const double *p = proj6 + 6 * n;
+      return p[0] * d[0] * d[0] + p[3] * d[1] * d[1] + p[5] * d[2] * d[2] +
+             2.0 * (p[1] * d[0] * d[1] + p[2] * d[0] * d[2] + p[4] * d[1] * d[2]);
+    };
+    for (size_t a = 0; a < nn; ++a)
+      for (uint32_t q = blocks.far_ptr[a]; q < blocks.far_ptr[a + 1]; ++q) {
+        size_t b = blocks.far_col[q], lo = std::min(a, b), hi = std::max(a, b);
+        double d[3] = {T.centroid[3 * lo] - T.centroid[3 * hi], T.centroid[3 * lo + 1] - T.centroid[3 * hi + 1],
+                       T.centroid[3 * lo + 2] - T.centroid[3 * hi + 2]};
+        double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        double h = std::pow(r2, neg_s);
+        double h1 = h;
+        if (kind == FACE) h1 = 0.5 * (qf(lo, d) + qf(hi, d)) / (r2 * r2) * h;
+        coef[q] = make_float2((float)h, (float)h1);
+      }
+    up_vec(far_coef, coef, s);
+    // element records
+    DevBuf<double> dp, dw, dn, dc;
+    dp.upload(pts, 3 * n_el, s);
+    dw.upload(wt, n_el, s);
+    if (nrm64) dn.upload(nrm64, 3 * n_el, s);
+    dc.upload(T.centroid.data(), T.centroid.size(), s);
+    DevBuf<uint32_t> ord;
+    ord.upload(T.order.data(), T.order.size(), s);
+    el.alloc(n_el);
+    if (kind == FACE) nrm.alloc(n_el);
+    hm_pack_kernel<<<nblk(n_el, 256), 256, 0, s>>>(dp.p, dw.p, nrm64 ? dn.p : nullptr, ord.p,
+                                                   leaf_of_pos.p, leaves.p, dc.p, (int)n_el, el.p,
+                                                   kind == FACE ? nrm.p : nullptr);
+    RSG_LAUNCHED(ctx, "hm_pack");
+    // far part of H~a: upward over psi = a (m = 1, 2 channels), far, chain sums
+    leaf_farA.alloc(nl);
+    reserve(4);
+    std::vector<float> ones(2 * n_el, 1.f);
+    DevBuf<float> mm;
+    mm.upload(ones.data(), ones.size(), s);
+    HDev d = dev(2);
+    d.m = mm.p;
+    hm_upward_kernel<<<nblk(nl, 128), 128, 0, s>>>(d);
+    RSG_LAUNCHED(ctx, "hm_upward");
+    hm_far_kernel<<<nblk(nn * 32, 256), 256, 0, s>>>(d, 1);
+    RSG_LAUNCHED(ctx, "hm_far");
+    hm_leaf_farA_kernel<<<nblk(nl, 128), 128, 0, s>>>(d, leaf_farA.p);
+    RSG_LAUNCHED(ctx, "hm_leaf_farA");
+    RSG_CUDA("upload", cudaStreamSynchronize(s));
+  }
+
+  // z = H~a m - H~(a m) for the C-channel m already in `m` (split: first kernel-1 channel).
+  void product(int CC, int split) {
+    cudaStream_t s = st();
+    size_t nn = tree.n_nodes(), nl = tree.leaves.size();
+    HDev d = dev(CC);
+    prof.begin(s, kind == FACE ? "metric_upward" : "vfrac_upward");
+    hm_upward_kernel<<<nblk(nl, 128), 128, 0, s>>>(d);
+    RSG_LAUNCHED(ctx, "hm_upward");
+    prof.end(s);
+    prof.begin(s, kind == FACE ? "metric_far" : "vfrac_far");
+    hm_far_kernel<<<nblk(nn * 32, 256), 256, 0, s>>>(d, split);
+    RSG_LAUNCHED(ctx, "hm_far");
+    prof.end(s);
+    prof.begin(s, kind == FACE ? "metric_rows" : "vfrac_rows");
+    unsigned g = nblk(nl * 32, 128);
+#define RSG_ROWS(K, N) hm_rows_kernel<K, N><<<g, 128, 0, s>>>(d, split)
+    if (kind == FACE) {
+      if (CC == 12) RSG_ROWS(FACE, 12);
+      else if (CC == 24) RSG_ROWS(FACE, 24);
+      else if (CC == 36) RSG_ROWS(FACE, 36);
+      else fail(RS_INTERNAL, "Internal", "product", "unsupported channel count");
+    } else {
+      if (CC == 4) RSG_ROWS(VERTEX, 4);
+      else if (CC == 8) RSG_ROWS(VERTEX, 8);
+      else if (CC == 12) RSG_ROWS(VERTEX, 12);
+      else fail(RS_INTERNAL, "Internal", "product", "unsupported channel count");
+    }
+#undef RSG_ROWS
+    RSG_LAUNCHED(ctx, "hm_rows");
+    prof.end(s);
+  }
+
+  void build_common(rs_ctx *c, Tree &&t, double chi, int leaf_pairs) {
+    ctx = c;
+    tree = std::move(t);
+    if (!(std::isfinite(chi) && chi >= 0.0))
+      fail(RS_INVALID_OPTION, "InvalidOption", "upload", "chi must be a finite number >= 0");
+    if (leaf_pairs < 0) fail(RS_INVALID_OPTION, "InvalidOption", "upload", "leaf_pairs must be >= 0");
+    blocks = classify_blocks(tree, chi, (size_t)leaf_pairs);
+  }
+};
+
+void check_exponents(double alpha, double beta) {
+  if (!std::isfinite(alpha) || !std::isfinite(beta) || alpha <= 1.0 || beta <= alpha + 2.0 ||
+      beta >= 2.0 * alpha + 2.0)
+    fail(RS_INVALID_EXPONENTS, "InvalidExponents", "metric",
+         "exponents must satisfy alpha > 1 and alpha + 2 < beta < 2 alpha + 2");
+}
+
+}  // namespace
+
+struct rs_metric {
+  HMat h;
+  int nv = 0, nf = 0;
+  FaceGeom geom;
+  DevBuf<uint32_t> faces, order, position, inc_off, inc;
+  DevBuf<float> g, area;
+  DevBuf<double> xbuf, ybuf;
+  FaceOps ops() const {
+    FaceOps o;
+    o.faces = faces.p, o.order = order.p, o.position = position.p, o.g = g.p, o.area = area.p;
+    o.inc_off = inc_off.p, o.inc = inc.p, o.nv = nv, o.nf = nf;
+    return o;
+  }
+};
+
+struct rs_vfrac {
+  HMat h;
+  int nv = 0;
+  DevBuf<uint32_t> order;
+  DevBuf<double> xbuf, ybuf;
+};
+
+namespace {
+
+// FaceMetricTree::from_parts / build (hierarchical.rs:302-363): df coefficients, projectors,
+// blocks, element records.
+void metric_setup(rs_metric *M, rs_ctx *ctx, int nv, int nf, const uint32_t *faces,
+                  const double *pos, double alpha, double beta, double chi, int leaf_size,
+                  int leaf_pairs) {
+  check_exponents(alpha, beta);
+  validate_topology(nv, nf, faces);
+  validate_positions(nv, nf, faces, pos);
+  ctx->use();
+  M->nv = nv, M->nf = nf;
+  M->geom = face_geometry(nf, faces, pos);
+  Tree T = build_face_tree(nf, faces, pos, M->geom, leaf_size);
+  M->h.kind = FACE;
+  M->h.n_el = nf;
+  M->h.neg_s = -(beta - 2.0) / alpha;
+  // projectors P = sum a N N^T / A per node (RS/src/spatial/mod.rs:268-290), bottom-up
+  size_t nn = T.n_nodes();
+  std::vector<double> ps(7 * nn, 0.0), proj(6 * nn);
+  for (size_t i = nn; i-- > 0;) {
+    double *o = &ps[7 * i];
+    if (T.right[i] == 0) {
+      for (uint32_t p = T.start[i]; p < T.end[i]; ++p) {
+        uint32_t f = T.order[p];
+        double a = M->geom.area[f];
+        const double *n = &M->geom.normal[3 * (size_t)f];
+        o[0] += a, o[1] += a * n[0] * n[0], o[2] += a * n[0] * n[1], o[3] += a * n[0] * n[2];
+        o[4] += a * n[1] * n[1], o[5] += a * n[1] * n[2], o[6] += a * n[2] * n[2];
+      }
+    } else {
+      for (int k = 0; k < 7; ++k) o[k] = ps[7 * (i + 1) + k] + ps[7 * (size_t)T.right[i] + k];
+    }
+    for (int k = 0; k < 6; ++k) proj[6 * i + k] = o[k + 1] / o[0];
+  }
+  M->h.build_common(ctx, std::move(T), chi, leaf_pairs);
+  cudaStream_t s = M->h.st();
+  // df coefficients (RS/src/metric/mod.rs:120-131) in FP64, stored FP32
+  std::vector<float> gh(9 * (size_t)nf), ah(nf);
+  for (int f = 0; f < nf; ++f) {
+    const double *p0 = pos + 3 * (size_t)faces[3 * f], *p1 = pos + 3 * (size_t)faces[3 * f + 1],
+                 *p2 = pos + 3 * (size_t)faces[3 * f + 2];
+    double u[3], w[3], n[3];
+    for (int k = 0; k < 3; ++k) u[k] = p1[k] - p0[k], w[k] = p2[k] - p0[k];
+    n[0] = u[1] * w[2] - u[2] * w[1], n[1] = u[2] * w[0] - u[0] * w[2], n[2] = u[0] * w[1] - u[1] * w[0];
+    double len = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    double sc = 1.0 / (len * len);
+    double ww[3] = {n[0] * sc, n[1] * sc, n[2] * sc};
+    const double *pa[3] = {p1, p2, p0}, *pb[3] = {p2, p0, p1};
+    for (int c = 0; c < 3; ++c) {
+      double e[3] = {pb[c][0] - pa[c][0], pb[c][1] - pa[c][1], pb[c][2] - pa[c][2]};
+      gh[9 * f + 3 * c + 0] = (float)(ww[1] * e[2] - ww[2] * e[1]);
+      gh[9 * f + 3 * c + 1] = (float)(ww[2] * e[0] - ww[0] * e[2]);
+      gh[9 * f + 3 * c + 2] = (float)(ww[0] * e[1] - ww[1] * e[0]);
+    }
+    ah[f] = (float)M->geom.area[f];
+  }
+  std::vector<uint32_t> fh(faces, faces + 3 * (size_t)nf), posn(nf);
+  for (int p = 0; p < nf; ++p) posn[M->h.tree.order[p]] = (uint32_t)p;
+  std::vector<uint32_t> ioff((size_t)nv + 1, 0), inc(3 * (size_t)nf);
+  for (int f = 0; f < nf; ++f)
+    for (int c = 0; c < 3; ++c) ioff[faces[3 * f + c] + 1]++;
+  for (int v = 0; v < nv; ++v) ioff[v + 1] += ioff[v];
+  {
+    std::vector<uint32_t> fill(ioff.begin(), ioff.end() - 1);
+    for (int f = 0; f < nf; ++f)
+      for (int c = 0; c < 3; ++c) inc[fill[faces[3 * f + c]]++] = ((uint32_t)f << 2) | c;
+  }
+  up_vec(M->faces, fh, s), up_vec(M->order, M->h.tree.order, s), up_vec(M->position, posn, s);
+  up_vec(M->g, gh, s), up_vec(M->area, ah, s), up_vec(M->inc_off, ioff, s), up_vec(M->inc, inc, s);
+  M->h.setup(M->geom.bary.data(), M->geom.area.data(), M->geom.normal.data(), proj.data());
+}
+
+// FaceMetricTree::apply_batch (hierarchical.rs:540-622) on device vectors: groups of <= 3.
+void metric_apply(rs_metric *M, double w_hi, double w_lo, int nb, const double *xs, double *ys) {
+  if (!(std::isfinite(w_hi) && std::isfinite(w_lo)))
+    fail(RS_INVALID_OPTION, "InvalidOption", "product", "finite weights");
+  cudaStream_t s = M->h.st();
+  size_t n3 = 3 * (size_t)M->nv;
+  for (int q0 = 0; q0 < nb; q0 += 3) {
+    int k = std::min(3, nb - q0);
+    int CC = 12 * k;
+    M->h.reserve(CC);
+    M->h.prof.begin(s, "metric_m");
+    face_m_kernel<<<nblk(M->nf, 256), 256, 0, s>>>(M->ops(), xs + q0 * n3, k, CC, M->h.m.p);
+    RSG_LAUNCHED(M->h.ctx, "face_m");
+    M->h.prof.end(s);
+    M->h.product(CC, 9 * k);
+    M->h.prof.begin(s, "metric_gather");
+    face_gather_kernel<<<nblk(M->nv, 128), 128, 0, s>>>(M->ops(), M->h.z.p, k, CC, w_hi, w_lo,
+                                                        ys + q0 * n3);
+    RSG_LAUNCHED(M->h.ctx, "face_gather");
+    M->h.prof.end(s);
+  }
+}
+
+void vfrac_apply(rs_vfrac *V, double scale, int nb, const double *xs, double *ys) {
+  cudaStream_t s = V->h.st();
+  size_t n3 = 3 * (size_t)V->nv;
+  for (int q0 = 0; q0 < nb; q0 += 3) {
+    int k = std::min(3, nb - q0);
+    int CC = 4 * k;  // 3 k channels padded to a multiple of 4
+    V->h.reserve(CC);
+    vertex_m_kernel<<<nblk(V->nv, 256), 256, 0, s>>>(V->order.p, xs + q0 * n3, V->nv, k, CC, V->h.m.p);
+    RSG_LAUNCHED(V->h.ctx, "vertex_m");
+    V->h.product(CC, CC);
+    vertex_out_kernel<<<nblk(V->nv, 256), 256, 0, s>>>(V->order.p, V->h.el.p, V->h.z.p, V->nv, k, CC,
+                                                       scale, ys + q0 * n3);
+    RSG_LAUNCHED(V->h.ctx, "vertex_out");
+  }
+}
+
+template <class F>
+void host_io(rs_ctx *ctx, DevBuf<double> &xb, DevBuf<double> &yb, size_t n, const double *xh,
+             double *yh, F &&apply) {
+  cudaStream_t s = ctx->stream;
+  if (xb.n < n) xb.alloc(n), yb.alloc(n);
+  double *stage = (double *)ctx->staging(n * sizeof(double));
+  std::memcpy(stage, xh, n * sizeof(double));
+  RSG_CUDA("upload", cudaMemcpyAsync(xb.p, stage, n * sizeof(double), cudaMemcpyHostToDevice, s));
+  apply(xb.p, yb.p);
+  RSG_CUDA("product", cudaMemcpyAsync(stage, yb.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  RSG_CUDA("product", cudaStreamSynchronize(s));
+  std::memcpy(yh, stage, n * sizeof(double));
+}
+
+}  // namespace
+
+extern "C" {
+
+int rs_metric_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const double *positions_host,
+                    double alpha, double beta, double chi, int leaf_size, int leaf_pairs,
+                    rs_metric **out) {
+  *out = nullptr;
+  return guard([&] {
+    auto M = std::make_unique<rs_metric>();
+    metric_setup(M.get(), ctx, nv, nf, faces, positions_host, alpha, beta, chi, leaf_size, leaf_pairs);
+    *out = M.release();
+  });
+}
+
+void rs_metric_free(rs_metric *M) {
+  if (!M) return;
+  cudaSetDevice(M->h.ctx->device);
+  cudaStreamSynchronize(M->h.ctx->stream);
+  delete M;
+}
+
+int rs_metric_apply(rs_metric *M, double w_hi, double w_lo, int nb, const double *xs_host,
+                    double *ys_host) {
+  return guard([&] {
+    M->h.ctx->use();
+    size_t n = (size_t)nb * 3 * M->nv;
+    host_io(M->h.ctx, M->xbuf, M->ybuf, n, xs_host, ys_host,
+            [&](const double *x, double *y) { metric_apply(M, w_hi, w_lo, nb, x, y); });
+  });
+}
+
+int rs_metric_apply_device(rs_metric *M, double w_hi, double w_lo, int nb, const double *xs_dev,
+                           double *ys_dev) {
+  return guard([&] {
+    M->h.ctx->use();
+    metric_apply(M, w_hi, w_lo, nb, xs_dev, ys_dev);
+  });
+}
+
+int rs_metric_stats(rs_metric *M, int64_t *o) {
+  return guard([&] {
+    o[0] = (int64_t)M->h.blocks.far_col.size();
+    o[1] = (int64_t)M->h.blocks.near_col.size();
+    o[2] = (int64_t)M->h.blocks.near_entries;
+    o[3] = (int64_t)M->h.blocks.depth;
+    o[4] = (int64_t)M->h.tree.n_nodes();
+  });
+}
+
+int rs_metric_blocks(rs_metric *M, uint32_t *far_ptr, uint32_t *far_col, uint32_t *near_ptr,
+                     uint32_t *near_col) {
+  return guard([&] {
+    const Blocks &B = M->h.blocks;
+    std::copy(B.far_ptr.begin(), B.far_ptr.end(), far_ptr);
+    std::copy(B.far_col.begin(), B.far_col.end(), far_col);
+    std::copy(B.near_ptr.begin(), B.near_ptr.end(), near_ptr);
+    std::copy(B.near_col.begin(), B.near_col.end(), near_col);
+  });
+}
+
+int rs_metric_profile(rs_metric *M, double w_hi, double w_lo, int nb, int reps, char *names,
+                      int names_len, double *ms, int max_kernels, int *n_kernels) {
+  return guard([&] {
+    M->h.ctx->use();
+    size_t n = (size_t)nb * 3 * M->nv;
+    if (M->xbuf.n < n) M->xbuf.alloc(n), M->ybuf.alloc(n);
+    RSG_CUDA("product", cudaMemsetAsync(M->xbuf.p, 0, n * sizeof(double), M->h.st()));
+    M->h.prof.start();
+    for (int r = 0; r < reps; ++r) metric_apply(M, w_hi, w_lo, nb, M->xbuf.p, M->ybuf.p);
+    M->h.prof.stop(M->h.st());
+    M->h.prof.report(names, names_len, ms, max_kernels, n_kernels, reps);
+  });
+}
+
+int rs_vfrac_build(rs_ctx *ctx, int nv, const double *positions_host, const double *mass_host,
+                   double tau, double chi, int leaf_size, int leaf_pairs, rs_vfrac **out) {
+  *out = nullptr;
+  return guard([&] {
+    if (!std::isfinite(tau) || nv <= 0)
+      fail(RS_INVALID_OPTION, "InvalidOption", "upload", "a finite order and at least one vertex");
+    for (int v = 0; v < nv; ++v)
+      if (!(std::isfinite(mass_host[v]) && mass_host[v] > 0.0))
+        fail(RS_INVALID_OPTION, "InvalidOption", "upload", "positive finite vertex areas");
+    ctx->use();
+    auto V = std::make_unique<rs_vfrac>();
+    V->nv = nv;
+    // vertex elements: point f_v, box of the point, mass a_v (hierarchical.rs:1041-1058)
+    std::vector<double> ebox(6 * (size_t)nv);
+    for (int v = 0; v < nv; ++v)
+      for (int k = 0; k < 3; ++k) ebox[6 * v + k] = ebox[6 * v + 3 + k] = positions_host[3 * v + k];
+    Tree T = build_tree((size_t)nv, positions_host, ebox.data(), mass_host, leaf_size);
+    V->h.kind = VERTEX;
+    V->h.n_el = nv;
+    V->h.neg_s = -(tau + 1.0);
+    V->h.build_common(ctx, std::move(T), chi, leaf_pairs);
+    up_vec(V->order, V->h.tree.order, V->h.st());
+    V->h.setup(positions_host, mass_host, nullptr, nullptr);
+    *out = V.release();
+  });
+}
+
+void rs_vfrac_free(rs_vfrac *V) {
+  if (!V) return;
+  cudaSetDevice(V->h.ctx->device);
+  cudaStreamSynchronize(V->h.ctx->stream);
+  delete V;
+}
+
+int rs_vfrac_apply(rs_vfrac *V, int nb, const double *xs_host, double *ys_host) {
+  return guard([&] {
+    V->h.ctx->use();
+    size_t n = (size_t)nb * 3 * V->nv;
+    host_io(V->h.ctx, V->xbuf, V->ybuf, n, xs_host, ys_host,
+            [&](const double *x, double *y) { vfrac_apply(V, 1.0, nb, x, y); });
+  });
+}
+
+int rs_vfrac_apply_device(rs_vfrac *V, int nb, const double *xs_dev, double *ys_dev) {
+  return guard([&] {
+    V->h.ctx->use();
+    vfrac_apply(V, 1.0, nb, xs_dev, ys_dev);
+  });
+}
+
+int rs_vfrac_stats(rs_vfrac *V, int64_t *o) {
+  return guard([&] {
+    o[0] = (int64_t)V->h.blocks.far_col.size();
+    o[1] = (int64_t)V->h.blocks.near_col.size();
+    o[2] = (int64_t)V->h.blocks.near_entries;
+    o[3] = (int64_t)V->h.blocks.depth;
+    o[4] = (int64_t)V->h.tree.n_nodes();
+  });
+}
+
+}  // extern "C"

@@ -82,6 +82,19 @@ def load_library(path: str | os.PathLike | None = None):
         "rs_bh_culprit": [_vp, _i64p],
         "rs_bh_profile": [_vp, C.c_double, C.c_double, C.c_int, C.c_char_p, C.c_int, _f64p,
                           C.c_int, C.POINTER(C.c_int)],
+        "rs_metric_build": [_vp, C.c_int, C.c_int, _u32p, _f64p, C.c_double, C.c_double, C.c_double,
+                            C.c_int, C.c_int, C.POINTER(_vp)],
+        "rs_metric_apply": [_vp, C.c_double, C.c_double, C.c_int, _f64p, _f64p],
+        "rs_metric_apply_device": [_vp, C.c_double, C.c_double, C.c_int, _vp, _vp],
+        "rs_metric_stats": [_vp, _i64p],
+        "rs_metric_blocks": [_vp, _u32p, _u32p, _u32p, _u32p],
+        "rs_metric_profile": [_vp, C.c_double, C.c_double, C.c_int, C.c_int, C.c_char_p, C.c_int,
+                              _f64p, C.c_int, C.POINTER(C.c_int)],
+        "rs_vfrac_build": [_vp, C.c_int, _f64p, _f64p, C.c_double, C.c_double, C.c_int, C.c_int,
+                           C.POINTER(_vp)],
+        "rs_vfrac_apply": [_vp, C.c_int, _f64p, _f64p],
+        "rs_vfrac_apply_device": [_vp, C.c_int, _vp, _vp],
+        "rs_vfrac_stats": [_vp, _i64p],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -89,8 +102,9 @@ def load_library(path: str | os.PathLike | None = None):
         f.restype = C.c_int
     L.rs_ctx_free.argtypes = [_vp]
     L.rs_ctx_free.restype = None
-    L.rs_bh_free.argtypes = [_vp]
-    L.rs_bh_free.restype = None
+    for name in ("rs_bh_free", "rs_metric_free", "rs_vfrac_free"):
+        getattr(L, name).argtypes = [_vp]
+        getattr(L, name).restype = None
     _lib = L
     return L
 
@@ -359,3 +373,103 @@ def energy(faces, positions, exponents: Exponents = Exponents(), eval=None,
     return EnergyReport(energy=E, differential=dE, subcritical=exponents.beta - exponents.alpha <= 4.0,
                         pairs_exact=s["pairs_exact"], nodes_lumped=s["n_lumped"],
                         seconds=time.perf_counter() - t0)
+
+
+@dataclass(frozen=True)
+class ClusterTreeOptions:
+    """Block cluster tree parameters (RS/src/metric/hierarchical.rs:63-108)."""
+
+    chi: float = 0.5
+    leaf_size: int = 8
+    leaf_pairs: int = 64
+
+
+def _profile_dict(names, ms, n):
+    raw = names.raw.split(b"\0")[: n.value]
+    return {k.decode(): float(v) for k, v in zip(raw, ms[: n.value])}
+
+
+class FaceMetricTree:
+    """The hierarchical Hs metric w_hi B~ + w_lo B~0 on the GPU (FaceMetricTree + GpuFaceMetric,
+    RS/src/metric/hierarchical.rs:279-812)."""
+
+    def __init__(self, faces, positions, exponents: Exponents = Exponents(),
+                 opts: ClusterTreeOptions = ClusterTreeOptions(), ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        faces, positions = _mesh(faces, positions)
+        self.n_vertices, self.n_faces = len(positions), len(faces)
+        h = _vp()
+        _check(_lib.rs_metric_build(self.ctx.handle, len(positions), len(faces), faces.ravel(),
+                                    positions.ravel(), exponents.alpha, exponents.beta, opts.chi,
+                                    opts.leaf_size, opts.leaf_pairs, C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.rs_metric_free(self._h)
+            self._h = None
+
+    def apply(self, x, w_hi: float = 1.0, w_lo: float = 1.0):
+        """y = (w_hi B~ + w_lo B~0) x for x of shape (3V,) or (nb, 3V) (interleaved 3 v + axis)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        xs = x.reshape(-1, 3 * self.n_vertices)
+        ys = np.empty_like(xs)
+        _check(_lib.rs_metric_apply(self._h, w_hi, w_lo, len(xs), xs.ravel(), ys.ravel()))
+        return ys.reshape(x.shape)
+
+    def apply_device(self, xs_ptr: int, ys_ptr: int, nb: int, w_hi=1.0, w_lo=1.0):
+        _check(_lib.rs_metric_apply_device(self._h, w_hi, w_lo, nb, _vp(xs_ptr), _vp(ys_ptr)))
+
+    def stats(self) -> dict:
+        o = np.zeros(5, np.int64)
+        _check(_lib.rs_metric_stats(self._h, o))
+        return dict(zip(["far_blocks", "near_blocks", "near_entries", "depth", "nodes"], map(int, o)))
+
+    def blocks(self) -> dict:
+        s = self.stats()
+        nn = s["nodes"]
+        fp, np_ = np.empty(nn + 1, np.uint32), np.empty(nn + 1, np.uint32)
+        fc = np.empty(max(s["far_blocks"], 1), np.uint32)
+        nc = np.empty(max(s["near_blocks"], 1), np.uint32)
+        _check(_lib.rs_metric_blocks(self._h, fp, fc, np_, nc))
+        return dict(far_ptr=fp, far_col=fc[: s["far_blocks"]], near_ptr=np_, near_col=nc[: s["near_blocks"]])
+
+    def profile(self, nb: int = 3, reps: int = 5, w_hi=1.0, w_lo=1.0) -> dict:
+        names = C.create_string_buffer(4096)
+        ms = np.zeros(32)
+        n = C.c_int()
+        _check(_lib.rs_metric_profile(self._h, w_hi, w_lo, nb, reps, names, 4096, ms, 32, C.byref(n)))
+        return _profile_dict(names, ms, n)
+
+
+class VertexFractionalTree:
+    """The vertex-pair fractional operator L^V_tau on the GPU (VertexFractionalTree +
+    GpuVertexFractional, RS/src/metric/hierarchical.rs:998-1346)."""
+
+    def __init__(self, positions, mass, tau: float, opts: ClusterTreeOptions = ClusterTreeOptions(),
+                 ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        positions = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        mass = np.ascontiguousarray(mass, dtype=np.float64)
+        self.n_vertices = len(positions)
+        h = _vp()
+        _check(_lib.rs_vfrac_build(self.ctx.handle, len(positions), positions.ravel(), mass, float(tau),
+                                   opts.chi, opts.leaf_size, opts.leaf_pairs, C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.rs_vfrac_free(self._h)
+            self._h = None
+
+    def apply(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        xs = x.reshape(-1, 3 * self.n_vertices)
+        ys = np.empty_like(xs)
+        _check(_lib.rs_vfrac_apply(self._h, len(xs), xs.ravel(), ys.ravel()))
+        return ys.reshape(x.shape)
+
+    def stats(self) -> dict:
+        o = np.zeros(5, np.int64)
+        _check(_lib.rs_vfrac_stats(self._h, o))
+        return dict(zip(["far_blocks", "near_blocks", "near_entries", "depth", "nodes"], map(int, o)))

@@ -156,6 +156,45 @@ int rs_bh_culprit(rs_bh *bh, int64_t *faces2);
 int rs_bh_profile(rs_bh *bh, double alpha, double beta, int reps, char *names, int names_len,
                   double *ms, int max_kernels, int *n_kernels);
 
+/* ---------------------------------------------------------------- Hs metric (H-matrix) */
+
+typedef struct rs_metric rs_metric; /* FaceMetricTree + GpuFaceMetric (RS/src/metric/hierarchical.rs:279-812) */
+typedef struct rs_vfrac rs_vfrac;   /* VertexFractionalTree + GpuVertexFractional (hierarchical.rs:998-1346) */
+
+/* FaceMetricTree::build / build_on_gpu (hierarchical.rs:302-468): face BVH (leaf_size <= 8),
+ * block cluster tree of h_hi = rho^-2s and h_lo = (nu_S^2 + nu_T^2)/2 rho^-4 rho^-2s with
+ * separation chi and leaf_pairs (ClusterTreeOptions, hierarchical.rs:63-108; defaults 0.5,
+ * 8, 64), far coefficients, and the far part of H~a. The near field is evaluated in every
+ * product on the device, not stored. */
+int rs_metric_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces,
+                    const double *positions_host, double alpha, double beta, double chi,
+                    int leaf_size, int leaf_pairs, rs_metric **out);
+void rs_metric_free(rs_metric *m);
+/* GpuFaceMetric::apply_batch (RS/src/gpu/mod.rs:318-341, hierarchical.rs:540-622):
+ * ys = (w_hi B~ + w_lo B~0) xs for nb interleaved 3V vectors (stacked). */
+int rs_metric_apply(rs_metric *m, double w_hi, double w_lo, int nb, const double *xs_host,
+                    double *ys_host);
+int rs_metric_apply_device(rs_metric *m, double w_hi, double w_lo, int nb, const double *xs_dev,
+                           double *ys_dev);
+/* BctStats (far blocks, near blocks, near entries, depth, nodes). */
+int rs_metric_stats(rs_metric *m, int64_t *out5);
+/* The blocks grouped by row node: far_ptr [nodes+1], far_col, near_ptr [nodes+1], near_col. */
+int rs_metric_blocks(rs_metric *m, uint32_t *far_ptr, uint32_t *far_col, uint32_t *near_ptr,
+                     uint32_t *near_col);
+/* Per-kernel average device time of `reps` products of nb vectors (as rs_bh_profile). */
+int rs_metric_profile(rs_metric *m, double w_hi, double w_lo, int nb, int reps, char *names,
+                      int names_len, double *ms, int max_kernels, int *n_kernels);
+
+/* VertexFractionalTree::build / build_on_gpu (hierarchical.rs:1017-1151): vertex BVH with
+ * masses `mass_host` (dual areas), kernel |f_v - f_w|^-(2 tau + 2). */
+int rs_vfrac_build(rs_ctx *ctx, int nv, const double *positions_host, const double *mass_host,
+                   double tau, double chi, int leaf_size, int leaf_pairs, rs_vfrac **out);
+void rs_vfrac_free(rs_vfrac *v);
+/* GpuVertexFractional::apply_batch (RS/src/gpu/mod.rs:361-371): ys = L^V_tau xs. */
+int rs_vfrac_apply(rs_vfrac *v, int nb, const double *xs_host, double *ys_host);
+int rs_vfrac_apply_device(rs_vfrac *v, int nb, const double *xs_dev, double *ys_dev);
+int rs_vfrac_stats(rs_vfrac *v, int64_t *out5);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,49 @@
+// Smoothed-aggregation algebraic multigrid for the preconditioner's Laplacian block
+// K = W + eps M (RS/src/solve/precond.rs:157-460 factors L' by a sparse LDL^T on the CPU; this
+// library solves it with multigrid V-cycles on the device instead, see saddle.cu).
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include "common.hpp"
+
+namespace rsg {
+
+struct Csr {
+  int n = 0, m = 0;  // rows, columns
+  std::vector<int> ptr, col;
+  std::vector<double> val;
+};
+
+// Host setup: strength (|a_ij| >= 0.08 sqrt(a_ii a_jj)), greedy aggregation, the tentative
+// prolongator of the constant near-null space, one damped-Jacobi smoothing step
+// (omega = 4 / (3 rho(D^-1 A))), Galerkin coarse operators, down to at most `coarse_max` rows;
+// the coarsest operator is inverted densely after adding z z^T (z its null vector).
+struct AmgHost {
+  std::vector<Csr> A, P, R;  // A[l] n_l x n_l, P[l] n_l x n_{l+1}, R[l] = P[l]^T
+  std::vector<std::vector<double>> dinv;  // damped inverse diagonals of A[l]
+  std::vector<double> coarse_inv;         // dense n_L x n_L
+};
+AmgHost amg_setup(const Csr &A, int coarse_max = 300, int max_levels = 12);
+
+// The hierarchy on the device and its V-cycle for C interleaved columns per row
+// (x[row * C + c]): pre- and post-smoothing by `sweeps` damped Jacobi steps, dense coarse solve.
+struct AmgDevice {
+  struct Level {
+    int n = 0;
+    DevBuf<int> ap, ac, pp, pc, rp, rc;
+    DevBuf<double> av, pv, rv, dinv;
+    DevBuf<double> x, b, r, t;  // C columns each
+  };
+  std::vector<Level> L;
+  DevBuf<double> cinv;
+  int C = 0, sweeps = 2;
+  void upload(const AmgHost &h, cudaStream_t s);
+  void reserve(int C_);
+  // x = V-cycle(b) on level 0; b and x are n_0 x C device arrays (x overwritten).
+  void vcycle(rs_ctx *ctx, const double *b, double *x, int C_);
+  // y = A_0 x for C columns.
+  void spmv0(rs_ctx *ctx, const double *x, double *y, int C_);
+};
+
+}  // namespace rsg

@@ -29,6 +29,7 @@
 #include "block_tree.hpp"
 #include "common.hpp"
 #include "host_tree.hpp"
+#include "hmat.hpp"
 #include "profile.hpp"
 
 namespace rsg {
@@ -223,16 +224,16 @@ struct FaceOps {
 // m per face in BVH order (FaceMetricTree::product, hierarchical.rs:711-746): per vector q,
 // 9 gradient channels 9q + 3k + r = sum_c x[3 t_c + k] g_c[r], then 3 average channels
 // 9 nb + 3q + k = (x_0 + x_1 + x_2)/3 for axis k.
-__global__ void face_m_kernel(FaceOps o, const double *__restrict__ xs, int nb, int C, float *m) {
+__global__ void face_m_kernel(FaceOps o, const double *__restrict__ xs, size_t ldx, int nb, int C,
+                              float *m) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= o.nf) return;
   uint32_t f = o.order[p];
   const uint32_t *t = o.faces + 3 * (size_t)f;
   const float *g = o.g + 9 * (size_t)f;
   float *mp = m + (size_t)p * C;
-  const size_t n3 = 3 * (size_t)o.nv;
   for (int q = 0; q < nb; ++q) {
-    const double *x = xs + q * n3;
+    const double *x = xs + q * ldx;
     for (int k = 0; k < 3; ++k) {
       float x0 = (float)x[3 * (size_t)t[0] + k], x1 = (float)x[3 * (size_t)t[1] + k],
             x2 = (float)x[3 * (size_t)t[2] + k];
@@ -245,10 +246,9 @@ __global__ void face_m_kernel(FaceOps o, const double *__restrict__ xs, int nb, 
 
 // y_v = 2 sum_{S ni v} a_S (w_hi g_c . z_hi + w_lo z_lo / 3) in FP64 (hierarchical.rs:779-811).
 __global__ void face_gather_kernel(FaceOps o, const float *__restrict__ z, int nb, int C,
-                                   double w_hi, double w_lo, double *__restrict__ ys) {
+                                   double w_hi, double w_lo, double *__restrict__ ys, size_t ldy) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= o.nv) return;
-  const size_t n3 = 3 * (size_t)o.nv;
   for (int q = 0; q < nb; ++q) {
     double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0;
     for (uint32_t e = o.inc_off[v]; e < o.inc_off[v + 1]; ++e) {
@@ -264,7 +264,7 @@ __global__ void face_gather_kernel(FaceOps o, const float *__restrict__ z, int n
       }
       acc0 += acc[0], acc1 += acc[1], acc2 += acc[2];
     }
-    double *y = ys + q * n3 + 3 * (size_t)v;
+    double *y = ys + q * ldy + 3 * (size_t)v;
     y[0] = 2.0 * acc0, y[1] = 2.0 * acc1, y[2] = 2.0 * acc2;
   }
 }
@@ -272,27 +272,27 @@ __global__ void face_gather_kernel(FaceOps o, const float *__restrict__ z, int n
 // ------------------------------------------------------------------ vertex prologue / epilogue
 
 // psi channels of the vertex operator: m = x per axis (ψ = a x in the upward/near sums).
-__global__ void vertex_m_kernel(const uint32_t *order, const double *__restrict__ xs, int nv,
-                                int nb, int C, float *m) {
+__global__ void vertex_m_kernel(const uint32_t *order, const double *__restrict__ xs, size_t ldx,
+                                int nv, int nb, int C, float *m) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= nv) return;
   uint32_t v = order[p];
   float *mp = m + (size_t)p * C;
   for (int q = 0; q < nb; ++q)
-    for (int k = 0; k < 3; ++k) mp[3 * q + k] = (float)xs[q * 3 * (size_t)nv + 3 * (size_t)v + k];
+    for (int k = 0; k < 3; ++k) mp[3 * q + k] = (float)xs[q * ldx + 3 * (size_t)v + k];
   for (int c = 3 * nb; c < C; ++c) mp[c] = 0.f;
 }
 
 // y = 2 a (H~a x - H~(a x)) = 2 a z (hierarchical.rs:1330-1343).
 __global__ void vertex_out_kernel(const uint32_t *order, const float4 *el, const float *z, int nv,
-                                  int nb, int C, double scale, double *__restrict__ ys) {
+                                  int nb, int C, double scale, double *__restrict__ ys, size_t ldy) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= nv) return;
   uint32_t v = order[p];
   double a = el[p].w;
   for (int q = 0; q < nb; ++q)
     for (int k = 0; k < 3; ++k)
-      ys[q * 3 * (size_t)nv + 3 * (size_t)v + k] = scale * 2.0 * a * (double)z[(size_t)p * C + 3 * q + k];
+      ys[q * ldy + 3 * (size_t)v + k] = scale * 2.0 * a * (double)z[(size_t)p * C + 3 * q + k];
 }
 
 // Element records relative to the leaf centroids, node centroids as float pairs; FP64 in.
@@ -600,44 +600,50 @@ void metric_setup(rs_metric *M, rs_ctx *ctx, int nv, int nf, const uint32_t *fac
   M->h.setup(M->geom.bary.data(), M->geom.area.data(), M->geom.normal.data(), proj.data());
 }
 
-// FaceMetricTree::apply_batch (hierarchical.rs:540-622) on device vectors: groups of <= 3.
-void metric_apply(rs_metric *M, double w_hi, double w_lo, int nb, const double *xs, double *ys) {
+}  // namespace
+
+// FaceMetricTree::apply_batch (hierarchical.rs:540-622) on device vectors with leading
+// dimensions ldx, ldy (>= 3V): groups of <= 3 vectors per tree pass.
+void rsg::metric_apply_strided(rs_metric *M, double w_hi, double w_lo, int nb, const double *xs,
+                               size_t ldx, double *ys, size_t ldy) {
   if (!(std::isfinite(w_hi) && std::isfinite(w_lo)))
     fail(RS_INVALID_OPTION, "InvalidOption", "product", "finite weights");
   cudaStream_t s = M->h.st();
-  size_t n3 = 3 * (size_t)M->nv;
   for (int q0 = 0; q0 < nb; q0 += 3) {
     int k = std::min(3, nb - q0);
     int CC = 12 * k;
     M->h.reserve(CC);
     M->h.prof.begin(s, "metric_m");
-    face_m_kernel<<<nblk(M->nf, 256), 256, 0, s>>>(M->ops(), xs + q0 * n3, k, CC, M->h.m.p);
+    face_m_kernel<<<nblk(M->nf, 256), 256, 0, s>>>(M->ops(), xs + q0 * ldx, ldx, k, CC, M->h.m.p);
     RSG_LAUNCHED(M->h.ctx, "face_m");
     M->h.prof.end(s);
     M->h.product(CC, 9 * k);
     M->h.prof.begin(s, "metric_gather");
     face_gather_kernel<<<nblk(M->nv, 128), 128, 0, s>>>(M->ops(), M->h.z.p, k, CC, w_hi, w_lo,
-                                                        ys + q0 * n3);
+                                                        ys + q0 * ldy, ldy);
     RSG_LAUNCHED(M->h.ctx, "face_gather");
     M->h.prof.end(s);
   }
 }
 
-void vfrac_apply(rs_vfrac *V, double scale, int nb, const double *xs, double *ys) {
+// VertexFractionalTree::apply_batch (hierarchical.rs:1274-1345) scaled by `scale`.
+void rsg::vfrac_apply_strided(rs_vfrac *V, double scale, int nb, const double *xs, size_t ldx,
+                              double *ys, size_t ldy) {
   cudaStream_t s = V->h.st();
-  size_t n3 = 3 * (size_t)V->nv;
   for (int q0 = 0; q0 < nb; q0 += 3) {
     int k = std::min(3, nb - q0);
     int CC = 4 * k;  // 3 k channels padded to a multiple of 4
     V->h.reserve(CC);
-    vertex_m_kernel<<<nblk(V->nv, 256), 256, 0, s>>>(V->order.p, xs + q0 * n3, V->nv, k, CC, V->h.m.p);
+    vertex_m_kernel<<<nblk(V->nv, 256), 256, 0, s>>>(V->order.p, xs + q0 * ldx, ldx, V->nv, k, CC, V->h.m.p);
     RSG_LAUNCHED(V->h.ctx, "vertex_m");
     V->h.product(CC, CC);
     vertex_out_kernel<<<nblk(V->nv, 256), 256, 0, s>>>(V->order.p, V->h.el.p, V->h.z.p, V->nv, k, CC,
-                                                       scale, ys + q0 * n3);
+                                                       scale, ys + q0 * ldy, ldy);
     RSG_LAUNCHED(V->h.ctx, "vertex_out");
   }
 }
+
+namespace {
 
 template <class F>
 void host_io(rs_ctx *ctx, DevBuf<double> &xb, DevBuf<double> &yb, size_t n, const double *xh,
@@ -681,7 +687,7 @@ int rs_metric_apply(rs_metric *M, double w_hi, double w_lo, int nb, const double
     M->h.ctx->use();
     size_t n = (size_t)nb * 3 * M->nv;
     host_io(M->h.ctx, M->xbuf, M->ybuf, n, xs_host, ys_host,
-            [&](const double *x, double *y) { metric_apply(M, w_hi, w_lo, nb, x, y); });
+            [&](const double *x, double *y) { metric_apply_strided(M, w_hi, w_lo, nb, x, 3 * (size_t)M->nv, y, 3 * (size_t)M->nv); });
   });
 }
 
@@ -689,7 +695,7 @@ int rs_metric_apply_device(rs_metric *M, double w_hi, double w_lo, int nb, const
                            double *ys_dev) {
   return guard([&] {
     M->h.ctx->use();
-    metric_apply(M, w_hi, w_lo, nb, xs_dev, ys_dev);
+    metric_apply_strided(M, w_hi, w_lo, nb, xs_dev, 3 * (size_t)M->nv, ys_dev, 3 * (size_t)M->nv);
   });
 }
 
@@ -722,7 +728,8 @@ int rs_metric_profile(rs_metric *M, double w_hi, double w_lo, int nb, int reps, 
     if (M->xbuf.n < n) M->xbuf.alloc(n), M->ybuf.alloc(n);
     RSG_CUDA("product", cudaMemsetAsync(M->xbuf.p, 0, n * sizeof(double), M->h.st()));
     M->h.prof.start();
-    for (int r = 0; r < reps; ++r) metric_apply(M, w_hi, w_lo, nb, M->xbuf.p, M->ybuf.p);
+    for (int r = 0; r < reps; ++r)
+      metric_apply_strided(M, w_hi, w_lo, nb, M->xbuf.p, 3 * (size_t)M->nv, M->ybuf.p, 3 * (size_t)M->nv);
     M->h.prof.stop(M->h.st());
     M->h.prof.report(names, names_len, ms, max_kernels, n_kernels, reps);
   });
@@ -767,14 +774,14 @@ int rs_vfrac_apply(rs_vfrac *V, int nb, const double *xs_host, double *ys_host) 
     V->h.ctx->use();
     size_t n = (size_t)nb * 3 * V->nv;
     host_io(V->h.ctx, V->xbuf, V->ybuf, n, xs_host, ys_host,
-            [&](const double *x, double *y) { vfrac_apply(V, 1.0, nb, x, y); });
+            [&](const double *x, double *y) { vfrac_apply_strided(V, 1.0, nb, x, 3 * (size_t)V->nv, y, 3 * (size_t)V->nv); });
   });
 }
 
 int rs_vfrac_apply_device(rs_vfrac *V, int nb, const double *xs_dev, double *ys_dev) {
   return guard([&] {
     V->h.ctx->use();
-    vfrac_apply(V, 1.0, nb, xs_dev, ys_dev);
+    vfrac_apply_strided(V, 1.0, nb, xs_dev, 3 * (size_t)V->nv, ys_dev, 3 * (size_t)V->nv);
   });
 }
 

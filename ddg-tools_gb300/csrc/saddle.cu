@@ -1,0 +1,592 @@
+// The hierarchical saddle solver of one step on the GPU (HierarchicalSaddle =
+// GmresSaddle<HierarchicalOperator, SparsePreconditioner>, RS/src/solve/iterative.rs:126-575,
+// RS/src/solve/precond.rs, RS/src/solve/gmres.rs) and the constrained direction
+// (SchurComplement, RS/src/solve/schur.rs), behind rs_solver_* of include/rsgpu.h.
+//
+//   A' [x; l] = [ w (B~ + c_lo B~0) x + C_Q^T l ; C_Q x ]                       (operator)
+//   P^-1 = L'^-1 + L'^-1 blockdiag((s L^V_{2-s} - K) x I3, 0) L'^-1             (augmented form)
+//   L' = [[K x I3, C_Q^T], [C_Q, 0]],  K = W + eps M
+//
+// C_Q holds the barycenter rows (global or per component: c_v = a_v / A_group per axis). The
+// reference factors L' by a sparse LDL^T; here L'^-1 is applied as: mu = 1_g^T r - eps A_g b
+// per group and axis (exact: 1^T K = eps m^T), y = MG(K, r - c mu) by smoothed-aggregation
+// multigrid V-cycles, then y is shifted by a constant per group so that C_Q y = b holds
+// exactly. The preconditioner is a fixed linear map (fixed V-cycles), so plain right
+// preconditioning applies; GMRES stores the preconditioned vectors anyway (flexible form).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <memory>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "amg.hpp"
+#include "common.hpp"
+#include "hmat.hpp"
+#include "host_tree.hpp"
+#include "krylov.hpp"
+
+namespace rsg {
+
+namespace {
+
+inline unsigned nblk(size_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
+constexpr int GB = 128;  // reduction blocks of the group sums
+
+// part[b][q][3 g + k] = sum over the block's vertices v of group g of wgt_v x_q[3 v + k]
+// (wgt = null: weight 1). x has leading dimension ld; G groups.
+__global__ void group_sums_partial(const double *__restrict__ x, size_t ld, int nb, int nv,
+                                   const uint32_t *__restrict__ group, const double *__restrict__ wgt,
+                                   int G, double *part) {
+  extern __shared__ double sh[];  // 3 G nb per block
+  const int K = 3 * G * nb;
+  for (int i = threadIdx.x; i < K; i += blockDim.x) sh[i] = 0.0;
+  __syncthreads();
+  const size_t chunk = (nv + gridDim.x - 1) / gridDim.x;
+  const size_t v0 = blockIdx.x * chunk, v1 = min((size_t)nv, v0 + chunk);
+  // each thread accumulates privately over a strided subset, then a fixed-order tree
+  for (int q = 0; q < nb; ++q)
+    for (int g = 0; g < G; ++g)
+      for (int k = 0; k < 3; ++k) {
+        double acc = 0.0;
+        for (size_t v = v0 + threadIdx.x; v < v1; v += blockDim.x)
+          if ((int)group[v] == g) acc += (wgt ? wgt[v] : 1.0) * x[q * ld + 3 * v + k];
+        // warp tree then lane-0 adds in warp order
+        for (int m = 16; m >= 1; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
+        __shared__ double wsum[32];
+        if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          double t = 0.0;
+          for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += wsum[w];
+          sh[(q * G + g) * 3 + k] = t;
+        }
+        __syncthreads();
+      }
+  for (int i = threadIdx.x; i < K; i += blockDim.x) part[(size_t)blockIdx.x * K + i] = sh[i];
+}
+
+__global__ void group_sums_final(const double *part, int nblocks, int K, double *out) {
+  int i = threadIdx.x + blockIdx.x * blockDim.x;
+  if (i >= K) return;
+  double s = 0.0;
+  for (int b = 0; b < nblocks; ++b) s += part[(size_t)b * K + i];
+  out[i] = s;
+}
+
+// Operator tail: y_pos += c_v l_{g(v)} and y_mult = C_Q x (from the group sums `cx`).
+__global__ void cq_apply_kernel(const double *__restrict__ x, double *__restrict__ y, size_t ld,
+                                int nb, int nv, const uint32_t *__restrict__ group,
+                                const double *__restrict__ c, int G, const double *__restrict__ cx) {
+  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  size_t nd = 3 * (size_t)nv;
+  if (t >= (size_t)nb * (nd + 3 * G)) return;
+  int q = (int)(t / (nd + 3 * G));
+  size_t i = t % (nd + 3 * G);
+  if (i < nd) {
+    size_t v = i / 3;
+    int k = (int)(i % 3);
+    y[q * ld + i] += c[v] * x[q * ld + nd + 3 * group[v] + k];
+  } else {
+    y[q * ld + i] = cx[(size_t)q * 3 * G + (i - nd)];
+  }
+}
+
+// mu = 1_g^T r - eps A_g b (per vector, group, axis), from the group sums s1 = 1_g^T r.
+__global__ void mu_kernel(const double *__restrict__ s1, const double *__restrict__ r, size_t ld,
+                          size_t nd, int nb, int G, const double *__restrict__ eps_area, double *mu) {
+  int t = threadIdx.x + blockIdx.x * blockDim.x;
+  if (t >= nb * 3 * G) return;
+  int q = t / (3 * G), i = t % (3 * G), g = i / 3;
+  mu[t] = s1[t] - eps_area[g] * r[q * ld + nd + i];
+}
+
+// AMG layout [v][3 nb] <- r_q[3 v + k] - c_v mu_{q, g(v), k}
+__global__ void to_mg_kernel(const double *__restrict__ r, size_t ld, int nb, int nv,
+                             const uint32_t *__restrict__ group, const double *__restrict__ c,
+                             const double *__restrict__ mu, int G, double *__restrict__ out) {
+  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= (size_t)nv * 3 * nb) return;
+  size_t v = t / (3 * nb);
+  int col = (int)(t % (3 * nb)), q = col / 3, k = col % 3;
+  double sub = mu ? c[v] * mu[(size_t)q * 3 * G + 3 * group[v] + k] : 0.0;
+  out[t] = r[q * ld + 3 * v + k] - sub;
+}
+
+// y_q[3 v + k] = yy[v][3 q + k] + shift_{q, g(v), k}, y_q[nd + 3 g + k] = mu (multipliers).
+__global__ void from_mg_kernel(const double *__restrict__ yy, double *__restrict__ y, size_t ld,
+                               int nb, int nv, const uint32_t *__restrict__ group, int G,
+                               const double *__restrict__ shift, const double *__restrict__ mu,
+                               const double *__restrict__ add) {
+  size_t nd = 3 * (size_t)nv;
+  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= (size_t)nb * (nd + 3 * G)) return;
+  int q = (int)(t / (nd + 3 * G));
+  size_t i = t % (nd + 3 * G);
+  double val;
+  if (i < nd) {
+    size_t v = i / 3;
+    int k = (int)(i % 3);
+    val = yy[v * 3 * nb + 3 * q + k] + shift[(size_t)q * 3 * G + 3 * group[v] + k];
+  } else {
+    val = mu[(size_t)q * 3 * G + (i - nd)];
+  }
+  y[q * ld + i] = add ? val + add[q * ld + i] : val;
+}
+
+// shift = b - C_Q y' per vector, group, axis (from the weighted group sums of y').
+__global__ void shift_kernel(const double *__restrict__ cy, const double *__restrict__ r, size_t ld,
+                             size_t nd, int nb, int G, double *shift) {
+  int t = threadIdx.x + blockIdx.x * blockDim.x;
+  if (t >= nb * 3 * G) return;
+  int q = t / (3 * G), i = t % (3 * G);
+  shift[t] = r[q * ld + nd + i] - cy[t];
+}
+
+// v_q[3 u + k] -= (K y)[u][3 q + k] and v_q multipliers = 0
+__global__ void sub_ky_kernel(double *__restrict__ v, size_t ld, int nb, int nv, int G,
+                              const double *__restrict__ ky) {
+  size_t nd = 3 * (size_t)nv;
+  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= (size_t)nb * (nd + 3 * G)) return;
+  int q = (int)(t / (nd + 3 * G));
+  size_t i = t % (nd + 3 * G);
+  if (i < nd) v[q * ld + i] -= ky[(i / 3) * 3 * nb + 3 * q + (i % 3)];
+  else v[q * ld + i] = 0.0;
+}
+
+// yy[v][3q + k] = x_q[3 v + k] (positions only)
+__global__ void pos_to_mg_kernel(const double *__restrict__ x, size_t ld, int nb, int nv,
+                                 double *__restrict__ out) {
+  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= (size_t)nv * 3 * nb) return;
+  size_t v = t / (3 * nb);
+  int col = (int)(t % (3 * nb)), q = col / 3, k = col % 3;
+  out[t] = x[q * ld + 3 * v + k];
+}
+
+// Planar symbol ratio 4 I(sigma) I(2 - s) of W^-1 L_{2-s} W^-1 B, I(t) = pi Gamma(1-t) /
+// (t 4^t Gamma(1+t)) (fractional_symbol_ratio, RS/src/solve/precond.rs:548-568).
+double symbol_ratio(double s) {
+  auto I = [](double t) { return M_PI * std::tgamma(1.0 - t) / (t * std::pow(4.0, t) * std::tgamma(1.0 + t)); };
+  return 4.0 * I(s - 1.0) * I(2.0 - s);
+}
+
+}  // namespace
+
+}  // namespace rsg
+
+using namespace rsg;
+
+struct rs_solver {
+  rs_ctx *ctx = nullptr;
+  int nv = 0, nf = 0, G = 1;
+  size_t nd = 0, n = 0;
+  rs_metric *metric = nullptr;
+  rs_vfrac *vfrac = nullptr;
+  double w_hi = 1.0, w_lo = 1.0, frac_scale = 1.0, eps = 0.0;
+  bool use_prec = true;
+  int vcycles = 1;
+  GmresOptions gopt;
+  FaceGeom geom;
+  std::vector<double> vmass;
+  std::vector<uint32_t> group_h;
+  AmgDevice amg;
+  DevBuf<uint32_t> group;
+  DevBuf<double> c, eps_area, part, s1, mu, cy, shift, mg_in, mg_out, mg_tmp, tmp, tmp2, ky;
+  std::vector<GmresReport> last;
+  Operator op, prec;
+
+  cudaStream_t st() const { return ctx->stream; }
+
+  // group sums (weighted by c or not) of nb vectors into out [nb][3G]
+  void group_sums(const double *x, size_t ld, int nb, const double *wgt, double *out) {
+    int K = 3 * G * nb;
+    if (part.n < (size_t)GB * K) part.alloc((size_t)GB * K);
+    group_sums_partial<<<GB, 256, (size_t)K * sizeof(double), st()>>>(x, ld, nb, nv, group.p, wgt, G, part.p);
+    RSG_LAUNCHED(ctx, "group_sums");
+    group_sums_final<<<nblk(K, 128), 128, 0, st()>>>(part.p, GB, K, out);
+    RSG_LAUNCHED(ctx, "group_sums_final");
+  }
+
+  void reserve(int nb) {
+    size_t K = (size_t)3 * G * nb;
+    if (s1.n < K) s1.alloc(K), mu.alloc(K), cy.alloc(K), shift.alloc(K);
+    size_t m = (size_t)nv * 3 * nb;
+    if (mg_in.n < m) mg_in.alloc(m), mg_out.alloc(m), mg_tmp.alloc(m), ky.alloc(m);
+    if (tmp.n < (size_t)nb * n) tmp.alloc((size_t)nb * n), tmp2.alloc((size_t)nb * n);
+  }
+
+  // A' x
+  void apply_op(int nb, const double *x, double *y) {
+    reserve(nb);
+    metric_apply_strided(metric, w_hi, w_lo, nb, x, n, y, n);
+    group_sums(x, n, nb, c.p, cy.p);
+    size_t tot = (size_t)nb * n;
+    cq_apply_kernel<<<nblk(tot, 256), 256, 0, st()>>>(x, y, n, nb, nv, group.p, c.p, G, cy.p);
+    RSG_LAUNCHED(ctx, "cq_apply");
+  }
+
+  // y = L'^-1 r (+ add)
+  void lsolve(int nb, const double *r, double *y, const double *add) {
+    group_sums(r, n, nb, nullptr, s1.p);
+    mu_kernel<<<nblk(3 * G * nb, 128), 128, 0, st()>>>(s1.p, r, n, nd, nb, G, eps_area.p, mu.p);
+    RSG_LAUNCHED(ctx, "mu");
+    size_t m = (size_t)nv * 3 * nb;
+    to_mg_kernel<<<nblk(m, 256), 256, 0, st()>>>(r, n, nb, nv, group.p, c.p, mu.p, G, mg_in.p);
+    RSG_LAUNCHED(ctx, "to_mg");
+    amg.vcycle(ctx, mg_in.p, mg_out.p, 3 * nb);
+    for (int it = 1; it < vcycles; ++it) {  // further cycles on the residual
+      amg.spmv0(ctx, mg_out.p, ky.p, 3 * nb);
+      // ky = rhs - A y
+      axpby(m, mg_in.p, ky.p);
+      amg.vcycle(ctx, ky.p, mg_tmp.p, 3 * nb);
+      add_into(m, mg_tmp.p, mg_out.p);
+    }
+    // shift: C_Q y = b
+    pos_copy_weighted(nb);
+    shift_kernel<<<nblk(3 * G * nb, 128), 128, 0, st()>>>(cy.p, r, n, nd, nb, G, shift.p);
+    RSG_LAUNCHED(ctx, "shift");
+    size_t tot = (size_t)nb * n;
+    from_mg_kernel<<<nblk(tot, 256), 256, 0, st()>>>(mg_out.p, y, n, nb, nv, group.p, G, shift.p, mu.p, add);
+    RSG_LAUNCHED(ctx, "from_mg");
+  }
+
+  // helpers on the multigrid layout
+  void axpby(size_t m, const double *b, double *y);
+  void add_into(size_t m, const double *x, double *y);
+  void pos_copy_weighted(int nb);
+
+  // z = P^-1 r (augmented form, precond.rs:1026-1079)
+  void apply_prec(int nb, const double *r, double *z) {
+    reserve(nb);
+    double *y = tmp.p, *v = tmp2.p;
+    lsolve(nb, r, y, nullptr);
+    vfrac_apply_strided(vfrac, frac_scale, nb, y, n, v, n);
+    size_t m = (size_t)nv * 3 * nb;
+    pos_to_mg_kernel<<<nblk(m, 256), 256, 0, st()>>>(y, n, nb, nv, mg_in.p);
+    RSG_LAUNCHED(ctx, "pos_to_mg");
+    amg.spmv0(ctx, mg_in.p, ky.p, 3 * nb);
+    size_t tot = (size_t)nb * n;
+    sub_ky_kernel<<<nblk(tot, 256), 256, 0, st()>>>(v, n, nb, nv, G, ky.p);
+    RSG_LAUNCHED(ctx, "sub_ky");
+    lsolve(nb, v, z, y);
+  }
+};
+
+namespace rsg {
+namespace {
+
+__global__ void axpby_kernel(size_t m, const double *b, double *y) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < m) y[i] = b[i] - y[i];
+}
+__global__ void add_kernel(size_t m, const double *x, double *y) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < m) y[i] += x[i];
+}
+// cy[q][3g + k] = sum_{v in g} c_v yy[v][3q + k]  (weighted group sums on the multigrid layout)
+__global__ void mg_group_partial(const double *__restrict__ yy, int nb, int nv,
+                                 const uint32_t *__restrict__ group, const double *__restrict__ c,
+                                 int G, double *part) {
+  const int K = 3 * G * nb;
+  const size_t chunk = (nv + gridDim.x - 1) / gridDim.x;
+  const size_t v0 = blockIdx.x * chunk, v1 = min((size_t)nv, v0 + chunk);
+  __shared__ double wsum[32];
+  for (int i = 0; i < K; ++i) {
+    int q = i / (3 * G), g = (i % (3 * G)) / 3, k = i % 3;
+    double acc = 0.0;
+    for (size_t v = v0 + threadIdx.x; v < v1; v += blockDim.x)
+      if ((int)group[v] == g) acc += c[v] * yy[v * 3 * nb + 3 * q + k];
+    for (int m = 16; m >= 1; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += wsum[w];
+      part[(size_t)blockIdx.x * K + i] = t;
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace
+}  // namespace rsg
+
+void rs_solver::axpby(size_t m, const double *b, double *y) {
+  axpby_kernel<<<nblk(m, 256), 256, 0, st()>>>(m, b, y);
+  RSG_LAUNCHED(ctx, "axpby");
+}
+void rs_solver::add_into(size_t m, const double *x, double *y) {
+  add_kernel<<<nblk(m, 256), 256, 0, st()>>>(m, x, y);
+  RSG_LAUNCHED(ctx, "add");
+}
+void rs_solver::pos_copy_weighted(int nb) {
+  int K = 3 * G * nb;
+  if (part.n < (size_t)GB * K) part.alloc((size_t)GB * K);
+  mg_group_partial<<<GB, 256, 0, st()>>>(mg_out.p, nb, nv, group.p, c.p, G, part.p);
+  RSG_LAUNCHED(ctx, "mg_group");
+  group_sums_final<<<nblk(K, 128), 128, 0, st()>>>(part.p, GB, K, cy.p);
+  RSG_LAUNCHED(ctx, "group_sums_final");
+}
+
+namespace rsg {
+namespace {
+
+// cotan stiffness W (RS/src/geometry.rs:217-249), scalar |V| x |V|, plus eps M on the diagonal.
+Csr laplacian_block(int nv, int nf, const uint32_t *faces, const double *pos, const std::vector<double> &mass,
+                    double eps_rel, double &eps_out) {
+  std::vector<std::vector<std::pair<int, double>>> rows(nv);
+  auto add = [&](int i, int j, double v) { rows[i].push_back({j, v}); };
+  for (int f = 0; f < nf; ++f) {
+    const uint32_t *t = faces + 3 * (size_t)f;
+    for (int c = 0; c < 3; ++c) {
+      const double *p = pos + 3 * (size_t)t[c];
+      const double *p1 = pos + 3 * (size_t)t[(c + 1) % 3];
+      const double *p2 = pos + 3 * (size_t)t[(c + 2) % 3];
+      double u[3] = {p1[0] - p[0], p1[1] - p[1], p1[2] - p[2]};
+      double w[3] = {p2[0] - p[0], p2[1] - p[1], p2[2] - p[2]};
+      double cr[3] = {u[1] * w[2] - u[2] * w[1], u[2] * w[0] - u[0] * w[2], u[0] * w[1] - u[1] * w[0]};
+      double cot = (u[0] * w[0] + u[1] * w[1] + u[2] * w[2]) /
+                   std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+      double h = 0.5 * cot;
+      int a = (int)t[(c + 1) % 3], b = (int)t[(c + 2) % 3];
+      add(a, b, -h), add(b, a, -h), add(a, a, h), add(b, b, h);
+    }
+  }
+  double trw = 0.0, trm = 0.0;
+  Csr K;
+  K.n = K.m = nv;
+  K.ptr.assign(nv + 1, 0);
+  for (int i = 0; i < nv; ++i) {
+    auto &r = rows[i];
+    std::sort(r.begin(), r.end(), [](auto &x, auto &y) { return x.first < y.first; });
+    for (size_t p = 0; p < r.size();) {
+      size_t q = p;
+      double v = 0.0;
+      while (q < r.size() && r[q].first == r[p].first) v += r[q++].second;
+      if (r[p].first == i) trw += v;
+      K.col.push_back(r[p].first);
+      K.val.push_back(v);
+      p = q;
+    }
+    K.ptr[i + 1] = (int)K.col.size();
+    trm += mass[i];
+  }
+  double eps = eps_rel * trw / trm;  // preconditioner_epsilon (RS/src/solve/dense.rs:529-533)
+  for (int i = 0; i < nv; ++i)
+    for (int p = K.ptr[i]; p < K.ptr[i + 1]; ++p)
+      if (K.col[p] == i) K.val[p] += eps * mass[i];
+  eps_out = eps;
+  return K;
+}
+
+std::vector<uint32_t> vertex_components(int nv, int nf, const uint32_t *faces, int &nc) {
+  std::vector<uint32_t> par(nv);
+  std::iota(par.begin(), par.end(), 0u);
+  auto find = [&](uint32_t x) {
+    while (par[x] != x) x = par[x] = par[par[x]];
+    return x;
+  };
+  for (int f = 0; f < nf; ++f)
+    for (int c = 1; c < 3; ++c) {
+      uint32_t a = find(faces[3 * f]), b = find(faces[3 * f + c]);
+      if (a != b) par[std::max(a, b)] = std::min(a, b);
+    }
+  // number components by lowest face index (the crate's component order)
+  std::vector<int64_t> id(nv, -1);
+  std::vector<uint32_t> comp(nv);
+  nc = 0;
+  for (int f = 0; f < nf; ++f) {
+    uint32_t r = find(faces[3 * f]);
+    if (id[r] < 0) id[r] = nc++;
+  }
+  for (int v = 0; v < nv; ++v) comp[v] = (uint32_t)id[find(v)];
+  return comp;
+}
+
+}  // namespace
+}  // namespace rsg
+
+extern "C" {
+
+int rs_solver_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const double *positions_host,
+                    double alpha, double beta, const rs_solver_options *o, rs_solver **out) {
+  *out = nullptr;
+  return guard([&] {
+    rs_solver_options def = rs_solver_options_default();
+    if (!o) o = &def;
+    validate_topology(nv, nf, faces);
+    validate_positions(nv, nf, faces, positions_host);
+    if (!(o->tp_weight > 0.0 && std::isfinite(o->tp_weight)))
+      fail(RS_INVALID_OPTION, "InvalidOption", "solver", "tp_weight must be finite and positive");
+    ctx->use();
+    auto S = std::make_unique<rs_solver>();
+    S->ctx = ctx;
+    S->nv = nv, S->nf = nf, S->nd = 3 * (size_t)nv;
+    S->geom = face_geometry(nf, faces, positions_host);
+    S->vmass.assign(nv, 0.0);
+    for (int f = 0; f < nf; ++f)
+      for (int c = 0; c < 3; ++c) S->vmass[faces[3 * f + c]] += S->geom.area[f] / 3.0;
+    // positional rows: barycenters (global or per component)
+    int ncomp = 0;
+    std::vector<uint32_t> comp = vertex_components(nv, nf, faces, ncomp);
+    bool per_comp = o->barycenter_per_component != 0;
+    S->G = per_comp ? ncomp : 1;
+    S->group_h.assign(nv, 0);
+    if (per_comp) S->group_h = comp;
+    std::vector<double> garea(S->G, 0.0), ch(nv);
+    for (int v = 0; v < nv; ++v) garea[S->group_h[v]] += S->vmass[v];
+    for (int v = 0; v < nv; ++v) ch[v] = S->vmass[v] / garea[S->group_h[v]];
+    S->n = S->nd + 3 * (size_t)S->G;
+    bool multi = !per_comp && ncomp > 1;  // translations_fixed_per_component (precond.rs:96-124)
+    double eps = 0.0;
+    Csr K = laplacian_block(nv, nf, faces, positions_host, S->vmass, multi ? o->eps_multi_rel : o->eps_rel, eps);
+    S->eps = eps;
+    std::vector<double> ea(S->G);
+    for (int g = 0; g < S->G; ++g) ea[g] = eps * garea[g];
+    cudaStream_t s = ctx->stream;
+    S->group.upload(S->group_h, s);
+    S->c.upload(ch, s);
+    S->eps_area.upload(ea, s);
+    // metric and fractional factor
+    rs_metric *m = nullptr;
+    int rc = rs_metric_build(ctx, nv, nf, faces, positions_host, alpha, beta, o->chi, o->leaf_size,
+                             o->leaf_pairs, &m);
+    if (rc) fail(rc, "Gpu", "solver", std::string("metric: ") + rs_last_error());
+    S->metric = m;
+    S->w_hi = o->tp_weight;
+    S->w_lo = o->tp_weight * (o->low_order ? 1.0 : 0.0);
+    double sexp = (beta - 2.0) / alpha;
+    rs_vfrac *vf = nullptr;
+    rc = rs_vfrac_build(ctx, nv, positions_host, S->vmass.data(), 2.0 - sexp, o->chi, o->leaf_size,
+                        o->leaf_pairs, &vf);
+    if (rc) fail(rc, "Gpu", "solver", std::string("fractional tree: ") + rs_last_error());
+    S->vfrac = vf;
+    S->frac_scale = 1.0 / (o->tp_weight * symbol_ratio(sexp));  // FractionalScale::Symbol
+    S->amg.upload(amg_setup(K), s);
+    S->vcycles = std::max(1, o->vcycles);
+    S->use_prec = o->preconditioner != 0;
+    S->gopt.restart = o->restart;
+    S->gopt.tolerance = o->tolerance;
+    S->gopt.max_iterations = o->max_iterations;
+    rs_solver *P = S.get();
+    S->op.n = S->n;
+    S->op.apply = [P](int nb, const double *x, double *y) { P->apply_op(nb, x, y); };
+    S->prec.n = S->n;
+    S->prec.apply = [P](int nb, const double *x, double *y) { P->apply_prec(nb, x, y); };
+    RSG_CUDA("solver", cudaStreamSynchronize(s));
+    *out = S.release();
+  });
+}
+
+void rs_solver_free(rs_solver *S) {
+  if (!S) return;
+  cudaSetDevice(S->ctx->device);
+  cudaStreamSynchronize(S->ctx->stream);
+  rs_metric_free(S->metric);
+  rs_vfrac_free(S->vfrac);
+  delete S;
+}
+
+int rs_solver_dims(rs_solver *S, int64_t *n_dofs, int64_t *n_constraints) {
+  return guard([&] {
+    *n_dofs = (int64_t)S->nd;
+    *n_constraints = (int64_t)(S->n - S->nd);
+  });
+}
+
+int rs_solver_apply_device(rs_solver *S, int nb, const double *x_dev, double *y_dev) {
+  return guard([&] {
+    S->ctx->use();
+    S->apply_op(nb, x_dev, y_dev);
+  });
+}
+
+int rs_solver_precondition_device(rs_solver *S, int nb, const double *r_dev, double *z_dev) {
+  return guard([&] {
+    S->ctx->use();
+    S->apply_prec(nb, r_dev, z_dev);
+  });
+}
+
+int rs_solver_solve_many_device(rs_solver *S, int nb, const double *rhs_dev, double *sol_dev,
+                                double *report) {
+  return guard([&] {
+    S->ctx->use();
+    if (nb < 1 || nb > 4) fail(RS_INVALID_OPTION, "InvalidOption", "solver", "1 to 4 right-hand sides per batch");
+    gmres_batch(S->ctx, S->op, S->use_prec ? &S->prec : nullptr, nb, rhs_dev, sol_dev, S->gopt, S->last);
+    if (report)
+      for (int q = 0; q < nb; ++q) {
+        report[5 * q + 0] = S->last[q].iterations;
+        report[5 * q + 1] = S->last[q].relative_residual;
+        report[5 * q + 2] = S->last[q].converged ? 1.0 : 0.0;
+        report[5 * q + 3] = S->last[q].seconds;
+        report[5 * q + 4] = S->last[q].cycles;
+      }
+  });
+}
+
+// Host-buffer variants: vectors of length n = 3V + k_Q, stacked.
+static void host_roundtrip(rs_solver *S, int nb, const double *in, double *out,
+                           const std::function<void(const double *, double *)> &f) {
+  size_t tot = (size_t)nb * S->n;
+  DevBuf<double> a(tot), b(tot);
+  a.upload(in, tot, S->st());
+  f(a.p, b.p);
+  b.download(out, tot, S->st());
+  RSG_CUDA("solver", cudaStreamSynchronize(S->st()));
+}
+
+int rs_solver_apply(rs_solver *S, int nb, const double *x, double *y) {
+  return guard([&] {
+    S->ctx->use();
+    host_roundtrip(S, nb, x, y, [&](const double *a, double *b) { S->apply_op(nb, a, b); });
+  });
+}
+
+int rs_solver_precondition(rs_solver *S, int nb, const double *r, double *z) {
+  return guard([&] {
+    S->ctx->use();
+    host_roundtrip(S, nb, r, z, [&](const double *a, double *b) { S->apply_prec(nb, a, b); });
+  });
+}
+
+int rs_solver_solve_many(rs_solver *S, int nb, const double *rhs, double *sol, double *report) {
+  return guard([&] {
+    S->ctx->use();
+    if (nb < 1 || nb > 4) fail(RS_INVALID_OPTION, "InvalidOption", "solver", "1 to 4 right-hand sides per batch");
+    host_roundtrip(S, nb, rhs, sol, [&](const double *a, double *b) {
+      gmres_batch(S->ctx, S->op, S->use_prec ? &S->prec : nullptr, nb, a, b, S->gopt, S->last);
+    });
+    if (report)
+      for (int q = 0; q < nb; ++q) {
+        report[5 * q + 0] = S->last[q].iterations;
+        report[5 * q + 1] = S->last[q].relative_residual;
+        report[5 * q + 2] = S->last[q].converged ? 1.0 : 0.0;
+        report[5 * q + 3] = S->last[q].seconds;
+        report[5 * q + 4] = S->last[q].cycles;
+      }
+  });
+}
+
+rs_solver_options rs_solver_options_default(void) {
+  rs_solver_options o;
+  o.chi = 0.5;
+  o.leaf_size = 8;
+  o.leaf_pairs = 64;
+  o.restart = 30;
+  o.tolerance = 1e-6;
+  o.max_iterations = 200;
+  o.tp_weight = 1.0;
+  o.low_order = 1;
+  o.eps_rel = 1e-10;
+  o.eps_multi_rel = 1e-4;
+  o.barycenter_per_component = 0;
+  o.vcycles = 1;
+  o.preconditioner = 1;
+  return o;
+}
+
+}  // extern "C"

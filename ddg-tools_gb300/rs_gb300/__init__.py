@@ -33,6 +33,16 @@ _vp = C.c_void_p
 _dp = C.POINTER(C.c_double)
 
 
+class SolverOptions(C.Structure):
+    """rs_solver_options of include/rsgpu.h (HierarchicalOptions, RS/src/solve/iterative.rs:348-395)."""
+
+    _fields_ = [("chi", C.c_double), ("leaf_size", C.c_int), ("leaf_pairs", C.c_int),
+                ("restart", C.c_int), ("tolerance", C.c_double), ("max_iterations", C.c_int),
+                ("tp_weight", C.c_double), ("low_order", C.c_int), ("eps_rel", C.c_double),
+                ("eps_multi_rel", C.c_double), ("barycenter_per_component", C.c_int),
+                ("vcycles", C.c_int), ("preconditioner", C.c_int)]
+
+
 class RsError(RuntimeError):
     """An error of the library: ``kind`` is the crate's RsError variant name, ``operation`` the
     failing operation word (RsError::Gpu { operation, detail }, RS/src/gpu/cuda.rs:19-24)."""
@@ -95,6 +105,15 @@ def load_library(path: str | os.PathLike | None = None):
         "rs_vfrac_apply": [_vp, C.c_int, _f64p, _f64p],
         "rs_vfrac_apply_device": [_vp, C.c_int, _vp, _vp],
         "rs_vfrac_stats": [_vp, _i64p],
+        "rs_solver_build": [_vp, C.c_int, C.c_int, _u32p, _f64p, C.c_double, C.c_double, C.c_void_p,
+                            C.POINTER(_vp)],
+        "rs_solver_dims": [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
+        "rs_solver_apply": [_vp, C.c_int, _f64p, _f64p],
+        "rs_solver_apply_device": [_vp, C.c_int, _vp, _vp],
+        "rs_solver_precondition": [_vp, C.c_int, _f64p, _f64p],
+        "rs_solver_precondition_device": [_vp, C.c_int, _vp, _vp],
+        "rs_solver_solve_many": [_vp, C.c_int, _f64p, _f64p, _f64p],
+        "rs_solver_solve_many_device": [_vp, C.c_int, _vp, _vp, _f64p],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -102,7 +121,9 @@ def load_library(path: str | os.PathLike | None = None):
         f.restype = C.c_int
     L.rs_ctx_free.argtypes = [_vp]
     L.rs_ctx_free.restype = None
-    for name in ("rs_bh_free", "rs_metric_free", "rs_vfrac_free"):
+    L.rs_solver_options_default.restype = SolverOptions
+    L.rs_solver_options_default.argtypes = []
+    for name in ("rs_bh_free", "rs_metric_free", "rs_vfrac_free", "rs_solver_free"):
         getattr(L, name).argtypes = [_vp]
         getattr(L, name).restype = None
     _lib = L
@@ -473,3 +494,64 @@ class VertexFractionalTree:
         o = np.zeros(5, np.int64)
         _check(_lib.rs_vfrac_stats(self._h, o))
         return dict(zip(["far_blocks", "near_blocks", "near_entries", "depth", "nodes"], map(int, o)))
+
+
+def solver_options(**kw) -> SolverOptions:
+    """The library defaults (rs_solver_options_default) with the given fields replaced."""
+    o = load_library().rs_solver_options_default()
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class SaddleSolver:
+    """The hierarchical saddle solver of one step on the GPU (HierarchicalSaddle,
+    RS/src/solve/iterative.rs:426-575): A' [x; l] = [a; b] by right-preconditioned GMRES."""
+
+    def __init__(self, faces, positions, exponents: Exponents = Exponents(),
+                 options: SolverOptions | None = None, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        faces, positions = _mesh(faces, positions)
+        o = options or solver_options()
+        h = _vp()
+        _check(_lib.rs_solver_build(self.ctx.handle, len(positions), len(faces), faces.ravel(),
+                                    positions.ravel(), exponents.alpha, exponents.beta, C.byref(o),
+                                    C.byref(h)))
+        self._h = h
+        nd, nc = C.c_int64(), C.c_int64()
+        _check(_lib.rs_solver_dims(h, C.byref(nd), C.byref(nc)))
+        self.n_dofs, self.n_constraints = nd.value, nc.value
+        self.n = self.n_dofs + self.n_constraints
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.rs_solver_free(self._h)
+            self._h = None
+
+    def _batch(self, fn, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        xs = x.reshape(-1, self.n)
+        ys = np.empty_like(xs)
+        _check(fn(self._h, len(xs), xs.ravel(), ys.ravel()))
+        return ys.reshape(x.shape)
+
+    def apply(self, x):
+        """A' x for x of shape (n,) or (nb, n), n = 3V + k_Q."""
+        return self._batch(_lib.rs_solver_apply, x)
+
+    def precondition(self, r):
+        """P^-1 r."""
+        return self._batch(_lib.rs_solver_precondition, r)
+
+    def solve_many(self, rhs):
+        """Solves A' y = rhs for up to 4 stacked right-hand sides; returns (y, reports)."""
+        rhs = np.ascontiguousarray(rhs, dtype=np.float64).reshape(-1, self.n)
+        out = np.empty_like(rhs)
+        rep = np.zeros(5 * len(rhs))
+        _check(_lib.rs_solver_solve_many(self._h, len(rhs), rhs.ravel(), out.ravel(), rep))
+        keys = ["iterations", "relative_residual", "converged", "seconds", "cycles"]
+        reports = [dict(zip(keys, rep[5 * i: 5 * i + 5])) for i in range(len(rhs))]
+        for r in reports:
+            r["iterations"] = int(r["iterations"])
+            r["converged"] = bool(r["converged"])
+        return out, reports

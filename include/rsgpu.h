@@ -195,6 +195,54 @@ int rs_vfrac_apply(rs_vfrac *v, int nb, const double *xs_host, double *ys_host);
 int rs_vfrac_apply_device(rs_vfrac *v, int nb, const double *xs_dev, double *ys_dev);
 int rs_vfrac_stats(rs_vfrac *v, int64_t *out5);
 
+/* ---------------------------------------------------------------- saddle solve */
+
+typedef struct rs_solver rs_solver; /* HierarchicalSaddle (RS/src/solve/iterative.rs:426-575) */
+
+/* Options of the hierarchical saddle solver (HierarchicalOptions, iterative.rs:348-395;
+ * PreconditionerOptions, RS/src/solve/precond.rs:466-583; GmresOptions, gmres.rs:135-190). */
+typedef struct rs_solver_options {
+  double chi;            /* block cluster tree separation (0.5) */
+  int leaf_size;         /* BVH leaf size, <= 8 (8) */
+  int leaf_pairs;        /* near-block size limit (64) */
+  int restart;           /* GMRES restart (30) */
+  double tolerance;      /* true relative residual (1e-6) */
+  int max_iterations;    /* GMRES iterations over all cycles (200) */
+  double tp_weight;      /* w_TP (1) */
+  int low_order;         /* keep B0 (1) */
+  double eps_rel;        /* eps_rel of eps = eps_rel tr W / tr M (1e-10) */
+  double eps_multi_rel;  /* eps when a global barycenter spans several components (1e-4) */
+  int barycenter_per_component; /* 1: one barycenter group per component, 0: global (0) */
+  int vcycles;           /* multigrid V-cycles per L' solve (1) */
+  int preconditioner;    /* 1: the fractional preconditioner, 0: none */
+} rs_solver_options;
+
+rs_solver_options rs_solver_options_default(void);
+
+/* hierarchical_saddle_with (iterative.rs:487-575) for a surface and positions: the metric
+ * operator A' = [w (B~ + c_lo B~0) + C_Q^T ; C_Q] with barycenter rows C_Q, and the augmented
+ * fractional preconditioner L'^-1 + L'^-1 ((s L^V_{2-s} - K) x I3) L'^-1 (L'^-1 applied by
+ * multigrid V-cycles on the device instead of the reference's sparse LDL^T). */
+int rs_solver_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces,
+                    const double *positions_host, double alpha, double beta,
+                    const rs_solver_options *opts, rs_solver **out);
+void rs_solver_free(rs_solver *s);
+/* n_dofs = 3V, n_constraints = k_Q (3 per barycenter group). Vectors are [x (3V); l (k_Q)]. */
+int rs_solver_dims(rs_solver *s, int64_t *n_dofs, int64_t *n_constraints);
+/* LinearOperator::apply_batch (gmres.rs:32-52): ys = A' xs for nb stacked vectors. */
+int rs_solver_apply(rs_solver *s, int nb, const double *xs_host, double *ys_host);
+int rs_solver_apply_device(rs_solver *s, int nb, const double *xs_dev, double *ys_dev);
+/* Preconditioner::apply_batch (gmres.rs:55-75): zs = P^-1 rs. */
+int rs_solver_precondition(rs_solver *s, int nb, const double *rs_host, double *zs_host);
+int rs_solver_precondition_device(rs_solver *s, int nb, const double *rs_dev, double *zs_dev);
+/* SaddleSolver::solve_many (RS/src/solve/mod.rs:107-130): right-preconditioned GMRES on the
+ * device for nb (1..4) right-hand sides [a; b] at once; report (5 per rhs): iterations, true
+ * relative residual, converged, seconds, cycles. SolverDiverged above 0.1 (gmres.rs:196). */
+int rs_solver_solve_many(rs_solver *s, int nb, const double *rhs_host, double *sol_host,
+                         double *report);
+int rs_solver_solve_many_device(rs_solver *s, int nb, const double *rhs_dev, double *sol_dev,
+                                double *report);
+
 #ifdef __cplusplus
 }
 #endif

@@ -538,9 +538,9 @@ __global__ void final_kernel(BhDev d) {
     const uint32_t p = s0 + t;
     const float *ow = reinterpret_cast<const float *>(d.own);
     float own = 0.f, ownn = 0.f;
-    for (uint32_t i = d.item_off[k]; i < d.item_off[k + 1]; ++i) {
-      own += ow[128 * (size_t)i + 8 * t + c];
-      ownn += ow[128 * (size_t)i + 8 * t + 4 + c];
+    for (uint32_t i = d.item_off[k]; i < d.item_off[k + 1]; ++i) {  // 64 floats per item
+      own += ow[64 * (size_t)i + 8 * t + c];
+      ownn += ow[64 * (size_t)i + 8 * t + 4 + c];
     }
     const float4 bu = d.leaf_bu[k];
     const float4 xa = d.fxa[p];  // offset X_T - X_leaf and a_T

@@ -37,19 +37,23 @@ namespace rsg {
 constexpr int FACE = 0, VERTEX = 1;
 
 struct HDev {
-  const uint32_t *start, *end, *right, *parent, *leaves, *chain_off, *chain, *leaf_of_pos;
-  const uint32_t *far_ptr, *far_col, *near_ptr, *near_col;
+  const uint32_t *start, *end, *right, *parent, *leaves, *chain_off, *chain;
+  const uint32_t *far_ptr, *far_col;
   const float2 *far_coef;    // per far block: (k_0, k_1)
-  const float4 *el;          // per BVH position: offset from the leaf centroid (xyz), weight a
+  const float4 *xh;          // per BVH position: position hi (xyz), weight a (w)
+  const float4 *xl;          // per BVH position: position lo (xyz): X = hi + lo to ~48 bits
   const float4 *nrm;         // per BVH position: normal (faces only)
-  const float4 *ch, *cl;     // per node: centroid as a float pair (hi xyz + weight w, lo xyz)
   const float2 *leaf_farA;   // per leaf: the far part of H~a along its chain (k_0, k_1)
+  const uint2 *cols;         // near column ranges [x, y) of every leaf's chain, leaf by leaf
+  const uint4 *items;        // per work item: leaf ordinal, column-range begin / end, -
+  const uint32_t *item_off;  // per leaf: its work items [item_off[k], item_off[k + 1])
   float *up;                 // per node: C channel sums
   float *farx;               // per node: C channel far sums
+  float *part;               // per work item: 8 rows x (C + 2) partial near sums
   uint32_t *count;           // per node: arrival counter of the upward pass
   const float *m;            // [n][C]
   float *z;                  // [n][C]
-  int n_nodes, n_leaves, n_el, C;
+  int n_nodes, n_leaves, n_el, n_items, C;
   float neg_s;               // kernel exponent applied to r^2
 };
 
@@ -64,27 +68,32 @@ __device__ __forceinline__ void near_kernel(float d0, float d1, float d2, const 
   if (KIND == FACE) {
     float a = np.x * d0 + np.y * d1 + np.z * d2;
     float b = nq.x * d0 + nq.y * d1 + nq.z * d2;
-    float ir2 = 1.f / r2;
+    float ir2 = __fdividef(1.f, r2);
     k1 = 0.5f * (a * a + b * b) * ir2 * ir2 * h;
   } else {
     k1 = h;
   }
 }
 
-// Bottom-up channel sums: one thread per leaf sums its elements, then climbs; at every parent
-// the second child to arrive adds left + right (fixed order, no waiting).
+// Bottom-up channel sums: one thread per leaf sums its elements in registers, then climbs; at
+// every parent the second child to arrive adds left + right (fixed order, no waiting).
+template <int CC>
 __global__ void hm_upward_kernel(HDev d) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= d.n_leaves) return;
-  const int C = d.C;
   uint32_t leaf = d.leaves[k];
-  float *u = d.up + (size_t)leaf * C;
-  for (int c = 0; c < C; ++c) u[c] = 0.f;
+  float u[CC];
+#pragma unroll
+  for (int c = 0; c < CC; ++c) u[c] = 0.f;
   for (uint32_t p = d.start[leaf]; p < d.end[leaf]; ++p) {
-    float a = d.el[p].w;
-    const float *mp = d.m + (size_t)p * C;
-    for (int c = 0; c < C; ++c) u[c] += a * mp[c];
+    float a = d.xh[p].w;
+    const float *mp = d.m + (size_t)p * CC;
+#pragma unroll
+    for (int c = 0; c < CC; ++c) u[c] += a * mp[c];
   }
+  float *o = d.up + (size_t)leaf * CC;
+#pragma unroll
+  for (int c = 0; c < CC; ++c) o[c] = u[c];
   uint32_t n = leaf;
   while (n != 0) {
     uint32_t par = d.parent[n];
@@ -92,71 +101,76 @@ __global__ void hm_upward_kernel(HDev d) {
     unsigned old = atomicAdd(&d.count[par], 1u);
     if ((old & 1u) == 0u) return;
     __threadfence();
-    const float *l = d.up + (size_t)(par + 1) * C;
-    const float *r = d.up + (size_t)d.right[par] * C;
-    float *o = d.up + (size_t)par * C;
-    for (int c = 0; c < C; ++c) o[c] = __ldcg(l + c) + __ldcg(r + c);
+    const float *l = d.up + (size_t)(par + 1) * CC;
+    const float *r = d.up + (size_t)d.right[par] * CC;
+    float *op = d.up + (size_t)par * CC;
+#pragma unroll
+    for (int c = 0; c < CC; ++c) op[c] = __ldcg(l + c) + __ldcg(r + c);
     n = par;
   }
 }
 
 // farx[a][c] = sum over the far blocks (a, b) of h(a, b)[kernel(c)] up[b][c] (block_tree.rs:
-// 564-578); one warp per node, lanes over channels. `split` = first channel of kernel 1.
+// 564-578); one warp per node, lanes strided over the node's far blocks, each summing all CC
+// channels, then a fixed butterfly over the lanes. `split` = first channel of kernel 1.
+template <int CC>
 __global__ void hm_far_kernel(HDev d, int split) {
   int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (a >= d.n_nodes) return;
-  const int C = d.C;
-  for (int c0 = 0; c0 < C; c0 += 32) {
-    int c = c0 + lane;
-    float acc = 0.f;
-    if (c < C)
-      for (uint32_t q = d.far_ptr[a]; q < d.far_ptr[a + 1]; ++q) {
-        float2 k = d.far_coef[q];
-        acc += (c < split ? k.x : k.y) * d.up[(size_t)d.far_col[q] * C + c];
-      }
-    if (c < C) d.farx[(size_t)a * C + c] = acc;
+  float acc[CC];
+#pragma unroll
+  for (int c = 0; c < CC; ++c) acc[c] = 0.f;
+  for (uint32_t q = d.far_ptr[a] + lane; q < d.far_ptr[a + 1]; q += 32) {
+    float2 k = d.far_coef[q];
+    const float *u = d.up + (size_t)d.far_col[q] * CC;
+#pragma unroll
+    for (int c = 0; c < CC; ++c) acc[c] += (c < split ? k.x : k.y) * u[c];
   }
+#pragma unroll
+  for (int c = 0; c < CC; ++c)
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], m);
+  float *o = d.farx + (size_t)a * CC;
+#pragma unroll
+  for (int c = 0; c < CC; ++c)
+    if (lane == (c & 31)) o[c] = acc[c];
 }
 
-// One warp per leaf; lane = r + 8 j: r the row (element) of the leaf, j one of four column
-// groups. The near blocks of the chain root -> leaf are streamed column by column (group j
-// takes every fourth column), each column's kernel values evaluated once per row and applied to
-// all C channels; H~a's near part is summed in the same loop. CC = C (compile-time).
+// Near sums of one work item (a slice of a leaf's chain near-column ranges). One warp per
+// item; lane = r + 8 j: r the row (element) of the leaf, j one of four column groups taking
+// every fourth column. Each column's kernel values are evaluated once per row and applied to
+// all CC channels; the near part of H~a is summed in the same loop. Lanes j = 0 write the
+// item's partial sums (CC + 2 per row).
 template <int KIND, int CC>
 __global__ void __launch_bounds__(128) hm_rows_kernel(HDev d, int split) {
   const int lane = threadIdx.x & 31;
   const int r = lane & 7, j = lane >> 3;
-  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (k >= d.n_leaves) return;
-  const uint32_t leaf = d.leaves[k];
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= d.n_items) return;
+  const uint4 it = d.items[w];
+  const uint32_t leaf = d.leaves[it.x];
   const uint32_t s0 = d.start[leaf], ns = d.end[leaf] - s0;
   const bool act = (uint32_t)r < ns;
   const uint32_t p = s0 + (act ? r : 0);
-  const float4 ep = d.el[p];
+  const float4 ph = d.xh[p], pl = d.xl[p];
   const float4 np = KIND == FACE ? d.nrm[p] : make_float4(0.f, 0.f, 0.f, 0.f);
-  const float4 cph = d.ch[leaf], cpl = d.cl[leaf];
   float acc[CC];
 #pragma unroll
   for (int c = 0; c < CC; ++c) acc[c] = 0.f;
   float sw0 = 0.f, sw1 = 0.f;
-  const uint32_t c0 = d.chain_off[k], c1 = d.chain_off[k + 1];
-  for (uint32_t ci = c0; ci < c1; ++ci) {
-    const uint32_t a = d.chain[ci];
-    for (uint32_t qb = d.near_ptr[a]; qb < d.near_ptr[a + 1]; ++qb) {
-      const uint32_t b = d.near_col[qb];
-      const uint32_t cs = d.start[b], ce = d.end[b];
-      for (uint32_t q = cs + j; q < ce; q += 4) {
-        if (!act || q == p) continue;
-        const uint32_t lq = d.leaves[d.leaf_of_pos[q]];
-        const float4 cqh = d.ch[lq], cql = d.cl[lq];
-        const float4 eq = d.el[q];
-        const float d0 = ((cph.x - cqh.x) + (cpl.x - cql.x)) + (ep.x - eq.x);
-        const float d1 = ((cph.y - cqh.y) + (cpl.y - cql.y)) + (ep.y - eq.y);
-        const float d2 = ((cph.z - cqh.z) + (cpl.z - cql.z)) + (ep.z - eq.z);
+  if (act)
+    for (uint32_t ri = it.y; ri < it.z; ++ri) {
+      const uint2 cr = d.cols[ri];
+      for (uint32_t q = cr.x + j; q < cr.y; q += 4) {
+        if (q == p) continue;
+        const float4 qh = d.xh[q], ql = d.xl[q];
+        const float d0 = (ph.x - qh.x) + (pl.x - ql.x);
+        const float d1 = (ph.y - qh.y) + (pl.y - ql.y);
+        const float d2 = (ph.z - qh.z) + (pl.z - ql.z);
         float k0, k1;
         near_kernel<KIND>(d0, d1, d2, np, KIND == FACE ? d.nrm[q] : np, d.neg_s, k0, k1);
-        const float w0 = k0 * eq.w, w1 = k1 * eq.w;
+        const float w0 = k0 * qh.w, w1 = k1 * qh.w;
         sw0 += w0;
         sw1 += w1;
         const float4 *mq = reinterpret_cast<const float4 *>(d.m + (size_t)q * CC);
@@ -171,7 +185,6 @@ __global__ void __launch_bounds__(128) hm_rows_kernel(HDev d, int split) {
         }
       }
     }
-  }
   // reduce over the four column groups
 #pragma unroll
   for (int c = 0; c < CC; ++c) {
@@ -182,21 +195,48 @@ __global__ void __launch_bounds__(128) hm_rows_kernel(HDev d, int split) {
   sw0 += __shfl_xor_sync(0xffffffffu, sw0, 16);
   sw1 += __shfl_xor_sync(0xffffffffu, sw1, 8);
   sw1 += __shfl_xor_sync(0xffffffffu, sw1, 16);
-  if (j != 0 || !act) return;
+  if (j != 0) return;
+  float *o = d.part + ((size_t)w * 8 + r) * (CC + 2);
+#pragma unroll
+  for (int c = 0; c < CC; ++c) o[c] = acc[c];
+  o[CC] = sw0, o[CC + 1] = sw1;
+}
+
+// Per leaf (thread per row): z = (H~a) m - H~(a m) from the items' near sums (in item order),
+// the far sums along the chain and the far part of H~a.
+template <int CC>
+__global__ void hm_epilogue_kernel(HDev d, int split) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  int k = t >> 3, r = t & 7;
+  if (k >= d.n_leaves) return;
+  const uint32_t leaf = d.leaves[k];
+  const uint32_t s0 = d.start[leaf];
+  if ((uint32_t)r >= d.end[leaf] - s0) return;
+  const uint32_t p = s0 + r;
+  float acc[CC];
+#pragma unroll
+  for (int c = 0; c < CC; ++c) acc[c] = 0.f;
+  float sw0 = 0.f, sw1 = 0.f;
+  for (uint32_t i = d.item_off[k]; i < d.item_off[k + 1]; ++i) {
+    const float *o = d.part + ((size_t)i * 8 + r) * (CC + 2);
+#pragma unroll
+    for (int c = 0; c < CC; ++c) acc[c] += o[c];
+    sw0 += o[CC], sw1 += o[CC + 1];
+  }
+  for (uint32_t ci = d.chain_off[k]; ci < d.chain_off[k + 1]; ++ci) {
+    const float *f = d.farx + (size_t)d.chain[ci] * CC;
+#pragma unroll
+    for (int c = 0; c < CC; ++c) acc[c] += f[c];
+  }
   const float2 fa = d.leaf_farA[k];
   const float ha0 = sw0 + fa.x, ha1 = sw1 + fa.y;
   const float *mp = d.m + (size_t)p * CC;
   float *zp = d.z + (size_t)p * CC;
 #pragma unroll
-  for (int c = 0; c < CC; ++c) {
-    float fx = 0.f;
-    for (uint32_t ci = c0; ci < c1; ++ci) fx += d.farx[(size_t)d.chain[ci] * CC + c];
-    zp[c] = (c < split ? ha0 : ha1) * mp[c] - (acc[c] + fx);
-  }
+  for (int c = 0; c < CC; ++c) zp[c] = (c < split ? ha0 : ha1) * mp[c] - acc[c];
 }
 
-// Far part of H~a per leaf (the far field of psi = a, pushed down the chain): same kernels as a
-// product, channel count 2.
+// Far part of H~a per leaf (the far field of psi = a, pushed down the chain).
 __global__ void hm_leaf_farA_kernel(HDev d, float2 *out) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= d.n_leaves) return;
@@ -295,17 +335,16 @@ __global__ void vertex_out_kernel(const uint32_t *order, const float4 *el, const
       ys[q * ldy + 3 * (size_t)v + k] = scale * 2.0 * a * (double)z[(size_t)p * C + 3 * q + k];
 }
 
-// Element records relative to the leaf centroids, node centroids as float pairs; FP64 in.
+// Element records: positions as float pairs (hi + lo), weights, normals; FP64 in.
 __global__ void hm_pack_kernel(const double *pts, const double *wt, const double *nrm64,
-                               const uint32_t *order, const uint32_t *leaf_of_pos,
-                               const uint32_t *leaves, const double *cent, int n, float4 *el,
-                               float4 *nrm) {
+                               const uint32_t *order, int n, float4 *xh, float4 *xl, float4 *nrm) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
   uint32_t e = order[p];
-  const double *c = cent + 3 * (size_t)leaves[leaf_of_pos[p]];
-  el[p] = make_float4((float)(pts[3 * (size_t)e] - c[0]), (float)(pts[3 * (size_t)e + 1] - c[1]),
-                      (float)(pts[3 * (size_t)e + 2] - c[2]), (float)wt[e]);
+  const double *x = pts + 3 * (size_t)e;
+  float h0 = (float)x[0], h1 = (float)x[1], h2 = (float)x[2];
+  xh[p] = make_float4(h0, h1, h2, (float)wt[e]);
+  xl[p] = make_float4((float)(x[0] - (double)h0), (float)(x[1] - (double)h1), (float)(x[2] - (double)h2), 0.f);
   if (nrm) nrm[p] = make_float4((float)nrm64[3 * (size_t)e], (float)nrm64[3 * (size_t)e + 1],
                                 (float)nrm64[3 * (size_t)e + 2], 0.f);
 }
@@ -332,25 +371,28 @@ struct HMat {
   int kind = FACE;
   Tree tree;
   Blocks blocks;
-  size_t n_el = 0;
+  size_t n_el = 0, n_items = 0;
   double neg_s = 0;
-  DevBuf<uint32_t> start, end, right, parent, leaves, chain_off, chain, leaf_of_pos;
-  DevBuf<uint32_t> far_ptr, far_col, near_ptr, near_col, count;
+  DevBuf<uint32_t> start, end, right, parent, leaves, chain_off, chain, item_off;
+  DevBuf<uint32_t> far_ptr, far_col, count;
+  DevBuf<uint2> cols;
+  DevBuf<uint4> items;
   DevBuf<float2> far_coef, leaf_farA;
-  DevBuf<float4> el, nrm, ch, cl;
-  DevBuf<float> up, farx, m, z;
-  int C = 0;
+  DevBuf<float4> xh, xl, nrm;
+  DevBuf<float> up, farx, part, m, z;
   Profiler prof;
 
   HDev dev(int C_) const {
     HDev d;
     d.start = start.p, d.end = end.p, d.right = right.p, d.parent = parent.p, d.leaves = leaves.p;
-    d.chain_off = chain_off.p, d.chain = chain.p, d.leaf_of_pos = leaf_of_pos.p;
-    d.far_ptr = far_ptr.p, d.far_col = far_col.p, d.near_ptr = near_ptr.p, d.near_col = near_col.p;
-    d.far_coef = far_coef.p, d.el = el.p, d.nrm = nrm.p, d.ch = ch.p, d.cl = cl.p;
-    d.leaf_farA = leaf_farA.p, d.up = up.p, d.farx = farx.p, d.count = count.p;
+    d.chain_off = chain_off.p, d.chain = chain.p;
+    d.far_ptr = far_ptr.p, d.far_col = far_col.p, d.far_coef = far_coef.p;
+    d.xh = xh.p, d.xl = xl.p, d.nrm = nrm.p, d.leaf_farA = leaf_farA.p;
+    d.cols = cols.p, d.items = items.p, d.item_off = item_off.p;
+    d.up = up.p, d.farx = farx.p, d.part = part.p, d.count = count.p;
     d.m = m.p, d.z = z.p;
     d.n_nodes = (int)tree.n_nodes(), d.n_leaves = (int)tree.leaves.size(), d.n_el = (int)n_el;
+    d.n_items = (int)n_items;
     d.C = C_;
     d.neg_s = (float)neg_s;
     return d;
@@ -362,20 +404,38 @@ struct HMat {
     size_t nn = tree.n_nodes();
     if ((size_t)C_ * nn > up.n) up.alloc((size_t)C_ * nn), farx.alloc((size_t)C_ * nn);
     if ((size_t)C_ * n_el > m.n) m.alloc((size_t)C_ * n_el), z.alloc((size_t)C_ * n_el);
+    if (n_items * 8 * (size_t)(C_ + 2) > part.n) part.alloc(std::max<size_t>(n_items * 8 * (size_t)(C_ + 2), 1));
   }
 
-  // Uploads the tree, the blocks, the element records and the far coefficients; computes the
-  // far part of H~a. pts/wt/nrm64 are per element (original order), FP64.
+  template <int CC>
+  void upward_far(const HDev &d, int split) {
+    size_t nn = tree.n_nodes(), nl = tree.leaves.size();
+    cudaStream_t s = st();
+    prof.begin(s, kind == FACE ? "metric_upward" : "vfrac_upward");
+    hm_upward_kernel<CC><<<nblk(nl, 128), 128, 0, s>>>(d);
+    RSG_LAUNCHED(ctx, "hm_upward");
+    prof.end(s);
+    prof.begin(s, kind == FACE ? "metric_far" : "vfrac_far");
+    hm_far_kernel<CC><<<nblk(nn * 32, 256), 256, 0, s>>>(d, split);
+    RSG_LAUNCHED(ctx, "hm_far");
+    prof.end(s);
+  }
+
+  // Uploads the tree, the near column ranges split into work items, the element records and
+  // the far coefficients; computes the far part of H~a. pts/wt/nrm64 are per element
+  // (original order), FP64.
   void setup(const double *pts, const double *wt, const double *nrm64, const double *proj6) {
     cudaStream_t s = st();
     const Tree &T = tree;
     size_t nn = T.n_nodes(), nl = T.leaves.size();
-    std::vector<uint32_t> parent_h(nn, 0), coff(nl + 1, 0), chain_h, lop(n_el);
+    std::vector<uint32_t> parent_h(nn, 0), coff(nl + 1, 0), chain_h, ioff(nl + 1, 0);
+    std::vector<uint2> cols_h;
+    std::vector<uint4> items_h;
+    const uint32_t kItemCols = 512;
     for (size_t i = 0; i < nn; ++i)
       if (T.right[i]) parent_h[i + 1] = (uint32_t)i, parent_h[T.right[i]] = (uint32_t)i;
     for (size_t k = 0; k < nl; ++k) {
       uint32_t l = T.leaves[k];
-      for (uint32_t p = T.start[l]; p < T.end[l]; ++p) lop[p] = (uint32_t)k;
       if (T.end[l] - T.start[l] > 8)
         fail(RS_INVALID_OPTION, "InvalidOption", "upload", "the GPU path needs leaf_size <= 8");
       size_t b = chain_h.size();
@@ -387,24 +447,31 @@ struct HMat {
       }
       std::reverse(chain_h.begin() + b, chain_h.end());
       coff[k + 1] = (uint32_t)chain_h.size();
+      // the near column ranges of the chain, in chain and block order; items cut at ranges
+      uint32_t r0 = (uint32_t)cols_h.size(), cnt = 0;
+      for (size_t ci = b; ci < chain_h.size(); ++ci)
+        for (uint32_t q = blocks.near_ptr[chain_h[ci]]; q < blocks.near_ptr[chain_h[ci] + 1]; ++q) {
+          uint32_t c = blocks.near_col[q];
+          uint32_t w = T.end[c] - T.start[c];
+          if (cnt > 0 && cnt + w > kItemCols) {
+            items_h.push_back(make_uint4((uint32_t)k, r0, (uint32_t)cols_h.size(), 0));
+            r0 = (uint32_t)cols_h.size();
+            cnt = 0;
+          }
+          cols_h.push_back(make_uint2(T.start[c], T.end[c]));
+          cnt += w;
+        }
+      items_h.push_back(make_uint4((uint32_t)k, r0, (uint32_t)cols_h.size(), 0));
+      ioff[k + 1] = (uint32_t)items_h.size();
     }
+    n_items = items_h.size();
     up_vec(start, T.start, s), up_vec(end, T.end, s), up_vec(right, T.right, s);
     up_vec(parent, parent_h, s), up_vec(leaves, T.leaves, s), up_vec(chain_off, coff, s);
-    up_vec(chain, chain_h, s), up_vec(leaf_of_pos, lop, s);
+    up_vec(chain, chain_h, s), up_vec(cols, cols_h, s), up_vec(items, items_h, s), up_vec(item_off, ioff, s);
     up_vec(far_ptr, blocks.far_ptr, s), up_vec(far_col, blocks.far_col, s);
-    up_vec(near_ptr, blocks.near_ptr, s), up_vec(near_col, blocks.near_col, s);
     count.alloc(nn);
     RSG_CUDA("upload", cudaMemsetAsync(count.p, 0, nn * sizeof(uint32_t), s));
-    // node centroids (float pairs) and far coefficients on the host in FP64 (kernel.far,
-    // hierarchical.rs:210-220 / 980-984), rounded once
-    std::vector<float4> chh(nn), clh(nn);
-    for (size_t i = 0; i < nn; ++i) {
-      const double *c = &T.centroid[3 * i];
-      float hx = (float)c[0], hy = (float)c[1], hz = (float)c[2];
-      chh[i] = make_float4(hx, hy, hz, (float)T.mass[i]);
-      clh[i] = make_float4((float)(c[0] - hx), (float)(c[1] - hy), (float)(c[2] - hz), 0.f);
-    }
-    up_vec(ch, chh, s), up_vec(cl, clh, s);
+    // far coefficients on the host in FP64 (kernel.far, hierarchical.rs:210-220 / 980-984)
     std::vector<float2> coef(blocks.far_col.size());
     auto qf = [&](size_t n, const double *d) {
       const double *p = proj6 + 6 * n;
@@ -424,18 +491,16 @@ struct HMat {
       }
     up_vec(far_coef, coef, s);
     // element records
-    DevBuf<double> dp, dw, dn, dc;
+    DevBuf<double> dp, dw, dn;
     dp.upload(pts, 3 * n_el, s);
     dw.upload(wt, n_el, s);
     if (nrm64) dn.upload(nrm64, 3 * n_el, s);
-    dc.upload(T.centroid.data(), T.centroid.size(), s);
     DevBuf<uint32_t> ord;
     ord.upload(T.order.data(), T.order.size(), s);
-    el.alloc(n_el);
+    xh.alloc(n_el), xl.alloc(n_el);
     if (kind == FACE) nrm.alloc(n_el);
-    hm_pack_kernel<<<nblk(n_el, 256), 256, 0, s>>>(dp.p, dw.p, nrm64 ? dn.p : nullptr, ord.p,
-                                                   leaf_of_pos.p, leaves.p, dc.p, (int)n_el, el.p,
-                                                   kind == FACE ? nrm.p : nullptr);
+    hm_pack_kernel<<<nblk(n_el, 256), 256, 0, s>>>(dp.p, dw.p, nrm64 ? dn.p : nullptr, ord.p, (int)n_el,
+                                                   xh.p, xl.p, kind == FACE ? nrm.p : nullptr);
     RSG_LAUNCHED(ctx, "hm_pack");
     // far part of H~a: upward over psi = a (m = 1, 2 channels), far, chain sums
     leaf_farA.alloc(nl);
@@ -445,45 +510,41 @@ struct HMat {
     mm.upload(ones.data(), ones.size(), s);
     HDev d = dev(2);
     d.m = mm.p;
-    hm_upward_kernel<<<nblk(nl, 128), 128, 0, s>>>(d);
-    RSG_LAUNCHED(ctx, "hm_upward");
-    hm_far_kernel<<<nblk(nn * 32, 256), 256, 0, s>>>(d, 1);
-    RSG_LAUNCHED(ctx, "hm_far");
+    upward_far<2>(d, 1);
     hm_leaf_farA_kernel<<<nblk(nl, 128), 128, 0, s>>>(d, leaf_farA.p);
     RSG_LAUNCHED(ctx, "hm_leaf_farA");
     RSG_CUDA("upload", cudaStreamSynchronize(s));
   }
 
-  // z = H~a m - H~(a m) for the C-channel m already in `m` (split: first kernel-1 channel).
-  void product(int CC, int split) {
+  template <int K, int CC>
+  void product_cc(int split) {
     cudaStream_t s = st();
-    size_t nn = tree.n_nodes(), nl = tree.leaves.size();
+    size_t nl = tree.leaves.size();
     HDev d = dev(CC);
-    prof.begin(s, kind == FACE ? "metric_upward" : "vfrac_upward");
-    hm_upward_kernel<<<nblk(nl, 128), 128, 0, s>>>(d);
-    RSG_LAUNCHED(ctx, "hm_upward");
-    prof.end(s);
-    prof.begin(s, kind == FACE ? "metric_far" : "vfrac_far");
-    hm_far_kernel<<<nblk(nn * 32, 256), 256, 0, s>>>(d, split);
-    RSG_LAUNCHED(ctx, "hm_far");
-    prof.end(s);
+    upward_far<CC>(d, split);
     prof.begin(s, kind == FACE ? "metric_rows" : "vfrac_rows");
-    unsigned g = nblk(nl * 32, 128);
-#define RSG_ROWS(K, N) hm_rows_kernel<K, N><<<g, 128, 0, s>>>(d, split)
-    if (kind == FACE) {
-      if (CC == 12) RSG_ROWS(FACE, 12);
-      else if (CC == 24) RSG_ROWS(FACE, 24);
-      else if (CC == 36) RSG_ROWS(FACE, 36);
-      else fail(RS_INTERNAL, "Internal", "product", "unsupported channel count");
-    } else {
-      if (CC == 4) RSG_ROWS(VERTEX, 4);
-      else if (CC == 8) RSG_ROWS(VERTEX, 8);
-      else if (CC == 12) RSG_ROWS(VERTEX, 12);
-      else fail(RS_INTERNAL, "Internal", "product", "unsupported channel count");
-    }
-#undef RSG_ROWS
+    hm_rows_kernel<K, CC><<<nblk(n_items * 32, 128), 128, 0, s>>>(d, split);
     RSG_LAUNCHED(ctx, "hm_rows");
     prof.end(s);
+    prof.begin(s, kind == FACE ? "metric_epilogue" : "vfrac_epilogue");
+    hm_epilogue_kernel<CC><<<nblk(nl * 8, 128), 128, 0, s>>>(d, split);
+    RSG_LAUNCHED(ctx, "hm_epilogue");
+    prof.end(s);
+  }
+
+  // z = H~a m - H~(a m) for the C-channel m already in `m` (split: first kernel-1 channel).
+  void product(int CC, int split) {
+    if (kind == FACE) {
+      if (CC == 12) product_cc<FACE, 12>(split);
+      else if (CC == 24) product_cc<FACE, 24>(split);
+      else if (CC == 36) product_cc<FACE, 36>(split);
+      else fail(RS_INTERNAL, "Internal", "product", "unsupported channel count");
+    } else {
+      if (CC == 4) product_cc<VERTEX, 4>(split);
+      else if (CC == 8) product_cc<VERTEX, 8>(split);
+      else if (CC == 12) product_cc<VERTEX, 12>(split);
+      else fail(RS_INTERNAL, "Internal", "product", "unsupported channel count");
+    }
   }
 
   void build_common(rs_ctx *c, Tree &&t, double chi, int leaf_pairs) {
@@ -637,7 +698,7 @@ void rsg::vfrac_apply_strided(rs_vfrac *V, double scale, int nb, const double *x
     vertex_m_kernel<<<nblk(V->nv, 256), 256, 0, s>>>(V->order.p, xs + q0 * ldx, ldx, V->nv, k, CC, V->h.m.p);
     RSG_LAUNCHED(V->h.ctx, "vertex_m");
     V->h.product(CC, CC);
-    vertex_out_kernel<<<nblk(V->nv, 256), 256, 0, s>>>(V->order.p, V->h.el.p, V->h.z.p, V->nv, k, CC,
+    vertex_out_kernel<<<nblk(V->nv, 256), 256, 0, s>>>(V->order.p, V->h.xh.p, V->h.z.p, V->nv, k, CC,
                                                        scale, ys + q0 * ldy, ldy);
     RSG_LAUNCHED(V->h.ctx, "vertex_out");
   }

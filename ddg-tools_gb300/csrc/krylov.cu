@@ -103,8 +103,9 @@ void gmres_batch(rs_ctx *ctx, const Operator &A, const Operator *P, int nb, cons
                  double *x, const GmresOptions &opt, std::vector<GmresReport> &reports) {
   using clk = std::chrono::steady_clock;
   auto t0 = clk::now();
-  if (opt.restart < 1 || opt.max_iterations < 1 || !(opt.tolerance > 0.0 && opt.tolerance < 1.0))
-    fail(RS_INVALID_OPTION, "InvalidOption", "gmres", "restart >= 1, max_iterations >= 1, tolerance in (0, 1)");
+  if (opt.restart < 1 || opt.restart > 63 || opt.max_iterations < 1 || !(opt.tolerance > 0.0 && opt.tolerance < 1.0))
+    fail(RS_INVALID_OPTION, "InvalidOption", "gmres",
+         "restart in 1..63, max_iterations >= 1, tolerance in (0, 1)");
   const size_t n = A.n;
   const int m = (int)std::min<size_t>((size_t)opt.restart, std::max<size_t>(n, 1));
   cudaStream_t s = ctx->stream;

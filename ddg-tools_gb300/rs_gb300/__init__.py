@@ -43,6 +43,15 @@ class SolverOptions(C.Structure):
                 ("vcycles", C.c_int), ("preconditioner", C.c_int)]
 
 
+class FlowOptions(C.Structure):
+    """rs_flow_options of include/rsgpu.h (FlowOptions, RS/src/step/options.rs:290-382)."""
+
+    _fields_ = [("alpha", C.c_double), ("beta", C.c_double), ("theta", C.c_double),
+                ("leaf_size", C.c_int), ("solver", SolverOptions), ("hold_area", C.c_int),
+                ("hold_volume", C.c_int), ("armijo_c", C.c_double), ("max_halvings", C.c_int),
+                ("newton_max", C.c_int)]
+
+
 class RsError(RuntimeError):
     """An error of the library: ``kind`` is the crate's RsError variant name, ``operation`` the
     failing operation word (RsError::Gpu { operation, detail }, RS/src/gpu/cuda.rs:19-24)."""
@@ -114,6 +123,9 @@ def load_library(path: str | os.PathLike | None = None):
         "rs_solver_precondition_device": [_vp, C.c_int, _vp, _vp],
         "rs_solver_solve_many": [_vp, C.c_int, _f64p, _f64p, _f64p],
         "rs_solver_solve_many_device": [_vp, C.c_int, _vp, _vp, _f64p],
+        "rs_flow_create": [_vp, C.c_int, C.c_int, _u32p, _f64p, C.c_void_p, C.POINTER(_vp)],
+        "rs_flow_step": [_vp, _f64p],
+        "rs_flow_positions": [_vp, _f64p],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -123,6 +135,10 @@ def load_library(path: str | os.PathLike | None = None):
     L.rs_ctx_free.restype = None
     L.rs_solver_options_default.restype = SolverOptions
     L.rs_solver_options_default.argtypes = []
+    L.rs_flow_options_default.restype = FlowOptions
+    L.rs_flow_options_default.argtypes = []
+    L.rs_flow_free.argtypes = [_vp]
+    L.rs_flow_free.restype = None
     for name in ("rs_bh_free", "rs_metric_free", "rs_vfrac_free", "rs_solver_free"):
         getattr(L, name).argtypes = [_vp]
         getattr(L, name).restype = None
@@ -555,3 +571,51 @@ class SaddleSolver:
             r["iterations"] = int(r["iterations"])
             r["converged"] = bool(r["converged"])
         return out, reports
+
+
+def flow_options(**kw) -> FlowOptions:
+    """The library defaults (rs_flow_options_default); keys of the solver options may be given
+    with a ``solver_`` prefix."""
+    o = load_library().rs_flow_options_default()
+    for k, v in kw.items():
+        if k.startswith("solver_"):
+            setattr(o.solver, k[7:], v)
+        else:
+            setattr(o, k, v)
+    return o
+
+
+FLOW_REPORT_KEYS = ["energy_before", "energy_after", "tau", "halvings", "gmres_area", "gmres_volume",
+                    "gmres_direction", "relative_residual", "seconds", "seconds_tree", "seconds_energy",
+                    "seconds_solver_build", "seconds_solve", "seconds_line_search", "seconds_projection",
+                    "accepted", "slope", "constraint_residual"]
+
+
+class Flow:
+    """The repulsive-surface flow (Session, RS/src/step/session.rs): one Hs descent step per
+    call of ``step()`` on the GPU (no remeshing, no collision detection)."""
+
+    def __init__(self, faces, positions, options: FlowOptions | None = None, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        faces, positions = _mesh(faces, positions)
+        self.n_vertices = len(positions)
+        o = options or flow_options()
+        h = _vp()
+        _check(_lib.rs_flow_create(self.ctx.handle, len(positions), len(faces), faces.ravel(),
+                                   positions.ravel(), C.byref(o), C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.rs_flow_free(self._h)
+            self._h = None
+
+    def step(self) -> dict:
+        rep = np.zeros(len(FLOW_REPORT_KEYS))
+        _check(_lib.rs_flow_step(self._h, rep))
+        return dict(zip(FLOW_REPORT_KEYS, rep.tolist()))
+
+    def positions(self) -> np.ndarray:
+        out = np.empty((self.n_vertices, 3))
+        _check(_lib.rs_flow_positions(self._h, out.ravel()))
+        return out

@@ -243,6 +243,42 @@ int rs_solver_solve_many(rs_solver *s, int nb, const double *rhs_host, double *s
 int rs_solver_solve_many_device(rs_solver *s, int nb, const double *rhs_dev, double *sol_dev,
                                 double *report);
 
+/* ---------------------------------------------------------------- one Hs step */
+
+typedef struct rs_flow rs_flow; /* Session (RS/src/step/session.rs:371-1369), step_inner's
+                                   energy / solve / line-search / projection parts */
+
+typedef struct rs_flow_options {
+  double alpha, beta;        /* exponents (6, 12) */
+  double theta;              /* Barnes-Hut opening (BhOptions, 0.5) */
+  int leaf_size;             /* (8) */
+  rs_solver_options solver;  /* FLOW_GMRES defaults: restart 60, tolerance 1e-3 */
+  int hold_area;             /* hold the initial total area (a Schur row) */
+  int hold_volume;           /* hold the initial volume (a Schur row) */
+  double armijo_c;           /* ArmijoRule::Standard c (1e-2) */
+  int max_halvings;          /* line-search halvings before a step is refused (30) */
+  int newton_max;            /* NewtonSteps::UntilTolerance max (5) */
+} rs_flow_options;
+
+rs_flow_options rs_flow_options_default(void);
+
+/* Session::new (session.rs:371): the surface, its positions and the options; the initial
+ * barycenter (always held), area and volume become the targets. */
+int rs_flow_create(rs_ctx *ctx, int nv, int nf, const uint32_t *faces,
+                   const double *positions_host, const rs_flow_options *opts, rs_flow **out);
+void rs_flow_free(rs_flow *f);
+
+#define RS_FLOW_REPORT_LEN 18
+/* Session::step (session.rs:724-747): one step. report[RS_FLOW_REPORT_LEN]:
+ *  0 energy before, 1 energy after, 2 accepted tau (0: refused), 3 halvings,
+ *  4..6 GMRES iterations of the solves (area row, volume row, direction),
+ *  7 worst true relative residual, 8 seconds of the step, 9 tree and lists, 10 energy,
+ *  11 solver build, 12 solves, 13 line search, 14 projection, 15 accepted (1/0),
+ *  16 slope g.x, 17 relative nonlinear-constraint residual after the projection. */
+int rs_flow_step(rs_flow *f, double *report);
+/* The current positions (V x 3). */
+int rs_flow_positions(rs_flow *f, double *positions_host);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,51 @@
+"""One Hs descent step on the GPU (Session::step_inner without remeshing / collisions):
+the energy decreases (Armijo), the held area and volume come back to their targets after the
+projection, the barycenter stays put, and the saddle solves converge."""
+import numpy as np
+import pytest
+
+import rs_oracle as O
+import rs_gb300 as R
+from rs_gb300 import generators as gen
+
+pytestmark = pytest.mark.gpu
+
+
+def _area_volume(P, F):
+    a, _, _ = O.face_geometry(P, F)
+    p0, p1, p2 = P[F[:, 0]], P[F[:, 1]], P[F[:, 2]]
+    vol = np.sum(np.einsum("ij,ij->i", p0, np.cross(p1, p2))) / 6.0
+    return a.sum(), vol
+
+
+@pytest.mark.parametrize("hold", [(0, 0), (1, 1)])
+def test_flow_steps(hold):
+    P, F = gen.noisy_torus(48, 24, 1.0, 0.3, 0.003, 7)
+    opts = R.flow_options(theta=0.5, hold_area=hold[0], hold_volume=hold[1], solver_tolerance=1e-6,
+                          solver_restart=30)
+    flow = R.Flow(F, P, opts)
+    A0, V0 = _area_volume(P, F)
+    a, _, _ = O.face_geometry(P, F)
+    energies = []
+    for _ in range(3):
+        rep = flow.step()
+        print(rep)
+        assert rep["accepted"] == 1.0
+        assert rep["energy_after"] < rep["energy_before"]
+        assert rep["relative_residual"] <= 1e-6
+        assert rep["slope"] > 0.0
+        energies.append(rep["energy_after"])
+    Q = flow.positions()
+    A1, V1 = _area_volume(Q, F)
+    if hold[0]:
+        assert abs(A1 - A0) / A0 < 1e-8
+        assert abs(V1 - V0) / abs(V0) < 1e-8
+    mass = np.zeros(len(P))
+    np.add.at(mass, F.ravel().astype(np.int64), np.repeat(a / 3.0, 3))
+    a1, _, _ = O.face_geometry(Q, F)
+    m1 = np.zeros(len(P))
+    np.add.at(m1, F.ravel().astype(np.int64), np.repeat(a1 / 3.0, 3))
+    b0 = (mass[:, None] * P).sum(0) / mass.sum()
+    b1 = (m1[:, None] * Q).sum(0) / m1.sum()
+    assert np.abs(b1 - b0).max() < 1e-10
+    assert energies == sorted(energies, reverse=True)

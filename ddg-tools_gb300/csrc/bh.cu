@@ -94,13 +94,16 @@ __global__ void refit_kernel(BhDev d, const double *__restrict__ pos) {
     if (p >= s1) break;
     double o0 = xb[i][0] - cx, o1 = xb[i][1] - cy, o2 = xb[i][2] - cz;
     float h0 = (float)o0, h1 = (float)o1, h2 = (float)o2;
+    // alpha = N . (X - X_leaf) as a float pair: hi in fnl.w, lo in fol.w
+    double alpha = nr[i][0] * o0 + nr[i][1] * o1 + nr[i][2] * o2;
+    float al = (float)alpha;
     d.fxa[p] = make_float4(h0, h1, h2, (float)ar[i]);
-    d.fol[p] = make_float4((float)(o0 - (double)h0), (float)(o1 - (double)h1), (float)(o2 - (double)h2), 0.f);
+    d.fol[p] = make_float4((float)(o0 - (double)h0), (float)(o1 - (double)h1), (float)(o2 - (double)h2),
+                           (float)(alpha - (double)al));
     float n0 = (float)nr[i][0], n1 = (float)nr[i][1], n2 = (float)nr[i][2];
     d.fnn[p] = make_float4(n0, n1, n2, 0.f);
-    double alpha = nr[i][0] * o0 + nr[i][1] * o1 + nr[i][2] * o2;
     d.fnl[p] = make_float4((float)(nr[i][0] - (double)n0), (float)(nr[i][1] - (double)n1),
-                           (float)(nr[i][2] - (double)n2), (float)alpha);
+                           (float)(nr[i][2] - (double)n2), al);
   }
   d.nmom[leaf] = make_double4(M0, M1, M2, A);
   store_centroid(d, leaf, cx, cy, cz, A);
@@ -265,17 +268,30 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &t) {
 // N . o for a unit normal and an offset both held as float pairs (hi + lo), compensated
 // (the Dot2 scheme of Ogita, Rump and Oishi, 2005): the sum of the three products carries its
 // rounding errors, which matters because it nearly cancels for a smooth surface.
-__device__ __forceinline__ float dot2(float nx, float ny, float nz, float lx, float ly, float lz,
-                                      float ox, float oy, float oz, float px, float py, float pz) {
-  float p0, e0, p1, e1, p2, e2, s, t0, u, t1;
+// The result is left unrounded as u + lo.
+__device__ __forceinline__ void dot2(float nx, float ny, float nz, float lx, float ly, float lz,
+                                     float ox, float oy, float oz, float px, float py, float pz,
+                                     float &u, float &lo) {
+  float p0, e0, p1, e1, p2, e2, s, t0, t1;
   two_prod(nx, ox, p0, e0);
   two_prod(ny, oy, p1, e1);
   two_prod(nz, oz, p2, e2);
   two_sum(p0, p1, s, t0);
   two_sum(s, p2, u, t1);
-  float lo = ((e0 + e1) + (e2 + t0)) + t1;
+  lo = ((e0 + e1) + (e2 + t0)) + t1;
   lo += (nx * px + ny * py + nz * pz) + (lx * ox + ly * oy + lz * oz);
-  return u + lo;
+}
+
+// X_L - X_C from two centroids held as float pairs, as a float pair (h + l) per axis.
+__device__ __forceinline__ void pair_diff(const float4 &ah, const float4 &al, const float4 &bh,
+                                          const float4 &bl, float (&h)[3], float (&l)[3]) {
+  float t0, t1, t2;
+  two_sum(ah.x, -bh.x, h[0], t0);
+  two_sum(ah.y, -bh.y, h[1], t1);
+  two_sum(ah.z, -bh.z, h[2], t2);
+  l[0] = t0 + (al.x - bl.x);
+  l[1] = t1 + (al.y - bl.y);
+  l[2] = t2 + (al.z - bl.z);
 }
 
 // The pair kernel. One warp per work item: a slice of one target leaf's lumped and exact
@@ -287,9 +303,13 @@ __device__ __forceinline__ float dot2(float nx, float ny, float nz, float lx, fl
 // accumulators and are written per work item (leaf_with_gradient, barnes_hut.rs:627-689; value
 // only: leaf_energy, barnes_hut.rs:583-614).
 //
-// For exact (near) pairs nu = N_S . (X_S - X_T) is formed as alpha_S + N_S.(X_L - X_C) -
-// N_S.(X_T - X_C) with float-pair normals and offsets and compensated dot products: on a
-// smooth surface nu is ~|v|^2 kappa, far below |v|, and plain FP32 loses it.
+// nu = N_S . (X_S - X_T) is formed from float pairs with compensated dot products: on a
+// smooth surface nu is ~|v|^2 kappa, far below |v|, plain FP32 loses it, and the differential
+// (a sum of large terms that cancel around every vertex) inherits the loss. Lumped entries:
+// nu = alpha_S + N_S.(X_L - X_C); exact entries: nu = [alpha_S + N_S.(X_L - X_C)] - N_S.(X_T - X_C)
+// with the bracket kept as a float pair per entry, and v = X_S - X_T summed with its rounding
+// error (leaf offsets can be large next to |v| in a stretched leaf). alpha_S = N_S.(X_S - X_L)
+// is a float pair from the FP64 refit.
 template <bool GRAD, bool FAST>
 __global__ void __launch_bounds__(128) bh_pair_kernel(BhDev d, Pow pw) {
   const int lane = threadIdx.x & 31;
@@ -310,6 +330,7 @@ __global__ void __launch_bounds__(128) bh_pair_kernel(BhDev d, Pow pw) {
     const float4 xs = act ? d.fxa[s0 + s] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 nS = act ? d.fnn[s0 + s] : make_float4(0.f, 0.f, 1.f, 0.f);
     const float4 nL = act ? d.fnl[s0 + s] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 xsl = act ? d.fol[s0 + s] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 cLh = d.nch[leaf], cLl = d.ncl[leaf];
     const float a_s = xs.w;
     Kahan e_acc, da_acc, dx0, dx1, dx2, dn0, dn1, dn2;
@@ -328,17 +349,21 @@ __global__ void __launch_bounds__(128) bh_pair_kernel(BhDev d, Pow pw) {
         if (q < lhi) {
           const uint32_t c = d.lumped[q];
           const float4 ch = d.nch[c], cl = d.ncl[c];
-          v0 = ((cLh.x - ch.x) + (cLl.x - cl.x)) + xs.x;
-          v1 = ((cLh.y - ch.y) + (cLl.y - cl.y)) + xs.y;
-          v2 = ((cLh.z - ch.z) + (cLl.z - cl.z)) + xs.z;
+          float h[3], l[3];
+          pair_diff(cLh, cLl, ch, cl, h, l);
+          v0 = (xs.x + h[0]) + l[0];
+          v1 = (xs.y + h[1]) + l[1];
+          v2 = (xs.z + h[2]) + l[2];
           Ac = ch.w;
-        }
-        if (ok) {
-          float r2 = v0 * v0 + v1 * v1 + v2 * v2;
-          float ir2 = __fdividef(1.f, r2);
-          float nu = nS.x * v0 + nS.y * v1 + nS.z * v2;
-          kernel_k<FAST>(pw, nu, r2, ir2, K, cn);
-          g = pw.beta * K * ir2;
+          if (ok) {
+            float u, lo;
+            dot2(nS.x, nS.y, nS.z, nL.x, nL.y, nL.z, h[0], h[1], h[2], l[0], l[1], l[2], u, lo);
+            const float nu = nL.w + (u + (lo + xsl.w));
+            float r2 = v0 * v0 + v1 * v1 + v2 * v2;
+            float ir2 = __fdividef(1.f, r2);
+            kernel_k<FAST>(pw, nu, r2, ir2, K, cn);
+            g = pw.beta * K * ir2;
+          }
         }
         be += a_s * K * Ac;
         if (GRAD) {
@@ -370,21 +395,18 @@ __global__ void __launch_bounds__(128) bh_pair_kernel(BhDev d, Pow pw) {
       const uint32_t q = base + j;
       const bool qok = q < ehi;
       uint32_t c = 0, cs = 0, nc = 0;
-      float d0 = 0.f, d1 = 0.f, d2 = 0.f, ab = 0.f;
+      float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f}, abh = 0.f, abl = 0.f;
       if (qok) {
         c = d.exact[q];
         cs = d.node_start[c];
         nc = d.node_end[c] - cs;
         const float4 ch = d.nch[c], cl = d.ncl[c];
-        // d = X_L - X_C as a float pair (hi + lo) from the centroids' float pairs
-        float h0, t0, h1, t1, h2, t2;
-        two_sum(cLh.x, -ch.x, h0, t0);
-        two_sum(cLh.y, -ch.y, h1, t1);
-        two_sum(cLh.z, -ch.z, h2, t2);
-        const float l0 = t0 + (cLl.x - cl.x), l1 = t1 + (cLl.y - cl.y), l2 = t2 + (cLl.z - cl.z);
-        d0 = h0 + l0, d1 = h1 + l1, d2 = h2 + l2;
-        // alpha_S + N_S . (X_L - X_C)
-        ab = nL.w + dot2(nS.x, nS.y, nS.z, nL.x, nL.y, nL.z, h0, h1, h2, l0, l1, l2);
+        pair_diff(cLh, cLl, ch, cl, h, l);  // X_L - X_C
+        // alpha_S + N_S . (X_L - X_C) as a float pair
+        float u, lo, t;
+        dot2(nS.x, nS.y, nS.z, nL.x, nL.y, nL.z, h[0], h[1], h[2], l[0], l[1], l[2], u, lo);
+        two_sum(nL.w, u, abh, t);
+        abl = (t + lo) + xsl.w;
       }
       float P[32];
       float row = 0.f, rx0 = 0.f, rx1 = 0.f, rx2 = 0.f, rn0 = 0.f, rn1 = 0.f, rn2 = 0.f;
@@ -397,12 +419,19 @@ __global__ void __launch_bounds__(128) bh_pair_kernel(BhDev d, Pow pw) {
           const bool self = (c == leaf) && (t == s);
           if (act && !self) {
             const float4 xl = d.fol[cs + t];  // offset lo part of T
-            v0 = (xs.x - xt.x) + d0;
-            v1 = (xs.y - xt.y) + d1;
-            v2 = (xs.z - xt.z) + d2;
+            float w0, e0, w1, e1, w2, e2;
+            two_sum(xs.x, -xt.x, w0, e0);
+            two_sum(xs.y, -xt.y, w1, e1);
+            two_sum(xs.z, -xt.z, w2, e2);
+            v0 = (w0 + h[0]) + ((e0 + l[0]) + (xsl.x - xl.x));
+            v1 = (w1 + h[1]) + ((e1 + l[1]) + (xsl.y - xl.y));
+            v2 = (w2 + h[2]) + ((e2 + l[2]) + (xsl.z - xl.z));
             float r2 = v0 * v0 + v1 * v1 + v2 * v2;
             float ir2 = __fdividef(1.f, r2);
-            float nu = ab - dot2(nS.x, nS.y, nS.z, nL.x, nL.y, nL.z, xt.x, xt.y, xt.z, xl.x, xl.y, xl.z);
+            float ph, pl, sh, se;
+            dot2(nS.x, nS.y, nS.z, nL.x, nL.y, nL.z, xt.x, xt.y, xt.z, xl.x, xl.y, xl.z, ph, pl);
+            two_sum(abh, -ph, sh, se);
+            const float nu = sh + (se + (abl - pl));
             kernel_k<FAST>(pw, nu, r2, ir2, K, cn);
             g = pw.beta * K * ir2;
           }
@@ -1066,6 +1095,7 @@ int rs_bh_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const double
     h->pos.upload(positions_host, 3 * (size_t)nv, h->st());
     refit_device(h.get());
     RSG_CUDA("upload", cudaStreamSynchronize(h->st()));
+    ctx_retain(ctx);
     *out = h.release();
   });
 }
@@ -1144,15 +1174,18 @@ int rs_bh_attach(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const doubl
     h->pos.upload(positions_host, 3 * (size_t)nv, s);
     refit_device(h.get());
     RSG_CUDA("upload", cudaStreamSynchronize(s));
+    ctx_retain(ctx);
     *out = h.release();
   });
 }
 
 void rs_bh_free(rs_bh *bh) {
   if (!bh) return;
-  cudaSetDevice(bh->ctx->device);
-  cudaStreamSynchronize(bh->ctx->stream);
+  rs_ctx *ctx = bh->ctx;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
   delete bh;
+  ctx_release(ctx);
 }
 
 int rs_bh_refit(rs_bh *h, const double *positions_host) {

@@ -2,6 +2,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include <cstdint>
 #include <cstring>
 #include <stdexcept>
@@ -93,6 +95,9 @@ struct DevBuf {
 }  // namespace rsg
 
 struct rs_ctx {
+  // Owners: the caller's handle plus every object built on the context (trees, operators,
+  // solvers, flows); the last release destroys it, so handles may be freed in any order.
+  std::atomic<int> refs{1};
   int device = 0;
   cudaStream_t stream = nullptr;
   int sm_count = 0;
@@ -105,6 +110,11 @@ struct rs_ctx {
   void *staging(size_t bytes);
   void use() const;  // makes the context's device current for the calling thread
 };
+
+namespace rsg {
+rs_ctx *ctx_retain(rs_ctx *ctx);
+void ctx_release(rs_ctx *ctx);
+}  // namespace rsg
 
 // Counts one kernel launch of `ctx` and checks the launch status.
 #define RSG_LAUNCHED(ctx, what)                                   \

@@ -40,6 +40,22 @@ void *rs_ctx::staging(size_t bytes) {
 
 void rs_ctx::use() const { RSG_CUDA("context", cudaSetDevice(device)); }
 
+rs_ctx *rsg::ctx_retain(rs_ctx *ctx) {
+  ctx->refs.fetch_add(1);
+  return ctx;
+}
+
+void rsg::ctx_release(rs_ctx *ctx) {
+  if (!ctx || ctx->refs.fetch_sub(1) != 1) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaStreamDestroy(ctx->stream);
+  }
+  if (ctx->pinned) cudaFreeHost(ctx->pinned);
+  delete ctx;
+}
+
 extern "C" {
 
 const char *rs_last_error(void) { return rsg::last_detail(); }
@@ -95,16 +111,7 @@ int rs_ctx_create(int ordinal, rs_ctx **out) {
   });
 }
 
-void rs_ctx_free(rs_ctx *ctx) {
-  if (!ctx) return;
-  cudaSetDevice(ctx->device);
-  if (ctx->stream) {
-    cudaStreamSynchronize(ctx->stream);
-    cudaStreamDestroy(ctx->stream);
-  }
-  if (ctx->pinned) cudaFreeHost(ctx->pinned);
-  delete ctx;
-}
+void rs_ctx_free(rs_ctx *ctx) { rsg::ctx_release(ctx); }
 
 int rs_ctx_stream(rs_ctx *ctx, void **stream) {
   return rsg::guard([&] { *stream = (void *)ctx->stream; });

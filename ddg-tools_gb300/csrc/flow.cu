@@ -182,11 +182,17 @@ int rs_flow_create(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const dou
     F->area0 = total_area(nf, faces, positions_host);
     F->vol0 = total_volume(nf, faces, positions_host);
     barycenter(nv, nf, faces, positions_host, F->bary0);
+    ctx_retain(ctx);
     *out = F.release();
   });
 }
 
-void rs_flow_free(rs_flow *F) { delete F; }
+void rs_flow_free(rs_flow *F) {
+  if (!F) return;
+  rs_ctx *ctx = F->ctx;
+  delete F;
+  ctx_release(ctx);
+}
 
 int rs_flow_positions(rs_flow *F, double *positions_host) {
   return guard([&] { std::memcpy(positions_host, F->pos.data(), F->pos.size() * sizeof(double)); });
@@ -252,12 +258,11 @@ int rs_flow_step(rs_flow *F, double *report) {
     std::vector<double> hs((size_t)nb * n);
     sol.download(hs.data(), hs.size(), s);
     RSG_CUDA("flow", cudaStreamSynchronize(s));
+    // GMRES iterations per right-hand side: the held rows (area, volume), then the direction
     double worst = 0.0;
-    for (int q = 0; q < nb; ++q) {
-      if (q < 3) rep[4 + q] = srep[5 * q];
-      worst = std::max(worst, srep[5 * q + 1]);
-    }
-    if (k < 2) rep[4 + k] = srep[5 * k], rep[4 + (k == 0 ? 2 : 2)] = srep[5 * k];
+    for (int q = 0; q < nb; ++q) worst = std::max(worst, srep[5 * q + 1]);
+    for (int i = 0; i < k; ++i) rep[4 + rows[i]] = srep[5 * i];
+    rep[6] = srep[5 * k];
     rep[7] = worst;
     const double *y = hs.data() + (size_t)k * n;
     // N = C_N Z (k x k), equilibrated, pivoted Cholesky with drop (schur.rs:230-289)

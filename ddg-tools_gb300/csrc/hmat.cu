@@ -35,6 +35,14 @@
 namespace rsg {
 
 constexpr int FACE = 0, VERTEX = 1;
+// Which of the two kernels a channel uses: FACE_CH (vector q owns channels 12q..12q+11, the
+// last three of them the averages, kernel 1), VERTEX_CH (kernel 0 throughout), ONES (channel
+// c uses kernel c: the two-channel pass that forms the far part of H~a).
+constexpr int FACE_CH = 0, VERTEX_CH = 1, ONES = 2;
+template <int SEL>
+__device__ __forceinline__ bool uses_k1(int c) {
+  return SEL == FACE_CH ? (c % 12) >= 9 : (SEL == ONES ? c == 1 : false);
+}
 
 struct HDev {
   const uint32_t *start, *end, *right, *parent, *leaves, *chain_off, *chain;
@@ -43,32 +51,72 @@ struct HDev {
   const float4 *xh;          // per BVH position: position hi (xyz), weight a (w)
   const float4 *xl;          // per BVH position: position lo (xyz): X = hi + lo to ~48 bits
   const float4 *nrm;         // per BVH position: normal (faces only)
-  const float2 *leaf_farA;   // per leaf: the far part of H~a along its chain (k_0, k_1)
+  const float2 *node_farA;   // per node: its far sums of psi = a (k_0, k_1), the far part of H~a
   const uint2 *cols;         // near column ranges [x, y) of every leaf's chain, leaf by leaf
   const uint4 *items;        // per work item: leaf ordinal, column-range begin / end, -
   const uint32_t *item_off;  // per leaf: its work items [item_off[k], item_off[k + 1])
-  float *up;                 // per node: C channel sums
+  float *up;                 // per node: C channel sums of a m (hi parts)
   float *farx;               // per node: C channel far sums
-  float *part;               // per work item: 8 rows x (C + 2) partial near sums
+  float2 *part;              // per work item: 8 rows x C near sums as float pairs
   uint32_t *count;           // per node: arrival counter of the upward pass
-  const float *m;            // [n][C]
-  float *z;                  // [n][C]
+  const float2 *m;           // [n][C] channel values as float pairs (hi, lo)
+  float2 *z;                 // [n][C] results as float pairs
   int n_nodes, n_leaves, n_el, n_items, C;
-  float neg_s;               // kernel exponent applied to r^2
+  float neg_s;               // kernel exponent e applied to r^2: r2^e
+  int pw_mode, pw_k;         // e = pw_k / pw_mode for pw_mode 2 or 3 (exact roots), else powf
 };
+
+// Error-free sum (Knuth): a + b = s + t exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &t) {
+  s = a + b;
+  const float bv = s - a;
+  t = (a - (s - bv)) + (b - bv);
+}
+
+// (h, l) += (oh, ol) for float pairs.
+__device__ __forceinline__ void pair_add(float &h, float &l, float oh, float ol) {
+  float s, t;
+  two_sum(h, oh, s, t);
+  h = s;
+  l = (l + ol) + t;
+}
+
+__device__ __forceinline__ float ipow(float x, int n) {
+  float r = 1.f;
+  for (; n > 0; --n) r *= x;
+  return r;
+}
+
+// r2^e. For e = k/3 or k/2 (the exponents of integer alpha, beta) the power is an integer
+// power times a correctly rounded root: a few roundings, independent of the size of
+// log r2 (exp2(e log2 r2) loses accuracy in proportion to it).
+__device__ __forceinline__ float r2pow(const HDev &d, float r2, float ir2) {
+  if (d.pw_mode == 3 || d.pw_mode == 2) {
+    const int q = d.pw_mode, k = d.pw_k;
+    const int a = (k >= 0) ? k / q : -((-k + q - 1) / q);  // floor(k / q)
+    const int b = k - q * a;                                // 0 .. q-1
+    float base = a >= 0 ? ipow(r2, a) : ipow(ir2, -a);
+    if (b) {
+      const float root = q == 3 ? cbrtf(r2) : sqrtf(r2);
+      base *= b == 1 ? root : root * root;
+    }
+    return base;
+  }
+  return powf(r2, d.neg_s);
+}
 
 // The near kernel values of an element pair (hierarchical.rs:185-189, 224-231 and 987-991):
 // faces: [r2^-s, (nu_p^2 + nu_q^2)/2 r2^-2 r2^-s]; vertices: [r2^e].
 template <int KIND>
-__device__ __forceinline__ void near_kernel(float d0, float d1, float d2, const float4 &np,
-                                            const float4 &nq, float neg_s, float &k0, float &k1) {
-  float r2 = d0 * d0 + d1 * d1 + d2 * d2;
-  float h = exp2f(neg_s * log2f(r2));
+__device__ __forceinline__ void near_kernel(const HDev &d, float d0, float d1, float d2,
+                                            const float4 &np, const float4 &nq, float &k0, float &k1) {
+  const float r2 = d0 * d0 + d1 * d1 + d2 * d2;
+  const float ir2 = __frcp_rn(r2);
+  const float h = r2pow(d, r2, ir2);
   k0 = h;
   if (KIND == FACE) {
-    float a = np.x * d0 + np.y * d1 + np.z * d2;
-    float b = nq.x * d0 + nq.y * d1 + nq.z * d2;
-    float ir2 = __fdividef(1.f, r2);
+    const float a = np.x * d0 + np.y * d1 + np.z * d2;
+    const float b = nq.x * d0 + nq.y * d1 + nq.z * d2;
     k1 = 0.5f * (a * a + b * b) * ir2 * ir2 * h;
   } else {
     k1 = h;
@@ -87,9 +135,9 @@ __global__ void hm_upward_kernel(HDev d) {
   for (int c = 0; c < CC; ++c) u[c] = 0.f;
   for (uint32_t p = d.start[leaf]; p < d.end[leaf]; ++p) {
     float a = d.xh[p].w;
-    const float *mp = d.m + (size_t)p * CC;
+    const float2 *mp = d.m + (size_t)p * CC;
 #pragma unroll
-    for (int c = 0; c < CC; ++c) u[c] += a * mp[c];
+    for (int c = 0; c < CC; ++c) u[c] += a * mp[c].x;
   }
   float *o = d.up + (size_t)leaf * CC;
 #pragma unroll
@@ -112,9 +160,9 @@ __global__ void hm_upward_kernel(HDev d) {
 
 // farx[a][c] = sum over the far blocks (a, b) of h(a, b)[kernel(c)] up[b][c] (block_tree.rs:
 // 564-578); one warp per node, lanes strided over the node's far blocks, each summing all CC
-// channels, then a fixed butterfly over the lanes. `split` = first channel of kernel 1.
-template <int CC>
-__global__ void hm_far_kernel(HDev d, int split) {
+// channels, then a fixed butterfly over the lanes.
+template <int SEL, int CC>
+__global__ void hm_far_kernel(HDev d) {
   int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (a >= d.n_nodes) return;
@@ -125,7 +173,7 @@ __global__ void hm_far_kernel(HDev d, int split) {
     float2 k = d.far_coef[q];
     const float *u = d.up + (size_t)d.far_col[q] * CC;
 #pragma unroll
-    for (int c = 0; c < CC; ++c) acc[c] += (c < split ? k.x : k.y) * u[c];
+    for (int c = 0; c < CC; ++c) acc[c] += (uses_k1<SEL>(c) ? k.y : k.x) * u[c];
   }
 #pragma unroll
   for (int c = 0; c < CC; ++c)
@@ -137,13 +185,17 @@ __global__ void hm_far_kernel(HDev d, int split) {
     if (lane == (c & 31)) o[c] = acc[c];
 }
 
-// Near sums of one work item (a slice of a leaf's chain near-column ranges). One warp per
-// item; lane = r + 8 j: r the row (element) of the leaf, j one of four column groups taking
-// every fourth column. Each column's kernel values are evaluated once per row and applied to
-// all CC channels; the near part of H~a is summed in the same loop. Lanes j = 0 write the
-// item's partial sums (CC + 2 per row).
+// Near sums of one work item (a slice of a leaf's chain near-column ranges) in difference
+// form: sum_q w_pq (m_p - m_q) for channels [c0, c0 + CC) of the row's element p. One warp
+// per item; lane = r + 8 j: r the row (element) of the leaf, j one of four column groups
+// taking every fourth column. The kernel values of a column are evaluated once per row and
+// applied to the CC channels. m_p - m_q is formed from the float pairs (exact for nearby
+// values) and the terms are summed with Kahan compensation, then combined over the groups as
+// float pairs: for a smooth input the terms are first-order quantities that cancel to a
+// second-order result, and the output stage (M^T, a discrete divergence) cancels once more,
+// so plain FP32 sums of H~a m and H~(a m) would lose about four digits.
 template <int KIND, int CC>
-__global__ void __launch_bounds__(128) hm_rows_kernel(HDev d, int split) {
+__global__ void __launch_bounds__(128) hm_rows_kernel(HDev d, int c0) {
   const int lane = threadIdx.x & 31;
   const int r = lane & 7, j = lane >> 3;
   const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -155,10 +207,18 @@ __global__ void __launch_bounds__(128) hm_rows_kernel(HDev d, int split) {
   const uint32_t p = s0 + (act ? r : 0);
   const float4 ph = d.xh[p], pl = d.xl[p];
   const float4 np = KIND == FACE ? d.nrm[p] : make_float4(0.f, 0.f, 0.f, 0.f);
-  float acc[CC];
+  const int C = d.C;
+  float mh[CC], ml[CC], ks[CC], kc[CC];
+  {
+    const float4 *mp = reinterpret_cast<const float4 *>(d.m + (size_t)p * C + c0);
 #pragma unroll
-  for (int c = 0; c < CC; ++c) acc[c] = 0.f;
-  float sw0 = 0.f, sw1 = 0.f;
+    for (int c2 = 0; c2 < CC / 2; ++c2) {
+      const float4 v = mp[c2];
+      mh[2 * c2] = v.x, ml[2 * c2] = v.y, mh[2 * c2 + 1] = v.z, ml[2 * c2 + 1] = v.w;
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < CC; ++c) ks[c] = 0.f, kc[c] = 0.f;
   if (act)
     for (uint32_t ri = it.y; ri < it.z; ++ri) {
       const uint2 cr = d.cols[ri];
@@ -169,43 +229,48 @@ __global__ void __launch_bounds__(128) hm_rows_kernel(HDev d, int split) {
         const float d1 = (ph.y - qh.y) + (pl.y - ql.y);
         const float d2 = (ph.z - qh.z) + (pl.z - ql.z);
         float k0, k1;
-        near_kernel<KIND>(d0, d1, d2, np, KIND == FACE ? d.nrm[q] : np, d.neg_s, k0, k1);
+        near_kernel<KIND>(d, d0, d1, d2, np, KIND == FACE ? d.nrm[q] : np, k0, k1);
         const float w0 = k0 * qh.w, w1 = k1 * qh.w;
-        sw0 += w0;
-        sw1 += w1;
-        const float4 *mq = reinterpret_cast<const float4 *>(d.m + (size_t)q * CC);
+        const float4 *mq = reinterpret_cast<const float4 *>(d.m + (size_t)q * C + c0);
 #pragma unroll
-        for (int c4 = 0; c4 < CC / 4; ++c4) {
-          const float4 v = mq[c4];
-          const int c = 4 * c4;
-          acc[c] += (c < split ? w0 : w1) * v.x;
-          acc[c + 1] += (c + 1 < split ? w0 : w1) * v.y;
-          acc[c + 2] += (c + 2 < split ? w0 : w1) * v.z;
-          acc[c + 3] += (c + 3 < split ? w0 : w1) * v.w;
+        for (int c2 = 0; c2 < CC / 2; ++c2) {
+          const float4 v = mq[c2];
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            const int c = 2 * c2 + e;
+            const float qhv = e ? v.z : v.x, qlv = e ? v.w : v.y;
+            const float dm = (mh[c] - qhv) + (ml[c] - qlv);
+            const float t = ((KIND == FACE && c >= 9) ? w1 : w0) * dm;
+            const float y = t - kc[c];
+            const float tt = ks[c] + y;
+            kc[c] = (tt - ks[c]) - y;
+            ks[c] = tt;
+          }
         }
       }
     }
-  // reduce over the four column groups
+  // combine the four column groups as float pairs (h, l) = (s, -c)
 #pragma unroll
   for (int c = 0; c < CC; ++c) {
-    acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 8);
-    acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], 16);
-  }
-  sw0 += __shfl_xor_sync(0xffffffffu, sw0, 8);
-  sw0 += __shfl_xor_sync(0xffffffffu, sw0, 16);
-  sw1 += __shfl_xor_sync(0xffffffffu, sw1, 8);
-  sw1 += __shfl_xor_sync(0xffffffffu, sw1, 16);
-  if (j != 0) return;
-  float *o = d.part + ((size_t)w * 8 + r) * (CC + 2);
+    float h = ks[c], l = -kc[c];
 #pragma unroll
-  for (int c = 0; c < CC; ++c) o[c] = acc[c];
-  o[CC] = sw0, o[CC + 1] = sw1;
+    for (int m = 8; m <= 16; m <<= 1) {
+      const float oh = __shfl_xor_sync(0xffffffffu, h, m), ol = __shfl_xor_sync(0xffffffffu, l, m);
+      pair_add(h, l, oh, ol);
+    }
+    ks[c] = h, kc[c] = l;
+  }
+  if (j != 0 || !act) return;
+  float2 *o = d.part + ((size_t)w * 8 + r) * C + c0;
+#pragma unroll
+  for (int c = 0; c < CC; ++c) o[c] = make_float2(ks[c], kc[c]);
 }
 
-// Per leaf (thread per row): z = (H~a) m - H~(a m) from the items' near sums (in item order),
-// the far sums along the chain and the far part of H~a.
-template <int CC>
-__global__ void hm_epilogue_kernel(HDev d, int split) {
+// Per leaf (thread per row): z = near + (m_p H~a_far - H~(a m)_far), the near sums of the
+// items (in item order, as float pairs) plus the far sums along the chain (root to leaf). The
+// far part of H~a is summed in the same order from node_farA, so m = 1 gives z = 0 exactly.
+template <int SEL, int CC>
+__global__ void hm_epilogue_kernel(HDev d) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   int k = t >> 3, r = t & 7;
   if (k >= d.n_leaves) return;
@@ -213,40 +278,35 @@ __global__ void hm_epilogue_kernel(HDev d, int split) {
   const uint32_t s0 = d.start[leaf];
   if ((uint32_t)r >= d.end[leaf] - s0) return;
   const uint32_t p = s0 + r;
-  float acc[CC];
+  float nh[CC], nl[CC], fx[CC];
 #pragma unroll
-  for (int c = 0; c < CC; ++c) acc[c] = 0.f;
-  float sw0 = 0.f, sw1 = 0.f;
+  for (int c = 0; c < CC; ++c) nh[c] = 0.f, nl[c] = 0.f, fx[c] = 0.f;
   for (uint32_t i = d.item_off[k]; i < d.item_off[k + 1]; ++i) {
-    const float *o = d.part + ((size_t)i * 8 + r) * (CC + 2);
+    const float2 *o = d.part + ((size_t)i * 8 + r) * CC;
 #pragma unroll
-    for (int c = 0; c < CC; ++c) acc[c] += o[c];
-    sw0 += o[CC], sw1 += o[CC + 1];
+    for (int c = 0; c < CC; ++c) {
+      const float2 v = o[c];
+      pair_add(nh[c], nl[c], v.x, v.y);
+    }
   }
+  float fa0 = 0.f, fa1 = 0.f;
   for (uint32_t ci = d.chain_off[k]; ci < d.chain_off[k + 1]; ++ci) {
-    const float *f = d.farx + (size_t)d.chain[ci] * CC;
+    const uint32_t a = d.chain[ci];
+    const float *f = d.farx + (size_t)a * CC;
 #pragma unroll
-    for (int c = 0; c < CC; ++c) acc[c] += f[c];
+    for (int c = 0; c < CC; ++c) fx[c] += f[c];
+    const float2 fa = d.node_farA[a];
+    fa0 += fa.x, fa1 += fa.y;
   }
-  const float2 fa = d.leaf_farA[k];
-  const float ha0 = sw0 + fa.x, ha1 = sw1 + fa.y;
-  const float *mp = d.m + (size_t)p * CC;
-  float *zp = d.z + (size_t)p * CC;
+  const float2 *mp = d.m + (size_t)p * CC;
+  float2 *zp = d.z + (size_t)p * CC;
 #pragma unroll
-  for (int c = 0; c < CC; ++c) zp[c] = (c < split ? ha0 : ha1) * mp[c] - acc[c];
-}
-
-// Far part of H~a per leaf (the far field of psi = a, pushed down the chain).
-__global__ void hm_leaf_farA_kernel(HDev d, float2 *out) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= d.n_leaves) return;
-  float f0 = 0.f, f1 = 0.f;
-  for (uint32_t ci = d.chain_off[k]; ci < d.chain_off[k + 1]; ++ci) {
-    uint32_t a = d.chain[ci];
-    f0 += d.farx[2 * (size_t)a];
-    f1 += d.farx[2 * (size_t)a + 1];
+  for (int c = 0; c < CC; ++c) {
+    const float far = fmaf(mp[c].x, uses_k1<SEL>(c) ? fa1 : fa0, -fx[c]);
+    float h = nh[c], l = nl[c];
+    pair_add(h, l, far, 0.f);
+    zp[c] = make_float2(h, l);
   }
-  out[k] = make_float2(f0, f1);
 }
 
 // ------------------------------------------------------------------ face prologue / epilogue
@@ -255,37 +315,44 @@ struct FaceOps {
   const uint32_t *faces;   // 3F original order
   const uint32_t *order;   // BVH position -> face
   const uint32_t *position;  // face -> BVH position
-  const float *g;          // 9 per face (original order): g_c (df_coefficients, mod.rs:120-131)
-  const float *area;       // per face
+  // FP64 both: the gradient rows of a face sum to zero and the area-weighted rows around a
+  // vertex sum to zero, and a smooth input leaves only what survives those cancellations
+  const double *g;         // 9 per face (original order): g_c (df_coefficients, mod.rs:120-131)
+  const double *area;      // per face
   const uint32_t *inc_off, *inc;  // vertex -> (face << 2 | corner), faces ascending
   int nv, nf;
 };
 
-// m per face in BVH order (FaceMetricTree::product, hierarchical.rs:711-746): per vector q,
-// 9 gradient channels 9q + 3k + r = sum_c x[3 t_c + k] g_c[r], then 3 average channels
-// 9 nb + 3q + k = (x_0 + x_1 + x_2)/3 for axis k.
+__device__ __forceinline__ float2 split_pair(double v) {
+  const float h = (float)v;
+  return make_float2(h, (float)(v - (double)h));
+}
+
+// m per face in BVH order (FaceMetricTree::product, hierarchical.rs:711-746), in FP64 and
+// stored as float pairs; vector q owns channels 12q + (3k + r) = sum_c x[3 t_c + k] g_c[r]
+// (gradient) and 12q + 9 + k = (x_0 + x_1 + x_2)/3 for axis k (average).
 __global__ void face_m_kernel(FaceOps o, const double *__restrict__ xs, size_t ldx, int nb, int C,
-                              float *m) {
+                              float2 *m) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= o.nf) return;
   uint32_t f = o.order[p];
   const uint32_t *t = o.faces + 3 * (size_t)f;
-  const float *g = o.g + 9 * (size_t)f;
-  float *mp = m + (size_t)p * C;
+  const double *g = o.g + 9 * (size_t)f;
+  float2 *mp = m + (size_t)p * C;
   for (int q = 0; q < nb; ++q) {
     const double *x = xs + q * ldx;
     for (int k = 0; k < 3; ++k) {
-      float x0 = (float)x[3 * (size_t)t[0] + k], x1 = (float)x[3 * (size_t)t[1] + k],
-            x2 = (float)x[3 * (size_t)t[2] + k];
-      for (int r = 0; r < 3; ++r) mp[9 * q + 3 * k + r] = x0 * g[r] + x1 * g[3 + r] + x2 * g[6 + r];
-      mp[9 * nb + 3 * q + k] = ((x0 + x1) + x2) * (1.f / 3.f);
+      const double x0 = x[3 * (size_t)t[0] + k], x1 = x[3 * (size_t)t[1] + k], x2 = x[3 * (size_t)t[2] + k];
+      for (int r = 0; r < 3; ++r)
+        mp[12 * q + 3 * k + r] = split_pair(x0 * g[r] + x1 * g[3 + r] + x2 * g[6 + r]);
+      mp[12 * q + 9 + k] = split_pair(((x0 + x1) + x2) / 3.0);
     }
   }
-  for (int c = 12 * nb; c < C; ++c) mp[c] = 0.f;
+  for (int c = 12 * nb; c < C; ++c) mp[c] = make_float2(0.f, 0.f);
 }
 
 // y_v = 2 sum_{S ni v} a_S (w_hi g_c . z_hi + w_lo z_lo / 3) in FP64 (hierarchical.rs:779-811).
-__global__ void face_gather_kernel(FaceOps o, const float *__restrict__ z, int nb, int C,
+__global__ void face_gather_kernel(FaceOps o, const float2 *__restrict__ z, int nb, int C,
                                    double w_hi, double w_lo, double *__restrict__ ys, size_t ldy) {
   int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= o.nv) return;
@@ -294,13 +361,15 @@ __global__ void face_gather_kernel(FaceOps o, const float *__restrict__ z, int n
     for (uint32_t e = o.inc_off[v]; e < o.inc_off[v + 1]; ++e) {
       uint32_t fc = o.inc[e], f = fc >> 2, c = fc & 3;
       double a = o.area[f];
-      const float *g = o.g + 9 * (size_t)f + 3 * c;
-      const float *zs = z + (size_t)o.position[f] * C;
+      const double *g = o.g + 9 * (size_t)f + 3 * c;
+      const float2 *zs = z + (size_t)o.position[f] * C + 12 * q;
       double acc[3];
       for (int k = 0; k < 3; ++k) {
-        const float *zh = zs + 9 * q + 3 * k;
-        double hi = (double)g[0] * zh[0] + (double)g[1] * zh[1] + (double)g[2] * zh[2];
-        acc[k] = a * (w_hi * hi + w_lo * (1.0 / 3.0) * (double)zs[9 * nb + 3 * q + k]);
+        const float2 *zh = zs + 3 * k;
+        double hi = g[0] * ((double)zh[0].x + zh[0].y) + g[1] * ((double)zh[1].x + zh[1].y) +
+                    g[2] * ((double)zh[2].x + zh[2].y);
+        double lo = (double)zs[9 + k].x + zs[9 + k].y;
+        acc[k] = a * (w_hi * hi + w_lo * (1.0 / 3.0) * lo);
       }
       acc0 += acc[0], acc1 += acc[1], acc2 += acc[2];
     }
@@ -311,28 +380,31 @@ __global__ void face_gather_kernel(FaceOps o, const float *__restrict__ z, int n
 
 // ------------------------------------------------------------------ vertex prologue / epilogue
 
-// psi channels of the vertex operator: m = x per axis (ψ = a x in the upward/near sums).
+// psi channels of the vertex operator: m = x per axis (psi = a x in the upward sums), vector q
+// at channels 4q + k (4q + 3 is padding).
 __global__ void vertex_m_kernel(const uint32_t *order, const double *__restrict__ xs, size_t ldx,
-                                int nv, int nb, int C, float *m) {
+                                int nv, int nb, int C, float2 *m) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= nv) return;
   uint32_t v = order[p];
-  float *mp = m + (size_t)p * C;
+  float2 *mp = m + (size_t)p * C;
+  for (int c = 0; c < C; ++c) mp[c] = make_float2(0.f, 0.f);
   for (int q = 0; q < nb; ++q)
-    for (int k = 0; k < 3; ++k) mp[3 * q + k] = (float)xs[q * ldx + 3 * (size_t)v + k];
-  for (int c = 3 * nb; c < C; ++c) mp[c] = 0.f;
+    for (int k = 0; k < 3; ++k) mp[4 * q + k] = split_pair(xs[q * ldx + 3 * (size_t)v + k]);
 }
 
 // y = 2 a (H~a x - H~(a x)) = 2 a z (hierarchical.rs:1330-1343).
-__global__ void vertex_out_kernel(const uint32_t *order, const float4 *el, const float *z, int nv,
+__global__ void vertex_out_kernel(const uint32_t *order, const float4 *el, const float2 *z, int nv,
                                   int nb, int C, double scale, double *__restrict__ ys, size_t ldy) {
   int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= nv) return;
   uint32_t v = order[p];
   double a = el[p].w;
   for (int q = 0; q < nb; ++q)
-    for (int k = 0; k < 3; ++k)
-      ys[q * ldy + 3 * (size_t)v + k] = scale * 2.0 * a * (double)z[(size_t)p * C + 3 * q + k];
+    for (int k = 0; k < 3; ++k) {
+      const float2 zz = z[(size_t)p * C + 4 * q + k];
+      ys[q * ldy + 3 * (size_t)v + k] = scale * 2.0 * a * ((double)zz.x + zz.y);
+    }
 }
 
 // Element records: positions as float pairs (hi + lo), weights, normals; FP64 in.
@@ -377,9 +449,11 @@ struct HMat {
   DevBuf<uint32_t> far_ptr, far_col, count;
   DevBuf<uint2> cols;
   DevBuf<uint4> items;
-  DevBuf<float2> far_coef, leaf_farA;
+  DevBuf<float2> far_coef, node_farA;
   DevBuf<float4> xh, xl, nrm;
-  DevBuf<float> up, farx, part, m, z;
+  DevBuf<float> up, farx;
+  DevBuf<float2> part, m, z;
+  int pw_mode = 0, pw_k = 0;
   Profiler prof;
 
   HDev dev(int C_) const {
@@ -387,7 +461,7 @@ struct HMat {
     d.start = start.p, d.end = end.p, d.right = right.p, d.parent = parent.p, d.leaves = leaves.p;
     d.chain_off = chain_off.p, d.chain = chain.p;
     d.far_ptr = far_ptr.p, d.far_col = far_col.p, d.far_coef = far_coef.p;
-    d.xh = xh.p, d.xl = xl.p, d.nrm = nrm.p, d.leaf_farA = leaf_farA.p;
+    d.xh = xh.p, d.xl = xl.p, d.nrm = nrm.p, d.node_farA = node_farA.p;
     d.cols = cols.p, d.items = items.p, d.item_off = item_off.p;
     d.up = up.p, d.farx = farx.p, d.part = part.p, d.count = count.p;
     d.m = m.p, d.z = z.p;
@@ -395,6 +469,7 @@ struct HMat {
     d.n_items = (int)n_items;
     d.C = C_;
     d.neg_s = (float)neg_s;
+    d.pw_mode = pw_mode, d.pw_k = pw_k;
     return d;
   }
   cudaStream_t st() const { return ctx->stream; }
@@ -404,11 +479,25 @@ struct HMat {
     size_t nn = tree.n_nodes();
     if ((size_t)C_ * nn > up.n) up.alloc((size_t)C_ * nn), farx.alloc((size_t)C_ * nn);
     if ((size_t)C_ * n_el > m.n) m.alloc((size_t)C_ * n_el), z.alloc((size_t)C_ * n_el);
-    if (n_items * 8 * (size_t)(C_ + 2) > part.n) part.alloc(std::max<size_t>(n_items * 8 * (size_t)(C_ + 2), 1));
+    if (n_items * 8 * (size_t)C_ > part.n) part.alloc(std::max<size_t>(n_items * 8 * (size_t)C_, 1));
   }
 
-  template <int CC>
-  void upward_far(const HDev &d, int split) {
+  // The exponent r2^e as an integer power times a cube or square root when 3e or 2e is an
+  // integer (integer alpha, beta), else powf.
+  void set_exponent(double e) {
+    neg_s = e;
+    pw_mode = 0, pw_k = 0;
+    for (int q : {1, 2, 3}) {
+      double k = e * q;
+      if (std::fabs(k - std::round(k)) < 1e-12 && std::fabs(k) <= 64) {
+        pw_mode = q == 1 ? 3 : q, pw_k = (int)std::round(k) * (q == 1 ? 3 : 1);
+        break;
+      }
+    }
+  }
+
+  template <int SEL, int CC>
+  void upward_far(const HDev &d) {
     size_t nn = tree.n_nodes(), nl = tree.leaves.size();
     cudaStream_t s = st();
     prof.begin(s, kind == FACE ? "metric_upward" : "vfrac_upward");
@@ -416,7 +505,7 @@ struct HMat {
     RSG_LAUNCHED(ctx, "hm_upward");
     prof.end(s);
     prof.begin(s, kind == FACE ? "metric_far" : "vfrac_far");
-    hm_far_kernel<CC><<<nblk(nn * 32, 256), 256, 0, s>>>(d, split);
+    hm_far_kernel<SEL, CC><<<nblk(nn * 32, 256), 256, 0, s>>>(d);
     RSG_LAUNCHED(ctx, "hm_far");
     prof.end(s);
   }
@@ -502,47 +591,54 @@ struct HMat {
     hm_pack_kernel<<<nblk(n_el, 256), 256, 0, s>>>(dp.p, dw.p, nrm64 ? dn.p : nullptr, ord.p, (int)n_el,
                                                    xh.p, xl.p, kind == FACE ? nrm.p : nullptr);
     RSG_LAUNCHED(ctx, "hm_pack");
-    // far part of H~a: upward over psi = a (m = 1, 2 channels), far, chain sums
-    leaf_farA.alloc(nl);
+    // far part of H~a: upward over psi = a (m = 1, 2 channels) and far sums per node
+    node_farA.alloc(nn);
     reserve(4);
-    std::vector<float> ones(2 * n_el, 1.f);
-    DevBuf<float> mm;
+    std::vector<float2> ones(2 * n_el, make_float2(1.f, 0.f));
+    DevBuf<float2> mm;
     mm.upload(ones.data(), ones.size(), s);
     HDev d = dev(2);
     d.m = mm.p;
-    upward_far<2>(d, 1);
-    hm_leaf_farA_kernel<<<nblk(nl, 128), 128, 0, s>>>(d, leaf_farA.p);
-    RSG_LAUNCHED(ctx, "hm_leaf_farA");
+    upward_far<ONES, 2>(d);
+    RSG_CUDA("upload", cudaMemcpyAsync(node_farA.p, farx.p, nn * sizeof(float2), cudaMemcpyDeviceToDevice, s));
     RSG_CUDA("upload", cudaStreamSynchronize(s));
   }
 
+  // z for the C-channel m already in `m` (faces: C = 12 nb, vertices: C = 4 nb).
   template <int K, int CC>
-  void product_cc(int split) {
+  void product_cc(int nb) {
     cudaStream_t s = st();
     size_t nl = tree.leaves.size();
     HDev d = dev(CC);
-    upward_far<CC>(d, split);
-    prof.begin(s, kind == FACE ? "metric_rows" : "vfrac_rows");
-    hm_rows_kernel<K, CC><<<nblk(n_items * 32, 128), 128, 0, s>>>(d, split);
-    RSG_LAUNCHED(ctx, "hm_rows");
+    constexpr int SEL = K == FACE ? FACE_CH : VERTEX_CH;
+    upward_far<SEL, CC>(d);
+    prof.begin(s, K == FACE ? "metric_rows" : "vfrac_rows");
+    if constexpr (K == FACE) {
+      for (int q = 0; q < nb; ++q) {  // one vector (12 channels) per pass
+        hm_rows_kernel<K, 12><<<nblk(n_items * 32, 128), 128, 0, s>>>(d, 12 * q);
+        RSG_LAUNCHED(ctx, "hm_rows");
+      }
+    } else {
+      hm_rows_kernel<K, CC><<<nblk(n_items * 32, 128), 128, 0, s>>>(d, 0);
+      RSG_LAUNCHED(ctx, "hm_rows");
+    }
     prof.end(s);
-    prof.begin(s, kind == FACE ? "metric_epilogue" : "vfrac_epilogue");
-    hm_epilogue_kernel<CC><<<nblk(nl * 8, 128), 128, 0, s>>>(d, split);
+    prof.begin(s, K == FACE ? "metric_epilogue" : "vfrac_epilogue");
+    hm_epilogue_kernel<SEL, CC><<<nblk(nl * 8, 128), 128, 0, s>>>(d);
     RSG_LAUNCHED(ctx, "hm_epilogue");
     prof.end(s);
   }
 
-  // z = H~a m - H~(a m) for the C-channel m already in `m` (split: first kernel-1 channel).
-  void product(int CC, int split) {
+  void product(int nb) {
     if (kind == FACE) {
-      if (CC == 12) product_cc<FACE, 12>(split);
-      else if (CC == 24) product_cc<FACE, 24>(split);
-      else if (CC == 36) product_cc<FACE, 36>(split);
+      if (nb == 1) product_cc<FACE, 12>(1);
+      else if (nb == 2) product_cc<FACE, 24>(2);
+      else if (nb == 3) product_cc<FACE, 36>(3);
       else fail(RS_INTERNAL, "Internal", "product", "unsupported channel count");
     } else {
-      if (CC == 4) product_cc<VERTEX, 4>(split);
-      else if (CC == 8) product_cc<VERTEX, 8>(split);
-      else if (CC == 12) product_cc<VERTEX, 12>(split);
+      if (nb == 1) product_cc<VERTEX, 4>(1);
+      else if (nb == 2) product_cc<VERTEX, 8>(2);
+      else if (nb == 3) product_cc<VERTEX, 12>(3);
       else fail(RS_INTERNAL, "Internal", "product", "unsupported channel count");
     }
   }
@@ -571,7 +667,7 @@ struct rs_metric {
   int nv = 0, nf = 0;
   FaceGeom geom;
   DevBuf<uint32_t> faces, order, position, inc_off, inc;
-  DevBuf<float> g, area;
+  DevBuf<double> g, area;
   DevBuf<double> xbuf, ybuf;
   FaceOps ops() const {
     FaceOps o;
@@ -604,7 +700,7 @@ void metric_setup(rs_metric *M, rs_ctx *ctx, int nv, int nf, const uint32_t *fac
   Tree T = build_face_tree(nf, faces, pos, M->geom, leaf_size);
   M->h.kind = FACE;
   M->h.n_el = nf;
-  M->h.neg_s = -(beta - 2.0) / alpha;
+  M->h.set_exponent(-(beta - 2.0) / alpha);
   // projectors P = sum a N N^T / A per node (RS/src/spatial/mod.rs:268-290), bottom-up
   size_t nn = T.n_nodes();
   std::vector<double> ps(7 * nn, 0.0), proj(6 * nn);
@@ -625,8 +721,8 @@ void metric_setup(rs_metric *M, rs_ctx *ctx, int nv, int nf, const uint32_t *fac
   }
   M->h.build_common(ctx, std::move(T), chi, leaf_pairs);
   cudaStream_t s = M->h.st();
-  // df coefficients (RS/src/metric/mod.rs:120-131) in FP64, stored FP32
-  std::vector<float> gh(9 * (size_t)nf), ah(nf);
+  // df coefficients (RS/src/metric/mod.rs:120-131) in FP64
+  std::vector<double> gh(9 * (size_t)nf), ah(nf);
   for (int f = 0; f < nf; ++f) {
     const double *p0 = pos + 3 * (size_t)faces[3 * f], *p1 = pos + 3 * (size_t)faces[3 * f + 1],
                  *p2 = pos + 3 * (size_t)faces[3 * f + 2];
@@ -639,11 +735,11 @@ void metric_setup(rs_metric *M, rs_ctx *ctx, int nv, int nf, const uint32_t *fac
     const double *pa[3] = {p1, p2, p0}, *pb[3] = {p2, p0, p1};
     for (int c = 0; c < 3; ++c) {
       double e[3] = {pb[c][0] - pa[c][0], pb[c][1] - pa[c][1], pb[c][2] - pa[c][2]};
-      gh[9 * f + 3 * c + 0] = (float)(ww[1] * e[2] - ww[2] * e[1]);
-      gh[9 * f + 3 * c + 1] = (float)(ww[2] * e[0] - ww[0] * e[2]);
-      gh[9 * f + 3 * c + 2] = (float)(ww[0] * e[1] - ww[1] * e[0]);
+      gh[9 * f + 3 * c + 0] = ww[1] * e[2] - ww[2] * e[1];
+      gh[9 * f + 3 * c + 1] = ww[2] * e[0] - ww[0] * e[2];
+      gh[9 * f + 3 * c + 2] = ww[0] * e[1] - ww[1] * e[0];
     }
-    ah[f] = (float)M->geom.area[f];
+    ah[f] = M->geom.area[f];
   }
   std::vector<uint32_t> fh(faces, faces + 3 * (size_t)nf), posn(nf);
   for (int p = 0; p < nf; ++p) posn[M->h.tree.order[p]] = (uint32_t)p;
@@ -678,7 +774,7 @@ void rsg::metric_apply_strided(rs_metric *M, double w_hi, double w_lo, int nb, c
     face_m_kernel<<<nblk(M->nf, 256), 256, 0, s>>>(M->ops(), xs + q0 * ldx, ldx, k, CC, M->h.m.p);
     RSG_LAUNCHED(M->h.ctx, "face_m");
     M->h.prof.end(s);
-    M->h.product(CC, 9 * k);
+    M->h.product(k);
     M->h.prof.begin(s, "metric_gather");
     face_gather_kernel<<<nblk(M->nv, 128), 128, 0, s>>>(M->ops(), M->h.z.p, k, CC, w_hi, w_lo,
                                                         ys + q0 * ldy, ldy);
@@ -697,7 +793,7 @@ void rsg::vfrac_apply_strided(rs_vfrac *V, double scale, int nb, const double *x
     V->h.reserve(CC);
     vertex_m_kernel<<<nblk(V->nv, 256), 256, 0, s>>>(V->order.p, xs + q0 * ldx, ldx, V->nv, k, CC, V->h.m.p);
     RSG_LAUNCHED(V->h.ctx, "vertex_m");
-    V->h.product(CC, CC);
+    V->h.product(k);
     vertex_out_kernel<<<nblk(V->nv, 256), 256, 0, s>>>(V->order.p, V->h.xh.p, V->h.z.p, V->nv, k, CC,
                                                        scale, ys + q0 * ldy, ldy);
     RSG_LAUNCHED(V->h.ctx, "vertex_out");
@@ -731,15 +827,18 @@ int rs_metric_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const do
   return guard([&] {
     auto M = std::make_unique<rs_metric>();
     metric_setup(M.get(), ctx, nv, nf, faces, positions_host, alpha, beta, chi, leaf_size, leaf_pairs);
+    ctx_retain(ctx);
     *out = M.release();
   });
 }
 
 void rs_metric_free(rs_metric *M) {
   if (!M) return;
-  cudaSetDevice(M->h.ctx->device);
-  cudaStreamSynchronize(M->h.ctx->stream);
+  rs_ctx *ctx = M->h.ctx;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
   delete M;
+  ctx_release(ctx);
 }
 
 int rs_metric_apply(rs_metric *M, double w_hi, double w_lo, int nb, const double *xs_host,
@@ -815,19 +914,22 @@ int rs_vfrac_build(rs_ctx *ctx, int nv, const double *positions_host, const doub
     Tree T = build_tree((size_t)nv, positions_host, ebox.data(), mass_host, leaf_size);
     V->h.kind = VERTEX;
     V->h.n_el = nv;
-    V->h.neg_s = -(tau + 1.0);
+    V->h.set_exponent(-(tau + 1.0));
     V->h.build_common(ctx, std::move(T), chi, leaf_pairs);
     up_vec(V->order, V->h.tree.order, V->h.st());
     V->h.setup(positions_host, mass_host, nullptr, nullptr);
+    ctx_retain(ctx);
     *out = V.release();
   });
 }
 
 void rs_vfrac_free(rs_vfrac *V) {
   if (!V) return;
-  cudaSetDevice(V->h.ctx->device);
-  cudaStreamSynchronize(V->h.ctx->stream);
+  rs_ctx *ctx = V->h.ctx;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
   delete V;
+  ctx_release(ctx);
 }
 
 int rs_vfrac_apply(rs_vfrac *V, int nb, const double *xs_host, double *ys_host) {

@@ -144,28 +144,6 @@ __global__ void shift_kernel(const double *__restrict__ cy, const double *__rest
   shift[t] = r[q * ld + nd + i] - cy[t];
 }
 
-// v_q[3 u + k] -= (K y)[u][3 q + k] and v_q multipliers = 0
-__global__ void sub_ky_kernel(double *__restrict__ v, size_t ld, int nb, int nv, int G,
-                              const double *__restrict__ ky) {
-  size_t nd = 3 * (size_t)nv;
-  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (t >= (size_t)nb * (nd + 3 * G)) return;
-  int q = (int)(t / (nd + 3 * G));
-  size_t i = t % (nd + 3 * G);
-  if (i < nd) v[q * ld + i] -= ky[(i / 3) * 3 * nb + 3 * q + (i % 3)];
-  else v[q * ld + i] = 0.0;
-}
-
-// yy[v][3q + k] = x_q[3 v + k] (positions only)
-__global__ void pos_to_mg_kernel(const double *__restrict__ x, size_t ld, int nb, int nv,
-                                 double *__restrict__ out) {
-  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (t >= (size_t)nv * 3 * nb) return;
-  size_t v = t / (3 * nb);
-  int col = (int)(t % (3 * nb)), q = col / 3, k = col % 3;
-  out[t] = x[q * ld + 3 * v + k];
-}
-
 // Planar symbol ratio 4 I(sigma) I(2 - s) of W^-1 L_{2-s} W^-1 B, I(t) = pi Gamma(1-t) /
 // (t 4^t Gamma(1+t)) (fractional_symbol_ratio, RS/src/solve/precond.rs:548-568).
 double symbol_ratio(double s) {
@@ -258,20 +236,23 @@ struct rs_solver {
   void add_into(size_t m, const double *x, double *y);
   void pos_copy_weighted(int nb);
 
-  // z = P^-1 r (augmented form, precond.rs:1026-1079)
+  // z = P^-1 r for the augmented preconditioner of precond.rs:1026-1079,
+  //   P^-1 = X + X (s L^V - K^) X,  X = L'^-1,  K^ = blockdiag(K x I3, 0),
+  // applied in the equivalent form X (s L^V + C^) X with C^ = [[0, C_Q^T], [C_Q, 0]]: from
+  // X L' X = X and L' = K^ + C^, X - X K^ X = X C^ X. The two agree for an exact X; for the
+  // multigrid X~ = K^-1 (I - E) the first form leaves X~ E, an order -2 error term that
+  // outgrows the order -2s main term at high frequencies (the iteration count then grows
+  // with the mesh), while the second form only perturbs the main term by (I - E) factors.
   void apply_prec(int nb, const double *r, double *z) {
     reserve(nb);
     double *y = tmp.p, *v = tmp2.p;
     lsolve(nb, r, y, nullptr);
     vfrac_apply_strided(vfrac, frac_scale, nb, y, n, v, n);
-    size_t m = (size_t)nv * 3 * nb;
-    pos_to_mg_kernel<<<nblk(m, 256), 256, 0, st()>>>(y, n, nb, nv, mg_in.p);
-    RSG_LAUNCHED(ctx, "pos_to_mg");
-    amg.spmv0(ctx, mg_in.p, ky.p, 3 * nb);
+    group_sums(y, n, nb, c.p, cy.p);
     size_t tot = (size_t)nb * n;
-    sub_ky_kernel<<<nblk(tot, 256), 256, 0, st()>>>(v, n, nb, nv, G, ky.p);
-    RSG_LAUNCHED(ctx, "sub_ky");
-    lsolve(nb, v, z, y);
+    cq_apply_kernel<<<nblk(tot, 256), 256, 0, st()>>>(y, v, n, nb, nv, group.p, c.p, G, cy.p);
+    RSG_LAUNCHED(ctx, "cq_apply");
+    lsolve(nb, v, z, nullptr);
   }
 };
 
@@ -336,7 +317,7 @@ namespace {
 
 // cotan stiffness W (RS/src/geometry.rs:217-249), scalar |V| x |V|, plus eps M on the diagonal.
 Csr laplacian_block(int nv, int nf, const uint32_t *faces, const double *pos, const std::vector<double> &mass,
-                    double eps_rel, double &eps_out) {
+                    double eps_rel, bool clamp, double &eps_out) {
   std::vector<std::vector<std::pair<int, double>>> rows(nv);
   auto add = [&](int i, int j, double v) { rows[i].push_back({j, v}); };
   for (int f = 0; f < nf; ++f) {
@@ -366,13 +347,21 @@ Csr laplacian_block(int nv, int nf, const uint32_t *faces, const double *pos, co
       size_t q = p;
       double v = 0.0;
       while (q < r.size() && r[q].first == r[p].first) v += r[q++].second;
-      if (r[p].first == i) trw += v;
       K.col.push_back(r[p].first);
       K.val.push_back(v);
       p = q;
     }
     K.ptr[i + 1] = (int)K.col.size();
     trm += mass[i];
+  }
+  for (int i = 0; i < nv; ++i) {
+    int dp = -1;
+    for (int p = K.ptr[i]; p < K.ptr[i + 1]; ++p)
+      if (K.col[p] == i) dp = p;
+    if (clamp)  // a positive off-diagonal is a negative edge weight: drop the edge
+      for (int p = K.ptr[i]; p < K.ptr[i + 1]; ++p)
+        if (K.col[p] != i && K.val[p] > 0.0) K.val[dp] += K.val[p], K.val[p] = 0.0;
+    trw += K.val[dp];
   }
   double eps = eps_rel * trw / trm;  // preconditioner_epsilon (RS/src/solve/dense.rs:529-533)
   for (int i = 0; i < nv; ++i)
@@ -442,7 +431,8 @@ int rs_solver_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const do
     S->n = S->nd + 3 * (size_t)S->G;
     bool multi = !per_comp && ncomp > 1;  // translations_fixed_per_component (precond.rs:96-124)
     double eps = 0.0;
-    Csr K = laplacian_block(nv, nf, faces, positions_host, S->vmass, multi ? o->eps_multi_rel : o->eps_rel, eps);
+    Csr K = laplacian_block(nv, nf, faces, positions_host, S->vmass, multi ? o->eps_multi_rel : o->eps_rel,
+                            o->clamp_laplacian != 0, eps);
     S->eps = eps;
     std::vector<double> ea(S->G);
     for (int g = 0; g < S->G; ++g) ea[g] = eps * garea[g];
@@ -477,17 +467,20 @@ int rs_solver_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const do
     S->prec.n = S->n;
     S->prec.apply = [P](int nb, const double *x, double *y) { P->apply_prec(nb, x, y); };
     RSG_CUDA("solver", cudaStreamSynchronize(s));
+    ctx_retain(ctx);
     *out = S.release();
   });
 }
 
 void rs_solver_free(rs_solver *S) {
   if (!S) return;
-  cudaSetDevice(S->ctx->device);
-  cudaStreamSynchronize(S->ctx->stream);
+  rs_ctx *ctx = S->ctx;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
   rs_metric_free(S->metric);
   rs_vfrac_free(S->vfrac);
   delete S;
+  ctx_release(ctx);
 }
 
 int rs_solver_dims(rs_solver *S, int64_t *n_dofs, int64_t *n_constraints) {
@@ -571,6 +564,21 @@ int rs_solver_solve_many(rs_solver *S, int nb, const double *rhs, double *sol, d
   });
 }
 
+int rs_solver_history(rs_solver *S, int q, double *estimates, int max_iter, int *n_iter,
+                      double *cycle_residuals, int max_cycles, int *n_cycles) {
+  return guard([&] {
+    if (q < 0 || q >= (int)S->last.size())
+      fail(RS_INVALID_OPTION, "InvalidOption", "solver", "no such right-hand side in the last solve");
+    const GmresReport &r = S->last[q];
+    int a = (int)std::min<size_t>(r.history.size(), (size_t)std::max(max_iter, 0));
+    int b = (int)std::min<size_t>(r.cycle_residuals.size(), (size_t)std::max(max_cycles, 0));
+    if (estimates) std::copy(r.history.begin(), r.history.begin() + a, estimates);
+    if (cycle_residuals) std::copy(r.cycle_residuals.begin(), r.cycle_residuals.begin() + b, cycle_residuals);
+    if (n_iter) *n_iter = (int)r.history.size();
+    if (n_cycles) *n_cycles = (int)r.cycle_residuals.size();
+  });
+}
+
 rs_solver_options rs_solver_options_default(void) {
   rs_solver_options o;
   o.chi = 0.5;
@@ -586,6 +594,7 @@ rs_solver_options rs_solver_options_default(void) {
   o.barycenter_per_component = 0;
   o.vcycles = 1;
   o.preconditioner = 1;
+  o.clamp_laplacian = 0;
   return o;
 }
 

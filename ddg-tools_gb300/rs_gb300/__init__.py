@@ -40,7 +40,8 @@ class SolverOptions(C.Structure):
                 ("restart", C.c_int), ("tolerance", C.c_double), ("max_iterations", C.c_int),
                 ("tp_weight", C.c_double), ("low_order", C.c_int), ("eps_rel", C.c_double),
                 ("eps_multi_rel", C.c_double), ("barycenter_per_component", C.c_int),
-                ("vcycles", C.c_int), ("preconditioner", C.c_int)]
+                ("vcycles", C.c_int), ("preconditioner", C.c_int),
+                ("clamp_laplacian", C.c_int)]
 
 
 class FlowOptions(C.Structure):
@@ -123,6 +124,8 @@ def load_library(path: str | os.PathLike | None = None):
         "rs_solver_precondition_device": [_vp, C.c_int, _vp, _vp],
         "rs_solver_solve_many": [_vp, C.c_int, _f64p, _f64p, _f64p],
         "rs_solver_solve_many_device": [_vp, C.c_int, _vp, _vp, _f64p],
+        "rs_solver_history": [_vp, C.c_int, _f64p, C.c_int, C.POINTER(C.c_int), _f64p, C.c_int,
+                              C.POINTER(C.c_int)],
         "rs_flow_create": [_vp, C.c_int, C.c_int, _u32p, _f64p, C.c_void_p, C.POINTER(_vp)],
         "rs_flow_step": [_vp, _f64p],
         "rs_flow_positions": [_vp, _f64p],
@@ -571,6 +574,15 @@ class SaddleSolver:
             r["iterations"] = int(r["iterations"])
             r["converged"] = bool(r["converged"])
         return out, reports
+
+    def history(self, q: int = 0):
+        """(per-iteration estimated relative residuals, explicit residual at every cycle start)
+        of right-hand side q of the last solve."""
+        ni, nc = C.c_int(), C.c_int()
+        _check(_lib.rs_solver_history(self._h, q, np.zeros(1), 0, C.byref(ni), np.zeros(1), 0, C.byref(nc)))
+        est, cyc = np.zeros(max(ni.value, 1)), np.zeros(max(nc.value, 1))
+        _check(_lib.rs_solver_history(self._h, q, est, ni.value, C.byref(ni), cyc, nc.value, C.byref(nc)))
+        return est[: ni.value], cyc[: nc.value]
 
 
 def flow_options(**kw) -> FlowOptions:

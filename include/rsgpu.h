@@ -66,6 +66,8 @@ int rs_device_count(int *count);
 /* A context on device `ordinal` with its own non-blocking stream
  * (GpuContext::new, RS/src/gpu/mod.rs:102-127; cuda.rs:100-119). */
 int rs_ctx_create(int ordinal, rs_ctx **out);
+/* Releases the caller's handle. Objects built on the context (rs_bh, rs_metric, rs_vfrac,
+ * rs_solver, rs_flow) hold it too, so handles may be freed in any order. */
 void rs_ctx_free(rs_ctx *ctx);
 /* The context's cudaStream_t, for callers that time or order work around it. */
 int rs_ctx_stream(rs_ctx *ctx, void **stream);
@@ -215,6 +217,8 @@ typedef struct rs_solver_options {
   int barycenter_per_component; /* 1: one barycenter group per component, 0: global (0) */
   int vcycles;           /* multigrid V-cycles per L' solve (1) */
   int preconditioner;    /* 1: the fractional preconditioner, 0: none */
+  int clamp_laplacian;   /* 1: edges with negative cotan weight dropped from the
+                            preconditioner's Laplacian (an M-matrix for multigrid), 0: cotan */
 } rs_solver_options;
 
 rs_solver_options rs_solver_options_default(void);
@@ -240,6 +244,12 @@ int rs_solver_precondition_device(rs_solver *s, int nb, const double *rs_dev, do
  * relative residual, converged, seconds, cycles. SolverDiverged above 0.1 (gmres.rs:196). */
 int rs_solver_solve_many(rs_solver *s, int nb, const double *rhs_host, double *sol_host,
                          double *report);
+/* The convergence history of right-hand side q of the last solve (GmresReport::history and the
+ * explicit residual of every cycle start, RS/src/solve/gmres.rs:200-225): up to max_iter
+ * estimated relative residuals per Arnoldi step and up to max_cycles explicit ones. No
+ * counterpart call in the crate, where the report is a returned struct. */
+int rs_solver_history(rs_solver *s, int q, double *estimates, int max_iter, int *n_iter,
+                      double *cycle_residuals, int max_cycles, int *n_cycles);
 int rs_solver_solve_many_device(rs_solver *s, int nb, const double *rhs_dev, double *sol_dev,
                                 double *report);
 

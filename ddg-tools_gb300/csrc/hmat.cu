@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cmath>
 #include <memory>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -959,3 +960,111 @@ int rs_vfrac_stats(rs_vfrac *V, int64_t *o) {
 }
 
 }  // extern "C"
+
+// ====================================================================== no-allocation product
+//
+// rs_metric_apply_device_noalloc: the metric product of rs_metric_apply_device with its
+// per-call scratch (channel values, results, near partial sums, node sums) carved from one
+// file-scope device array instead of buffers that the first call of a size allocates. It is
+// for callers that must not allocate while the product runs: a host whose device memory is
+// entirely reserved by its own pool after set-up, and a caller on a latency-critical stream,
+// since cudaMalloc and cudaFree can synchronize the whole device.
+//
+// Limits: the scratch is kNoAllocScratchBytes per device, shared by every call in the process,
+// so calls that overlap in time (two host threads, or two streams in flight) race on it and
+// must be serialized by the caller. The first call on a device looks up the array's address
+// (cudaGetSymbolAddress, with that device current); when that call is made inside a stream
+// capture the lookup should have been done before it, by one earlier call.
+
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;  // 64 MiB
+constexpr int kNoAllocMaxDevices = 64;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+unsigned char *noalloc_scratch(int device) {
+  static std::mutex mu;
+  static unsigned char *addr[kNoAllocMaxDevices] = {};
+  if (device < 0 || device >= kNoAllocMaxDevices)
+    fail(RS_INVALID_OPTION, "InvalidOption", "product", "device ordinal out of range for the no-alloc scratch");
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[device]) {
+    void *p = nullptr;
+    RSG_CUDA("product", cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    addr[device] = static_cast<unsigned char *>(p);
+  }
+  return addr[device];
+}
+
+inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+// Scratch bytes of one tree pass with C channels (the layout carved below).
+size_t noalloc_bytes(const HMat &h, int C) {
+  size_t nn = h.tree.n_nodes();
+  return 2 * align256(nn * C * sizeof(float)) + 2 * align256(h.n_el * C * sizeof(float2)) +
+         align256(std::max<size_t>(h.n_items, 1) * 8 * C * sizeof(float2));
+}
+
+HDev noalloc_dev(const HMat &h, int C, unsigned char *base) {
+  HDev d = h.dev(C);
+  size_t nn = h.tree.n_nodes(), off = 0;
+  auto take = [&](size_t bytes) {
+    unsigned char *p = base + off;
+    off += align256(bytes);
+    return p;
+  };
+  d.up = reinterpret_cast<float *>(take(nn * C * sizeof(float)));
+  d.farx = reinterpret_cast<float *>(take(nn * C * sizeof(float)));
+  d.m = reinterpret_cast<const float2 *>(take(h.n_el * C * sizeof(float2)));
+  d.z = reinterpret_cast<float2 *>(take(h.n_el * C * sizeof(float2)));
+  d.part = reinterpret_cast<float2 *>(take(std::max<size_t>(h.n_items, 1) * 8 * C * sizeof(float2)));
+  return d;
+}
+
+// The face product of one group of k <= 3 vectors on the given scratch (the kernels and order
+// of HMat::product_cc and metric_apply_strided).
+template <int CC>
+void noalloc_face_group(rs_metric *M, const HDev &d, int k, const double *xs, size_t ldx, double w_hi,
+                        double w_lo, double *ys, size_t ldy) {
+  HMat &h = M->h;
+  cudaStream_t s = h.st();
+  float2 *m = const_cast<float2 *>(d.m);
+  face_m_kernel<<<nblk(M->nf, 256), 256, 0, s>>>(M->ops(), xs, ldx, k, CC, m);
+  RSG_LAUNCHED(h.ctx, "face_m");
+  h.upward_far<FACE_CH, CC>(d);
+  for (int q = 0; q < k; ++q) {
+    hm_rows_kernel<FACE, 12><<<nblk(h.n_items * 32, 128), 128, 0, s>>>(d, 12 * q);
+    RSG_LAUNCHED(h.ctx, "hm_rows");
+  }
+  hm_epilogue_kernel<FACE_CH, CC><<<nblk(h.tree.leaves.size() * 8, 128), 128, 0, s>>>(d);
+  RSG_LAUNCHED(h.ctx, "hm_epilogue");
+  face_gather_kernel<<<nblk(M->nv, 128), 128, 0, s>>>(M->ops(), d.z, k, CC, w_hi, w_lo, ys, ldy);
+  RSG_LAUNCHED(h.ctx, "face_gather");
+}
+
+}  // namespace
+
+extern "C" int rs_metric_apply_device_noalloc(rs_metric *M, double w_hi, double w_lo, int nb,
+                                              const double *xs_dev, double *ys_dev) {
+  return guard([&] {
+    if (nb < 1) fail(RS_INVALID_OPTION, "InvalidOption", "product", "at least one vector");
+    if (!(std::isfinite(w_hi) && std::isfinite(w_lo)))
+      fail(RS_INVALID_OPTION, "InvalidOption", "product", "finite weights");
+    const int Cmax = 12 * std::min(3, nb);
+    const size_t need = noalloc_bytes(M->h, Cmax);
+    if (need > kNoAllocScratchBytes)
+      fail(RS_INVALID_OPTION, "InvalidOption", "product",
+           "the no-alloc product of " + std::to_string(std::min(3, nb)) + " vector(s) on this mesh needs " +
+               std::to_string(need >> 20) + " MiB of scratch, above its 64 MiB; use rs_metric_apply_device");
+    M->h.ctx->use();
+    unsigned char *base = noalloc_scratch(M->h.ctx->device);
+    const size_t ld = 3 * (size_t)M->nv;
+    for (int q0 = 0; q0 < nb; q0 += 3) {
+      const int k = std::min(3, nb - q0);
+      HDev d = noalloc_dev(M->h, 12 * k, base);
+      if (k == 1) noalloc_face_group<12>(M, d, 1, xs_dev + q0 * ld, ld, w_hi, w_lo, ys_dev + q0 * ld, ld);
+      else if (k == 2) noalloc_face_group<24>(M, d, 2, xs_dev + q0 * ld, ld, w_hi, w_lo, ys_dev + q0 * ld, ld);
+      else noalloc_face_group<36>(M, d, 3, xs_dev + q0 * ld, ld, w_hi, w_lo, ys_dev + q0 * ld, ld);
+    }
+  });
+}

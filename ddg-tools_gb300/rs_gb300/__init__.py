@@ -124,6 +124,7 @@ def load_library(path: str | os.PathLike | None = None):
         "rs_solver_precondition_device": [_vp, C.c_int, _vp, _vp],
         "rs_solver_solve_many": [_vp, C.c_int, _f64p, _f64p, _f64p],
         "rs_solver_solve_many_device": [_vp, C.c_int, _vp, _vp, _f64p],
+        "rs_metric_apply_device_noalloc": [_vp, C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p],
         "rs_solver_history": [_vp, C.c_int, _f64p, C.c_int, C.POINTER(C.c_int), _f64p, C.c_int,
                               C.POINTER(C.c_int)],
         "rs_flow_create": [_vp, C.c_int, C.c_int, _u32p, _f64p, C.c_void_p, C.POINTER(_vp)],

@@ -178,6 +178,16 @@ int rs_metric_apply(rs_metric *m, double w_hi, double w_lo, int nb, const double
                     double *ys_host);
 int rs_metric_apply_device(rs_metric *m, double w_hi, double w_lo, int nb, const double *xs_dev,
                            double *ys_dev);
+/* rs_metric_apply_device without device allocation. No counterpart in the reference: the
+ * crate's products allocate on the host heap only. Same result as rs_metric_apply_device;
+ * the per-call scratch (at most 64 MiB per device: InvalidOption above that, e.g. three
+ * vectors on 80,000 faces) lives in one file-scope device array, so it serves callers that
+ * must not allocate while the product runs (a host whose device memory is held by its own
+ * pool after set-up; a latency-critical stream, as cudaMalloc/cudaFree can synchronize the
+ * device). Calls that overlap in time race on the shared scratch: serialize them. The first
+ * call on a device looks up the scratch address; make that call outside any stream capture. */
+int rs_metric_apply_device_noalloc(rs_metric *m, double w_hi, double w_lo, int nb,
+                                   const double *xs_dev, double *ys_dev);
 /* BctStats (far blocks, near blocks, near entries, depth, nodes). */
 int rs_metric_stats(rs_metric *m, int64_t *out5);
 /* The blocks grouped by row node: far_ptr [nodes+1], far_col, near_ptr [nodes+1], near_col. */

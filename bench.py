@@ -1,21 +1,29 @@
 #!/usr/bin/env python
 """Benchmark of the GB300 Repulsive-Surfaces hot path (one JSON line on stdout).
 
-Workload (default ``--workload c2``): the Barnes-Hut tangent-point energy and its exact
-differential on the 81,920-face icosphere of configuration c2 (level 6, spherical-harmonic
-noise, alpha 6, beta 12, theta 0.25, leaf 8), FP32 pairs with Kahan accumulation, FP64 energy.
-A step is one refit of the frozen tree to the (resident) positions plus one energy +
-differential evaluation. The metric is the pair throughput in GFLOP/s, counting 61 FLOP per
-pair interaction (one exact ordered pair or one lumped leaf-face/node term).
+Default workload (``--workload flow``): Hs-flow steps on the 204,800-face torus of the step
+configuration (320x320 grid, R = 1, r = 0.3, alpha 6, beta 12): Barnes-Hut energy and
+differential (theta 0.25), hierarchical metric (chi 0.5, leaf 8), barycenter + area + volume
+constraints (three right-hand sides per step), the fractional preconditioner, GMRES restart 30
+to a true relative residual of 1e-6, Armijo line search and projection. One step = one
+``rs_flow_step`` (trees, lists and solver rebuilt for the step, as the crate does). The noise
+is N(0, 0.001) per coordinate: the specified N(0, 0.01) exceeds the torus' minor edge length
+(0.0059) and crumples it so that no solver reaches 1e-6 (``--workload flow-spec`` runs it).
 
-* ``value``: device-resident inputs, CUDA events on the library's stream around every step,
-  L2 flushed (256 MiB write) between steps.
-* ``e2e``: the same metric through the public C-ABI call with host buffers (positions in,
-  energy and differential out) timed on the wall clock.
-* ``roofline``: the pair kernel (bh_pair), FP32-bound, against the measured FP32 FMA peak.
-* ``cpu_baseline``: the FP64 C++ restatement of the reference (the oracle; the Rust crate
-  cannot be built here) on the host cores, one full evaluation of the same workload.
-* ``--impl reference``: that CPU implementation as the reference arm.
+* ``value``: steps/s from CUDA events on the library's stream around every step (the steps
+  move gigabytes, far above L2).
+* ``e2e``: the same through the public call with the positions read back to the host after
+  every step, on the wall clock; h2d/d2h bytes from the library's copy counters.
+* ``roofline``: the dominant kernel of the step, the metric's near-field kernel (hm_rows),
+  FP32-bound, against the measured FP32 FMA peak; the pair kernel is reported beside it.
+* ``cpu_baseline`` / ``--impl reference``: the FP64 C++ restatement of the reference (the
+  oracle; the Rust crate cannot be built here) on the host cores: one BH energy + differential
+  and one metric product of the same mesh, combined with the step's measured GMRES iteration
+  counts into a CPU step time (preconditioner and set-up not counted: an upper bound on the
+  CPU's steps/s).
+
+``--workload c2`` / ``c3``: the Barnes-Hut pair kernel alone (GFLOP/s, 61 FLOP per pair
+interaction) on the 81,920-face icosphere or the specified torus.
 
 Multi-GPU (torchrun): every rank runs an independent replica (the path has no exchange
 step); value = all ranks' work / the slowest rank's time.
@@ -42,6 +50,14 @@ FLOP_PER_INTERACTION = 61  # energy + gradient, SURVEY's count (FMA = 2, Kahan n
 def workload(name: str):
     from rs_gb300 import generators as gen
 
+    if name == "flow":
+        P, F = gen.config_c3s()
+        return P, F, 0.25, ("torus 320x320 R=1 r=0.3 (102,400 vertices, 204,800 faces), N(0,0.001) "
+                            "noise per coordinate, seed 3")
+    if name == "flow-spec":
+        P, F = gen.config_c3()
+        return P, F, 0.25, ("torus 320x320 R=1 r=0.3 (102,400 vertices, 204,800 faces), N(0,0.01) "
+                            "noise per coordinate, seed 3 (as specified; crumpled)")
     if name == "c2":
         P, F = gen.config_c2()
         return P, F, 0.25, ("icosphere level 6 (40,962 vertices, 81,920 faces), 8 spherical-"
@@ -178,23 +194,223 @@ def _lumped_interactions(bh) -> int:
     return int(np.sum(np.diff(L["lumped_off"]) * ns))
 
 
+FLOW_METRIC = "Hs-flow steps/s @204,800 faces (plain preconditioner, rel.res 1e-6)"
+# Near-field work of the metric per near entry and vector when the near field is recomputed on
+# the fly (kernel 20 FLOP + 2 per channel, C = 12 channels per vector).
+NEAR_FLOP_PER_ENTRY = 44
+# Operator applications per step assumed by the CPU reference arm (which has no preconditioned
+# solver of its own): the GPU arm's mean on this workload, GMRES iterations of the three
+# right-hand sides.
+REFERENCE_ITERATIONS_PER_STEP = 150
+
+
+def flow_options(R):
+    return R.flow_options(theta=0.25, hold_area=1, hold_volume=1, solver_chi=0.5, solver_restart=30,
+                          solver_tolerance=1e-6, solver_max_iterations=300)
+
+
+def cpu_flow_step(P, F, theta, iterations, threads=None):
+    """The FP64 oracle on the host cores: one BH energy + differential and one metric product
+    of the mesh, combined into a step of `iterations` operator applications."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import rs_oracle as O
+
+    O.build()
+    n = threads or os.cpu_count() or 1
+    O.set_threads(n)
+    bh = O.BhTree(P, F, theta=theta)
+    t0 = time.perf_counter()
+    bh.energy_and_differential()
+    t_bh = time.perf_counter() - t0
+    m = O.FaceMetricTree(P, F, chi=0.5)
+    x = np.random.default_rng(0).standard_normal(3 * len(P))
+    t0 = time.perf_counter()
+    m.apply(x)
+    t_prod = time.perf_counter() - t0
+    t_step = t_bh + iterations * t_prod
+    return 1.0 / t_step, t_bh, t_prod, n
+
+
+def run_reference_flow(args, rank):
+    if rank != 0:
+        return 0
+    P, F, theta, desc = workload(args.workload)
+    v, t_bh, t_prod, n = cpu_flow_step(P, F, theta, REFERENCE_ITERATIONS_PER_STEP)
+    sample = (f"one BH energy+differential ({t_bh:.2f} s) and one metric product ({t_prod:.2f} s) of the "
+              f"workload by the FP64 C++ restatement on {n} threads, combined as a step of "
+              f"{REFERENCE_ITERATIONS_PER_STEP} operator applications (preconditioner and set-up not "
+              "counted); the reference crate (Rust) cannot be built here")
+    line = {
+        "impl": "reference", "metric": FLOW_METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus,
+        "steps": 1, "warmup": 0, "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.workload}: {desc}", "theta": theta, "chi": 0.5, "alpha": 6, "beta": 12},
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": n, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def bench_flow(args, rank, world, local):
+    import torch
+
+    import rs_gb300 as R
+
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    warmup = max(3, args.warmup)
+    P, F, theta, desc = workload(args.workload)
+    ctx = R.Context(local)
+    dev = torch.device(f"cuda:{local}")
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    flow = R.Flow(F, P, flow_options(R), ctx)
+    for _ in range(warmup):
+        flow.step()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    reps = []
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    l0 = ctx.launch_count()
+    with Clocks(local) as clk:
+        for a, b in evs:
+            a.record(stream)
+            reps.append(flow.step())
+            b.record(stream)
+        stream.synchronize()
+    launches = ctx.launch_count() - l0
+    ms = [a.elapsed_time(b) for a, b in evs]
+    t_total = sum(ms) / 1e3
+    if world > 1:
+        tt = torch.tensor([t_total], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_total = float(tt.item())
+    value = world * args.steps / t_total
+
+    # e2e: the public call with host positions read back after every step, wall clock
+    if world > 1:
+        torch.distributed.barrier()
+    c0 = R.copy_counters()
+    t0 = time.perf_counter()
+    e2e_reps = []
+    for _ in range(args.steps):
+        e2e_reps.append(flow.step())
+        Q = flow.positions()
+    t_e2e = time.perf_counter() - t0
+    c1 = R.copy_counters()
+    if world > 1:
+        tt = torch.tensor([t_e2e], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_e2e = float(tt.item())
+    e2e = world * args.steps / t_e2e
+
+    # roofline: the metric's near-field kernel on the current surface (one vector per launch)
+    m = R.FaceMetricTree(F, Q, R.Exponents(), R.ClusterTreeOptions(chi=0.5), ctx)
+    mst = m.stats()
+    mprof = m.profile(1, 5)
+    t_rows = mprof.get("metric_rows")
+    peak = ctx.fp32_peak_tflops()
+    rows_flop = NEAR_FLOP_PER_ENTRY * mst["near_entries"]
+    achieved = rows_flop / (t_rows * 1e-3) / 1e12 if t_rows else None
+    # the pair kernel on the same surface
+    bh = R.BhTree.build(F, Q, R.BhOptions(theta, 8), ctx)
+    bs = bh.sizes()
+    n_int = bs["pairs_exact"] + bs["lumped_interactions"]
+    bprof = bh.profile(R.Exponents(), reps=5)
+    t_pair = bprof.get("bh_pair_grad")
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+        if rank != 0:
+            dist.destroy_process_group()
+            return 0
+
+    def mean(key, rr=reps):
+        return float(np.mean([r[key] for r in rr]))
+
+    its = [r["gmres_area"] + r["gmres_volume"] + r["gmres_direction"] for r in reps]
+    line = {
+        "metric": FLOW_METRIC, "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": warmup, "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded mesh generator of the configuration)",
+        "config": {"workload": f"{args.workload}: {desc}", "theta": theta, "chi": 0.5, "alpha": 6, "beta": 12,
+                   "leaf_size": 8, "constraints": "barycenter + area + volume (3 right-hand sides per step)",
+                   "gmres": "restart 30, true relative residual 1e-6, FP64 Arnoldi (CGS2)",
+                   "preconditioner": "fractional (plain), multigrid L' with 3 V-cycles",
+                   "l2": "not flushed: every step moves several GB (trees, lists, solver rebuilt)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "steps_report": {
+            "gmres_iterations_per_step": float(np.mean(its)),
+            "gmres_iterations": [[int(r["gmres_area"]), int(r["gmres_volume"]), int(r["gmres_direction"])]
+                                 for r in reps],
+            "relative_residual_max": max(r["relative_residual"] for r in reps),
+            "energy": [reps[0]["energy_before"], reps[-1]["energy_after"]],
+            "accepted": int(sum(r["accepted"] for r in reps)),
+            "seconds": {k: mean(k) for k in ("seconds", "seconds_tree", "seconds_energy", "seconds_solver_build",
+                                               "seconds_solve", "seconds_line_search", "seconds_projection")},
+        },
+        "e2e": {"value": e2e, "unit": "steps/s",
+                "h2d_bytes_per_step": int((c1[0] - c0[0]) / args.steps),
+                "d2h_bytes_per_step": int((c1[1] - c0[1]) / args.steps)},
+        "roofline": {"bound": "fp32", "kernel": "hm_rows (metric near field, one vector)",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": (achieved / peak) if achieved else None,
+                     "peak_source": "measured FP32 FMA throughput (rs_fp32_peak); "
+                                    "MEASURED_PEAKS.json has no FP32 figure",
+                     "work": f"{NEAR_FLOP_PER_ENTRY} FLOP x {mst['near_entries']} near entries per launch",
+                     "traffic": traffic_from_profiles("hm_rows", args.workload),
+                     "kernel_ms": mprof},
+        "pair_kernel": {"gflops": FLOP_PER_INTERACTION * n_int / (t_pair * 1e-3) / 1e9 if t_pair else None,
+                        "interactions": n_int, "ms": t_pair,
+                        "frac": (FLOP_PER_INTERACTION * n_int / (t_pair * 1e-3) / 1e12 / peak) if t_pair else None},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        its_mean = float(np.mean(its))
+        v, t_bh, t_prod, n = cpu_flow_step(F=F, P=Q, theta=theta, iterations=its_mean)
+        line["cpu_baseline"] = {
+            "value": v, "unit": "steps/s", "cores": n, "kind": "port",
+            "sample": f"one BH energy+differential ({t_bh:.2f} s) and one metric product ({t_prod:.2f} s) "
+                      f"of the current surface by the FP64 C++ restatement on {n} threads, combined as a "
+                      f"step of {its_mean:.0f} operator applications (the measured GMRES iterations; "
+                      "preconditioner and set-up not counted)"}
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 METRIC = "pair GFLOP/s, Barnes-Hut energy+differential (61 FLOP/interaction)"
 
 
 def main() -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3"])
+    ap.add_argument("--workload", default="flow", choices=["flow", "flow-spec", "c2", "c3"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 5 if args.workload.startswith("flow") else 20
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
+        if args.workload.startswith("flow"):
+            return run_reference_flow(args, rank)
         return run_reference(args, rank)
+    if args.workload.startswith("flow"):
+        return bench_flow(args, rank, world, local)
 
     import torch
 

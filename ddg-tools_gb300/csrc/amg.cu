@@ -69,6 +69,65 @@ __global__ void dense_solve_kernel(int n, const double *__restrict__ inv, const 
   x[(size_t)i * C + c] = acc;
 }
 
+constexpr int kDotBlocks = 120;  // fixed split of the column dot products (deterministic)
+
+// part[b][c] = sum over rows i of block b's range of a[i][c] * w[i][c]
+__global__ void col_dots_partial(int n, int C, const double *__restrict__ a, const double *__restrict__ w,
+                                 double *part) {
+  __shared__ double sh[12][128];
+  const int chunk = (n + gridDim.x - 1) / gridDim.x;
+  const int i0 = blockIdx.x * chunk, i1 = min(n, i0 + chunk);
+  for (int c = 0; c < C; ++c) {
+    double acc = 0.0;
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) acc = fma(a[(size_t)i * C + c], w[(size_t)i * C + c], acc);
+    sh[c][threadIdx.x] = acc;
+  }
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if ((int)threadIdx.x < st)
+      for (int c = 0; c < C; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int c = 0; c < C; ++c) part[(size_t)blockIdx.x * C + c] = sh[c][0];
+}
+
+// Scalars of one CG step, per column: slot layout s[0..C) = r.z, s[C..2C) = step length alpha
+// (mode 0: alpha = rz / (p.q) from the partial sums; a non-positive curvature stops the column),
+// mode 1: beta = rz_new / rz into s[2C..3C) and rz = rz_new.
+__global__ void cg_scalars(int C, const double *part, double *s, int mode) {
+  int c = threadIdx.x;
+  if (c >= C) return;
+  double t = 0.0;
+  for (int b = 0; b < kDotBlocks; ++b) t += part[(size_t)b * C + c];
+  if (mode == 0) {
+    s[C + c] = (t > 0.0 && s[c] > 0.0) ? s[c] / t : 0.0;
+  } else if (mode == 1) {
+    s[2 * C + c] = s[c] > 0.0 ? t / s[c] : 0.0;
+    s[c] = t;
+  } else {
+    s[c] = t;
+  }
+}
+
+// x += alpha p, r -= alpha q (per column)
+__global__ void cg_update(int n, int C, const double *__restrict__ s, const double *__restrict__ p,
+                          const double *__restrict__ q, double *__restrict__ x, double *__restrict__ r) {
+  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= (size_t)n * C) return;
+  const double a = s[C + t % C];
+  x[t] = fma(a, p[t], x[t]);
+  r[t] = fma(-a, q[t], r[t]);
+}
+
+// p = z + beta p
+__global__ void cg_direction(int n, int C, const double *__restrict__ s, const double *__restrict__ z,
+                             double *__restrict__ p) {
+  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= (size_t)n * C) return;
+  p[t] = fma(s[2 * C + t % C], p[t], z[t]);
+}
+
 template <class T>
 void up(DevBuf<T> &d, const std::vector<T> &v, cudaStream_t s) {
   d.alloc(std::max<size_t>(v.size(), 1));
@@ -161,6 +220,39 @@ void AmgDevice::vcycle(rs_ctx *ctx, const double *b, double *x, int C_) {
       RSG_LAUNCHED(ctx, "amg_jacobi");
       RSG_CUDA("preconditioner", cudaMemcpyAsync(xl, v.t.p, (size_t)v.n * C_ * sizeof(double), cudaMemcpyDeviceToDevice, s));
     }
+  }
+}
+
+void AmgDevice::pcg(rs_ctx *ctx, const double *b, double *x, int C_, int iters) {
+  reserve(C_);
+  cudaStream_t s = ctx->stream;
+  const int n = L[0].n;
+  const size_t m = (size_t)n * C_;
+  if (cg_r.n < m) cg_r.alloc(m), cg_z.alloc(m), cg_p.alloc(m), cg_q.alloc(m);
+  if (cg_part.n < (size_t)kDotBlocks * 12) cg_part.alloc((size_t)kDotBlocks * 12), cg_s.alloc(36);
+  const unsigned g = nblk(m, 256);
+  auto dots = [&](const double *a, const double *w, int mode) {
+    col_dots_partial<<<kDotBlocks, 128, 0, s>>>(n, C_, a, w, cg_part.p);
+    RSG_LAUNCHED(ctx, "cg_dots");
+    cg_scalars<<<1, 32, 0, s>>>(C_, cg_part.p, cg_s.p, mode);
+    RSG_LAUNCHED(ctx, "cg_scalars");
+  };
+  // x = 0, r = b, z = M r, p = z, rz = r.z
+  RSG_CUDA("preconditioner", cudaMemsetAsync(x, 0, m * sizeof(double), s));
+  RSG_CUDA("preconditioner", cudaMemcpyAsync(cg_r.p, b, m * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  vcycle(ctx, cg_r.p, cg_z.p, C_);
+  RSG_CUDA("preconditioner", cudaMemcpyAsync(cg_p.p, cg_z.p, m * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  dots(cg_r.p, cg_z.p, 2);
+  for (int it = 0; it < iters; ++it) {
+    spmv0(ctx, cg_p.p, cg_q.p, C_);
+    dots(cg_p.p, cg_q.p, 0);
+    cg_update<<<g, 256, 0, s>>>(n, C_, cg_s.p, cg_p.p, cg_q.p, x, cg_r.p);
+    RSG_LAUNCHED(ctx, "cg_update");
+    if (it + 1 == iters) break;
+    vcycle(ctx, cg_r.p, cg_z.p, C_);
+    dots(cg_r.p, cg_z.p, 1);
+    cg_direction<<<g, 256, 0, s>>>(n, C_, cg_s.p, cg_z.p, cg_p.p);
+    RSG_LAUNCHED(ctx, "cg_direction");
   }
 }
 

@@ -44,6 +44,12 @@ struct AmgDevice {
   void vcycle(rs_ctx *ctx, const double *b, double *x, int C_);
   // y = A_0 x for C columns.
   void spmv0(rs_ctx *ctx, const double *x, double *y, int C_);
+  // x ~ A_0^-1 b by `iters` steps of conjugate gradients per column, preconditioned by one
+  // V-cycle each (x_0 = 0; iters = 1 is the V-cycle with the optimal step length). The
+  // scalars stay on the device (no host synchronization); a fixed number of steps makes it a
+  // nonlinear map of b, which flexible GMRES (the stored preconditioned vectors) allows.
+  void pcg(rs_ctx *ctx, const double *b, double *x, int C_, int iters);
+  DevBuf<double> cg_r, cg_z, cg_p, cg_q, cg_part, cg_s;  // n_0 x C each; partial sums; scalars
 };
 
 }  // namespace rsg

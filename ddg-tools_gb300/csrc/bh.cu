@@ -961,7 +961,7 @@ void build_lists_device(rs_bh *h) {
                                                       h->partner_off.p, pbase.p, overflow.p);
   RSG_LAUNCHED(h->ctx, "lists_fill");
   uint32_t tp32 = (uint32_t)tp;
-  RSG_CUDA("upload", cudaMemcpyAsync(h->partner_off.p + te, &tp32, sizeof(uint32_t),
+  RSG_CUDA("upload", rsg::copy_async(h->partner_off.p + te, &tp32, sizeof(uint32_t),
                                      cudaMemcpyHostToDevice, s));
   RSG_CUDA("upload", cudaStreamSynchronize(s));
   finish_lists(h, lo, eo);
@@ -1047,7 +1047,7 @@ void evaluate(rs_bh *h, const Pow &pw, bool fast, bool grad, double *energy_dev,
 void find_culprit(rs_bh *h, const Pow &pw, bool fast) {
   cudaStream_t s = h->st();
   unsigned long long init = ~0ull, rank = ~0ull;
-  RSG_CUDA("product", cudaMemcpyAsync(h->culprit_key.p, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+  RSG_CUDA("product", rsg::copy_async(h->culprit_key.p, &init, sizeof(init), cudaMemcpyHostToDevice, s));
   size_t nl = h->tree.leaves.size();
   if (fast) culprit_kernel<true><<<blocks(nl, 128), 128, 0, s>>>(h->dev(), pw, h->culprit_key.p);
   else culprit_kernel<false><<<blocks(nl, 128), 128, 0, s>>>(h->dev(), pw, h->culprit_key.p);
@@ -1060,7 +1060,7 @@ void find_culprit(rs_bh *h, const Pow &pw, bool fast) {
   std::vector<uint32_t> eo(nl + 1);
   uint32_t c = 0;
   h->exact_off.download(eo.data(), nl + 1, s);
-  RSG_CUDA("product", cudaMemcpyAsync(&c, h->exact.p + q, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  RSG_CUDA("product", rsg::copy_async(&c, h->exact.p + q, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
   RSG_CUDA("product", cudaStreamSynchronize(s));
   size_t k = (size_t)(std::upper_bound(eo.begin(), eo.end(), q) - eo.begin()) - 1;
   const Tree &T = h->tree;

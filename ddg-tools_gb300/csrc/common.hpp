@@ -14,6 +14,17 @@
 
 namespace rsg {
 
+// Bytes the library copied host -> device and device -> host (process-wide; rs_copy_counters).
+inline std::atomic<uint64_t> g_h2d_bytes{0}, g_d2h_bytes{0};
+
+// cudaMemcpyAsync of a host <-> device copy, counted.
+inline cudaError_t copy_async(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind, cudaStream_t s) {
+  if (kind == cudaMemcpyHostToDevice) g_h2d_bytes += bytes;
+  else if (kind == cudaMemcpyDeviceToHost) g_d2h_bytes += bytes;
+  return cudaMemcpyAsync(dst, src, bytes, kind, s);
+}
+
+
 // An error carrying the RsError kind, the operation word and a detail string
 // (RsError::Gpu { operation, detail }, RS/src/gpu/cuda.rs:19-24).
 struct Error : std::runtime_error {
@@ -84,11 +95,11 @@ struct DevBuf {
   size_t bytes() const { return n * sizeof(T); }
   void upload(const T *h, size_t count, cudaStream_t s) {
     if (count != n) alloc(count);
-    if (count) RSG_CUDA("upload", cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+    if (count) RSG_CUDA("upload", rsg::copy_async(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
   }
   void upload(const std::vector<T> &v, cudaStream_t s) { upload(v.data(), v.size(), s); }
   void download(T *h, size_t count, cudaStream_t s) const {
-    if (count) RSG_CUDA("product", cudaMemcpyAsync(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, s));
+    if (count) RSG_CUDA("product", rsg::copy_async(h, p, count * sizeof(T), cudaMemcpyDeviceToHost, s));
   }
 };
 

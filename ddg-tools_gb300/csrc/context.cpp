@@ -117,6 +117,13 @@ int rs_ctx_stream(rs_ctx *ctx, void **stream) {
   return rsg::guard([&] { *stream = (void *)ctx->stream; });
 }
 
+int rs_copy_counters(uint64_t *h2d_bytes, uint64_t *d2h_bytes) {
+  return rsg::guard([&] {
+    if (h2d_bytes) *h2d_bytes = rsg::g_h2d_bytes.load();
+    if (d2h_bytes) *d2h_bytes = rsg::g_d2h_bytes.load();
+  });
+}
+
 int rs_ctx_synchronize(rs_ctx *ctx) {
   return rsg::guard([&] {
     ctx->use();

@@ -237,7 +237,7 @@ int rs_flow_step(rs_flow *F, double *report) {
     double E0 = 0.0;
     e_dev.download(&E0, 1, s);
     std::vector<double> g(nd);
-    RSG_CUDA("flow", cudaMemcpyAsync(g.data(), rhs.p + (size_t)k * n, nd * sizeof(double), cudaMemcpyDeviceToHost, s));
+    RSG_CUDA("flow", rsg::copy_async(g.data(), rhs.p + (size_t)k * n, nd * sizeof(double), cudaMemcpyDeviceToHost, s));
     RSG_CUDA("flow", cudaStreamSynchronize(s));
     rep[10] = since(t);
     if (!std::isfinite(E0)) fail(RS_NONFINITE_ENERGY, "NonFiniteEnergy", "flow", "non-finite energy");
@@ -248,7 +248,7 @@ int rs_flow_step(rs_flow *F, double *report) {
     for (int i = 0; i < k; ++i) {
       if (rows[i] == 0) area_gradient(nv, nf, faces, F->pos.data(), cn[i].data());
       else volume_gradient(nv, nf, faces, F->pos.data(), cn[i].data());
-      RSG_CUDA("flow", cudaMemcpyAsync(rhs.p + (size_t)i * n, cn[i].data(), nd * sizeof(double), cudaMemcpyHostToDevice, s));
+      RSG_CUDA("flow", rsg::copy_async(rhs.p + (size_t)i * n, cn[i].data(), nd * sizeof(double), cudaMemcpyHostToDevice, s));
     }
     // 3. one batch: Z columns and y
     t = clk::now();

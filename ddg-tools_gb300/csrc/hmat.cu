@@ -48,16 +48,16 @@ __device__ __forceinline__ bool uses_k1(int c) {
 struct HDev {
   const uint32_t *start, *end, *right, *parent, *leaves, *chain_off, *chain;
   const uint32_t *far_ptr, *far_col;
-  const float2 *far_coef;    // per far block: (k_0, k_1)
+  const double2 *far_coef;   // per far block: (k_0, k_1)
   const float4 *xh;          // per BVH position: position hi (xyz), weight a (w)
   const float4 *xl;          // per BVH position: position lo (xyz): X = hi + lo to ~48 bits
   const float4 *nrm;         // per BVH position: normal (faces only)
-  const float2 *node_farA;   // per node: its far sums of psi = a (k_0, k_1), the far part of H~a
+  const double2 *node_farA;  // per node: its far sums of psi = a (k_0, k_1), the far part of H~a
   const uint2 *cols;         // near column ranges [x, y) of every leaf's chain, leaf by leaf
   const uint4 *items;        // per work item: leaf ordinal, column-range begin / end, -
   const uint32_t *item_off;  // per leaf: its work items [item_off[k], item_off[k + 1])
-  float *up;                 // per node: C channel sums of a m (hi parts)
-  float *farx;               // per node: C channel far sums
+  double *up;                // per node: C channel sums of a m (FP64)
+  double *farx;              // per node: C channel far sums (FP64)
   float2 *part;              // per work item: 8 rows x C near sums as float pairs
   uint32_t *count;           // per node: arrival counter of the upward pass
   const float2 *m;           // [n][C] channel values as float pairs (hi, lo)
@@ -124,23 +124,26 @@ __device__ __forceinline__ void near_kernel(const HDev &d, float d0, float d1, f
   }
 }
 
-// Bottom-up channel sums: one thread per leaf sums its elements in registers, then climbs; at
-// every parent the second child to arrive adds left + right (fixed order, no waiting).
+// Bottom-up channel sums in FP64: one thread per leaf sums its elements in registers, then
+// climbs; at every parent the second child to arrive adds left + right (fixed order, no
+// waiting). The far field is FP64 end to end (upward, far sums, chain push-down): its sums
+// cancel against m_p H~a for a smooth input just as the near sums do, and at O(nodes) and
+// O(far blocks) work the FP64 rate costs little.
 template <int CC>
 __global__ void hm_upward_kernel(HDev d) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= d.n_leaves) return;
   uint32_t leaf = d.leaves[k];
-  float u[CC];
+  double u[CC];
 #pragma unroll
-  for (int c = 0; c < CC; ++c) u[c] = 0.f;
+  for (int c = 0; c < CC; ++c) u[c] = 0.0;
   for (uint32_t p = d.start[leaf]; p < d.end[leaf]; ++p) {
-    float a = d.xh[p].w;
+    const double a = d.xh[p].w;
     const float2 *mp = d.m + (size_t)p * CC;
 #pragma unroll
-    for (int c = 0; c < CC; ++c) u[c] += a * mp[c].x;
+    for (int c = 0; c < CC; ++c) u[c] = fma(a, (double)mp[c].x + (double)mp[c].y, u[c]);
   }
-  float *o = d.up + (size_t)leaf * CC;
+  double *o = d.up + (size_t)leaf * CC;
 #pragma unroll
   for (int c = 0; c < CC; ++c) o[c] = u[c];
   uint32_t n = leaf;
@@ -150,9 +153,9 @@ __global__ void hm_upward_kernel(HDev d) {
     unsigned old = atomicAdd(&d.count[par], 1u);
     if ((old & 1u) == 0u) return;
     __threadfence();
-    const float *l = d.up + (size_t)(par + 1) * CC;
-    const float *r = d.up + (size_t)d.right[par] * CC;
-    float *op = d.up + (size_t)par * CC;
+    const double *l = d.up + (size_t)(par + 1) * CC;
+    const double *r = d.up + (size_t)d.right[par] * CC;
+    double *op = d.up + (size_t)par * CC;
 #pragma unroll
     for (int c = 0; c < CC; ++c) op[c] = __ldcg(l + c) + __ldcg(r + c);
     n = par;
@@ -160,27 +163,27 @@ __global__ void hm_upward_kernel(HDev d) {
 }
 
 // farx[a][c] = sum over the far blocks (a, b) of h(a, b)[kernel(c)] up[b][c] (block_tree.rs:
-// 564-578); one warp per node, lanes strided over the node's far blocks, each summing all CC
-// channels, then a fixed butterfly over the lanes.
+// 564-578), FP64; one warp per node, lanes strided over the node's far blocks, each summing
+// all CC channels, then a fixed butterfly over the lanes.
 template <int SEL, int CC>
 __global__ void hm_far_kernel(HDev d) {
   int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   if (a >= d.n_nodes) return;
-  float acc[CC];
+  double acc[CC];
 #pragma unroll
-  for (int c = 0; c < CC; ++c) acc[c] = 0.f;
+  for (int c = 0; c < CC; ++c) acc[c] = 0.0;
   for (uint32_t q = d.far_ptr[a] + lane; q < d.far_ptr[a + 1]; q += 32) {
-    float2 k = d.far_coef[q];
-    const float *u = d.up + (size_t)d.far_col[q] * CC;
+    const double2 k = d.far_coef[q];
+    const double *u = d.up + (size_t)d.far_col[q] * CC;
 #pragma unroll
-    for (int c = 0; c < CC; ++c) acc[c] += (uses_k1<SEL>(c) ? k.y : k.x) * u[c];
+    for (int c = 0; c < CC; ++c) acc[c] = fma(uses_k1<SEL>(c) ? k.y : k.x, u[c], acc[c]);
   }
 #pragma unroll
   for (int c = 0; c < CC; ++c)
 #pragma unroll
     for (int m = 16; m >= 1; m >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], m);
-  float *o = d.farx + (size_t)a * CC;
+  double *o = d.farx + (size_t)a * CC;
 #pragma unroll
   for (int c = 0; c < CC; ++c)
     if (lane == (c & 31)) o[c] = acc[c];
@@ -191,8 +194,8 @@ __global__ void hm_far_kernel(HDev d) {
 // per item; lane = r + 8 j: r the row (element) of the leaf, j one of four column groups
 // taking every fourth column. The kernel values of a column are evaluated once per row and
 // applied to the CC channels. m_p - m_q is formed from the float pairs (exact for nearby
-// values) and the terms are summed with Kahan compensation, then combined over the groups as
-// float pairs: for a smooth input the terms are first-order quantities that cancel to a
+// values), each product w (m_p - m_q) is split exactly, the terms are summed with Kahan
+// compensation and their low parts apart, then combined over the groups as float pairs: for a smooth input the terms are first-order quantities that cancel to a
 // second-order result, and the output stage (M^T, a discrete divergence) cancels once more,
 // so plain FP32 sums of H~a m and H~(a m) would lose about four digits.
 template <int KIND, int CC>
@@ -209,7 +212,7 @@ __global__ void __launch_bounds__(128) hm_rows_kernel(HDev d, int c0) {
   const float4 ph = d.xh[p], pl = d.xl[p];
   const float4 np = KIND == FACE ? d.nrm[p] : make_float4(0.f, 0.f, 0.f, 0.f);
   const int C = d.C;
-  float mh[CC], ml[CC], ks[CC], kc[CC];
+  float mh[CC], ml[CC], ks[CC], kc[CC], kl[CC];
   {
     const float4 *mp = reinterpret_cast<const float4 *>(d.m + (size_t)p * C + c0);
 #pragma unroll
@@ -219,7 +222,7 @@ __global__ void __launch_bounds__(128) hm_rows_kernel(HDev d, int c0) {
     }
   }
 #pragma unroll
-  for (int c = 0; c < CC; ++c) ks[c] = 0.f, kc[c] = 0.f;
+  for (int c = 0; c < CC; ++c) ks[c] = 0.f, kc[c] = 0.f, kl[c] = 0.f;
   if (act)
     for (uint32_t ri = it.y; ri < it.z; ++ri) {
       const uint2 cr = d.cols[ri];
@@ -240,9 +243,18 @@ __global__ void __launch_bounds__(128) hm_rows_kernel(HDev d, int c0) {
           for (int e = 0; e < 2; ++e) {
             const int c = 2 * c2 + e;
             const float qhv = e ? v.z : v.x, qlv = e ? v.w : v.y;
-            const float dm = (mh[c] - qhv) + (ml[c] - qlv);
-            const float t = ((KIND == FACE && c >= 9) ? w1 : w0) * dm;
-            const float y = t - kc[c];
+            const float wk = (KIND == FACE && c >= 9) ? w1 : w0;
+            // w (m_p - m_q) = w dh + w dl with mh_p - mh_q = dh + de split exactly (values of
+            // opposite sign near a zero of the field do not subtract exactly) and
+            // dl = ml_p - ml_q + de; the product w dh is split exactly (pr + pe) as well, so
+            // that no rounding that depends on the input reaches the sum above eps^2
+            float dh, de;
+            two_sum(mh[c], -qhv, dh, de);
+            const float dl = (ml[c] - qlv) + de;
+            const float pr = wk * dh;
+            const float pe = fmaf(wk, dh, -pr);
+            kl[c] = fmaf(wk, dl, kl[c] + pe);
+            const float y = pr - kc[c];
             const float tt = ks[c] + y;
             kc[c] = (tt - ks[c]) - y;
             ks[c] = tt;
@@ -253,7 +265,7 @@ __global__ void __launch_bounds__(128) hm_rows_kernel(HDev d, int c0) {
   // combine the four column groups as float pairs (h, l) = (s, -c)
 #pragma unroll
   for (int c = 0; c < CC; ++c) {
-    float h = ks[c], l = -kc[c];
+    float h = ks[c], l = kl[c] - kc[c];
 #pragma unroll
     for (int m = 8; m <= 16; m <<= 1) {
       const float oh = __shfl_xor_sync(0xffffffffu, h, m), ol = __shfl_xor_sync(0xffffffffu, l, m);
@@ -268,8 +280,9 @@ __global__ void __launch_bounds__(128) hm_rows_kernel(HDev d, int c0) {
 }
 
 // Per leaf (thread per row): z = near + (m_p H~a_far - H~(a m)_far), the near sums of the
-// items (in item order, as float pairs) plus the far sums along the chain (root to leaf). The
-// far part of H~a is summed in the same order from node_farA, so m = 1 gives z = 0 exactly.
+// items (in item order, as float pairs) plus the far sums along the chain (root to leaf) in
+// FP64. The far part of H~a was summed with the same operations from psi = a, so m = 1 gives
+// z = 0 exactly. Channels are taken twelve at a time to bound the registers.
 template <int SEL, int CC>
 __global__ void hm_epilogue_kernel(HDev d) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -279,34 +292,42 @@ __global__ void hm_epilogue_kernel(HDev d) {
   const uint32_t s0 = d.start[leaf];
   if ((uint32_t)r >= d.end[leaf] - s0) return;
   const uint32_t p = s0 + r;
-  float nh[CC], nl[CC], fx[CC];
-#pragma unroll
-  for (int c = 0; c < CC; ++c) nh[c] = 0.f, nl[c] = 0.f, fx[c] = 0.f;
-  for (uint32_t i = d.item_off[k]; i < d.item_off[k + 1]; ++i) {
-    const float2 *o = d.part + ((size_t)i * 8 + r) * CC;
-#pragma unroll
-    for (int c = 0; c < CC; ++c) {
-      const float2 v = o[c];
-      pair_add(nh[c], nl[c], v.x, v.y);
-    }
-  }
-  float fa0 = 0.f, fa1 = 0.f;
+  constexpr int G = CC < 12 ? CC : 12;
+  static_assert(CC % G == 0, "channel groups");
+  double fa0 = 0.0, fa1 = 0.0;
   for (uint32_t ci = d.chain_off[k]; ci < d.chain_off[k + 1]; ++ci) {
-    const uint32_t a = d.chain[ci];
-    const float *f = d.farx + (size_t)a * CC;
-#pragma unroll
-    for (int c = 0; c < CC; ++c) fx[c] += f[c];
-    const float2 fa = d.node_farA[a];
+    const double2 fa = d.node_farA[d.chain[ci]];
     fa0 += fa.x, fa1 += fa.y;
   }
   const float2 *mp = d.m + (size_t)p * CC;
   float2 *zp = d.z + (size_t)p * CC;
+#pragma unroll 1
+  for (int c0 = 0; c0 < CC; c0 += G) {
+    float nh[G], nl[G];
+    double fx[G];
 #pragma unroll
-  for (int c = 0; c < CC; ++c) {
-    const float far = fmaf(mp[c].x, uses_k1<SEL>(c) ? fa1 : fa0, -fx[c]);
-    float h = nh[c], l = nl[c];
-    pair_add(h, l, far, 0.f);
-    zp[c] = make_float2(h, l);
+    for (int c = 0; c < G; ++c) nh[c] = 0.f, nl[c] = 0.f, fx[c] = 0.0;
+    for (uint32_t i = d.item_off[k]; i < d.item_off[k + 1]; ++i) {
+      const float2 *o = d.part + ((size_t)i * 8 + r) * CC + c0;
+#pragma unroll
+      for (int c = 0; c < G; ++c) {
+        const float2 v = o[c];
+        pair_add(nh[c], nl[c], v.x, v.y);
+      }
+    }
+    for (uint32_t ci = d.chain_off[k]; ci < d.chain_off[k + 1]; ++ci) {
+      const double *f = d.farx + (size_t)d.chain[ci] * CC + c0;
+#pragma unroll
+      for (int c = 0; c < G; ++c) fx[c] += f[c];
+    }
+#pragma unroll
+    for (int c = 0; c < G; ++c) {
+      const float2 mv = mp[c0 + c];
+      const double far = ((double)mv.x + (double)mv.y) * (uses_k1<SEL>(c0 + c) ? fa1 : fa0) - fx[c];
+      const double zz = ((double)nh[c] + (double)nl[c]) + far;
+      const float zh = (float)zz;
+      zp[c0 + c] = make_float2(zh, (float)(zz - (double)zh));
+    }
   }
 }
 
@@ -450,9 +471,9 @@ struct HMat {
   DevBuf<uint32_t> far_ptr, far_col, count;
   DevBuf<uint2> cols;
   DevBuf<uint4> items;
-  DevBuf<float2> far_coef, node_farA;
+  DevBuf<double2> far_coef, node_farA;
   DevBuf<float4> xh, xl, nrm;
-  DevBuf<float> up, farx;
+  DevBuf<double> up, farx;
   DevBuf<float2> part, m, z;
   int pw_mode = 0, pw_k = 0;
   Profiler prof;
@@ -562,7 +583,7 @@ struct HMat {
     count.alloc(nn);
     RSG_CUDA("upload", cudaMemsetAsync(count.p, 0, nn * sizeof(uint32_t), s));
     // far coefficients on the host in FP64 (kernel.far, hierarchical.rs:210-220 / 980-984)
-    std::vector<float2> coef(blocks.far_col.size());
+    std::vector<double2> coef(blocks.far_col.size());
     auto qf = [&](size_t n, const double *d) {
       const double *p = proj6 + 6 * n;
       return p[0] * d[0] * d[0] + p[3] * d[1] * d[1] + p[5] * d[2] * d[2] +
@@ -577,7 +598,7 @@ struct HMat {
         double h = std::pow(r2, neg_s);
         double h1 = h;
         if (kind == FACE) h1 = 0.5 * (qf(lo, d) + qf(hi, d)) / (r2 * r2) * h;
-        coef[q] = make_float2((float)h, (float)h1);
+        coef[q] = make_double2(h, h1);
       }
     up_vec(far_coef, coef, s);
     // element records
@@ -601,7 +622,7 @@ struct HMat {
     HDev d = dev(2);
     d.m = mm.p;
     upward_far<ONES, 2>(d);
-    RSG_CUDA("upload", cudaMemcpyAsync(node_farA.p, farx.p, nn * sizeof(float2), cudaMemcpyDeviceToDevice, s));
+    RSG_CUDA("upload", cudaMemcpyAsync(node_farA.p, farx.p, nn * sizeof(double2), cudaMemcpyDeviceToDevice, s));
     RSG_CUDA("upload", cudaStreamSynchronize(s));
   }
 
@@ -810,9 +831,9 @@ void host_io(rs_ctx *ctx, DevBuf<double> &xb, DevBuf<double> &yb, size_t n, cons
   if (xb.n < n) xb.alloc(n), yb.alloc(n);
   double *stage = (double *)ctx->staging(n * sizeof(double));
   std::memcpy(stage, xh, n * sizeof(double));
-  RSG_CUDA("upload", cudaMemcpyAsync(xb.p, stage, n * sizeof(double), cudaMemcpyHostToDevice, s));
+  RSG_CUDA("upload", rsg::copy_async(xb.p, stage, n * sizeof(double), cudaMemcpyHostToDevice, s));
   apply(xb.p, yb.p);
-  RSG_CUDA("product", cudaMemcpyAsync(stage, yb.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  RSG_CUDA("product", rsg::copy_async(stage, yb.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
   RSG_CUDA("product", cudaStreamSynchronize(s));
   std::memcpy(yh, stage, n * sizeof(double));
 }
@@ -1001,7 +1022,7 @@ inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 // Scratch bytes of one tree pass with C channels (the layout carved below).
 size_t noalloc_bytes(const HMat &h, int C) {
   size_t nn = h.tree.n_nodes();
-  return 2 * align256(nn * C * sizeof(float)) + 2 * align256(h.n_el * C * sizeof(float2)) +
+  return 2 * align256(nn * C * sizeof(double)) + 2 * align256(h.n_el * C * sizeof(float2)) +
          align256(std::max<size_t>(h.n_items, 1) * 8 * C * sizeof(float2));
 }
 
@@ -1013,8 +1034,8 @@ HDev noalloc_dev(const HMat &h, int C, unsigned char *base) {
     off += align256(bytes);
     return p;
   };
-  d.up = reinterpret_cast<float *>(take(nn * C * sizeof(float)));
-  d.farx = reinterpret_cast<float *>(take(nn * C * sizeof(float)));
+  d.up = reinterpret_cast<double *>(take(nn * C * sizeof(double)));
+  d.farx = reinterpret_cast<double *>(take(nn * C * sizeof(double)));
   d.m = reinterpret_cast<const float2 *>(take(h.n_el * C * sizeof(float2)));
   d.z = reinterpret_cast<float2 *>(take(h.n_el * C * sizeof(float2)));
   d.part = reinterpret_cast<float2 *>(take(std::max<size_t>(h.n_items, 1) * 8 * C * sizeof(float2)));

@@ -115,14 +115,14 @@ void gmres_batch(rs_ctx *ctx, const Operator &A, const Operator *P, int nb, cons
   // one norm: dots of w with itself, then sqrt
   auto norm_dev = [&](Rhs &q, const double *v, double *out) {
     const double *ptrs[1] = {v};
-    RSG_CUDA("gmres", cudaMemcpyAsync(q.wptr.p, ptrs, sizeof(ptrs), cudaMemcpyHostToDevice, s));
+    RSG_CUDA("gmres", rsg::copy_async(q.wptr.p, ptrs, sizeof(ptrs), cudaMemcpyHostToDevice, s));
     dev_dots(ctx, q.wptr.p, 1, v, n, out);
     sqrt_kernel<<<1, 1, 0, s>>>(out);
     RSG_LAUNCHED(ctx, "sqrt");
   };
   auto host_value = [&](const double *dev) {
     double v;
-    RSG_CUDA("gmres", cudaMemcpyAsync(&v, dev, sizeof(double), cudaMemcpyDeviceToHost, s));
+    RSG_CUDA("gmres", rsg::copy_async(&v, dev, sizeof(double), cudaMemcpyDeviceToHost, s));
     RSG_CUDA("gmres", cudaStreamSynchronize(s));
     return v;
   };
@@ -138,8 +138,8 @@ void gmres_batch(rs_ctx *ctx, const Operator &A, const Operator *P, int nb, cons
     std::vector<const double *> vp(m + 1), zp(m);
     for (int i = 0; i <= m; ++i) vp[i] = Q.V.p + (size_t)i * n;
     for (int i = 0; i < m; ++i) zp[i] = Q.Z.p + (size_t)i * n;
-    RSG_CUDA("gmres", cudaMemcpyAsync(Q.vptr.p, vp.data(), vp.size() * sizeof(void *), cudaMemcpyHostToDevice, s));
-    RSG_CUDA("gmres", cudaMemcpyAsync(Q.zptr.p, zp.data(), zp.size() * sizeof(void *), cudaMemcpyHostToDevice, s));
+    RSG_CUDA("gmres", rsg::copy_async(Q.vptr.p, vp.data(), vp.size() * sizeof(void *), cudaMemcpyHostToDevice, s));
+    RSG_CUDA("gmres", rsg::copy_async(Q.zptr.p, zp.data(), zp.size() * sizeof(void *), cudaMemcpyHostToDevice, s));
     norm_dev(Q, b + (size_t)q * n, Q.h.p);
     Q.bnorm = host_value(Q.h.p);
     Q.H.assign((size_t)(m + 1) * m, 0.0);
@@ -252,7 +252,7 @@ void gmres_batch(rs_ctx *ctx, const Operator &A, const Operator *P, int nb, cons
     }
     std::vector<double> hh((size_t)na * (2 * (m + 2) + 1));
     for (int i = 0; i < na; ++i)
-      RSG_CUDA("gmres", cudaMemcpyAsync(hh.data() + (size_t)i * (2 * (m + 2) + 1), R[act[i]].h.p,
+      RSG_CUDA("gmres", rsg::copy_async(hh.data() + (size_t)i * (2 * (m + 2) + 1), R[act[i]].h.p,
                                         (2 * (m + 2) + 1) * sizeof(double), cudaMemcpyDeviceToHost, s));
     RSG_CUDA("gmres", cudaStreamSynchronize(s));
     bool any_end = false;
@@ -300,7 +300,7 @@ void gmres_batch(rs_ctx *ctx, const Operator &A, const Operator *P, int nb, cons
         double d = Q.H[(size_t)t * m + t];
         y[t] = d != 0.0 ? sum / d : 0.0;
       }
-      RSG_CUDA("gmres", cudaMemcpyAsync(Q.h.p, y.data(), kk * sizeof(double), cudaMemcpyHostToDevice, s));
+      RSG_CUDA("gmres", rsg::copy_async(Q.h.p, y.data(), kk * sizeof(double), cudaMemcpyHostToDevice, s));
       axpy_many_kernel<<<nb_(n, 256), 256, 0, s>>>(Q.zptr.p, kk, Q.h.p, 1.0, x + (size_t)act[i] * n, n);
       RSG_LAUNCHED(ctx, "axpy_many");
       RSG_CUDA("gmres", cudaStreamSynchronize(s));  // y lives on the host stack
@@ -339,10 +339,10 @@ double dev_norm(rs_ctx *ctx, const double *w, size_t n) {
   DevBuf<const double *> p(1);
   DevBuf<double> out(1);
   const double *ptrs[1] = {w};
-  RSG_CUDA("gmres", cudaMemcpyAsync(p.p, ptrs, sizeof(ptrs), cudaMemcpyHostToDevice, ctx->stream));
+  RSG_CUDA("gmres", rsg::copy_async(p.p, ptrs, sizeof(ptrs), cudaMemcpyHostToDevice, ctx->stream));
   dev_dots(ctx, p.p, 1, w, n, out.p);
   double v;
-  RSG_CUDA("gmres", cudaMemcpyAsync(&v, out.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  RSG_CUDA("gmres", rsg::copy_async(&v, out.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   RSG_CUDA("gmres", cudaStreamSynchronize(ctx->stream));
   return std::sqrt(v);
 }

@@ -166,6 +166,7 @@ struct rs_solver {
   double w_hi = 1.0, w_lo = 1.0, frac_scale = 1.0, eps = 0.0;
   bool use_prec = true;
   int vcycles = 1;
+  double build_times[6] = {0, 0, 0, 0, 0, 0};
   GmresOptions gopt;
   FaceGeom geom;
   std::vector<double> vmass;
@@ -214,14 +215,7 @@ struct rs_solver {
     size_t m = (size_t)nv * 3 * nb;
     to_mg_kernel<<<nblk(m, 256), 256, 0, st()>>>(r, n, nb, nv, group.p, c.p, mu.p, G, mg_in.p);
     RSG_LAUNCHED(ctx, "to_mg");
-    amg.vcycle(ctx, mg_in.p, mg_out.p, 3 * nb);
-    for (int it = 1; it < vcycles; ++it) {  // further cycles on the residual
-      amg.spmv0(ctx, mg_out.p, ky.p, 3 * nb);
-      // ky = rhs - A y
-      axpby(m, mg_in.p, ky.p);
-      amg.vcycle(ctx, ky.p, mg_tmp.p, 3 * nb);
-      add_into(m, mg_tmp.p, mg_out.p);
-    }
+    amg.pcg(ctx, mg_in.p, mg_out.p, 3 * nb, vcycles);
     // shift: C_Q y = b
     pos_copy_weighted(nb);
     shift_kernel<<<nblk(3 * G * nb, 128), 128, 0, st()>>>(cy.p, r, n, nd, nb, G, shift.p);
@@ -411,6 +405,13 @@ int rs_solver_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const do
     if (!(o->tp_weight > 0.0 && std::isfinite(o->tp_weight)))
       fail(RS_INVALID_OPTION, "InvalidOption", "solver", "tp_weight must be finite and positive");
     ctx->use();
+    using clk = std::chrono::steady_clock;
+    auto t_all = clk::now(), t_ph = t_all;
+    auto lap = [&](double &slot) {
+      auto now = clk::now();
+      slot = std::chrono::duration<double>(now - t_ph).count();
+      t_ph = now;
+    };
     auto S = std::make_unique<rs_solver>();
     S->ctx = ctx;
     S->nv = nv, S->nf = nf, S->nd = 3 * (size_t)nv;
@@ -431,8 +432,10 @@ int rs_solver_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const do
     S->n = S->nd + 3 * (size_t)S->G;
     bool multi = !per_comp && ncomp > 1;  // translations_fixed_per_component (precond.rs:96-124)
     double eps = 0.0;
+    t_ph = clk::now();
     Csr K = laplacian_block(nv, nf, faces, positions_host, S->vmass, multi ? o->eps_multi_rel : o->eps_rel,
                             o->clamp_laplacian != 0, eps);
+    double t_lap = std::chrono::duration<double>(clk::now() - t_ph).count();
     S->eps = eps;
     std::vector<double> ea(S->G);
     for (int g = 0; g < S->G; ++g) ea[g] = eps * garea[g];
@@ -441,11 +444,13 @@ int rs_solver_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const do
     S->c.upload(ch, s);
     S->eps_area.upload(ea, s);
     // metric and fractional factor
+    t_ph = clk::now();
     rs_metric *m = nullptr;
     int rc = rs_metric_build(ctx, nv, nf, faces, positions_host, alpha, beta, o->chi, o->leaf_size,
                              o->leaf_pairs, &m);
     if (rc) fail(rc, "Gpu", "solver", std::string("metric: ") + rs_last_error());
     S->metric = m;
+    lap(S->build_times[0]);
     S->w_hi = o->tp_weight;
     S->w_lo = o->tp_weight * (o->low_order ? 1.0 : 0.0);
     double sexp = (beta - 2.0) / alpha;
@@ -454,8 +459,12 @@ int rs_solver_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const do
                         o->leaf_pairs, &vf);
     if (rc) fail(rc, "Gpu", "solver", std::string("fractional tree: ") + rs_last_error());
     S->vfrac = vf;
+    lap(S->build_times[1]);
+    S->build_times[2] = t_lap;
     S->frac_scale = 1.0 / (o->tp_weight * symbol_ratio(sexp));  // FractionalScale::Symbol
-    S->amg.upload(amg_setup(K), s);
+    AmgHost amg_h = amg_setup(K);
+    lap(S->build_times[3]);
+    S->amg.upload(amg_h, s);
     S->vcycles = std::max(1, o->vcycles);
     S->use_prec = o->preconditioner != 0;
     S->gopt.restart = o->restart;
@@ -467,6 +476,8 @@ int rs_solver_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const do
     S->prec.n = S->n;
     S->prec.apply = [P](int nb, const double *x, double *y) { P->apply_prec(nb, x, y); };
     RSG_CUDA("solver", cudaStreamSynchronize(s));
+    lap(S->build_times[4]);
+    S->build_times[5] = std::chrono::duration<double>(clk::now() - t_all).count();
     ctx_retain(ctx);
     *out = S.release();
   });
@@ -481,6 +492,10 @@ void rs_solver_free(rs_solver *S) {
   rs_vfrac_free(S->vfrac);
   delete S;
   ctx_release(ctx);
+}
+
+int rs_solver_build_times(rs_solver *S, double *out6) {
+  return guard([&] { std::copy(S->build_times, S->build_times + 6, out6); });
 }
 
 int rs_solver_dims(rs_solver *S, int64_t *n_dofs, int64_t *n_constraints) {
@@ -592,7 +607,7 @@ rs_solver_options rs_solver_options_default(void) {
   o.eps_rel = 1e-10;
   o.eps_multi_rel = 1e-4;
   o.barycenter_per_component = 0;
-  o.vcycles = 1;
+  o.vcycles = 3;
   o.preconditioner = 1;
   o.clamp_laplacian = 0;
   return o;

@@ -125,6 +125,8 @@ def load_library(path: str | os.PathLike | None = None):
         "rs_solver_solve_many": [_vp, C.c_int, _f64p, _f64p, _f64p],
         "rs_solver_solve_many_device": [_vp, C.c_int, _vp, _vp, _f64p],
         "rs_metric_apply_device_noalloc": [_vp, C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p],
+        "rs_copy_counters": [C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)],
+        "rs_solver_build_times": [_vp, _f64p],
         "rs_solver_history": [_vp, C.c_int, _f64p, C.c_int, C.POINTER(C.c_int), _f64p, C.c_int,
                               C.POINTER(C.c_int)],
         "rs_flow_create": [_vp, C.c_int, C.c_int, _u32p, _f64p, C.c_void_p, C.POINTER(_vp)],
@@ -576,6 +578,13 @@ class SaddleSolver:
             r["converged"] = bool(r["converged"])
         return out, reports
 
+    def build_times(self) -> dict:
+        """Host seconds of the solver's set-up by phase."""
+        o = np.zeros(6)
+        _check(_lib.rs_solver_build_times(self._h, o))
+        return dict(zip(["metric", "vertex_fractional", "laplacian", "multigrid_setup", "multigrid_upload",
+                         "total"], o.tolist()))
+
     def history(self, q: int = 0):
         """(per-iteration estimated relative residuals, explicit residual at every cycle start)
         of right-hand side q of the last solve."""
@@ -632,3 +641,10 @@ class Flow:
         out = np.empty((self.n_vertices, 3))
         _check(_lib.rs_flow_positions(self._h, out.ravel()))
         return out
+
+
+def copy_counters() -> tuple[int, int]:
+    """(host->device, device->host) bytes the library has copied in this process."""
+    a, b = C.c_uint64(), C.c_uint64()
+    _check(load_library().rs_copy_counters(C.byref(a), C.byref(b)))
+    return a.value, b.value

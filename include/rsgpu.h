@@ -77,6 +77,9 @@ int rs_ctx_info(rs_ctx *ctx, char *name, int name_len, int *sm_count, int *cc_ma
                 int *cc_minor);
 /* Kernel launches issued by this context since creation (all entry points). */
 int rs_ctx_launch_count(rs_ctx *ctx, int64_t *count);
+/* Bytes the library has copied host -> device and device -> host since the process started
+ * (all contexts). No counterpart in the crate. */
+int rs_copy_counters(uint64_t *h2d_bytes, uint64_t *d2h_bytes);
 
 /* Measured FP32 (non-tensor) FMA throughput of the context's device in TFLOP/s: the
  * denominator of the pair kernel's roofline. No reference counterpart (a measurement aid). */
@@ -225,7 +228,8 @@ typedef struct rs_solver_options {
   double eps_rel;        /* eps_rel of eps = eps_rel tr W / tr M (1e-10) */
   double eps_multi_rel;  /* eps when a global barycenter spans several components (1e-4) */
   int barycenter_per_component; /* 1: one barycenter group per component, 0: global (0) */
-  int vcycles;           /* multigrid V-cycles per L' solve (1) */
+  int vcycles;           /* conjugate-gradient steps, each preconditioned by one multigrid
+                            V-cycle, per L' solve (3) */
   int preconditioner;    /* 1: the fractional preconditioner, 0: none */
   int clamp_laplacian;   /* 1: edges with negative cotan weight dropped from the
                             preconditioner's Laplacian (an M-matrix for multigrid), 0: cotan */
@@ -243,6 +247,9 @@ int rs_solver_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces,
 void rs_solver_free(rs_solver *s);
 /* n_dofs = 3V, n_constraints = k_Q (3 per barycenter group). Vectors are [x (3V); l (k_Q)]. */
 int rs_solver_dims(rs_solver *s, int64_t *n_dofs, int64_t *n_constraints);
+/* Host seconds of rs_solver_build by phase: [metric tree and upload, vertex fractional tree,
+ * Laplacian block, multigrid set-up, multigrid upload, total]. No counterpart in the crate. */
+int rs_solver_build_times(rs_solver *s, double *out6);
 /* LinearOperator::apply_batch (gmres.rs:32-52): ys = A' xs for nb stacked vectors. */
 int rs_solver_apply(rs_solver *s, int nb, const double *xs_host, double *ys_host);
 int rs_solver_apply_device(rs_solver *s, int nb, const double *xs_dev, double *ys_dev);

@@ -58,6 +58,10 @@ def workload(name: str):
         P, F = gen.config_c3()
         return P, F, 0.25, ("torus 320x320 R=1 r=0.3 (102,400 vertices, 204,800 faces), N(0,0.01) "
                             "noise per coordinate, seed 3 (as specified; crumpled)")
+    if name == "matvec":
+        P, F = gen.config_c3s()
+        return P, F, 0.25, ("torus 320x320 R=1 r=0.3 (102,400 vertices, 204,800 faces), N(0,0.001) "
+                            "noise per coordinate, seed 3")
     if name == "c2":
         P, F = gen.config_c2()
         return P, F, 0.25, ("icosphere level 6 (40,962 vertices, 81,920 faces), 8 spherical-"
@@ -133,6 +137,13 @@ def traffic_from_profiles(kernel: str, workload_name: str):
             except ValueError:
                 return None
     return None
+
+
+def _scaled_traffic(kernel, workload_name, units, units_profiled):
+    """DRAM bytes per launch of a committed ncu summary, scaled by the units one launch
+    processes here over the units of the profiled launch (the kernel's traffic grows with them)."""
+    t = traffic_from_profiles(kernel, workload_name)
+    return None if t is None else t * units / units_profiled
 
 
 def cpu_baseline(P, F, theta, sizes, threads=None):
@@ -365,7 +376,7 @@ def bench_flow(args, rank, world, local):
                      "peak_source": "measured FP32 FMA throughput (rs_fp32_peak); "
                                     "MEASURED_PEAKS.json has no FP32 figure",
                      "work": f"{NEAR_FLOP_PER_ENTRY} FLOP x {mst['near_entries']} near entries per launch",
-                     "traffic": traffic_from_profiles("hm_rows", args.workload),
+                     "traffic": _scaled_traffic("hm_rows", "matvec", mst["near_entries"], 103578780),
                      "kernel_ms": mprof},
         "pair_kernel": {"gflops": FLOP_PER_INTERACTION * n_int / (t_pair * 1e-3) / 1e9 if t_pair else None,
                         "interactions": n_int, "ms": t_pair,
@@ -388,6 +399,108 @@ def bench_flow(args, rank, world, local):
     return 0
 
 
+MATVEC_METRIC = "Hs metric products/s @204,800 faces (hierarchical, chi 0.5, one vector)"
+
+
+def bench_matvec(args, rank, world, local):
+    """The hierarchical metric product alone (rs_metric_apply_device, one vector per step)."""
+    import torch
+
+    import rs_gb300 as R
+
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    warmup = max(3, args.warmup)
+    P, F, theta, desc = workload(args.workload)
+    ctx = R.Context(local)
+    dev = torch.device(f"cuda:{local}")
+    stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
+    m = R.FaceMetricTree(F, P, R.Exponents(), R.ClusterTreeOptions(chi=0.5), ctx)
+    st = m.stats()
+    with torch.cuda.stream(stream):
+        x = torch.from_numpy(np.random.default_rng(0).standard_normal(3 * len(P))).to(dev)
+        y = torch.zeros_like(x)
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+        for _ in range(warmup):
+            m.apply_device(x.data_ptr(), y.data_ptr(), 1)
+        stream.synchronize()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+        l0 = ctx.launch_count()
+        with Clocks(local) as clk:
+            for a, b in evs:
+                flush.fill_(1)
+                a.record(stream)
+                m.apply_device(x.data_ptr(), y.data_ptr(), 1)
+                b.record(stream)
+            stream.synchronize()
+        launches = ctx.launch_count() - l0
+    t_total = sum(a.elapsed_time(b) for a, b in evs) / 1e3
+    if world > 1:
+        tt = torch.tensor([t_total], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_total = float(tt.item())
+    value = world * args.steps / t_total
+    xh = np.random.default_rng(1).standard_normal(3 * len(P))
+    m.apply(xh)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        yh = m.apply(xh)
+    t_e2e = time.perf_counter() - t0
+    prof = m.profile(1, 5)
+    peak = ctx.fp32_peak_tflops()
+    t_rows = prof.get("metric_rows")
+    achieved = NEAR_FLOP_PER_ENTRY * st["near_entries"] / (t_rows * 1e-3) / 1e12 if t_rows else None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+        if rank != 0:
+            dist.destroy_process_group()
+            return 0
+    line = {
+        "metric": MATVEC_METRIC, "value": value, "unit": "products/s", "n_gpus": world, "steps": args.steps,
+        "warmup": warmup, "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded mesh generator of the configuration)",
+        "config": {"workload": f"matvec: {desc}", "chi": 0.5, "alpha": 6, "beta": 12, "leaf_size": 8,
+                   "leaf_pairs": 64, **st, "l2": "flushed (256 MiB) between steps",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": world * args.steps / t_e2e, "unit": "products/s",
+                "h2d_bytes_per_step": int(xh.nbytes), "d2h_bytes_per_step": int(xh.nbytes)},
+        "roofline": {"bound": "fp32", "kernel": "hm_rows (metric near field, one vector)", "achieved": achieved,
+                     "peak": peak, "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
+                     "peak_source": "measured FP32 FMA throughput (rs_fp32_peak)",
+                     "work": f"{NEAR_FLOP_PER_ENTRY} FLOP x {st['near_entries']} near entries per launch",
+                     "traffic": traffic_from_profiles("hm_rows", "matvec"), "kernel_ms": prof},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import rs_oracle as O
+
+        O.build()
+        n = os.cpu_count() or 1
+        O.set_threads(n)
+        om = O.FaceMetricTree(P, F, chi=0.5)
+        t0 = time.perf_counter()
+        om.apply(xh)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": 1.0 / dt, "unit": "products/s", "cores": n, "kind": "port",
+                                "sample": f"one product ({dt:.2f} s) by the FP64 C++ restatement, {n} threads"}
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 METRIC = "pair GFLOP/s, Barnes-Hut energy+differential (61 FLOP/interaction)"
 
 
@@ -397,7 +510,7 @@ def main() -> int:
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="flow", choices=["flow", "flow-spec", "c2", "c3"])
+    ap.add_argument("--workload", default="flow", choices=["flow", "flow-spec", "matvec", "c2", "c3"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.steps is None:
@@ -411,6 +524,8 @@ def main() -> int:
         return run_reference(args, rank)
     if args.workload.startswith("flow"):
         return bench_flow(args, rank, world, local)
+    if args.workload == "matvec":
+        return bench_matvec(args, rank, world, local)
 
     import torch
 

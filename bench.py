@@ -354,7 +354,7 @@ def bench_flow(args, rank, world, local):
         "config": {"workload": f"{args.workload}: {desc}", "theta": theta, "chi": 0.5, "alpha": 6, "beta": 12,
                    "leaf_size": 8, "constraints": "barycenter + area + volume (3 right-hand sides per step)",
                    "gmres": "restart 30, true relative residual 1e-6, FP64 Arnoldi (CGS2)",
-                   "preconditioner": "fractional (plain), multigrid L' with 3 V-cycles",
+                   "preconditioner": "fractional (plain); L' by 6 multigrid-preconditioned CG steps",
                    "l2": "not flushed: every step moves several GB (trees, lists, solver rebuilt)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "steps_report": {

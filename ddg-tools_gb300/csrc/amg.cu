@@ -8,54 +8,66 @@ namespace {
 
 inline unsigned nblk(size_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
 
-// y = A x (accumulate: y += A x)
-template <bool ACC>
+// y = A x (accumulate: y += A x); C columns per row, a compile-time width so that the
+// accumulators stay in registers.
+template <bool ACC, int C>
 __global__ void spmv_c_kernel(int n, const int *__restrict__ ap, const int *__restrict__ ac,
-                              const double *__restrict__ av, const double *__restrict__ x, int C,
+                              const double *__restrict__ av, const double *__restrict__ x,
                               double *__restrict__ y) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double acc[12];
+  double acc[C];
+#pragma unroll
   for (int c = 0; c < C; ++c) acc[c] = ACC ? y[(size_t)i * C + c] : 0.0;
   for (int p = ap[i]; p < ap[i + 1]; ++p) {
     double a = av[p];
     const double *xr = x + (size_t)ac[p] * C;
+#pragma unroll
     for (int c = 0; c < C; ++c) acc[c] = fma(a, xr[c], acc[c]);
   }
+#pragma unroll
   for (int c = 0; c < C; ++c) y[(size_t)i * C + c] = acc[c];
 }
 
-// out = x + dinv (b - A x); x = null means x = 0 (out = dinv b). Also r = b - A x if r != null.
+// out = x + dinv (b - A x); x = null means x = 0 (out = dinv b).
+template <int C>
 __global__ void jacobi_kernel(int n, const int *__restrict__ ap, const int *__restrict__ ac,
                               const double *__restrict__ av, const double *__restrict__ dinv,
-                              const double *__restrict__ b, const double *__restrict__ x, int C,
+                              const double *__restrict__ b, const double *__restrict__ x,
                               double *__restrict__ out) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double acc[12];
+  double acc[C];
+#pragma unroll
   for (int c = 0; c < C; ++c) acc[c] = b[(size_t)i * C + c];
   if (x)
     for (int p = ap[i]; p < ap[i + 1]; ++p) {
       double a = av[p];
       const double *xr = x + (size_t)ac[p] * C;
+#pragma unroll
       for (int c = 0; c < C; ++c) acc[c] = fma(-a, xr[c], acc[c]);
     }
   double d = dinv[i];
+#pragma unroll
   for (int c = 0; c < C; ++c) out[(size_t)i * C + c] = (x ? x[(size_t)i * C + c] : 0.0) + d * acc[c];
 }
 
+template <int C>
 __global__ void residual_kernel(int n, const int *__restrict__ ap, const int *__restrict__ ac,
                                 const double *__restrict__ av, const double *__restrict__ b,
-                                const double *__restrict__ x, int C, double *__restrict__ r) {
+                                const double *__restrict__ x, double *__restrict__ r) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double acc[12];
+  double acc[C];
+#pragma unroll
   for (int c = 0; c < C; ++c) acc[c] = b[(size_t)i * C + c];
   for (int p = ap[i]; p < ap[i + 1]; ++p) {
     double a = av[p];
     const double *xr = x + (size_t)ac[p] * C;
+#pragma unroll
     for (int c = 0; c < C; ++c) acc[c] = fma(-a, xr[c], acc[c]);
   }
+#pragma unroll
   for (int c = 0; c < C; ++c) r[(size_t)i * C + c] = acc[c];
 }
 
@@ -137,6 +149,9 @@ void up(DevBuf<T> &d, const std::vector<T> &v, cudaStream_t s) {
 }  // namespace
 
 void AmgDevice::upload(const AmgHost &h, cudaStream_t s) {
+  for (auto &gr : graphs)
+    if (gr.exec) cudaGraphExecDestroy(gr.exec);
+  graphs.clear();
   size_t nl = h.A.size();
   L.clear();
   L.resize(nl);
@@ -155,23 +170,25 @@ void AmgDevice::upload(const AmgHost &h, cudaStream_t s) {
 }
 
 void AmgDevice::reserve(int C_) {
-  if (C_ <= C) return;
   if (C_ > 12) fail(RS_INTERNAL, "Internal", "preconditioner", "at most 12 multigrid columns");
-  C = C_;
+  if (C >= 12) return;
+  // buffers for the widest batch at once: graphs captured for a width keep their pointers
+  C = 12;
   for (auto &v : L) {
     size_t m = (size_t)v.n * C;
     v.x.alloc(m), v.b.alloc(m), v.r.alloc(m), v.t.alloc(m);
   }
 }
 
-void AmgDevice::spmv0(rs_ctx *ctx, const double *x, double *y, int C_) {
+template <int CC>
+void AmgDevice::spmv0_t(rs_ctx *ctx, const double *x, double *y) {
   Level &v = L[0];
-  spmv_c_kernel<false><<<nblk(v.n, 128), 128, 0, ctx->stream>>>(v.n, v.ap.p, v.ac.p, v.av.p, x, C_, y);
+  spmv_c_kernel<false, CC><<<nblk(v.n, 128), 128, 0, ctx->stream>>>(v.n, v.ap.p, v.ac.p, v.av.p, x, y);
   RSG_LAUNCHED(ctx, "amg_spmv");
 }
 
-void AmgDevice::vcycle(rs_ctx *ctx, const double *b, double *x, int C_) {
-  reserve(C_);
+template <int CC>
+void AmgDevice::vcycle_t(rs_ctx *ctx, const double *b, double *x) {
   cudaStream_t s = ctx->stream;
   const int nl = (int)L.size();
   // down: level l solves A_l x_l = b_l (b_0 = b), x_l starts at 0
@@ -181,21 +198,21 @@ void AmgDevice::vcycle(rs_ctx *ctx, const double *b, double *x, int C_) {
     double *xl = (l == 0) ? x : v.x.p;
     const unsigned g = nblk(v.n, 128);
     // pre-smoothing from x = 0
-    jacobi_kernel<<<g, 128, 0, s>>>(v.n, v.ap.p, v.ac.p, v.av.p, v.dinv.p, bl, nullptr, C_, v.t.p);
+    jacobi_kernel<CC><<<g, 128, 0, s>>>(v.n, v.ap.p, v.ac.p, v.av.p, v.dinv.p, bl, nullptr, v.t.p);
     RSG_LAUNCHED(ctx, "amg_jacobi");
     const double *cur = v.t.p;
     double *nxt = xl;
     for (int k = 1; k < sweeps; ++k) {
-      jacobi_kernel<<<g, 128, 0, s>>>(v.n, v.ap.p, v.ac.p, v.av.p, v.dinv.p, bl, cur, C_, nxt);
+      jacobi_kernel<CC><<<g, 128, 0, s>>>(v.n, v.ap.p, v.ac.p, v.av.p, v.dinv.p, bl, cur, nxt);
       RSG_LAUNCHED(ctx, "amg_jacobi");
       std::swap(cur, *(const double **)&nxt);
     }
     if (cur != xl)
-      RSG_CUDA("preconditioner", cudaMemcpyAsync(xl, cur, (size_t)v.n * C_ * sizeof(double), cudaMemcpyDeviceToDevice, s));
-    residual_kernel<<<g, 128, 0, s>>>(v.n, v.ap.p, v.ac.p, v.av.p, bl, xl, C_, v.r.p);
+      RSG_CUDA("preconditioner", cudaMemcpyAsync(xl, cur, (size_t)v.n * CC * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    residual_kernel<CC><<<g, 128, 0, s>>>(v.n, v.ap.p, v.ac.p, v.av.p, bl, xl, v.r.p);
     RSG_LAUNCHED(ctx, "amg_residual");
     Level &w = L[l + 1];
-    spmv_c_kernel<false><<<nblk(w.n, 128), 128, 0, s>>>(w.n, v.rp.p, v.rc.p, v.rv.p, v.r.p, C_, w.b.p);
+    spmv_c_kernel<false, CC><<<nblk(w.n, 128), 128, 0, s>>>(w.n, v.rp.p, v.rc.p, v.rv.p, v.r.p, w.b.p);
     RSG_LAUNCHED(ctx, "amg_restrict");
     bl = w.b.p;
   }
@@ -203,33 +220,52 @@ void AmgDevice::vcycle(rs_ctx *ctx, const double *b, double *x, int C_) {
   {
     Level &v = L[nl - 1];
     double *xl = (nl == 1) ? x : v.x.p;
-    dense_solve_kernel<<<nblk((size_t)v.n * C_, 128), 128, 0, s>>>(v.n, cinv.p, bl, C_, xl);
+    dense_solve_kernel<<<nblk((size_t)v.n * CC, 128), 128, 0, s>>>(v.n, cinv.p, bl, CC, xl);
     RSG_LAUNCHED(ctx, "amg_coarse");
   }
   // up: x_l += P x_{l+1}, post-smoothing
   for (int l = nl - 2; l >= 0; --l) {
     Level &v = L[l];
     double *xl = (l == 0) ? x : v.x.p;
-    const double *xc = (l + 1 == nl - 1 && nl == 1) ? x : L[l + 1].x.p;
-    spmv_c_kernel<true><<<nblk(v.n, 128), 128, 0, s>>>(v.n, v.pp.p, v.pc.p, v.pv.p, xc, C_, xl);
+    const double *xc = L[l + 1].x.p;
+    spmv_c_kernel<true, CC><<<nblk(v.n, 128), 128, 0, s>>>(v.n, v.pp.p, v.pc.p, v.pv.p, xc, xl);
     RSG_LAUNCHED(ctx, "amg_prolong");
     const double *blv = (l == 0) ? b : v.b.p;
     const unsigned g = nblk(v.n, 128);
     for (int k = 0; k < sweeps; ++k) {
-      jacobi_kernel<<<g, 128, 0, s>>>(v.n, v.ap.p, v.ac.p, v.av.p, v.dinv.p, blv, xl, C_, v.t.p);
+      jacobi_kernel<CC><<<g, 128, 0, s>>>(v.n, v.ap.p, v.ac.p, v.av.p, v.dinv.p, blv, xl, v.t.p);
       RSG_LAUNCHED(ctx, "amg_jacobi");
-      RSG_CUDA("preconditioner", cudaMemcpyAsync(xl, v.t.p, (size_t)v.n * C_ * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      RSG_CUDA("preconditioner", cudaMemcpyAsync(xl, v.t.p, (size_t)v.n * CC * sizeof(double), cudaMemcpyDeviceToDevice, s));
     }
   }
 }
 
-void AmgDevice::pcg(rs_ctx *ctx, const double *b, double *x, int C_, int iters) {
+#define RSG_AMG_WIDTH(CALL)                                                              \
+  switch (C_) {                                                                          \
+    case 3: CALL(3); break;                                                              \
+    case 6: CALL(6); break;                                                              \
+    case 9: CALL(9); break;                                                              \
+    case 12: CALL(12); break;                                                            \
+    default: fail(RS_INTERNAL, "Internal", "preconditioner", "multigrid width 3, 6, 9 or 12"); \
+  }
+
+void AmgDevice::spmv0(rs_ctx *ctx, const double *x, double *y, int C_) {
+#define RSG_CALL(W) spmv0_t<W>(ctx, x, y)
+  RSG_AMG_WIDTH(RSG_CALL)
+#undef RSG_CALL
+}
+
+void AmgDevice::vcycle(rs_ctx *ctx, const double *b, double *x, int C_) {
   reserve(C_);
+#define RSG_CALL(W) vcycle_t<W>(ctx, b, x)
+  RSG_AMG_WIDTH(RSG_CALL)
+#undef RSG_CALL
+}
+
+void AmgDevice::pcg_body(rs_ctx *ctx, const double *b, double *x, int C_, int iters) {
   cudaStream_t s = ctx->stream;
   const int n = L[0].n;
   const size_t m = (size_t)n * C_;
-  if (cg_r.n < m) cg_r.alloc(m), cg_z.alloc(m), cg_p.alloc(m), cg_q.alloc(m);
-  if (cg_part.n < (size_t)kDotBlocks * 12) cg_part.alloc((size_t)kDotBlocks * 12), cg_s.alloc(36);
   const unsigned g = nblk(m, 256);
   auto dots = [&](const double *a, const double *w, int mode) {
     col_dots_partial<<<kDotBlocks, 128, 0, s>>>(n, C_, a, w, cg_part.p);
@@ -254,6 +290,57 @@ void AmgDevice::pcg(rs_ctx *ctx, const double *b, double *x, int C_, int iters) 
     cg_direction<<<g, 256, 0, s>>>(n, C_, cg_s.p, cg_z.p, cg_p.p);
     RSG_LAUNCHED(ctx, "cg_direction");
   }
+}
+
+// The conjugate-gradient solve is a few hundred small launches (levels x sweeps x steps) with
+// all scalars on the device, so it is captured once per (b, x, width, steps) into a CUDA graph
+// and replayed: the buffers it touches are allocated for the widest batch before the first
+// capture and never move.
+void AmgDevice::pcg(rs_ctx *ctx, const double *b, double *x, int C_, int iters) {
+  reserve(C_);
+  const size_t m = (size_t)L[0].n * 12;
+  if (cg_r.n < m) cg_r.alloc(m), cg_z.alloc(m), cg_p.alloc(m), cg_q.alloc(m);
+  if (cg_part.n < (size_t)kDotBlocks * 12) cg_part.alloc((size_t)kDotBlocks * 12), cg_s.alloc(36);
+  cudaStream_t s = ctx->stream;
+  for (auto &gr : graphs)
+    if (gr.b == b && gr.x == x && gr.C == C_ && gr.iters == iters) {
+      RSG_CUDA("preconditioner", cudaGraphLaunch(gr.exec, s));
+      ctx->launches += gr.launches;
+      return;
+    }
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  RSG_CUDA("preconditioner", cudaStreamIsCapturing(s, &cs));
+  if (cs != cudaStreamCaptureStatusNone) {  // the caller is capturing already: record inline
+    pcg_body(ctx, b, x, C_, iters);
+    return;
+  }
+  Graph gr;
+  gr.b = b, gr.x = x, gr.C = C_, gr.iters = iters;
+  const int64_t l0 = ctx->launches;
+  RSG_CUDA("preconditioner", cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  try {
+    pcg_body(ctx, b, x, C_, iters);
+  } catch (...) {
+    cudaGraph_t dummy = nullptr;
+    cudaStreamEndCapture(s, &dummy);
+    if (dummy) cudaGraphDestroy(dummy);
+    throw;
+  }
+  cudaGraph_t graph = nullptr;
+  RSG_CUDA("preconditioner", cudaStreamEndCapture(s, &graph));
+  gr.launches = ctx->launches - l0;
+  ctx->launches = l0;
+  cudaError_t e = cudaGraphInstantiate(&gr.exec, graph, 0);
+  cudaGraphDestroy(graph);
+  RSG_CUDA("preconditioner", e);
+  graphs.push_back(gr);
+  RSG_CUDA("preconditioner", cudaGraphLaunch(gr.exec, s));
+  ctx->launches += gr.launches;
+}
+
+AmgDevice::~AmgDevice() {
+  for (auto &gr : graphs)
+    if (gr.exec) cudaGraphExecDestroy(gr.exec);
 }
 
 }  // namespace rsg

@@ -50,6 +50,25 @@ struct AmgDevice {
   // nonlinear map of b, which flexible GMRES (the stored preconditioned vectors) allows.
   void pcg(rs_ctx *ctx, const double *b, double *x, int C_, int iters);
   DevBuf<double> cg_r, cg_z, cg_p, cg_q, cg_part, cg_s;  // n_0 x C each; partial sums; scalars
+  struct Graph {
+    const double *b = nullptr;
+    double *x = nullptr;
+    int C = 0, iters = 0;
+    int64_t launches = 0;
+    cudaGraphExec_t exec = nullptr;
+  };
+  std::vector<Graph> graphs;  // captured conjugate-gradient solves
+  AmgDevice() = default;
+  AmgDevice(const AmgDevice &) = delete;
+  AmgDevice &operator=(const AmgDevice &) = delete;
+  ~AmgDevice();
+
+ private:
+  template <int CC>
+  void vcycle_t(rs_ctx *ctx, const double *b, double *x);
+  template <int CC>
+  void spmv0_t(rs_ctx *ctx, const double *x, double *y);
+  void pcg_body(rs_ctx *ctx, const double *b, double *x, int C_, int iters);
 };
 
 }  // namespace rsg

@@ -253,7 +253,17 @@ int rs_flow_step(rs_flow *F, double *report) {
     // 3. one batch: Z columns and y
     t = clk::now();
     double srep[20] = {0};
-    check(rs_solver_solve_many_device(sv.p, nb, rhs.p, sol.p, srep), "flow (solve)");
+    int code = rs_solver_solve_many_device(sv.p, nb, rhs.p, sol.p, srep);
+    if (code == RS_SOLVER_DIVERGED) {
+      // the crate's recovery (RobustHierarchical::escalate, direction.rs:269-379): repeat the
+      // solves with restart 60 and at least four times the iteration cap (800 or more)
+      const rs_solver_options &so = F->o.solver;
+      check(rs_solver_set_gmres(sv.p, 60, std::max(4 * so.max_iterations, 800), so.tolerance),
+            "flow (solve)");
+      rep[18] += 1.0;
+      code = rs_solver_solve_many_device(sv.p, nb, rhs.p, sol.p, srep);
+    }
+    check(code, "flow (solve)");
     rep[12] = since(t);
     std::vector<double> hs((size_t)nb * n);
     sol.download(hs.data(), hs.size(), s);

@@ -53,7 +53,7 @@ struct HDev {
   const float4 *xl;          // per BVH position: position lo (xyz): X = hi + lo to ~48 bits
   const float4 *nrm;         // per BVH position: normal (faces only)
   const double2 *node_farA;  // per node: its far sums of psi = a (k_0, k_1), the far part of H~a
-  const uint2 *cols;         // near column ranges [x, y) of every leaf's chain, leaf by leaf
+  const uint32_t *colidx;    // near columns of every leaf's chain, flattened, leaf by leaf
   const uint4 *items;        // per work item: leaf ordinal, column-range begin / end, -
   const uint32_t *item_off;  // per leaf: its work items [item_off[k], item_off[k + 1])
   double *up;                // per node: C channel sums of a m (FP64)
@@ -189,30 +189,36 @@ __global__ void hm_far_kernel(HDev d) {
     if (lane == (c & 31)) o[c] = acc[c];
 }
 
-// Near sums of one work item (a slice of a leaf's chain near-column ranges) in difference
-// form: sum_q w_pq (m_p - m_q) for channels [c0, c0 + CC) of the row's element p. One warp
-// per item; lane = r + 8 j: r the row (element) of the leaf, j one of four column groups
-// taking every fourth column. The kernel values of a column are evaluated once per row and
-// applied to the CC channels. m_p - m_q is formed from the float pairs (exact for nearby
-// values), each product w (m_p - m_q) is split exactly, the terms are summed with Kahan
-// compensation and their low parts apart, then combined over the groups as float pairs: for a smooth input the terms are first-order quantities that cancel to a
-// second-order result, and the output stage (M^T, a discrete divergence) cancels once more,
-// so plain FP32 sums of H~a m and H~(a m) would lose about four digits.
+// Near sums of one work item (a slice of the flattened near columns of a leaf's root-to-leaf
+// chain) in difference form: sum_q w_pq (m_p - m_q) for channels [c0, c0 + CC) of the row's
+// element p. One warp per item; the leaf's ns rows (3 to 8) each take G = 32 / ns lanes
+// (lane = r G + j), lane j of a row taking every G-th column, so that small leaves keep the
+// warp busy. The kernel values of a column are evaluated once per row and applied to the CC
+// channels. m_p - m_q is formed from the float pairs and split exactly, each product
+// w (m_p - m_q) is split exactly too, and the terms are summed as float pairs: the high parts
+// by error-free additions (two_sum), whose errors gather with the low parts in a second
+// float. (Kahan summation would leave an error of eps times each lane's partial sum, a
+// first-order quantity.) The G partial sums of a row are then added in lane order as float
+// pairs (through shared memory). For a smooth input the terms are first-order quantities
+// that cancel to a second-order result, and the output stage (M^T, a discrete divergence)
+// cancels once more, so plain FP32 sums of H~a m and H~(a m) would lose about four digits.
 template <int KIND, int CC>
 __global__ void __launch_bounds__(128) hm_rows_kernel(HDev d, int c0) {
-  const int lane = threadIdx.x & 31;
-  const int r = lane & 7, j = lane >> 3;
+  __shared__ float2 red[4][32][CC];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (w >= d.n_items) return;
-  const uint4 it = d.items[w];
+  const uint4 it = d.items[w];  // leaf ordinal, flat column range [y, z)
   const uint32_t leaf = d.leaves[it.x];
   const uint32_t s0 = d.start[leaf], ns = d.end[leaf] - s0;
+  const int G = 32 / (int)ns;
+  const int r = lane / G, j = lane - r * G;
   const bool act = (uint32_t)r < ns;
   const uint32_t p = s0 + (act ? r : 0);
   const float4 ph = d.xh[p], pl = d.xl[p];
   const float4 np = KIND == FACE ? d.nrm[p] : make_float4(0.f, 0.f, 0.f, 0.f);
   const int C = d.C;
-  float mh[CC], ml[CC], ks[CC], kc[CC], kl[CC];
+  float mh[CC], ml[CC], ks[CC], kc[CC];
   {
     const float4 *mp = reinterpret_cast<const float4 *>(d.m + (size_t)p * C + c0);
 #pragma unroll
@@ -222,61 +228,54 @@ __global__ void __launch_bounds__(128) hm_rows_kernel(HDev d, int c0) {
     }
   }
 #pragma unroll
-  for (int c = 0; c < CC; ++c) ks[c] = 0.f, kc[c] = 0.f, kl[c] = 0.f;
+  for (int c = 0; c < CC; ++c) ks[c] = 0.f, kc[c] = 0.f;
   if (act)
-    for (uint32_t ri = it.y; ri < it.z; ++ri) {
-      const uint2 cr = d.cols[ri];
-      for (uint32_t q = cr.x + j; q < cr.y; q += 4) {
-        if (q == p) continue;
-        const float4 qh = d.xh[q], ql = d.xl[q];
-        const float d0 = (ph.x - qh.x) + (pl.x - ql.x);
-        const float d1 = (ph.y - qh.y) + (pl.y - ql.y);
-        const float d2 = (ph.z - qh.z) + (pl.z - ql.z);
-        float k0, k1;
-        near_kernel<KIND>(d, d0, d1, d2, np, KIND == FACE ? d.nrm[q] : np, k0, k1);
-        const float w0 = k0 * qh.w, w1 = k1 * qh.w;
-        const float4 *mq = reinterpret_cast<const float4 *>(d.m + (size_t)q * C + c0);
+    for (uint32_t idx = it.y + j; idx < it.z; idx += G) {
+      const uint32_t q = d.colidx[idx];
+      if (q == p) continue;
+      const float4 qh = d.xh[q], ql = d.xl[q];
+      const float d0 = (ph.x - qh.x) + (pl.x - ql.x);
+      const float d1 = (ph.y - qh.y) + (pl.y - ql.y);
+      const float d2 = (ph.z - qh.z) + (pl.z - ql.z);
+      float k0, k1;
+      near_kernel<KIND>(d, d0, d1, d2, np, KIND == FACE ? d.nrm[q] : np, k0, k1);
+      const float w0 = k0 * qh.w, w1 = k1 * qh.w;
+      const float4 *mq = reinterpret_cast<const float4 *>(d.m + (size_t)q * C + c0);
 #pragma unroll
-        for (int c2 = 0; c2 < CC / 2; ++c2) {
-          const float4 v = mq[c2];
+      for (int c2 = 0; c2 < CC / 2; ++c2) {
+        const float4 v = mq[c2];
 #pragma unroll
-          for (int e = 0; e < 2; ++e) {
-            const int c = 2 * c2 + e;
-            const float qhv = e ? v.z : v.x, qlv = e ? v.w : v.y;
-            const float wk = (KIND == FACE && c >= 9) ? w1 : w0;
-            // w (m_p - m_q) = w dh + w dl with mh_p - mh_q = dh + de split exactly (values of
-            // opposite sign near a zero of the field do not subtract exactly) and
-            // dl = ml_p - ml_q + de; the product w dh is split exactly (pr + pe) as well, so
-            // that no rounding that depends on the input reaches the sum above eps^2
-            float dh, de;
-            two_sum(mh[c], -qhv, dh, de);
-            const float dl = (ml[c] - qlv) + de;
-            const float pr = wk * dh;
-            const float pe = fmaf(wk, dh, -pr);
-            kl[c] = fmaf(wk, dl, kl[c] + pe);
-            const float y = pr - kc[c];
-            const float tt = ks[c] + y;
-            kc[c] = (tt - ks[c]) - y;
-            ks[c] = tt;
-          }
+        for (int e = 0; e < 2; ++e) {
+          const int c = 2 * c2 + e;
+          const float qhv = e ? v.z : v.x, qlv = e ? v.w : v.y;
+          const float wk = (KIND == FACE && c >= 9) ? w1 : w0;
+          // w (m_p - m_q) = pr + pe + w dl exactly up to eps^2 terms: mh_p - mh_q = dh + de
+          // (two_sum), dl = ml_p - ml_q + de, w dh = pr + pe (FMA); the low parts enter the
+          // Kahan compensation, so no rounding that depends on the input reaches the sum
+          float dh, de;
+          two_sum(mh[c], -qhv, dh, de);
+          const float dl = (ml[c] - qlv) + de;
+          const float pr = wk * dh;
+          const float lo = fmaf(wk, dl, fmaf(wk, dh, -pr));
+          float sn, se;
+          two_sum(ks[c], pr, sn, se);
+          ks[c] = sn;
+          kc[c] += se + lo;
         }
       }
     }
-  // combine the four column groups as float pairs (h, l) = (s, -c)
+  // the G lanes of a row: partial sums (s, t) added in lane order as float pairs
 #pragma unroll
-  for (int c = 0; c < CC; ++c) {
-    float h = ks[c], l = kl[c] - kc[c];
-#pragma unroll
-    for (int m = 8; m <= 16; m <<= 1) {
-      const float oh = __shfl_xor_sync(0xffffffffu, h, m), ol = __shfl_xor_sync(0xffffffffu, l, m);
-      pair_add(h, l, oh, ol);
-    }
-    ks[c] = h, kc[c] = l;
-  }
-  if (j != 0 || !act) return;
+  for (int c = 0; c < CC; ++c) red[wib][lane][c] = make_float2(ks[c], kc[c]);
+  __syncwarp();
+  if (!act || j != 0) return;
   float2 *o = d.part + ((size_t)w * 8 + r) * C + c0;
 #pragma unroll
-  for (int c = 0; c < CC; ++c) o[c] = make_float2(ks[c], kc[c]);
+  for (int c = 0; c < CC; ++c) {
+    float h = red[wib][lane][c].x, l = red[wib][lane][c].y;
+    for (int g = 1; g < G; ++g) pair_add(h, l, red[wib][lane + g][c].x, red[wib][lane + g][c].y);
+    o[c] = make_float2(h, l);
+  }
 }
 
 // Per leaf (thread per row): z = near + (m_p H~a_far - H~(a m)_far), the near sums of the
@@ -469,7 +468,7 @@ struct HMat {
   double neg_s = 0;
   DevBuf<uint32_t> start, end, right, parent, leaves, chain_off, chain, item_off;
   DevBuf<uint32_t> far_ptr, far_col, count;
-  DevBuf<uint2> cols;
+  DevBuf<uint32_t> colidx;
   DevBuf<uint4> items;
   DevBuf<double2> far_coef, node_farA;
   DevBuf<float4> xh, xl, nrm;
@@ -484,7 +483,7 @@ struct HMat {
     d.chain_off = chain_off.p, d.chain = chain.p;
     d.far_ptr = far_ptr.p, d.far_col = far_col.p, d.far_coef = far_coef.p;
     d.xh = xh.p, d.xl = xl.p, d.nrm = nrm.p, d.node_farA = node_farA.p;
-    d.cols = cols.p, d.items = items.p, d.item_off = item_off.p;
+    d.colidx = colidx.p, d.items = items.p, d.item_off = item_off.p;
     d.up = up.p, d.farx = farx.p, d.part = part.p, d.count = count.p;
     d.m = m.p, d.z = z.p;
     d.n_nodes = (int)tree.n_nodes(), d.n_leaves = (int)tree.leaves.size(), d.n_el = (int)n_el;
@@ -540,7 +539,7 @@ struct HMat {
     const Tree &T = tree;
     size_t nn = T.n_nodes(), nl = T.leaves.size();
     std::vector<uint32_t> parent_h(nn, 0), coff(nl + 1, 0), chain_h, ioff(nl + 1, 0);
-    std::vector<uint2> cols_h;
+    std::vector<uint32_t> cols_h;
     std::vector<uint4> items_h;
     const uint32_t kItemCols = 512;
     for (size_t i = 0; i < nn; ++i)
@@ -558,27 +557,27 @@ struct HMat {
       }
       std::reverse(chain_h.begin() + b, chain_h.end());
       coff[k + 1] = (uint32_t)chain_h.size();
-      // the near column ranges of the chain, in chain and block order; items cut at ranges
-      uint32_t r0 = (uint32_t)cols_h.size(), cnt = 0;
+      // the near columns of the chain (chain order, block order, element order), flattened and
+      // cut into items of at most kItemCols columns
+      const uint32_t c_begin = (uint32_t)cols_h.size();
       for (size_t ci = b; ci < chain_h.size(); ++ci)
         for (uint32_t q = blocks.near_ptr[chain_h[ci]]; q < blocks.near_ptr[chain_h[ci] + 1]; ++q) {
           uint32_t c = blocks.near_col[q];
-          uint32_t w = T.end[c] - T.start[c];
-          if (cnt > 0 && cnt + w > kItemCols) {
-            items_h.push_back(make_uint4((uint32_t)k, r0, (uint32_t)cols_h.size(), 0));
-            r0 = (uint32_t)cols_h.size();
-            cnt = 0;
-          }
-          cols_h.push_back(make_uint2(T.start[c], T.end[c]));
-          cnt += w;
+          for (uint32_t e = T.start[c]; e < T.end[c]; ++e) cols_h.push_back(e);
         }
-      items_h.push_back(make_uint4((uint32_t)k, r0, (uint32_t)cols_h.size(), 0));
+      const uint32_t c_end = (uint32_t)cols_h.size();
+      uint32_t x = c_begin;
+      do {
+        uint32_t y = std::min(c_end, x + kItemCols);
+        items_h.push_back(make_uint4((uint32_t)k, x, y, 0));
+        x = y;
+      } while (x < c_end);
       ioff[k + 1] = (uint32_t)items_h.size();
     }
     n_items = items_h.size();
     up_vec(start, T.start, s), up_vec(end, T.end, s), up_vec(right, T.right, s);
     up_vec(parent, parent_h, s), up_vec(leaves, T.leaves, s), up_vec(chain_off, coff, s);
-    up_vec(chain, chain_h, s), up_vec(cols, cols_h, s), up_vec(items, items_h, s), up_vec(item_off, ioff, s);
+    up_vec(chain, chain_h, s), up_vec(colidx, cols_h, s), up_vec(items, items_h, s), up_vec(item_off, ioff, s);
     up_vec(far_ptr, blocks.far_ptr, s), up_vec(far_col, blocks.far_col, s);
     count.alloc(nn);
     RSG_CUDA("upload", cudaMemsetAsync(count.p, 0, nn * sizeof(uint32_t), s));

@@ -3,6 +3,7 @@
 // copy) and runs the Givens rotations and the stop test, as GmresRun::after_arnoldi does
 // (RS/src/solve/gmres.rs:454-513).
 #include "krylov.hpp"
+#include "profile.hpp"
 
 #include <chrono>
 #include <cmath>
@@ -235,6 +236,7 @@ void gmres_batch(rs_ctx *ctx, const Operator &A, const Operator *P, int nb, cons
       A.apply(na, xbuf.p, ybuf.p);
     }
     // classical Gram-Schmidt, twice; h = h1 + h2, then |w|
+    if (opt.prof) opt.prof->begin(s, "gmres_orthogonalize");
     for (int i = 0; i < na; ++i) {
       Rhs &Q = R[act[i]];
       Q.rep.operator_applications++;
@@ -250,6 +252,7 @@ void gmres_batch(rs_ctx *ctx, const Operator &A, const Operator *P, int nb, cons
       RSG_LAUNCHED(ctx, "axpy_many");
       norm_dev(Q, w, Q.h.p + 2 * (m + 2));
     }
+    if (opt.prof) opt.prof->end(s);
     std::vector<double> hh((size_t)na * (2 * (m + 2) + 1));
     for (int i = 0; i < na; ++i)
       RSG_CUDA("gmres", rsg::copy_async(hh.data() + (size_t)i * (2 * (m + 2) + 1), R[act[i]].h.p,

@@ -14,10 +14,12 @@ struct Operator {
   std::function<void(int nb, const double *x, double *y)> apply;
 };
 
+struct Profiler;
 struct GmresOptions {  // GmresOptions (RS/src/solve/gmres.rs:135-190)
   int restart = 30;
   double tolerance = 1e-6;
   int max_iterations = 200;
+  Profiler *prof = nullptr;  // phase timing (orthogonalization) when active
 };
 
 struct GmresReport {  // GmresReport (gmres.rs:200-225)

@@ -1,5 +1,6 @@
 // Per-kernel CUDA-event timing of the entry points (rs_*_profile): when active, every launch
-// is bracketed by two events on the launching stream; averages per kernel name.
+// (or phase; begin/end pairs may nest) is bracketed by two events on the launching stream;
+// averages per name.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -19,8 +20,7 @@ struct Profiler {
     cudaEvent_t a, b;
   };
   std::vector<Rec> recs;
-  std::string pending;
-  cudaEvent_t pending_ev = nullptr;
+  std::vector<std::pair<std::string, cudaEvent_t>> open;  // begun, not yet ended
 
   void start() {
     clear();
@@ -31,16 +31,15 @@ struct Profiler {
     cudaEvent_t e;
     RSG_CUDA("launch", cudaEventCreate(&e));
     RSG_CUDA("launch", cudaEventRecord(e, s));
-    pending = name;
-    pending_ev = e;
+    open.push_back({name, e});
   }
   void end(cudaStream_t s) {
-    if (!active || !pending_ev) return;
+    if (!active || open.empty()) return;
     cudaEvent_t e;
     RSG_CUDA("launch", cudaEventCreate(&e));
     RSG_CUDA("launch", cudaEventRecord(e, s));
-    recs.push_back({pending, pending_ev, e});
-    pending_ev = nullptr;
+    recs.push_back({open.back().first, open.back().second, e});
+    open.pop_back();
   }
   void stop(cudaStream_t s) {
     active = false;
@@ -70,8 +69,8 @@ struct Profiler {
   void clear() {
     for (auto &r : recs) cudaEventDestroy(r.a), cudaEventDestroy(r.b);
     recs.clear();
-    if (pending_ev) cudaEventDestroy(pending_ev);
-    pending_ev = nullptr;
+    for (auto &p : open) cudaEventDestroy(p.second);
+    open.clear();
   }
   ~Profiler() { clear(); }
 };

@@ -26,6 +26,7 @@
 #include "hmat.hpp"
 #include "host_tree.hpp"
 #include "krylov.hpp"
+#include "profile.hpp"
 
 namespace rsg {
 
@@ -167,6 +168,7 @@ struct rs_solver {
   bool use_prec = true;
   int vcycles = 1;
   double build_times[6] = {0, 0, 0, 0, 0, 0};
+  Profiler prof;
   GmresOptions gopt;
   FaceGeom geom;
   std::vector<double> vmass;
@@ -200,11 +202,13 @@ struct rs_solver {
   // A' x
   void apply_op(int nb, const double *x, double *y) {
     reserve(nb);
+    prof.begin(st(), "operator");
     metric_apply_strided(metric, w_hi, w_lo, nb, x, n, y, n);
     group_sums(x, n, nb, c.p, cy.p);
     size_t tot = (size_t)nb * n;
     cq_apply_kernel<<<nblk(tot, 256), 256, 0, st()>>>(x, y, n, nb, nv, group.p, c.p, G, cy.p);
     RSG_LAUNCHED(ctx, "cq_apply");
+    prof.end(st());
   }
 
   // y = L'^-1 r (+ add)
@@ -215,7 +219,9 @@ struct rs_solver {
     size_t m = (size_t)nv * 3 * nb;
     to_mg_kernel<<<nblk(m, 256), 256, 0, st()>>>(r, n, nb, nv, group.p, c.p, mu.p, G, mg_in.p);
     RSG_LAUNCHED(ctx, "to_mg");
+    prof.begin(st(), "precondition_multigrid_cg");
     amg.pcg(ctx, mg_in.p, mg_out.p, 3 * nb, vcycles);
+    prof.end(st());
     // shift: C_Q y = b
     pos_copy_weighted(nb);
     shift_kernel<<<nblk(3 * G * nb, 128), 128, 0, st()>>>(cy.p, r, n, nd, nb, G, shift.p);
@@ -239,14 +245,18 @@ struct rs_solver {
   // with the mesh), while the second form only perturbs the main term by (I - E) factors.
   void apply_prec(int nb, const double *r, double *z) {
     reserve(nb);
+    prof.begin(st(), "precondition");
     double *y = tmp.p, *v = tmp2.p;
     lsolve(nb, r, y, nullptr);
+    prof.begin(st(), "precondition_fractional");
     vfrac_apply_strided(vfrac, frac_scale, nb, y, n, v, n);
+    prof.end(st());
     group_sums(y, n, nb, c.p, cy.p);
     size_t tot = (size_t)nb * n;
     cq_apply_kernel<<<nblk(tot, 256), 256, 0, st()>>>(y, v, n, nb, nv, group.p, c.p, G, cy.p);
     RSG_LAUNCHED(ctx, "cq_apply");
     lsolve(nb, v, z, nullptr);
+    prof.end(st());
   }
 };
 
@@ -494,6 +504,44 @@ void rs_solver_free(rs_solver *S) {
   ctx_release(ctx);
 }
 
+int rs_solver_profile(rs_solver *S, int nb, const double *rhs, char *names, int names_len, double *ms,
+                      int max_kernels, int *n_kernels) {
+  return guard([&] {
+    S->ctx->use();
+    if (nb < 1 || nb > 4) fail(RS_INVALID_OPTION, "InvalidOption", "solver", "1 to 4 right-hand sides per batch");
+    size_t tot = (size_t)nb * S->n;
+    DevBuf<double> a(tot), b(tot);
+    a.upload(rhs, tot, S->st());
+    GmresOptions o = S->gopt;
+    o.prof = &S->prof;
+    S->prof.start();
+    S->prof.begin(S->st(), "solve");
+    gmres_batch(S->ctx, S->op, S->use_prec ? &S->prec : nullptr, nb, a.p, b.p, o, S->last);
+    S->prof.end(S->st());
+    S->prof.stop(S->st());
+    S->prof.report(names, names_len, ms, max_kernels, n_kernels, 1);
+  });
+}
+
+int rs_solver_multigrid_levels(rs_solver *S, int64_t *out, int max_levels, int *n_levels) {
+  return guard([&] {
+    int n = (int)S->amg.L.size();
+    for (int l = 0; l < n && l < max_levels; ++l) {
+      out[2 * l] = S->amg.L[l].n;
+      out[2 * l + 1] = (int64_t)S->amg.L[l].av.n;
+    }
+    *n_levels = n;
+  });
+}
+
+int rs_solver_set_gmres(rs_solver *S, int restart, int max_iterations, double tolerance) {
+  return guard([&] {
+    if (restart < 1 || restart > 63 || max_iterations < 1 || !(tolerance > 0.0 && tolerance < 1.0))
+      fail(RS_INVALID_OPTION, "InvalidOption", "solver", "restart in 1..63, max_iterations >= 1, tolerance in (0, 1)");
+    S->gopt.restart = restart, S->gopt.max_iterations = max_iterations, S->gopt.tolerance = tolerance;
+  });
+}
+
 int rs_solver_build_times(rs_solver *S, double *out6) {
   return guard([&] { std::copy(S->build_times, S->build_times + 6, out6); });
 }
@@ -607,7 +655,7 @@ rs_solver_options rs_solver_options_default(void) {
   o.eps_rel = 1e-10;
   o.eps_multi_rel = 1e-4;
   o.barycenter_per_component = 0;
-  o.vcycles = 3;
+  o.vcycles = 6;
   o.preconditioner = 1;
   o.clamp_laplacian = 0;
   return o;

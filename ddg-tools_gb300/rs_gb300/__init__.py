@@ -127,6 +127,9 @@ def load_library(path: str | os.PathLike | None = None):
         "rs_metric_apply_device_noalloc": [_vp, C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p],
         "rs_copy_counters": [C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)],
         "rs_solver_build_times": [_vp, _f64p],
+        "rs_solver_set_gmres": [_vp, C.c_int, C.c_int, C.c_double],
+        "rs_solver_multigrid_levels": [_vp, _i64p, C.c_int, C.POINTER(C.c_int)],
+        "rs_solver_profile": [_vp, C.c_int, _f64p, C.c_char_p, C.c_int, _f64p, C.c_int, C.POINTER(C.c_int)],
         "rs_solver_history": [_vp, C.c_int, _f64p, C.c_int, C.POINTER(C.c_int), _f64p, C.c_int,
                               C.POINTER(C.c_int)],
         "rs_flow_create": [_vp, C.c_int, C.c_int, _u32p, _f64p, C.c_void_p, C.POINTER(_vp)],
@@ -578,6 +581,22 @@ class SaddleSolver:
             r["converged"] = bool(r["converged"])
         return out, reports
 
+    def profile(self, rhs) -> dict:
+        """Milliseconds per phase of one solve of the stacked right-hand sides."""
+        rhs = np.ascontiguousarray(rhs, dtype=np.float64).reshape(-1, self.n)
+        names = C.create_string_buffer(4096)
+        ms = np.zeros(64)
+        n = C.c_int()
+        _check(_lib.rs_solver_profile(self._h, len(rhs), rhs.ravel(), names, 4096, ms, 64, C.byref(n)))
+        return _profile_dict(names, ms, n)
+
+    def multigrid_levels(self) -> list[tuple[int, int]]:
+        """(rows, nonzeros) of every multigrid level, finest first."""
+        out = np.zeros(64, np.int64)
+        n = C.c_int()
+        _check(_lib.rs_solver_multigrid_levels(self._h, out, 32, C.byref(n)))
+        return [(int(out[2 * i]), int(out[2 * i + 1])) for i in range(min(n.value, 32))]
+
     def build_times(self) -> dict:
         """Host seconds of the solver's set-up by phase."""
         o = np.zeros(6)
@@ -610,7 +629,7 @@ def flow_options(**kw) -> FlowOptions:
 FLOW_REPORT_KEYS = ["energy_before", "energy_after", "tau", "halvings", "gmres_area", "gmres_volume",
                     "gmres_direction", "relative_residual", "seconds", "seconds_tree", "seconds_energy",
                     "seconds_solver_build", "seconds_solve", "seconds_line_search", "seconds_projection",
-                    "accepted", "slope", "constraint_residual"]
+                    "accepted", "slope", "constraint_residual", "fallbacks"]
 
 
 class Flow:

@@ -229,7 +229,7 @@ typedef struct rs_solver_options {
   double eps_multi_rel;  /* eps when a global barycenter spans several components (1e-4) */
   int barycenter_per_component; /* 1: one barycenter group per component, 0: global (0) */
   int vcycles;           /* conjugate-gradient steps, each preconditioned by one multigrid
-                            V-cycle, per L' solve (3) */
+                            V-cycle, per L' solve (6) */
   int preconditioner;    /* 1: the fractional preconditioner, 0: none */
   int clamp_laplacian;   /* 1: edges with negative cotan weight dropped from the
                             preconditioner's Laplacian (an M-matrix for multigrid), 0: cotan */
@@ -250,6 +250,18 @@ int rs_solver_dims(rs_solver *s, int64_t *n_dofs, int64_t *n_constraints);
 /* Host seconds of rs_solver_build by phase: [metric tree and upload, vertex fractional tree,
  * Laplacian block, multigrid set-up, multigrid upload, total]. No counterpart in the crate. */
 int rs_solver_build_times(rs_solver *s, double *out6);
+/* Changes the GMRES settings of later solves (GmresOptions, RS/src/solve/gmres.rs:135-190). */
+int rs_solver_set_gmres(rs_solver *s, int restart, int max_iterations, double tolerance);
+/* Rows and nonzeros of every multigrid level of the preconditioner's Laplacian block, finest
+ * first: out[2 l] = rows, out[2 l + 1] = nonzeros (the coarsest level is inverted densely).
+ * No counterpart in the crate. */
+int rs_solver_multigrid_levels(rs_solver *s, int64_t *out, int max_levels, int *n_levels);
+/* Solves nb host right-hand sides once with phase timing (CUDA events on the context's
+ * stream) and reports the milliseconds spent per phase for that solve: solve, operator,
+ * precondition, precondition_multigrid_cg, precondition_fractional, gmres_orthogonalize.
+ * Names are NUL-separated in `names`. No counterpart in the crate. */
+int rs_solver_profile(rs_solver *s, int nb, const double *rhs_host, char *names, int names_len,
+                      double *ms, int max_kernels, int *n_kernels);
 /* LinearOperator::apply_batch (gmres.rs:32-52): ys = A' xs for nb stacked vectors. */
 int rs_solver_apply(rs_solver *s, int nb, const double *xs_host, double *ys_host);
 int rs_solver_apply_device(rs_solver *s, int nb, const double *xs_dev, double *ys_dev);
@@ -295,13 +307,15 @@ int rs_flow_create(rs_ctx *ctx, int nv, int nf, const uint32_t *faces,
                    const double *positions_host, const rs_flow_options *opts, rs_flow **out);
 void rs_flow_free(rs_flow *f);
 
-#define RS_FLOW_REPORT_LEN 18
+#define RS_FLOW_REPORT_LEN 19
 /* Session::step (session.rs:724-747): one step. report[RS_FLOW_REPORT_LEN]:
  *  0 energy before, 1 energy after, 2 accepted tau (0: refused), 3 halvings,
  *  4..6 GMRES iterations of the solves (area row, volume row, direction),
  *  7 worst true relative residual, 8 seconds of the step, 9 tree and lists, 10 energy,
  *  11 solver build, 12 solves, 13 line search, 14 projection, 15 accepted (1/0),
- *  16 slope g.x, 17 relative nonlinear-constraint residual after the projection. */
+ *  16 slope g.x, 17 relative nonlinear-constraint residual after the projection,
+ *  18 fallbacks: solves repeated with restart 60 and the larger iteration cap after GMRES
+ *     ended above the divergence threshold (RobustHierarchical, direction.rs:269-379). */
 int rs_flow_step(rs_flow *f, double *report);
 /* The current positions (V x 3). */
 int rs_flow_positions(rs_flow *f, double *positions_host);

@@ -2,7 +2,9 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
+#include <thread>
 
 #include <cstdint>
 #include <cstring>
@@ -124,6 +126,22 @@ struct rs_ctx {
 
 namespace rsg {
 rs_ctx *ctx_retain(rs_ctx *ctx);
+
+// f(begin, end) over [0, n) in contiguous chunks on up to 16 host threads (the host set-up
+// loops of the trees and blocks). Results that depend on the chunking must not be produced.
+template <class Fn>
+void parallel_for(size_t n, Fn f, size_t min_chunk = 4096) {
+  size_t hw = std::thread::hardware_concurrency();
+  size_t t = std::min<size_t>(std::min<size_t>(hw ? hw : 1, 16), (n + min_chunk - 1) / min_chunk);
+  if (t <= 1) {
+    f((size_t)0, n);
+    return;
+  }
+  std::vector<std::thread> pool;
+  for (size_t i = 1; i < t; ++i) pool.emplace_back([&, i] { f(n * i / t, n * (i + 1) / t); });
+  f((size_t)0, n / t);
+  for (auto &th : pool) th.join();
+}
 void ctx_release(rs_ctx *ctx);
 }  // namespace rsg
 

@@ -200,6 +200,7 @@ int rs_flow_positions(rs_flow *F, double *positions_host) {
 
 int rs_flow_step(rs_flow *F, double *report) {
   return guard([&] {
+    TrustedTopology trusted;  // validated by rs_flow_create; the face list never changes
     auto t_step = clk::now();
     rs_ctx *ctx = F->ctx;
     ctx->use();

@@ -538,42 +538,59 @@ struct HMat {
     cudaStream_t s = st();
     const Tree &T = tree;
     size_t nn = T.n_nodes(), nl = T.leaves.size();
-    std::vector<uint32_t> parent_h(nn, 0), coff(nl + 1, 0), chain_h, ioff(nl + 1, 0);
-    std::vector<uint32_t> cols_h;
-    std::vector<uint4> items_h;
+    std::vector<uint32_t> parent_h(nn, 0), coff(nl + 1, 0), ioff(nl + 1, 0);
     const uint32_t kItemCols = 512;
     for (size_t i = 0; i < nn; ++i)
       if (T.right[i]) parent_h[i + 1] = (uint32_t)i, parent_h[T.right[i]] = (uint32_t)i;
-    for (size_t k = 0; k < nl; ++k) {
-      uint32_t l = T.leaves[k];
-      if (T.end[l] - T.start[l] > 8)
+    for (size_t k = 0; k < nl; ++k)
+      if (T.end[T.leaves[k]] - T.start[T.leaves[k]] > 8)
         fail(RS_INVALID_OPTION, "InvalidOption", "upload", "the GPU path needs leaf_size <= 8");
-      size_t b = chain_h.size();
-      uint32_t a = l;
-      for (;;) {
-        chain_h.push_back(a);
-        if (a == 0) break;
-        a = parent_h[a];
-      }
-      std::reverse(chain_h.begin() + b, chain_h.end());
-      coff[k + 1] = (uint32_t)chain_h.size();
-      // the near columns of the chain (chain order, block order, element order), flattened and
-      // cut into items of at most kItemCols columns
-      const uint32_t c_begin = (uint32_t)cols_h.size();
-      for (size_t ci = b; ci < chain_h.size(); ++ci)
-        for (uint32_t q = blocks.near_ptr[chain_h[ci]]; q < blocks.near_ptr[chain_h[ci] + 1]; ++q) {
-          uint32_t c = blocks.near_col[q];
-          for (uint32_t e = T.start[c]; e < T.end[c]; ++e) cols_h.push_back(e);
+    // per leaf: its root-to-leaf chain and the near columns of the chain (chain order, block
+    // order, element order), flattened and cut into items of at most kItemCols columns; two
+    // parallel passes (sizes, then fill at the prefix offsets)
+    std::vector<uint64_t> ncol(nl + 1, 0);
+    parallel_for(nl, [&](size_t k0, size_t k1) {
+      for (size_t k = k0; k < k1; ++k) {
+        uint32_t depth = 1;
+        uint64_t cols = 0;
+        for (uint32_t a = T.leaves[k];; a = parent_h[a]) {
+          for (uint32_t q = blocks.near_ptr[a]; q < blocks.near_ptr[a + 1]; ++q) {
+            uint32_t c = blocks.near_col[q];
+            cols += T.end[c] - T.start[c];
+          }
+          if (a == 0) break;
+          ++depth;
         }
-      const uint32_t c_end = (uint32_t)cols_h.size();
-      uint32_t x = c_begin;
-      do {
-        uint32_t y = std::min(c_end, x + kItemCols);
-        items_h.push_back(make_uint4((uint32_t)k, x, y, 0));
-        x = y;
-      } while (x < c_end);
-      ioff[k + 1] = (uint32_t)items_h.size();
-    }
+        coff[k + 1] = depth;
+        ncol[k + 1] = cols;
+        ioff[k + 1] = (uint32_t)std::max<uint64_t>(1, (cols + kItemCols - 1) / kItemCols);
+      }
+    });
+    for (size_t k = 0; k < nl; ++k) coff[k + 1] += coff[k], ncol[k + 1] += ncol[k], ioff[k + 1] += ioff[k];
+    if (ncol[nl] > UINT32_MAX) fail(RS_INVALID_OPTION, "InvalidOption", "upload", "near field too large");
+    std::vector<uint32_t> chain_h(coff[nl]), cols_h(ncol[nl]);
+    std::vector<uint4> items_h(ioff[nl]);
+    parallel_for(nl, [&](size_t k0, size_t k1) {
+      for (size_t k = k0; k < k1; ++k) {
+        uint32_t *ch = chain_h.data() + coff[k];
+        uint32_t depth = coff[k + 1] - coff[k];
+        uint32_t a = T.leaves[k];
+        for (uint32_t i = depth; i-- > 0; a = parent_h[a]) ch[i] = a;
+        uint32_t x = (uint32_t)ncol[k];
+        for (uint32_t i = 0; i < depth; ++i)
+          for (uint32_t q = blocks.near_ptr[ch[i]]; q < blocks.near_ptr[ch[i] + 1]; ++q) {
+            uint32_t c = blocks.near_col[q];
+            for (uint32_t e = T.start[c]; e < T.end[c]; ++e) cols_h[x++] = e;
+          }
+        const uint32_t c_end = (uint32_t)ncol[k + 1];
+        uint32_t y0 = (uint32_t)ncol[k];
+        for (uint32_t it = ioff[k]; it < ioff[k + 1]; ++it) {
+          uint32_t y1 = std::min(c_end, y0 + kItemCols);
+          items_h[it] = make_uint4((uint32_t)k, y0, y1, 0);
+          y0 = y1;
+        }
+      }
+    });
     n_items = items_h.size();
     up_vec(start, T.start, s), up_vec(end, T.end, s), up_vec(right, T.right, s);
     up_vec(parent, parent_h, s), up_vec(leaves, T.leaves, s), up_vec(chain_off, coff, s);
@@ -588,17 +605,19 @@ struct HMat {
       return p[0] * d[0] * d[0] + p[3] * d[1] * d[1] + p[5] * d[2] * d[2] +
              2.0 * (p[1] * d[0] * d[1] + p[2] * d[0] * d[2] + p[4] * d[1] * d[2]);
     };
-    for (size_t a = 0; a < nn; ++a)
-      for (uint32_t q = blocks.far_ptr[a]; q < blocks.far_ptr[a + 1]; ++q) {
-        size_t b = blocks.far_col[q], lo = std::min(a, b), hi = std::max(a, b);
-        double d[3] = {T.centroid[3 * lo] - T.centroid[3 * hi], T.centroid[3 * lo + 1] - T.centroid[3 * hi + 1],
-                       T.centroid[3 * lo + 2] - T.centroid[3 * hi + 2]};
-        double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-        double h = std::pow(r2, neg_s);
-        double h1 = h;
-        if (kind == FACE) h1 = 0.5 * (qf(lo, d) + qf(hi, d)) / (r2 * r2) * h;
-        coef[q] = make_double2(h, h1);
-      }
+    parallel_for(nn, [&](size_t a0, size_t a1) {
+      for (size_t a = a0; a < a1; ++a)
+        for (uint32_t q = blocks.far_ptr[a]; q < blocks.far_ptr[a + 1]; ++q) {
+          size_t b = blocks.far_col[q], lo = std::min(a, b), hi = std::max(a, b);
+          double d[3] = {T.centroid[3 * lo] - T.centroid[3 * hi], T.centroid[3 * lo + 1] - T.centroid[3 * hi + 1],
+                         T.centroid[3 * lo + 2] - T.centroid[3 * hi + 2]};
+          double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+          double h = std::pow(r2, neg_s);
+          double h1 = h;
+          if (kind == FACE) h1 = 0.5 * (qf(lo, d) + qf(hi, d)) / (r2 * r2) * h;
+          coef[q] = make_double2(h, h1);
+        }
+    }, 256);
     up_vec(far_coef, coef, s);
     // element records
     DevBuf<double> dp, dw, dn;

@@ -16,8 +16,10 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <future>
 #include <numeric>
 #include <string>
+#include <thread>
 
 #include "common.hpp"
 
@@ -25,7 +27,15 @@ namespace rsg {
 
 static std::string s(size_t x) { return std::to_string(x); }
 
+namespace {
+thread_local bool g_topology_trusted = false;
+}
+
+TrustedTopology::TrustedTopology() : prev(g_topology_trusted) { g_topology_trusted = true; }
+TrustedTopology::~TrustedTopology() { g_topology_trusted = prev; }
+
 void validate_topology(int nv, int nf, const uint32_t *faces) {
+  if (g_topology_trusted) return;
   if (nf <= 0) fail(RS_TOPOLOGY, "NoFaces", "surface", "the face list is empty");
   if (nv < 0) fail(RS_TOPOLOGY, "TooLarge", "surface", "negative vertex count");
   for (int f = 0; f < nf; ++f) {  // surface.rs:144-161
@@ -212,83 +222,134 @@ inline int64_t tkey(double x) {
 
 }  // namespace
 
+namespace {
+
+// The split recursion of build_tree over one subtree: nodes in pre-order relative to the
+// subtree (right = index of the right child within the subtree, 0 for a leaf). Subtrees of
+// the top levels run as concurrent tasks; their ranges of the presorted orders, of `tmp` and
+// of `order` are disjoint, and the element flags are per element, so nothing is shared.
+struct SplitCtx {
+  const double *ebox;
+  int leaf_size;
+  size_t n;
+  std::vector<uint32_t> *srt;  // [3]
+  std::vector<uint8_t> *left_flag;
+  std::vector<uint32_t> *tmp;
+  std::vector<uint32_t> *order;
+};
+
+struct LocalNodes {
+  std::vector<uint32_t> start, end, right;
+};
+
+void split_range(const SplitCtx &c, size_t start, size_t end, size_t depth, LocalNodes &out, int par_depth) {
+  const uint32_t id = (uint32_t)out.start.size();
+  out.start.push_back((uint32_t)start);
+  out.end.push_back((uint32_t)end);
+  out.right.push_back(0);
+  const size_t cnt = end - start;
+  if (cnt <= (size_t)c.leaf_size) {
+    // A leaf keeps its parent's sort (axis (depth-1) mod 3); a root leaf is unsorted.
+    if (depth == 0)
+      for (size_t i = 0; i < c.n; ++i) (*c.order)[i] = (uint32_t)i;
+    else
+      std::copy(c.srt[(depth - 1) % 3].begin() + start, c.srt[(depth - 1) % 3].begin() + end,
+                c.order->begin() + start);
+    return;
+  }
+  const int axis = (int)(depth % 3);
+  const uint32_t *sl = c.srt[axis].data() + start;
+  std::vector<Box> suffix(cnt);
+  Box acc;
+  for (size_t k = cnt; k-- > 0;) {
+    acc.join(c.ebox + 6 * (size_t)sl[k]);
+    suffix[k] = acc;
+  }
+  Box prefix;
+  double best_cost = INFINITY;
+  size_t best_k = cnt / 2;
+  size_t lo = (size_t)std::ceil(0.25 * (double)cnt);
+  lo = std::min(std::max<size_t>(lo, 1), cnt / 2);
+  for (size_t k = 1; k <= cnt - lo; ++k) {
+    prefix.join(c.ebox + 6 * (size_t)sl[k - 1]);
+    if (k < lo) continue;
+    double cost = prefix.diam2() + suffix[k].diam2();
+    if (cost < best_cost) best_cost = cost, best_k = k;
+  }
+  for (size_t k = 0; k < cnt; ++k) (*c.left_flag)[sl[k]] = k < best_k;
+  uint32_t *tmp = c.tmp->data() + start;
+  for (int b = 0; b < 3; ++b) {
+    if (b == axis) continue;
+    uint32_t *o = c.srt[b].data() + start;
+    size_t nl = 0, nr = best_k;
+    for (size_t k = 0; k < cnt; ++k) {
+      uint32_t e = o[k];
+      tmp[(*c.left_flag)[e] ? nl++ : nr++] = e;
+    }
+    std::copy(tmp, tmp + cnt, o);
+  }
+  const size_t split = start + best_k;
+  auto append = [&](const LocalNodes &sub) {
+    const uint32_t off = (uint32_t)out.start.size();
+    for (size_t i = 0; i < sub.start.size(); ++i) {
+      out.start.push_back(sub.start[i]);
+      out.end.push_back(sub.end[i]);
+      out.right.push_back(sub.right[i] ? sub.right[i] + off : 0);
+    }
+  };
+  if (par_depth > 0 && cnt > 4096) {
+    LocalNodes left, right;
+    auto fut = std::async(std::launch::async, [&] { split_range(c, start, split, depth + 1, left, par_depth - 1); });
+    split_range(c, split, end, depth + 1, right, par_depth - 1);
+    fut.get();
+    append(left);
+    out.right[id] = (uint32_t)out.start.size();
+    append(right);
+  } else {
+    split_range(c, start, split, depth + 1, out, 0);
+    out.right[id] = (uint32_t)out.start.size();
+    split_range(c, split, end, depth + 1, out, 0);
+  }
+}
+
+}  // namespace
+
 Tree build_tree(size_t n, const double *pts, const double *ebox, const double *mass,
                 int leaf_size) {
   if (leaf_size < 1) fail(RS_INVALID_OPTION, "InvalidOption", "tree", "leaf_size must be at least 1");
   if (n == 0) fail(RS_INVALID_OPTION, "InvalidOption", "tree", "at least 1 element");
   Tree T;
   T.order.resize(n);
-  // Presorted orders per axis, partitioned stably at every split.
+  // Presorted orders per axis (one thread per axis), partitioned stably at every split.
   std::vector<uint32_t> srt[3];
-  for (int a = 0; a < 3; ++a) {
-    srt[a].resize(n);
-    std::vector<int64_t> key(n);
-    for (size_t i = 0; i < n; ++i) key[i] = tkey(pts[3 * i + a]);
-    std::iota(srt[a].begin(), srt[a].end(), 0u);
-    std::sort(srt[a].begin(), srt[a].end(), [&](uint32_t x, uint32_t y) {
-      return key[x] != key[y] ? key[x] < key[y] : x < y;
-    });
+  {
+    auto presort = [&](int a) {
+      srt[a].resize(n);
+      std::vector<int64_t> key(n);
+      for (size_t i = 0; i < n; ++i) key[i] = tkey(pts[3 * i + a]);
+      std::iota(srt[a].begin(), srt[a].end(), 0u);
+      std::sort(srt[a].begin(), srt[a].end(), [&](uint32_t x, uint32_t y) {
+        return key[x] != key[y] ? key[x] < key[y] : x < y;
+      });
+    };
+    if (n > 65536) {
+      auto f1 = std::async(std::launch::async, presort, 1);
+      auto f2 = std::async(std::launch::async, presort, 2);
+      presort(0);
+      f1.get(), f2.get();
+    } else {
+      for (int a = 0; a < 3; ++a) presort(a);
+    }
   }
   std::vector<uint8_t> left_flag(n, 0);
   std::vector<uint32_t> tmp(n);
-  std::vector<Box> suffix;
-  struct Item {
-    size_t start, end, depth;
-    uint32_t patch;
-  };
-  std::vector<Item> stack{{0, n, 0, UINT32_MAX}};
-  while (!stack.empty()) {
-    Item it = stack.back();
-    stack.pop_back();
-    uint32_t id = (uint32_t)T.start.size();
-    if (it.patch != UINT32_MAX) T.right[it.patch] = id;
-    T.start.push_back((uint32_t)it.start);
-    T.end.push_back((uint32_t)it.end);
-    T.right.push_back(0);
-    size_t cnt = it.end - it.start;
-    if (cnt <= (size_t)leaf_size) {
-      // A leaf keeps its parent's sort (axis (depth-1) mod 3); a root leaf is unsorted.
-      if (it.depth == 0)
-        for (size_t i = 0; i < n; ++i) T.order[i] = (uint32_t)i;
-      else
-        std::copy(srt[(it.depth - 1) % 3].begin() + it.start, srt[(it.depth - 1) % 3].begin() + it.end,
-                  T.order.begin() + it.start);
-      continue;
-    }
-    int axis = (int)(it.depth % 3);
-    const uint32_t *sl = srt[axis].data() + it.start;
-    suffix.assign(cnt, Box());
-    Box acc;
-    for (size_t k = cnt; k-- > 0;) {
-      acc.join(ebox + 6 * (size_t)sl[k]);
-      suffix[k] = acc;
-    }
-    Box prefix;
-    double best_cost = INFINITY;
-    size_t best_k = cnt / 2;
-    size_t lo = (size_t)std::ceil(0.25 * (double)cnt);
-    lo = std::min(std::max<size_t>(lo, 1), cnt / 2);
-    for (size_t k = 1; k <= cnt - lo; ++k) {
-      prefix.join(ebox + 6 * (size_t)sl[k - 1]);
-      if (k < lo) continue;
-      double cost = prefix.diam2() + suffix[k].diam2();
-      if (cost < best_cost) best_cost = cost, best_k = k;
-    }
-    for (size_t k = 0; k < cnt; ++k) left_flag[sl[k]] = k < best_k;
-    for (int b = 0; b < 3; ++b) {
-      if (b == axis) continue;
-      uint32_t *o = srt[b].data() + it.start;
-      size_t nl = 0, nr = best_k;
-      for (size_t k = 0; k < cnt; ++k) {
-        uint32_t e = o[k];
-        tmp[left_flag[e] ? nl++ : nr++] = e;
-      }
-      std::copy(tmp.begin(), tmp.begin() + cnt, o);
-    }
-    size_t split = it.start + best_k;
-    stack.push_back({split, it.end, it.depth + 1, id});
-    stack.push_back({it.start, split, it.depth + 1, UINT32_MAX});
-  }
+  SplitCtx c{ebox, leaf_size, n, srt, &left_flag, &tmp, &T.order};
+  LocalNodes nodes;
+  const int par_depth = std::thread::hardware_concurrency() > 1 ? 4 : 0;  // up to 16 subtrees
+  split_range(c, 0, n, 0, nodes, par_depth);
+  T.start = std::move(nodes.start);
+  T.end = std::move(nodes.end);
+  T.right = std::move(nodes.right);
   // Node data as Bvh::refit (bvh.rs:226-260, summarize 314-330).
   size_t nn = T.start.size();
   T.box.resize(6 * nn);

@@ -10,6 +10,17 @@ namespace rsg {
 
 // Surface::new topology checks (RS/src/surface.rs:132-330).
 void validate_topology(int nv, int nf, const uint32_t *faces);
+
+// While alive on a thread, validate_topology on that thread returns at once: for a caller that
+// validated the face list itself and rebuilds trees over it every step (the flow session,
+// whose topology never changes).
+struct TrustedTopology {
+  TrustedTopology();
+  ~TrustedTopology();
+  TrustedTopology(const TrustedTopology &) = delete;
+  TrustedTopology &operator=(const TrustedTopology &) = delete;
+  bool prev;
+};
 // Surface::validate_positions (RS/src/surface.rs:513-541).
 void validate_positions(int nv, int nf, const uint32_t *faces, const double *pos);
 

@@ -90,6 +90,18 @@ def test_face_tree_matches_oracle_bitwise(name, mesh, leaf):
     assert np.array_equal(T["radius"], Cl["radius"])
 
 
+@pytest.mark.parametrize("name", ["c2", "c3s"])
+def test_large_face_tree_matches_oracle_bitwise(name):
+    """Sizes where the build sorts the three axes concurrently and splits the top subtrees as
+    parallel tasks (81,920 and 204,800 faces)."""
+    P, F = gen.CONFIGS[name]()
+    T = R.face_tree(F, P, leaf_size=8)
+    bh = O.BhTree(P, F, theta=0.5, leaf_size=8)
+    U = bh.tree()
+    for k in ("start", "end", "right", "order"):
+        assert np.array_equal(T[k], U[k]), k
+
+
 def test_generators_match_reference_recipes():
     P, F = gen.icosphere(3)
     assert P.shape == (642, 3) and F.shape == (1280, 3)

@@ -144,6 +144,8 @@ struct rs_flow {
   std::vector<double> pos;
   rs_flow_options o;
   double l0 = 0.0, last_tau = 0.0, area0 = 0.0, vol0 = 0.0, bary0[3] = {0, 0, 0};
+  rs_learned *lmodel = nullptr;
+  int l_cheap = 2, l_cap = 0;
   int iteration = 0;
 };
 
@@ -194,6 +196,14 @@ void rs_flow_free(rs_flow *F) {
   ctx_release(ctx);
 }
 
+int rs_flow_set_learned(rs_flow *F, rs_learned *model, int cheap_steps, int max_iterations) {
+  return guard([&] {
+    if (model && (cheap_steps < 1 || max_iterations < 0))
+      fail(RS_INVALID_OPTION, "InvalidOption", "flow", "cheap_steps >= 1, max_iterations >= 0");
+    F->lmodel = model, F->l_cheap = cheap_steps, F->l_cap = max_iterations;
+  });
+}
+
 int rs_flow_positions(rs_flow *F, double *positions_host) {
   return guard([&] { std::memcpy(positions_host, F->pos.data(), F->pos.size() * sizeof(double)); });
 }
@@ -220,6 +230,12 @@ int rs_flow_step(rs_flow *F, double *report) {
     sv.del = rs_solver_free;
     check(rs_solver_build(ctx, nv, nf, faces, F->pos.data(), F->o.alpha, F->o.beta, &F->o.solver, &sv.p),
           "flow (solver)");
+    Owned<rs_lgraph> lg;
+    lg.del = rs_lgraph_free;
+    if (F->lmodel) {
+      check(rs_lgraph_create(ctx, nv, nf, faces, F->pos.data(), &lg.p), "flow (solver)");
+      check(rs_solver_set_learned(sv.p, F->lmodel, lg.p, F->l_cheap, F->l_cap), "flow (solver)");
+    }
     rep[11] = since(t);
     int64_t ndof = 0, nq = 0;
     check(rs_solver_dims(sv.p, &ndof, &nq), "flow");
@@ -397,6 +413,11 @@ int rs_flow_step(rs_flow *F, double *report) {
       F->iteration++;
     }
     rep[14] = since(t);
+    if (F->lmodel) {
+      int64_t ls = 0, lf = 0;
+      check(rs_solver_learned_counts(sv.p, &ls, &lf), "flow");
+      rep[19] = (double)ls, rep[20] = (double)lf;
+    }
     rep[0] = E0;
     rep[1] = E1;
     rep[2] = accepted ? tau : 0.0;

@@ -26,6 +26,7 @@
 #include "hmat.hpp"
 #include "host_tree.hpp"
 #include "krylov.hpp"
+#include "learned.hpp"
 #include "profile.hpp"
 
 namespace rsg {
@@ -169,6 +170,13 @@ struct rs_solver {
   int vcycles = 1;
   double build_times[6] = {0, 0, 0, 0, 0, 0};
   Profiler prof;
+  // learned preconditioner (optional): z = learned(r, P_cheap^-1 r), plain solver as fallback
+  rs_learned *lmodel = nullptr;
+  rs_lgraph *lgraph = nullptr;
+  int l_cheap = 2, l_cap = 0;
+  int64_t l_solves = 0, l_fallbacks = 0;
+  DevBuf<double> lbuf;
+  Operator lprec;
   GmresOptions gopt;
   FaceGeom geom;
   std::vector<double> vmass;
@@ -211,8 +219,8 @@ struct rs_solver {
     prof.end(st());
   }
 
-  // y = L'^-1 r (+ add)
-  void lsolve(int nb, const double *r, double *y, const double *add) {
+  // y = L'^-1 r (+ add) by `steps` multigrid-preconditioned CG steps (0: the solver's setting)
+  void lsolve(int nb, const double *r, double *y, const double *add, int steps = 0) {
     group_sums(r, n, nb, nullptr, s1.p);
     mu_kernel<<<nblk(3 * G * nb, 128), 128, 0, st()>>>(s1.p, r, n, nd, nb, G, eps_area.p, mu.p);
     RSG_LAUNCHED(ctx, "mu");
@@ -220,7 +228,7 @@ struct rs_solver {
     to_mg_kernel<<<nblk(m, 256), 256, 0, st()>>>(r, n, nb, nv, group.p, c.p, mu.p, G, mg_in.p);
     RSG_LAUNCHED(ctx, "to_mg");
     prof.begin(st(), "precondition_multigrid_cg");
-    amg.pcg(ctx, mg_in.p, mg_out.p, 3 * nb, vcycles);
+    amg.pcg(ctx, mg_in.p, mg_out.p, 3 * nb, steps > 0 ? steps : vcycles);
     prof.end(st());
     // shift: C_Q y = b
     pos_copy_weighted(nb);
@@ -243,11 +251,11 @@ struct rs_solver {
   // multigrid X~ = K^-1 (I - E) the first form leaves X~ E, an order -2 error term that
   // outgrows the order -2s main term at high frequencies (the iteration count then grows
   // with the mesh), while the second form only perturbs the main term by (I - E) factors.
-  void apply_prec(int nb, const double *r, double *z) {
+  void apply_prec(int nb, const double *r, double *z, int steps = 0) {
     reserve(nb);
     prof.begin(st(), "precondition");
     double *y = tmp.p, *v = tmp2.p;
-    lsolve(nb, r, y, nullptr);
+    lsolve(nb, r, y, nullptr, steps);
     prof.begin(st(), "precondition_fractional");
     vfrac_apply_strided(vfrac, frac_scale, nb, y, n, v, n);
     prof.end(st());
@@ -255,8 +263,38 @@ struct rs_solver {
     size_t tot = (size_t)nb * n;
     cq_apply_kernel<<<nblk(tot, 256), 256, 0, st()>>>(y, v, n, nb, nv, group.p, c.p, G, cy.p);
     RSG_LAUNCHED(ctx, "cq_apply");
-    lsolve(nb, v, z, nullptr);
+    lsolve(nb, v, z, nullptr, steps);
     prof.end(st());
+  }
+
+  // the learned preconditioner: y = P^-1 r with l_cheap CG steps, then the network's correction
+  void apply_learned(int nb, const double *r, double *z) {
+    if (lbuf.n < (size_t)nb * n) lbuf.alloc((size_t)nb * n);
+    apply_prec(nb, r, lbuf.p, l_cheap);
+    prof.begin(st(), "precondition_learned");
+    learned_apply(lmodel, lgraph, nb, r, lbuf.p, n, n, z);
+    prof.end(st());
+  }
+
+  // GMRES with the learned preconditioner when one is set (capped at l_cap iterations), the
+  // plain preconditioner otherwise or when the learned solve does not converge
+  void solve(int nb, const double *b, double *x, const GmresOptions &o) {
+    if (lmodel && use_prec) {
+      GmresOptions ol = o;
+      if (l_cap > 0) ol.max_iterations = l_cap;
+      l_solves++;
+      bool ok = true;
+      try {
+        gmres_batch(ctx, op, &lprec, nb, b, x, ol, last);
+        for (auto &r : last) ok = ok && r.converged;
+      } catch (const Error &e) {
+        if (e.code != RS_SOLVER_DIVERGED) throw;
+        ok = false;
+      }
+      if (ok) return;
+      l_fallbacks++;
+    }
+    gmres_batch(ctx, op, use_prec ? &prec : nullptr, nb, b, x, o, last);
   }
 };
 
@@ -485,6 +523,8 @@ int rs_solver_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const do
     S->op.apply = [P](int nb, const double *x, double *y) { P->apply_op(nb, x, y); };
     S->prec.n = S->n;
     S->prec.apply = [P](int nb, const double *x, double *y) { P->apply_prec(nb, x, y); };
+    S->lprec.n = S->n;
+    S->lprec.apply = [P](int nb, const double *x, double *y) { P->apply_learned(nb, x, y); };
     RSG_CUDA("solver", cudaStreamSynchronize(s));
     lap(S->build_times[4]);
     S->build_times[5] = std::chrono::duration<double>(clk::now() - t_all).count();
@@ -516,7 +556,7 @@ int rs_solver_profile(rs_solver *S, int nb, const double *rhs, char *names, int 
     o.prof = &S->prof;
     S->prof.start();
     S->prof.begin(S->st(), "solve");
-    gmres_batch(S->ctx, S->op, S->use_prec ? &S->prec : nullptr, nb, a.p, b.p, o, S->last);
+    S->solve(nb, a.p, b.p, o);
     S->prof.end(S->st());
     S->prof.stop(S->st());
     S->prof.report(names, names_len, ms, max_kernels, n_kernels, 1);
@@ -539,6 +579,24 @@ int rs_solver_set_gmres(rs_solver *S, int restart, int max_iterations, double to
     if (restart < 1 || restart > 63 || max_iterations < 1 || !(tolerance > 0.0 && tolerance < 1.0))
       fail(RS_INVALID_OPTION, "InvalidOption", "solver", "restart in 1..63, max_iterations >= 1, tolerance in (0, 1)");
     S->gopt.restart = restart, S->gopt.max_iterations = max_iterations, S->gopt.tolerance = tolerance;
+  });
+}
+
+int rs_solver_set_learned(rs_solver *S, rs_learned *model, rs_lgraph *graph, int cheap_steps,
+                          int max_iterations) {
+  return guard([&] {
+    if (model && !graph) fail(RS_INVALID_OPTION, "InvalidOption", "solver", "a learned model needs its surface graph");
+    if (model && (cheap_steps < 1 || max_iterations < 0))
+      fail(RS_INVALID_OPTION, "InvalidOption", "solver", "cheap_steps >= 1, max_iterations >= 0");
+    S->lmodel = model, S->lgraph = graph;
+    S->l_cheap = cheap_steps, S->l_cap = max_iterations;
+  });
+}
+
+int rs_solver_learned_counts(rs_solver *S, int64_t *solves, int64_t *fallbacks) {
+  return guard([&] {
+    *solves = S->l_solves;
+    *fallbacks = S->l_fallbacks;
   });
 }
 
@@ -572,7 +630,7 @@ int rs_solver_solve_many_device(rs_solver *S, int nb, const double *rhs_dev, dou
   return guard([&] {
     S->ctx->use();
     if (nb < 1 || nb > 4) fail(RS_INVALID_OPTION, "InvalidOption", "solver", "1 to 4 right-hand sides per batch");
-    gmres_batch(S->ctx, S->op, S->use_prec ? &S->prec : nullptr, nb, rhs_dev, sol_dev, S->gopt, S->last);
+    S->solve(nb, rhs_dev, sol_dev, S->gopt);
     if (report)
       for (int q = 0; q < nb; ++q) {
         report[5 * q + 0] = S->last[q].iterations;
@@ -614,7 +672,7 @@ int rs_solver_solve_many(rs_solver *S, int nb, const double *rhs, double *sol, d
     S->ctx->use();
     if (nb < 1 || nb > 4) fail(RS_INVALID_OPTION, "InvalidOption", "solver", "1 to 4 right-hand sides per batch");
     host_roundtrip(S, nb, rhs, sol, [&](const double *a, double *b) {
-      gmres_batch(S->ctx, S->op, S->use_prec ? &S->prec : nullptr, nb, a, b, S->gopt, S->last);
+      S->solve(nb, a, b, S->gopt);
     });
     if (report)
       for (int q = 0; q < nb; ++q) {

@@ -127,6 +127,18 @@ def load_library(path: str | os.PathLike | None = None):
         "rs_metric_apply_device_noalloc": [_vp, C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p],
         "rs_copy_counters": [C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)],
         "rs_solver_build_times": [_vp, _f64p],
+        "rs_learned_create": [_vp, C.c_uint64, C.POINTER(_vp)],
+        "rs_learned_parameter_count": [_vp, C.POINTER(C.c_int64)],
+        "rs_learned_get_parameters": [_vp, np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")],
+        "rs_learned_set_parameters": [_vp, np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")],
+        "rs_learned_get_gradient": [_vp, np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")],
+        "rs_lgraph_create": [_vp, C.c_int, C.c_int, _u32p, _f64p, C.POINTER(_vp)],
+        "rs_learned_apply_device": [_vp, _vp, C.c_int, _vp, _vp, _vp],
+        "rs_learned_loss_and_gradient_device": [_vp, _vp, _vp, _vp, _vp, C.POINTER(C.c_double)],
+        "rs_learned_adam_step": [_vp, C.c_double, C.c_double],
+        "rs_solver_set_learned": [_vp, _vp, _vp, C.c_int, C.c_int],
+        "rs_solver_learned_counts": [_vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
+        "rs_flow_set_learned": [_vp, _vp, C.c_int, C.c_int],
         "rs_solver_set_gmres": [_vp, C.c_int, C.c_int, C.c_double],
         "rs_solver_multigrid_levels": [_vp, _i64p, C.c_int, C.POINTER(C.c_int)],
         "rs_solver_profile": [_vp, C.c_int, _f64p, C.c_char_p, C.c_int, _f64p, C.c_int, C.POINTER(C.c_int)],
@@ -148,6 +160,9 @@ def load_library(path: str | os.PathLike | None = None):
     L.rs_flow_options_default.argtypes = []
     L.rs_flow_free.argtypes = [_vp]
     L.rs_flow_free.restype = None
+    for name in ("rs_learned_free", "rs_lgraph_free"):
+        getattr(L, name).argtypes = [_vp]
+        getattr(L, name).restype = None
     for name in ("rs_bh_free", "rs_metric_free", "rs_vfrac_free", "rs_solver_free"):
         getattr(L, name).argtypes = [_vp]
         getattr(L, name).restype = None
@@ -597,6 +612,18 @@ class SaddleSolver:
         _check(_lib.rs_solver_multigrid_levels(self._h, out, 32, C.byref(n)))
         return [(int(out[2 * i]), int(out[2 * i + 1])) for i in range(min(n.value, 32))]
 
+    def set_learned(self, model: "LearnedModel | None", graph: "SurfaceGraph | None" = None,
+                    cheap_steps: int = 2, max_iterations: int = 0) -> None:
+        """Uses the learned preconditioner (plain as the fallback), or the plain one again."""
+        self._learned = (model, graph)  # keep both alive while the solver uses them
+        _check(_lib.rs_solver_set_learned(self._h, model._h if model else None, graph._h if graph else None,
+                                          cheap_steps, max_iterations))
+
+    def learned_counts(self) -> tuple[int, int]:
+        a, b = C.c_int64(), C.c_int64()
+        _check(_lib.rs_solver_learned_counts(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
     def build_times(self) -> dict:
         """Host seconds of the solver's set-up by phase."""
         o = np.zeros(6)
@@ -629,7 +656,8 @@ def flow_options(**kw) -> FlowOptions:
 FLOW_REPORT_KEYS = ["energy_before", "energy_after", "tau", "halvings", "gmres_area", "gmres_volume",
                     "gmres_direction", "relative_residual", "seconds", "seconds_tree", "seconds_energy",
                     "seconds_solver_build", "seconds_solve", "seconds_line_search", "seconds_projection",
-                    "accepted", "slope", "constraint_residual", "fallbacks"]
+                    "accepted", "slope", "constraint_residual", "fallbacks", "learned_solves",
+                    "learned_fallbacks"]
 
 
 class Flow:
@@ -656,6 +684,10 @@ class Flow:
         _check(_lib.rs_flow_step(self._h, rep))
         return dict(zip(FLOW_REPORT_KEYS, rep.tolist()))
 
+    def set_learned(self, model: "LearnedModel | None", cheap_steps: int = 2, max_iterations: int = 0) -> None:
+        self._learned = model
+        _check(_lib.rs_flow_set_learned(self._h, model._h if model else None, cheap_steps, max_iterations))
+
     def positions(self) -> np.ndarray:
         out = np.empty((self.n_vertices, 3))
         _check(_lib.rs_flow_positions(self._h, out.ravel()))
@@ -667,3 +699,70 @@ def copy_counters() -> tuple[int, int]:
     a, b = C.c_uint64(), C.c_uint64()
     _check(load_library().rs_copy_counters(C.byref(a), C.byref(b)))
     return a.value, b.value
+
+
+class SurfaceGraph:
+    """A surface for the learned preconditioner: one-ring adjacency and static vertex features."""
+
+    def __init__(self, faces, positions, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        faces, positions = _mesh(faces, positions)
+        self.n_vertices = len(positions)
+        h = _vp()
+        _check(_lib.rs_lgraph_create(self.ctx.handle, len(positions), len(faces), faces.ravel(),
+                                     positions.ravel(), C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.rs_lgraph_free(self._h)
+            self._h = None
+
+
+class LearnedModel:
+    """The learned preconditioner network (parameters, Adam state) on the device."""
+
+    def __init__(self, seed: int = 0, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        h = _vp()
+        _check(_lib.rs_learned_create(self.ctx.handle, seed, C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.rs_learned_free(self._h)
+            self._h = None
+
+    @property
+    def n_parameters(self) -> int:
+        n = C.c_int64()
+        _check(_lib.rs_learned_parameter_count(self._h, C.byref(n)))
+        return n.value
+
+    def get_parameters(self) -> np.ndarray:
+        w = np.empty(self.n_parameters, np.float32)
+        _check(_lib.rs_learned_get_parameters(self._h, w))
+        return w
+
+    def get_gradient(self) -> np.ndarray:
+        g = np.empty(self.n_parameters, np.float32)
+        _check(_lib.rs_learned_get_gradient(self._h, g))
+        return g
+
+    def set_parameters(self, w) -> None:
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        if w.size != self.n_parameters:
+            raise ValueError(f"expected {self.n_parameters} parameters, got {w.size}")
+        _check(_lib.rs_learned_set_parameters(self._h, w))
+
+    def apply_device(self, graph: SurfaceGraph, nb: int, r_ptr: int, y_ptr: int, z_ptr: int) -> None:
+        _check(_lib.rs_learned_apply_device(self._h, graph._h, nb, _vp(r_ptr), _vp(y_ptr), _vp(z_ptr)))
+
+    def loss_and_gradient_device(self, graph: SurfaceGraph, r_ptr: int, y_ptr: int, zt_ptr: int) -> float:
+        out = C.c_double()
+        _check(_lib.rs_learned_loss_and_gradient_device(self._h, graph._h, _vp(r_ptr), _vp(y_ptr), _vp(zt_ptr),
+                                                        C.byref(out)))
+        return out.value
+
+    def adam_step(self, lr: float = 1e-3, clip: float = 1.0) -> None:
+        _check(_lib.rs_learned_adam_step(self._h, lr, clip))

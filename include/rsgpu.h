@@ -307,7 +307,43 @@ int rs_flow_create(rs_ctx *ctx, int nv, int nf, const uint32_t *faces,
                    const double *positions_host, const rs_flow_options *opts, rs_flow **out);
 void rs_flow_free(rs_flow *f);
 
-#define RS_FLOW_REPORT_LEN 19
+/* ---------------------------------------------------------------- learned preconditioner
+ * No counterpart in the crate. A per-vertex network with one-ring message passing (three
+ * layers, hidden width 64, SiLU; BF16 weights, FP32 accumulation) maps a residual r and the
+ * cheap plain-preconditioned y = P_cheap^-1 r, with the surface's positions, normals and dual
+ * areas, to z = y + rms(y) N(.), an approximation of A'^-1 r for flexible GMRES. The plain
+ * preconditioner stays the fallback: a learned solve that does not reach the tolerance within
+ * its iteration cap is repeated with the plain one. */
+typedef struct rs_learned rs_learned; /* the network: parameters, Adam state, activations */
+typedef struct rs_lgraph rs_lgraph;   /* a surface: one-ring adjacency and static features */
+int rs_learned_create(rs_ctx *ctx, uint64_t seed, rs_learned **out);
+void rs_learned_free(rs_learned *m);
+int rs_learned_parameter_count(rs_learned *m, int64_t *count);
+int rs_learned_get_parameters(rs_learned *m, float *host);
+int rs_learned_set_parameters(rs_learned *m, const float *host);
+/* The accumulated gradient (cleared by rs_learned_adam_step and rs_learned_set_parameters). */
+int rs_learned_get_gradient(rs_learned *m, float *host);
+int rs_lgraph_create(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const double *positions_host,
+                     rs_lgraph **out);
+void rs_lgraph_free(rs_lgraph *g);
+/* z = y + rms(y) N(features(r, y)) for nb stacked 3V vectors on the device. */
+int rs_learned_apply_device(rs_learned *m, rs_lgraph *g, int nb, const double *r_dev,
+                            const double *y_dev, double *z_dev);
+/* One training sample (3V device vectors): the loss |z - zt|^2 / max(|zt|^2, |y|^2) and its gradient,
+ * added to the accumulated gradient. */
+int rs_learned_loss_and_gradient_device(rs_learned *m, rs_lgraph *g, const double *r_dev,
+                                        const double *y_dev, const double *zt_dev, double *loss);
+/* Adam on the accumulated gradient (clipped to [-clip, clip] per parameter when clip > 0),
+ * which it then clears. */
+int rs_learned_adam_step(rs_learned *m, double lr, double clip);
+/* Sets (model != NULL) or clears the learned preconditioner of a solver: cheap_steps CG steps
+ * for y, GMRES capped at max_iterations (0: the solver's cap) before the plain fallback. */
+int rs_solver_set_learned(rs_solver *s, rs_learned *model, rs_lgraph *graph, int cheap_steps,
+                          int max_iterations);
+/* Learned solves and how many of them fell back to the plain preconditioner. */
+int rs_solver_learned_counts(rs_solver *s, int64_t *solves, int64_t *fallbacks);
+
+#define RS_FLOW_REPORT_LEN 21
 /* Session::step (session.rs:724-747): one step. report[RS_FLOW_REPORT_LEN]:
  *  0 energy before, 1 energy after, 2 accepted tau (0: refused), 3 halvings,
  *  4..6 GMRES iterations of the solves (area row, volume row, direction),
@@ -315,10 +351,14 @@ void rs_flow_free(rs_flow *f);
  *  11 solver build, 12 solves, 13 line search, 14 projection, 15 accepted (1/0),
  *  16 slope g.x, 17 relative nonlinear-constraint residual after the projection,
  *  18 fallbacks: solves repeated with restart 60 and the larger iteration cap after GMRES
- *     ended above the divergence threshold (RobustHierarchical, direction.rs:269-379). */
+ *     ended above the divergence threshold (RobustHierarchical, direction.rs:269-379),
+ *  19 learned-preconditioner solves, 20 of them repeated with the plain preconditioner. */
 int rs_flow_step(rs_flow *f, double *report);
 /* The current positions (V x 3). */
 int rs_flow_positions(rs_flow *f, double *positions_host);
+/* Uses (model != NULL) or stops using a learned preconditioner in the following steps (see
+ * rs_solver_set_learned); the model must outlive its use. No counterpart in the crate. */
+int rs_flow_set_learned(rs_flow *f, rs_learned *model, int cheap_steps, int max_iterations);
 
 #ifdef __cplusplus
 }

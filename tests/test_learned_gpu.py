@@ -1,0 +1,154 @@
+"""The learned preconditioner's hand-written kernels against a plain PyTorch fp32 reference of
+the same network (CPU autograd): forward output, loss and parameter gradient of one sample,
+the Adam step, and its use as the flexible-GMRES preconditioner with the plain fallback."""
+import numpy as np
+import pytest
+
+import rs_gb300 as R
+from rs_gb300 import generators as gen
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+H, IN, OUT = 64, 13, 3
+
+
+def unpack(w):
+    """The parameter layout of rs_learned: W1s W1n b1 W2s W2n b2 W3s W3n b3 (row-major [out][in])."""
+    sizes = [(H, IN), (H, IN), (H,), (H, H), (H, H), (H,), (OUT, H), (OUT, H), (OUT,)]
+    out, k = [], 0
+    for s in sizes:
+        n = int(np.prod(s))
+        out.append(w[k:k + n].reshape(s))
+        k += n
+    assert k == len(w)
+    return out
+
+
+def one_ring(F, nv):
+    nb = [set() for _ in range(nv)]
+    for a, b, c in F.astype(np.int64):
+        for x, y in ((a, b), (b, c), (c, a)):
+            nb[x].add(y), nb[y].add(x)
+    rows = np.concatenate([[v] * len(s) for v, s in enumerate(nb)]).astype(np.int64)
+    cols = np.concatenate([sorted(s) for s in nb]).astype(np.int64)
+    deg = np.array([len(s) for s in nb], np.float32)
+    A = torch.sparse_coo_tensor(torch.tensor(np.stack([rows, cols])), torch.tensor(1.0 / deg[rows]),
+                                (nv, nv)).coalesce()
+    return A
+
+
+def static_features(P, F):
+    import rs_oracle as O
+    a, N, _ = O.face_geometry(P, F)
+    nv = len(P)
+    area = np.zeros(nv)
+    nrm = np.zeros((nv, 3))
+    Fi = F.astype(np.int64)
+    for c in range(3):
+        np.add.at(area, Fi[:, c], a / 3.0)
+        np.add.at(nrm, Fi[:, c], a[:, None] * N)
+    cen = P.mean(0)
+    R_ = np.sqrt(((P - cen) ** 2).sum(1).mean())
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    return np.concatenate([(P - cen) / R_, nrm, (area / area.mean())[:, None]], 1).astype(np.float32)
+
+
+def reference(w, stat, A, r, y, zt=None):
+    """Forward (BF16-rounded weights, fp32 arithmetic), and loss + gradient if zt is given."""
+    wt = torch.tensor(w, dtype=torch.float32).to(torch.bfloat16).to(torch.float32).requires_grad_(True)
+    W1s, W1n, b1, W2s, W2n, b2, W3s, W3n, b3 = unpack(wt)
+    rr = r.reshape(-1, 3)
+    yy = y.reshape(-1, 3)
+    sr = float(np.sqrt((r ** 2).mean()))
+    sy = float(np.sqrt((y ** 2).mean()))
+    X = torch.tensor(np.concatenate([stat, rr / sr, yy / sy], 1), dtype=torch.float32)
+    silu = torch.nn.functional.silu
+    h1 = silu(X @ W1s.T + torch.sparse.mm(A, X) @ W1n.T + b1)
+    h2 = silu(h1 @ W2s.T + torch.sparse.mm(A, h1) @ W2n.T + b2)
+    o = h2 @ W3s.T + torch.sparse.mm(A, h2) @ W3n.T + b3
+    z = torch.tensor(yy) + sy * o.double()
+    if zt is None:
+        return z.detach().numpy().ravel(), None, None
+    ztt = torch.tensor(zt.reshape(-1, 3))
+    loss = ((z - ztt) ** 2).sum() / max(float((ztt ** 2).sum()), float((torch.tensor(yy) ** 2).sum()))
+    loss.backward()
+    return z.detach().numpy().ravel(), float(loss.detach()), wt.grad.numpy().astype(np.float64)
+
+
+@pytest.fixture(scope="module")
+def setup():
+    ctx = R.Context(0)
+    P, F = gen.noisy_torus(40, 20, 1.0, 0.35, 0.004, 21)
+    g = R.SurfaceGraph(F, P, ctx)
+    m = R.LearnedModel(seed=3, ctx=ctx)
+    w = m.get_parameters()
+    rng = np.random.default_rng(5)
+    w = (w + 0.05 * rng.standard_normal(w.size)).astype(np.float32)  # an output layer far from zero
+    m.set_parameters(w)
+    return ctx, P, F, g, m, w
+
+
+def test_forward_matches_torch(setup):
+    ctx, P, F, g, m, w = setup
+    rng = np.random.default_rng(1)
+    r = rng.standard_normal(3 * len(P))
+    y = rng.standard_normal(3 * len(P)) * 0.1
+    rd, yd = torch.tensor(r).cuda(), torch.tensor(y).cuda()
+    zd = torch.zeros_like(rd)
+    torch.cuda.synchronize()
+    m.apply_device(g, 1, rd.data_ptr(), yd.data_ptr(), zd.data_ptr())
+    ctx.synchronize()
+    z_ref, _, _ = reference(w, static_features(P, F), one_ring(F, len(P)), r, y)
+    z = zd.cpu().numpy()
+    assert np.linalg.norm(z - z_ref) <= 1e-5 * np.linalg.norm(z_ref)
+
+
+def test_loss_and_gradient_match_torch(setup):
+    ctx, P, F, g, m, w = setup
+    rng = np.random.default_rng(2)
+    r = rng.standard_normal(3 * len(P))
+    y = rng.standard_normal(3 * len(P)) * 0.1
+    zt = y + 0.02 * rng.standard_normal(3 * len(P))
+    rd, yd, zd = (torch.tensor(v).cuda() for v in (r, y, zt))
+    torch.cuda.synchronize()
+    m.set_parameters(w)  # clears the accumulated gradient
+    loss = m.loss_and_gradient_device(g, rd.data_ptr(), yd.data_ptr(), zd.data_ptr())
+    _, loss_ref, grad_ref = reference(w, static_features(P, F), one_ring(F, len(P)), r, y, zt)
+    assert abs(loss - loss_ref) <= 1e-5 * abs(loss_ref)
+    grad = m.get_gradient().astype(np.float64)
+    assert np.linalg.norm(grad - grad_ref) <= 1e-3 * np.linalg.norm(grad_ref)
+    # a second sample accumulates
+    m.loss_and_gradient_device(g, rd.data_ptr(), yd.data_ptr(), zd.data_ptr())
+    assert np.linalg.norm(m.get_gradient() - 2 * grad) <= 1e-5 * np.linalg.norm(grad)
+
+
+def test_training_reduces_the_loss(setup):
+    ctx, P, F, g, m, w = setup
+    rng = np.random.default_rng(3)
+    r = rng.standard_normal(3 * len(P))
+    y = rng.standard_normal(3 * len(P)) * 0.1
+    zt = y + 0.05 * np.repeat(np.sin(3 * P[:, :1]), 3, 1).ravel()
+    rd, yd, zd = (torch.tensor(v).cuda() for v in (r, y, zt))
+    torch.cuda.synchronize()
+    m.set_parameters(w)
+    first = m.loss_and_gradient_device(g, rd.data_ptr(), yd.data_ptr(), zd.data_ptr())
+    m.adam_step(3e-3, 1.0)
+    for _ in range(60):
+        last = m.loss_and_gradient_device(g, rd.data_ptr(), yd.data_ptr(), zd.data_ptr())
+        m.adam_step(3e-3, 1.0)
+    assert last < 0.5 * first
+
+
+def test_learned_preconditioner_solves_with_fallback(setup):
+    ctx, P, F, g, m, w = setup
+    S = R.SaddleSolver(F, P, R.Exponents(), R.solver_options(tolerance=1e-6), ctx)
+    rhs = np.zeros((1, S.n))
+    rhs[0, :S.n_dofs] = np.random.default_rng(4).standard_normal(S.n_dofs)
+    y_plain, rep_plain = S.solve_many(rhs)
+    S.set_learned(m, g, cheap_steps=2, max_iterations=40)
+    y, rep = S.solve_many(rhs)
+    assert rep[0]["converged"] and rep[0]["relative_residual"] <= 1e-6
+    solves, fallbacks = S.learned_counts()
+    assert solves == 1 and fallbacks in (0, 1)
+    assert np.linalg.norm(y - y_plain) <= 1e-4 * np.linalg.norm(y_plain)

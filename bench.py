@@ -320,6 +320,27 @@ def bench_flow(args, rank, world, local):
         t_e2e = float(tt.item())
     e2e = world * args.steps / t_e2e
 
+    # the learned preconditioner on the same flow (continuing from here), plain as its fallback
+    learned = None
+    try:
+        from rs_gb300 import learned as LR
+
+        lm = R.LearnedModel(seed=1, ctx=ctx)
+        if LR.load(lm):
+            flow.set_learned(lm, cheap_steps=2, max_iterations=100)
+            lreps, t0 = [], time.perf_counter()
+            for _ in range(max(1, min(3, args.steps))):
+                lreps.append(flow.step())
+            t_l = time.perf_counter() - t0
+            flow.set_learned(None)
+            learned = {"steps_per_s": len(lreps) / t_l, "vs_plain_e2e": (len(lreps) / t_l) / (args.steps / t_e2e),
+                       "steps": len(lreps), "learned_solves": int(sum(r["learned_solves"] for r in lreps)),
+                       "fallbacks_to_plain": int(sum(r["learned_fallbacks"] for r in lreps)),
+                       "relative_residual_max": max(r["relative_residual"] for r in lreps),
+                       "setting": "y = plain preconditioner with 2 CG steps, z = y + network correction; "
+                                  "GMRES capped at 100 iterations before the plain fallback"}
+    except R.RsError as e:
+        learned = {"error": str(e)}
     # roofline: the metric's near-field kernel on the current surface (one vector per launch)
     m = R.FaceMetricTree(F, Q, R.Exponents(), R.ClusterTreeOptions(chi=0.5), ctx)
     mst = m.stats()
@@ -381,6 +402,7 @@ def bench_flow(args, rank, world, local):
         "pair_kernel": {"gflops": FLOP_PER_INTERACTION * n_int / (t_pair * 1e-3) / 1e9 if t_pair else None,
                         "interactions": n_int, "ms": t_pair,
                         "frac": (FLOP_PER_INTERACTION * n_int / (t_pair * 1e-3) / 1e12 / peak) if t_pair else None},
+        "learned_preconditioner": learned,
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }

@@ -311,7 +311,7 @@ __device__ __forceinline__ void pair_diff(const float4 &ah, const float4 &al, co
 // error (leaf offsets can be large next to |v| in a stretched leaf). alpha_S = N_S.(X_S - X_L)
 // is a float pair from the FP64 refit.
 template <bool GRAD, bool FAST>
-__global__ void __launch_bounds__(128) bh_pair_kernel(BhDev d, Pow pw) {
+__global__ void __launch_bounds__(128, 5) bh_pair_kernel(BhDev d, Pow pw) {
   const int lane = threadIdx.x & 31;
   const int s = lane & 7;
   const int j = lane >> 3;
@@ -481,12 +481,15 @@ __global__ void __launch_bounds__(128) bh_pair_kernel(BhDev d, Pow pw) {
 
 // b_C, u_C per node over the transposed lumped lists (barnes_hut.rs:505-520): one warp per
 // node, lanes strided over the entries (Kahan), then a fixed shuffle tree.
-__global__ void node_sums_kernel(BhDev d) {
-  int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// Node terms summed per chunk of a node's transposed lumped list (one warp per chunk), then
+// per node over its chunks in order.
+__global__ void node_partial_kernel(BhDev d) {
+  int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
-  if (n >= d.n_nodes) return;
+  if (w >= d.n_nchunks) return;
+  const uint4 ch = d.nchunk[w];
   Kahan b, u0, u1, u2;
-  for (uint32_t e = d.lumped_t_off[n] + lane; e < d.lumped_t_off[n + 1]; e += 32) {
+  for (uint32_t e = ch.y + lane; e < ch.z; e += 32) {
     float4 t = d.node_term[d.lumped_t[e]];
     b.add(t.x), u0.add(t.y), u1.add(t.z), u2.add(t.w);
   }
@@ -498,7 +501,18 @@ __global__ void node_sums_kernel(BhDev d) {
     r2 += __shfl_xor_sync(0xffffffffu, r2, m);
     r3 += __shfl_xor_sync(0xffffffffu, r3, m);
   }
-  if (lane == 0) d.node_sum[n] = make_float4(r0, r1, r2, r3);
+  if (lane == 0) d.npart[w] = make_float4(r0, r1, r2, r3);
+}
+
+__global__ void node_sums_kernel(BhDev d) {
+  int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= d.n_nodes) return;
+  float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (uint32_t c = d.nchunk_off[n]; c < d.nchunk_off[n + 1]; ++c) {
+    const float4 p = d.npart[c];
+    s.x += p.x, s.y += p.y, s.z += p.z, s.w += p.w;
+  }
+  d.node_sum[n] = s;
 }
 
 // Downward pass per leaf along its root -> leaf chain (barnes_hut.rs:521-538), in FP64 (about
@@ -522,21 +536,21 @@ __global__ void downward_kernel(BhDev d) {
   d.leaf_bu[k] = make_float4((float)beta, (float)U0, (float)U1, (float)U2);
 }
 
-// Per leaf (one warp): own + partner (transposed exact lists) + cluster part
-// (barnes_hut.rs:539-567), written by face id. Lanes stride over the leaf's transposed exact
-// entries, each summing the leaf's (<= 8) partner slots of an entry into 8 x 4 registers; a
-// transposing reduce over the 32 lanes leaves lane 4 t + c with component c of face t.
-__global__ void final_kernel(BhDev d) {
-  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+// Partner sums per chunk of a leaf's transposed exact list (one warp per chunk): lanes stride
+// over the chunk's entries, each summing the leaf's (<= 8) partner slots of an entry into
+// 8 x 4 registers; a transposing reduce over the 32 lanes leaves lane 4 t + c with component c
+// of face t, written to the chunk's 32 partial sums.
+__global__ void final_partial_kernel(BhDev d) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (k >= d.n_leaves) return;
-  const uint32_t leaf = d.leaves[k];
-  const uint32_t s0 = d.node_start[leaf];
-  const uint32_t ns = d.node_end[leaf] - s0;
+  if (w >= d.n_fchunks) return;
+  const uint4 ch = d.fchunk[w];
+  const uint32_t leaf = d.leaves[ch.x];
+  const uint32_t ns = d.node_end[leaf] - d.node_start[leaf];
   float acc[32];
 #pragma unroll
   for (int i = 0; i < 32; ++i) acc[i] = 0.f;
-  for (uint32_t e = d.exact_t_off[k] + lane; e < d.exact_t_off[k + 1]; e += 32) {
+  for (uint32_t e = ch.y + lane; e < ch.z; e += 32) {
     const float4 *pp = d.partner + d.partner_off[d.exact_t[e]];
 #pragma unroll
     for (int t = 0; t < 8; ++t)
@@ -561,26 +575,38 @@ __global__ void final_kernel(BhDev d) {
 #pragma unroll
   for (int i = 0; i < 2; ++i)
     r2[i] = (b1 ? r4[2 + i] : r4[i]) + __shfl_xor_sync(0xffffffffu, b1 ? r4[i] : r4[2 + i], 2);
-  float part = (b0 ? r2[1] : r2[0]) + __shfl_xor_sync(0xffffffffu, b0 ? r2[0] : r2[1], 1);
+  d.fpart[32 * (size_t)w + lane] = (b0 ? r2[1] : r2[0]) + __shfl_xor_sync(0xffffffffu, b0 ? r2[0] : r2[1], 1);
+}
+
+// Per leaf (one warp, lane 4 t + c = component c of face t): own + partner (the leaf's chunks in
+// order) + cluster part (barnes_hut.rs:539-567), written by face id.
+__global__ void final_kernel(BhDev d) {
+  const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (k >= d.n_leaves) return;
+  const uint32_t leaf = d.leaves[k];
+  const uint32_t s0 = d.node_start[leaf];
+  const uint32_t ns = d.node_end[leaf] - s0;
   const uint32_t t = lane >> 2, c = lane & 3;
-  if (t < ns) {
-    const uint32_t p = s0 + t;
-    const float *ow = reinterpret_cast<const float *>(d.own);
-    float own = 0.f, ownn = 0.f;
-    for (uint32_t i = d.item_off[k]; i < d.item_off[k + 1]; ++i) {  // 64 floats per item
-      own += ow[64 * (size_t)i + 8 * t + c];
-      ownn += ow[64 * (size_t)i + 8 * t + 4 + c];
-    }
-    const float4 bu = d.leaf_bu[k];
-    const float4 xa = d.fxa[p];  // offset X_T - X_leaf and a_T
-    float cl;
-    if (c == 0) cl = bu.x + (bu.y * xa.x + bu.z * xa.y + bu.w * xa.z);
-    else cl = xa.w * (c == 1 ? bu.y : (c == 2 ? bu.z : bu.w));
-    const uint32_t f = d.order[p];
-    float *out = reinterpret_cast<float *>(d.partials);
-    out[8 * (size_t)f + c] = (own + part) + cl;
-    out[8 * (size_t)f + 4 + c] = ownn;
+  if (t >= ns) return;
+  float part = 0.f;
+  for (uint32_t ch = d.fchunk_off[k]; ch < d.fchunk_off[k + 1]; ++ch) part += d.fpart[32 * (size_t)ch + lane];
+  const uint32_t p = s0 + t;
+  const float *ow = reinterpret_cast<const float *>(d.own);
+  float own = 0.f, ownn = 0.f;
+  for (uint32_t i = d.item_off[k]; i < d.item_off[k + 1]; ++i) {  // 64 floats per item
+    own += ow[64 * (size_t)i + 8 * t + c];
+    ownn += ow[64 * (size_t)i + 8 * t + 4 + c];
   }
+  const float4 bu = d.leaf_bu[k];
+  const float4 xa = d.fxa[p];  // offset X_T - X_leaf and a_T
+  float cl;
+  if (c == 0) cl = bu.x + (bu.y * xa.x + bu.z * xa.y + bu.w * xa.z);
+  else cl = xa.w * (c == 1 ? bu.y : (c == 2 ? bu.z : bu.w));
+  const uint32_t f = d.order[p];
+  float *out = reinterpret_cast<float *>(d.partials);
+  out[8 * (size_t)f + c] = (own + part) + cl;
+  out[8 * (size_t)f + 4 + c] = ownn;
 }
 
 // Pull-back to the vertices (face_pull_back, RS/src/geometry.rs:87-110, summed over the
@@ -688,6 +714,11 @@ struct rs_bh {
   DevBuf<double> box, radius;
   DevBuf<uint32_t> lumped_off, lumped, exact_off, exact, partner_off, lumped_t_off, lumped_t,
       exact_t_off, exact_t;
+  DevBuf<uint4> fchunk, nchunk;
+  DevBuf<uint32_t> fchunk_off, nchunk_off;
+  DevBuf<float> fpart;
+  DevBuf<float4> npart;
+  size_t n_fchunks = 0, n_nchunks = 0;
   // per evaluation
   DevBuf<double> pos;
   DevBuf<float4> fxa, fnn, fol, fnl, own, node_term, partner, node_sum, leaf_bu, partials;
@@ -711,6 +742,9 @@ struct rs_bh {
     d.lumped_off = lumped_off.p, d.lumped = lumped.p, d.exact_off = exact_off.p, d.exact = exact.p;
     d.partner_off = partner_off.p, d.lumped_t_off = lumped_t_off.p, d.lumped_t = lumped_t.p;
     d.exact_t_off = exact_t_off.p, d.exact_t = exact_t.p;
+    d.fchunk = fchunk.p, d.nchunk = nchunk.p, d.fchunk_off = fchunk_off.p, d.nchunk_off = nchunk_off.p;
+    d.fpart = fpart.p, d.npart = npart.p;
+    d.n_fchunks = (int)n_fchunks, d.n_nchunks = (int)n_nchunks;
     d.n_vertices = nv, d.n_faces = nf, d.n_nodes = (int)tree.n_nodes();
     d.n_leaves = (int)tree.leaves.size();
     d.fxa = fxa.p, d.fnn = fnn.p, d.ncA = ncA.p, d.nmom = nmom.p, d.refit_count = refit_count.p;
@@ -871,6 +905,36 @@ void finish_lists(rs_bh *h, const std::vector<uint32_t> &lo, const std::vector<u
     }
     transpose(key.p, h->n_exact, nl, h->exact_t_off, h->exact_t, "exact_t");
   }
+  // Chunks of the transposed lists: at most 256 exact entries (partner slots of a leaf) or 1024
+  // lumped entries (node terms of a node) per warp; every leaf / node has at least one chunk.
+  {
+    std::vector<uint32_t> et(nl + 1), lt(nn + 1);
+    h->exact_t_off.download(et.data(), nl + 1, s);
+    h->lumped_t_off.download(lt.data(), nn + 1, s);
+    RSG_CUDA("upload", cudaStreamSynchronize(s));
+    auto chunks = [](const std::vector<uint32_t> &off, size_t m, uint32_t len, std::vector<uint4> &ch,
+                     std::vector<uint32_t> &choff) {
+      choff.assign(m + 1, 0);
+      for (size_t k = 0; k < m; ++k) {
+        uint32_t x = off[k];
+        do {
+          uint32_t y = std::min(off[k + 1], x + len);
+          ch.push_back(make_uint4((uint32_t)k, x, y, 0));
+          x = y;
+        } while (x < off[k + 1]);
+        choff[k + 1] = (uint32_t)ch.size();
+      }
+    };
+    std::vector<uint4> fc, nc;
+    std::vector<uint32_t> fco, nco;
+    chunks(et, nl, 256, fc, fco);
+    chunks(lt, nn, 1024, nc, nco);
+    h->n_fchunks = fc.size(), h->n_nchunks = nc.size();
+    upload_vec(h->fchunk, fc, s), upload_vec(h->fchunk_off, fco, s);
+    upload_vec(h->nchunk, nc, s), upload_vec(h->nchunk_off, nco, s);
+    h->fpart.alloc(32 * fc.size());
+    h->npart.alloc(nc.size());
+  }
   // Work items: every leaf's lumped and exact ranges split into slices of at most ~512
   // lumped / ~128 exact entries (a few leaves of a degenerate tree open every other leaf);
   // warps take them from an atomic ticket, most work first.
@@ -1020,7 +1084,9 @@ void evaluate(rs_bh *h, const Pow &pw, bool fast, bool grad, double *energy_dev,
   P.end(s);
   if (grad) {
     P.begin(s, "node_sums");
-    node_sums_kernel<<<blocks(nn * 32, 256), 256, 0, s>>>(d);
+    node_partial_kernel<<<blocks((size_t)h->n_nchunks * 32, 256), 256, 0, s>>>(d);
+    RSG_LAUNCHED(h->ctx, "node_sums");
+    node_sums_kernel<<<blocks(nn, 256), 256, 0, s>>>(d);
     RSG_LAUNCHED(h->ctx, "node_sums");
     P.end(s);
     P.begin(s, "downward");
@@ -1028,6 +1094,8 @@ void evaluate(rs_bh *h, const Pow &pw, bool fast, bool grad, double *energy_dev,
     RSG_LAUNCHED(h->ctx, "downward");
     P.end(s);
     P.begin(s, "final");
+    final_partial_kernel<<<blocks((size_t)h->n_fchunks * 32, 256), 256, 0, s>>>(d);
+    RSG_LAUNCHED(h->ctx, "final");
     final_kernel<<<blocks(nl * 32, 256), 256, 0, s>>>(d);
     RSG_LAUNCHED(h->ctx, "final");
     P.end(s);

@@ -18,6 +18,14 @@
 namespace rsg {
 
 struct BhDev {
+  // chunks of the transposed lists (long lists of degenerate leaves / big nodes are split):
+  // fchunk = (leaf ordinal, exact_t begin, end, -), fchunk_off per leaf; nchunk likewise for
+  // the transposed lumped list per node; fpart / npart hold the chunks' partial sums
+  const uint4 *fchunk, *nchunk;
+  const uint32_t *fchunk_off, *nchunk_off;
+  float *fpart;
+  float4 *npart;
+  int n_fchunks, n_nchunks;
   // topology (fixed per step)
   const uint32_t *faces;       // 3F, original face order
   const uint32_t *order;       // F: BVH position -> face

@@ -203,7 +203,7 @@ __global__ void hm_far_kernel(HDev d) {
 // that cancel to a second-order result, and the output stage (M^T, a discrete divergence)
 // cancels once more, so plain FP32 sums of H~a m and H~(a m) would lose about four digits.
 template <int KIND, int CC>
-__global__ void __launch_bounds__(128) hm_rows_kernel(HDev d, int c0) {
+__global__ void __launch_bounds__(128, 5) hm_rows_kernel(HDev d, int c0) {
   __shared__ float2 red[4][32][CC];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;

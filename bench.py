@@ -212,7 +212,7 @@ NEAR_FLOP_PER_ENTRY = 44
 # Operator applications per step assumed by the CPU reference arm (which has no preconditioned
 # solver of its own): the GPU arm's mean on this workload, GMRES iterations of the three
 # right-hand sides.
-REFERENCE_ITERATIONS_PER_STEP = 150
+REFERENCE_ITERATIONS_PER_STEP = 188
 
 
 def flow_options(R):

@@ -194,7 +194,7 @@ __global__ void hm_far_kernel(HDev d) {
 // element p. One warp per item; the leaf's ns rows (3 to 8) each take G = 32 / ns lanes
 // (lane = r G + j), lane j of a row taking every G-th column, so that small leaves keep the
 // warp busy. The kernel values of a column are evaluated once per row and applied to the CC
-// channels. m_p - m_q is formed from the float pairs and split exactly, each product
+// channels. m_p - m_q is formed exactly from the float pairs (their hi parts share a grid), each product
 // w (m_p - m_q) is split exactly too, and the terms are summed as float pairs: the high parts
 // by error-free additions (two_sum), whose errors gather with the low parts in a second
 // float. (Kahan summation would leave an error of eps times each lane's partial sum, a
@@ -249,12 +249,11 @@ __global__ void __launch_bounds__(128, 5) hm_rows_kernel(HDev d, int c0) {
           const int c = 2 * c2 + e;
           const float qhv = e ? v.z : v.x, qlv = e ? v.w : v.y;
           const float wk = (KIND == FACE && c >= 9) ? w1 : w0;
-          // w (m_p - m_q) = pr + pe + w dl exactly up to eps^2 terms: mh_p - mh_q = dh + de
-          // (two_sum), dl = ml_p - ml_q + de, w dh = pr + pe (FMA); the low parts enter the
-          // Kahan compensation, so no rounding that depends on the input reaches the sum
-          float dh, de;
-          two_sum(mh[c], -qhv, dh, de);
-          const float dl = (ml[c] - qlv) + de;
+          // w (m_p - m_q) = pr + pe + w dl up to eps^2 terms: dh = mh_p - mh_q is exact (the
+          // hi parts share a grid), dl = ml_p - ml_q, w dh = pr + pe (FMA), so no rounding that
+          // depends on the input reaches the sum above eps^2
+          const float dh = mh[c] - qhv;
+          const float dl = ml[c] - qlv;
           const float pr = wk * dh;
           const float lo = fmaf(wk, dl, fmaf(wk, dh, -pr));
           float sn, se;
@@ -344,32 +343,55 @@ struct FaceOps {
   int nv, nf;
 };
 
-__device__ __forceinline__ float2 split_pair(double v) {
-  const float h = (float)v;
-  return make_float2(h, (float)(v - (double)h));
+// Channel values as float pairs on a common grid per channel: hi = k Q with Q = 2^(e - 22) for
+// the channel's largest magnitude 2^e <= max < 2^(e+1), so |k| < 2^24 and the difference of two
+// hi values is exact in FP32; lo = v - hi (|lo| <= Q / 2) rounded to FP32. The near field then
+// forms m_p - m_q with two plain subtractions. qmax holds the channels' largest |v| as the bit
+// patterns of non-negative doubles (ordered like the integers).
+__device__ __forceinline__ float2 split_q(double v, unsigned long long qbits) {
+  const double mx = __longlong_as_double((long long)qbits);
+  if (!(mx > 0.0)) return make_float2(0.f, 0.f);
+  const double Q = ldexp(1.0, ilogb(mx) - 22);
+  const double hi = rint(v / Q) * Q;
+  return make_float2((float)hi, (float)(v - hi));
+}
+
+// pass 0: the channels' largest magnitudes (a warp maximum, then one atomic per warp and
+// channel; every lane of the warp takes part, `act` false contributing 0); pass 1: the split
+// values
+__device__ __forceinline__ void emit(float2 *mp, int c, double v, unsigned long long *qmax, int pass, bool act) {
+  if (pass == 0) {
+    double a = act ? fabs(v) : 0.0;
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) a = fmax(a, __shfl_xor_sync(0xffffffffu, a, m));
+    if ((threadIdx.x & 31) == 0 && a > 0.0) atomicMax(qmax + c, (unsigned long long)__double_as_longlong(a));
+  } else if (act) {
+    mp[c] = split_q(v, qmax[c]);
+  }
 }
 
 // m per face in BVH order (FaceMetricTree::product, hierarchical.rs:711-746), in FP64 and
 // stored as float pairs; vector q owns channels 12q + (3k + r) = sum_c x[3 t_c + k] g_c[r]
 // (gradient) and 12q + 9 + k = (x_0 + x_1 + x_2)/3 for axis k (average).
 __global__ void face_m_kernel(FaceOps o, const double *__restrict__ xs, size_t ldx, int nb, int C,
-                              float2 *m) {
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= o.nf) return;
-  uint32_t f = o.order[p];
+                              float2 *m, unsigned long long *qmax, int pass) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool act = p < o.nf;  // the whole warp runs the loops (warp maxima in pass 0)
+  const uint32_t f = act ? o.order[p] : 0;
   const uint32_t *t = o.faces + 3 * (size_t)f;
   const double *g = o.g + 9 * (size_t)f;
-  float2 *mp = m + (size_t)p * C;
+  float2 *mp = m + (size_t)(act ? p : 0) * C;
   for (int q = 0; q < nb; ++q) {
     const double *x = xs + q * ldx;
     for (int k = 0; k < 3; ++k) {
       const double x0 = x[3 * (size_t)t[0] + k], x1 = x[3 * (size_t)t[1] + k], x2 = x[3 * (size_t)t[2] + k];
       for (int r = 0; r < 3; ++r)
-        mp[12 * q + 3 * k + r] = split_pair(x0 * g[r] + x1 * g[3 + r] + x2 * g[6 + r]);
-      mp[12 * q + 9 + k] = split_pair(((x0 + x1) + x2) / 3.0);
+        emit(mp, 12 * q + 3 * k + r, x0 * g[r] + x1 * g[3 + r] + x2 * g[6 + r], qmax, pass, act);
+      emit(mp, 12 * q + 9 + k, ((x0 + x1) + x2) / 3.0, qmax, pass, act);
     }
   }
-  for (int c = 12 * nb; c < C; ++c) mp[c] = make_float2(0.f, 0.f);
+  if (pass == 1 && act)
+    for (int c = 12 * nb; c < C; ++c) mp[c] = make_float2(0.f, 0.f);
 }
 
 // y_v = 2 sum_{S ni v} a_S (w_hi g_c . z_hi + w_lo z_lo / 3) in FP64 (hierarchical.rs:779-811).
@@ -404,14 +426,15 @@ __global__ void face_gather_kernel(FaceOps o, const float2 *__restrict__ z, int 
 // psi channels of the vertex operator: m = x per axis (psi = a x in the upward sums), vector q
 // at channels 4q + k (4q + 3 is padding).
 __global__ void vertex_m_kernel(const uint32_t *order, const double *__restrict__ xs, size_t ldx,
-                                int nv, int nb, int C, float2 *m) {
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= nv) return;
-  uint32_t v = order[p];
-  float2 *mp = m + (size_t)p * C;
-  for (int c = 0; c < C; ++c) mp[c] = make_float2(0.f, 0.f);
+                                int nv, int nb, int C, float2 *m, unsigned long long *qmax, int pass) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool act = p < nv;  // the whole warp runs the loops (warp maxima in pass 0)
+  const uint32_t v = act ? order[p] : 0;
+  float2 *mp = m + (size_t)(act ? p : 0) * C;
+  if (pass == 1 && act)
+    for (int c = 0; c < C; ++c) mp[c] = make_float2(0.f, 0.f);
   for (int q = 0; q < nb; ++q)
-    for (int k = 0; k < 3; ++k) mp[4 * q + k] = split_pair(xs[q * ldx + 3 * (size_t)v + k]);
+    for (int k = 0; k < 3; ++k) emit(mp, 4 * q + k, xs[q * ldx + 3 * (size_t)v + k], qmax, pass, act);
 }
 
 // y = 2 a (H~a x - H~(a x)) = 2 a z (hierarchical.rs:1330-1343).
@@ -474,6 +497,7 @@ struct HMat {
   DevBuf<float4> xh, xl, nrm;
   DevBuf<double> up, farx;
   DevBuf<float2> part, m, z;
+  DevBuf<unsigned long long> qmax;  // per channel: largest |m| (see split_q)
   int pw_mode = 0, pw_k = 0;
   Profiler prof;
 
@@ -811,8 +835,12 @@ void rsg::metric_apply_strided(rs_metric *M, double w_hi, double w_lo, int nb, c
     int CC = 12 * k;
     M->h.reserve(CC);
     M->h.prof.begin(s, "metric_m");
-    face_m_kernel<<<nblk(M->nf, 256), 256, 0, s>>>(M->ops(), xs + q0 * ldx, ldx, k, CC, M->h.m.p);
-    RSG_LAUNCHED(M->h.ctx, "face_m");
+    if (M->h.qmax.n < 64) M->h.qmax.alloc(64);
+    RSG_CUDA("product", cudaMemsetAsync(M->h.qmax.p, 0, CC * sizeof(unsigned long long), s));
+    for (int pass = 0; pass < 2; ++pass) {
+      face_m_kernel<<<nblk(M->nf, 256), 256, 0, s>>>(M->ops(), xs + q0 * ldx, ldx, k, CC, M->h.m.p, M->h.qmax.p, pass);
+      RSG_LAUNCHED(M->h.ctx, "face_m");
+    }
     M->h.prof.end(s);
     M->h.product(k);
     M->h.prof.begin(s, "metric_gather");
@@ -831,8 +859,13 @@ void rsg::vfrac_apply_strided(rs_vfrac *V, double scale, int nb, const double *x
     int k = std::min(3, nb - q0);
     int CC = 4 * k;  // 3 k channels padded to a multiple of 4
     V->h.reserve(CC);
-    vertex_m_kernel<<<nblk(V->nv, 256), 256, 0, s>>>(V->order.p, xs + q0 * ldx, ldx, V->nv, k, CC, V->h.m.p);
-    RSG_LAUNCHED(V->h.ctx, "vertex_m");
+    if (V->h.qmax.n < 64) V->h.qmax.alloc(64);
+    RSG_CUDA("product", cudaMemsetAsync(V->h.qmax.p, 0, CC * sizeof(unsigned long long), s));
+    for (int pass = 0; pass < 2; ++pass) {
+      vertex_m_kernel<<<nblk(V->nv, 256), 256, 0, s>>>(V->order.p, xs + q0 * ldx, ldx, V->nv, k, CC, V->h.m.p,
+                                                       V->h.qmax.p, pass);
+      RSG_LAUNCHED(V->h.ctx, "vertex_m");
+    }
     V->h.product(k);
     vertex_out_kernel<<<nblk(V->nv, 256), 256, 0, s>>>(V->order.p, V->h.xh.p, V->h.z.p, V->nv, k, CC,
                                                        scale, ys + q0 * ldy, ldy);
@@ -1041,7 +1074,7 @@ inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 size_t noalloc_bytes(const HMat &h, int C) {
   size_t nn = h.tree.n_nodes();
   return 2 * align256(nn * C * sizeof(double)) + 2 * align256(h.n_el * C * sizeof(float2)) +
-         align256(std::max<size_t>(h.n_items, 1) * 8 * C * sizeof(float2));
+         align256(std::max<size_t>(h.n_items, 1) * 8 * C * sizeof(float2)) + align256(64 * sizeof(unsigned long long));
 }
 
 HDev noalloc_dev(const HMat &h, int C, unsigned char *base) {
@@ -1060,16 +1093,24 @@ HDev noalloc_dev(const HMat &h, int C, unsigned char *base) {
   return d;
 }
 
+// the per-channel magnitudes of the no-alloc product, after the buffers of noalloc_dev
+unsigned long long *noalloc_qmax(const HMat &h, int C, unsigned char *base) {
+  return reinterpret_cast<unsigned long long *>(base + noalloc_bytes(h, C) - align256(64 * sizeof(unsigned long long)));
+}
+
 // The face product of one group of k <= 3 vectors on the given scratch (the kernels and order
 // of HMat::product_cc and metric_apply_strided).
 template <int CC>
-void noalloc_face_group(rs_metric *M, const HDev &d, int k, const double *xs, size_t ldx, double w_hi,
-                        double w_lo, double *ys, size_t ldy) {
+void noalloc_face_group(rs_metric *M, const HDev &d, unsigned long long *qmax, int k, const double *xs, size_t ldx,
+                        double w_hi, double w_lo, double *ys, size_t ldy) {
   HMat &h = M->h;
   cudaStream_t s = h.st();
   float2 *m = const_cast<float2 *>(d.m);
-  face_m_kernel<<<nblk(M->nf, 256), 256, 0, s>>>(M->ops(), xs, ldx, k, CC, m);
-  RSG_LAUNCHED(h.ctx, "face_m");
+  RSG_CUDA("product", cudaMemsetAsync(qmax, 0, CC * sizeof(unsigned long long), s));
+  for (int pass = 0; pass < 2; ++pass) {
+    face_m_kernel<<<nblk(M->nf, 256), 256, 0, s>>>(M->ops(), xs, ldx, k, CC, m, qmax, pass);
+    RSG_LAUNCHED(h.ctx, "face_m");
+  }
   h.upward_far<FACE_CH, CC>(d);
   for (int q = 0; q < k; ++q) {
     hm_rows_kernel<FACE, 12><<<nblk(h.n_items * 32, 128), 128, 0, s>>>(d, 12 * q);
@@ -1101,9 +1142,10 @@ extern "C" int rs_metric_apply_device_noalloc(rs_metric *M, double w_hi, double 
     for (int q0 = 0; q0 < nb; q0 += 3) {
       const int k = std::min(3, nb - q0);
       HDev d = noalloc_dev(M->h, 12 * k, base);
-      if (k == 1) noalloc_face_group<12>(M, d, 1, xs_dev + q0 * ld, ld, w_hi, w_lo, ys_dev + q0 * ld, ld);
-      else if (k == 2) noalloc_face_group<24>(M, d, 2, xs_dev + q0 * ld, ld, w_hi, w_lo, ys_dev + q0 * ld, ld);
-      else noalloc_face_group<36>(M, d, 3, xs_dev + q0 * ld, ld, w_hi, w_lo, ys_dev + q0 * ld, ld);
+      unsigned long long *qm = noalloc_qmax(M->h, 12 * k, base);
+      if (k == 1) noalloc_face_group<12>(M, d, qm, 1, xs_dev + q0 * ld, ld, w_hi, w_lo, ys_dev + q0 * ld, ld);
+      else if (k == 2) noalloc_face_group<24>(M, d, qm, 2, xs_dev + q0 * ld, ld, w_hi, w_lo, ys_dev + q0 * ld, ld);
+      else noalloc_face_group<36>(M, d, qm, 3, xs_dev + q0 * ld, ld, w_hi, w_lo, ys_dev + q0 * ld, ld);
     }
   });
 }

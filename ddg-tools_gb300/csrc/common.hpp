@@ -116,7 +116,7 @@ struct rs_ctx {
   int sm_count = 0;
   int cc_major = 0, cc_minor = 0;
   std::string name;
-  int64_t launches = 0;
+  std::atomic<int64_t> launches{0};  // kernel launches (host threads may build concurrently)
   // Pinned staging buffer for host <-> device copies of the entry points with host arrays.
   void *pinned = nullptr;
   size_t pinned_bytes = 0;

@@ -20,6 +20,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "common.hpp"
@@ -219,24 +220,36 @@ int rs_flow_step(rs_flow *F, double *report) {
     const uint32_t *faces = F->faces.data();
     const size_t nd = 3 * (size_t)nv;
     double rep[RS_FLOW_REPORT_LEN] = {0};
-    // 1. energy and differential
+    // 1. trees: the BH tree and lists here, the solver's set-up (mostly host work: block trees,
+    // far coefficients, multigrid hierarchy) on a second host thread at the same time; both
+    // enqueue on the context's stream, on disjoint buffers
     auto t = clk::now();
     Owned<rs_bh> bh;
     bh.del = rs_bh_free;
-    check(rs_bh_build(ctx, nv, nf, faces, F->pos.data(), F->o.theta, F->o.leaf_size, &bh.p), "flow (tree)");
-    rep[9] = since(t);
-    t = clk::now();
     Owned<rs_solver> sv;
     sv.del = rs_solver_free;
-    check(rs_solver_build(ctx, nv, nf, faces, F->pos.data(), F->o.alpha, F->o.beta, &F->o.solver, &sv.p),
-          "flow (solver)");
     Owned<rs_lgraph> lg;
     lg.del = rs_lgraph_free;
-    if (F->lmodel) {
-      check(rs_lgraph_create(ctx, nv, nf, faces, F->pos.data(), &lg.p), "flow (solver)");
-      check(rs_solver_set_learned(sv.p, F->lmodel, lg.p, F->l_cheap, F->l_cap), "flow (solver)");
-    }
-    rep[11] = since(t);
+    int w_code = 0;
+    std::string w_kind, w_op, w_msg;
+    double t_solver = 0.0;
+    std::thread worker([&] {
+      TrustedTopology trusted_here;
+      auto t0 = clk::now();
+      int c = rs_solver_build(ctx, nv, nf, faces, F->pos.data(), F->o.alpha, F->o.beta, &F->o.solver, &sv.p);
+      if (c == 0 && F->lmodel) {
+        c = rs_lgraph_create(ctx, nv, nf, faces, F->pos.data(), &lg.p);
+        if (c == 0) c = rs_solver_set_learned(sv.p, F->lmodel, lg.p, F->l_cheap, F->l_cap);
+      }
+      if (c != 0) w_code = c, w_kind = rs_last_error_kind(), w_op = rs_last_error_operation(), w_msg = rs_last_error();
+      t_solver = since(t0);
+    });
+    const int b_code = rs_bh_build(ctx, nv, nf, faces, F->pos.data(), F->o.theta, F->o.leaf_size, &bh.p);
+    rep[9] = since(t);
+    worker.join();
+    check(b_code, "flow (tree)");
+    if (w_code != 0) fail(w_code, w_kind.c_str(), w_op.c_str(), w_msg);
+    rep[11] = t_solver;
     int64_t ndof = 0, nq = 0;
     check(rs_solver_dims(sv.p, &ndof, &nq), "flow");
     const size_t n = nd + (size_t)nq;

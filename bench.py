@@ -341,6 +341,25 @@ def bench_flow(args, rank, world, local):
                                   "GMRES capped at 100 iterations before the plain fallback"}
     except R.RsError as e:
         learned = {"error": str(e)}
+    # phases of one step's solve (three right-hand sides) on the current surface
+    solve_phases = None
+    try:
+        S = R.SaddleSolver(F, Q, R.Exponents(), R.solver_options(chi=0.5, restart=30, tolerance=1e-6,
+                                                                  max_iterations=300), ctx)
+        bh0 = R.BhTree.build(F, Q, R.BhOptions(theta, 8), ctx)
+        _, dE = bh0.energy_and_differential(R.Exponents())
+        from rs_gb300 import learned as LR
+
+        ga, gv = LR._constraint_gradients(Q, F)
+        rhs = np.zeros((3, S.n))
+        rhs[0, :S.n_dofs], rhs[1, :S.n_dofs], rhs[2, :S.n_dofs] = ga.ravel(), gv.ravel(), dE.ravel()
+        solve_phases = {k: round(v, 2) for k, v in S.profile(rhs).items()}
+        solve_phases["iterations"] = [len(S.history(q)[0]) for q in range(3)]
+        solve_phases["multigrid_levels"] = S.multigrid_levels()
+        solve_phases["build_s"] = {k: round(v, 4) for k, v in S.build_times().items()}
+        del S, bh0
+    except R.RsError as e:
+        solve_phases = {"error": str(e)}
     # roofline: the metric's near-field kernel on the current surface (one vector per launch)
     m = R.FaceMetricTree(F, Q, R.Exponents(), R.ClusterTreeOptions(chi=0.5), ctx)
     mst = m.stats()
@@ -402,6 +421,7 @@ def bench_flow(args, rank, world, local):
         "pair_kernel": {"gflops": FLOP_PER_INTERACTION * n_int / (t_pair * 1e-3) / 1e9 if t_pair else None,
                         "interactions": n_int, "ms": t_pair,
                         "frac": (FLOP_PER_INTERACTION * n_int / (t_pair * 1e-3) / 1e12 / peak) if t_pair else None},
+        "solve_phases_ms": solve_phases,
         "learned_preconditioner": learned,
         "gpu_launches": launches,
         "clocks": clk.summary(),

@@ -9,6 +9,12 @@
 
 namespace rsg {
 
+// Storage and arithmetic type of the device hierarchy and its conjugate-gradient vectors: FP32.
+// The multigrid solve is a preconditioner inside flexible FP64 GMRES, so its rounding only
+// perturbs the preconditioner; GB300 runs FP32 at many times its FP64 rate. Dot products
+// are added up in FP64 across blocks.
+using mgreal = float;
+
 struct Csr {
   int n = 0, m = 0;  // rows, columns
   std::vector<int> ptr, col;
@@ -28,31 +34,37 @@ AmgHost amg_setup(const Csr &A, int coarse_max = 300, int max_levels = 12);
 
 // The hierarchy on the device and its V-cycle for C interleaved columns per row
 // (x[row * C + c]): pre- and post-smoothing by `sweeps` damped Jacobi steps, dense coarse solve.
+// Each sparse product gives a row to a group of 1-32 lanes sized to the matrix's mean row length
+// (the coarse operators of smoothed aggregation have 40-70 nonzeros per row on a few hundred
+// rows, where one thread per row would leave the GPU idle behind long serial loops).
 struct AmgDevice {
   struct Level {
     int n = 0;
+    int tpr_a = 1, tpr_r = 1, tpr_p = 1;  // lanes per row of A, R (rows of level l+1) and P
     DevBuf<int> ap, ac, pp, pc, rp, rc;
-    DevBuf<double> av, pv, rv, dinv;
-    DevBuf<double> x, b, r, t;  // C columns each
+    DevBuf<mgreal> av, pv, rv, dinv;
+    DevBuf<mgreal> x, b, r, t;  // C columns each
   };
   std::vector<Level> L;
-  DevBuf<double> cinv;
+  DevBuf<mgreal> cinv;
   int C = 0, sweeps = 2;
   void upload(const AmgHost &h, cudaStream_t s);
   void reserve(int C_);
   // x = V-cycle(b) on level 0; b and x are n_0 x C device arrays (x overwritten).
-  void vcycle(rs_ctx *ctx, const double *b, double *x, int C_);
+  void vcycle(rs_ctx *ctx, const mgreal *b, mgreal *x, int C_);
   // y = A_0 x for C columns.
-  void spmv0(rs_ctx *ctx, const double *x, double *y, int C_);
+  void spmv0(rs_ctx *ctx, const mgreal *x, mgreal *y, int C_);
   // x ~ A_0^-1 b by `iters` steps of conjugate gradients per column, preconditioned by one
   // V-cycle each (x_0 = 0; iters = 1 is the V-cycle with the optimal step length). The
   // scalars stay on the device (no host synchronization); a fixed number of steps makes it a
   // nonlinear map of b, which flexible GMRES (the stored preconditioned vectors) allows.
-  void pcg(rs_ctx *ctx, const double *b, double *x, int C_, int iters);
-  DevBuf<double> cg_r, cg_z, cg_p, cg_q, cg_part, cg_s;  // n_0 x C each; partial sums; scalars
+  void pcg(rs_ctx *ctx, const mgreal *b, mgreal *x, int C_, int iters);
+  DevBuf<mgreal> cg_r, cg_z, cg_p, cg_q;  // n_0 x C each
+  DevBuf<double> cg_part, cg_s;           // per-block partial sums; scalars
+  DevBuf<unsigned> cg_ticket;  // blocks done in the current dot-product launch (0 between launches)
   struct Graph {
-    const double *b = nullptr;
-    double *x = nullptr;
+    const mgreal *b = nullptr;
+    mgreal *x = nullptr;
     int C = 0, iters = 0;
     int64_t launches = 0;
     cudaGraphExec_t exec = nullptr;
@@ -65,10 +77,10 @@ struct AmgDevice {
 
  private:
   template <int CC>
-  void vcycle_t(rs_ctx *ctx, const double *b, double *x);
+  void vcycle_t(rs_ctx *ctx, const mgreal *b, mgreal *x);
   template <int CC>
-  void spmv0_t(rs_ctx *ctx, const double *x, double *y);
-  void pcg_body(rs_ctx *ctx, const double *b, double *x, int C_, int iters);
+  void spmv0_t(rs_ctx *ctx, const mgreal *x, mgreal *y);
+  void pcg_body(rs_ctx *ctx, const mgreal *b, mgreal *x, int C_, int iters);
 };
 
 }  // namespace rsg

@@ -52,7 +52,8 @@ struct HDev {
   const float4 *xh;          // per BVH position: position hi (xyz), weight a (w)
   const float4 *xl;          // per BVH position: position lo (xyz): X = hi + lo to ~48 bits
   const float4 *nrm;         // per BVH position: normal (faces only)
-  const double2 *node_farA;  // per node: its far sums of psi = a (k_0, k_1), the far part of H~a
+  const double2 *leaf_farA;  // per leaf: far sums of psi = a (k_0, k_1) along its chain, the far part of H~a
+  double *leafsum;           // per leaf: C channel far sums along its chain
   const uint32_t *colidx;    // near columns of every leaf's chain, flattened, leaf by leaf
   const uint4 *items;        // per work item: leaf ordinal, column-range begin / end, -
   const uint32_t *item_off;  // per leaf: its work items [item_off[k], item_off[k + 1])
@@ -277,10 +278,22 @@ __global__ void __launch_bounds__(128, 5) hm_rows_kernel(HDev d, int c0) {
   }
 }
 
+// Per (leaf, channel): the far sums along the leaf's chain (root to leaf), FP64, shared by the
+// leaf's rows. With psi = a (CC = 2, ONES) the same sums give the far part of H~a per leaf.
+template <int CC>
+__global__ void hm_chain_sum_kernel(HDev d, const double *__restrict__ src, double *__restrict__ dst) {
+  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= (size_t)d.n_leaves * CC) return;
+  const int k = (int)(t / CC), c = (int)(t % CC);
+  double s = 0.0;
+  for (uint32_t ci = d.chain_off[k]; ci < d.chain_off[k + 1]; ++ci) s += src[(size_t)d.chain[ci] * CC + c];
+  dst[t] = s;
+}
+
 // Per leaf (thread per row): z = near + (m_p H~a_far - H~(a m)_far), the near sums of the
-// items (in item order, as float pairs) plus the far sums along the chain (root to leaf) in
-// FP64. The far part of H~a was summed with the same operations from psi = a, so m = 1 gives
-// z = 0 exactly. Channels are taken twelve at a time to bound the registers.
+// items (in item order, as float pairs) plus the leaf's chain sums of the far field (FP64,
+// hm_chain_sum_kernel). The far part of H~a was summed with the same operations from psi = a,
+// so m = 1 gives z = 0 exactly. Channels are taken twelve at a time to bound the registers.
 template <int SEL, int CC>
 __global__ void hm_epilogue_kernel(HDev d) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -292,11 +305,8 @@ __global__ void hm_epilogue_kernel(HDev d) {
   const uint32_t p = s0 + r;
   constexpr int G = CC < 12 ? CC : 12;
   static_assert(CC % G == 0, "channel groups");
-  double fa0 = 0.0, fa1 = 0.0;
-  for (uint32_t ci = d.chain_off[k]; ci < d.chain_off[k + 1]; ++ci) {
-    const double2 fa = d.node_farA[d.chain[ci]];
-    fa0 += fa.x, fa1 += fa.y;
-  }
+  const double2 fa = d.leaf_farA[k];
+  const double fa0 = fa.x, fa1 = fa.y;
   const float2 *mp = d.m + (size_t)p * CC;
   float2 *zp = d.z + (size_t)p * CC;
 #pragma unroll 1
@@ -304,7 +314,7 @@ __global__ void hm_epilogue_kernel(HDev d) {
     float nh[G], nl[G];
     double fx[G];
 #pragma unroll
-    for (int c = 0; c < G; ++c) nh[c] = 0.f, nl[c] = 0.f, fx[c] = 0.0;
+    for (int c = 0; c < G; ++c) nh[c] = 0.f, nl[c] = 0.f, fx[c] = d.leafsum[(size_t)k * CC + c0 + c];
     for (uint32_t i = d.item_off[k]; i < d.item_off[k + 1]; ++i) {
       const float2 *o = d.part + ((size_t)i * 8 + r) * CC + c0;
 #pragma unroll
@@ -312,11 +322,6 @@ __global__ void hm_epilogue_kernel(HDev d) {
         const float2 v = o[c];
         pair_add(nh[c], nl[c], v.x, v.y);
       }
-    }
-    for (uint32_t ci = d.chain_off[k]; ci < d.chain_off[k + 1]; ++ci) {
-      const double *f = d.farx + (size_t)d.chain[ci] * CC + c0;
-#pragma unroll
-      for (int c = 0; c < G; ++c) fx[c] += f[c];
     }
 #pragma unroll
     for (int c = 0; c < G; ++c) {
@@ -493,7 +498,8 @@ struct HMat {
   DevBuf<uint32_t> far_ptr, far_col, count;
   DevBuf<uint32_t> colidx;
   DevBuf<uint4> items;
-  DevBuf<double2> far_coef, node_farA;
+  DevBuf<double2> far_coef, leaf_farA;
+  DevBuf<double> leafsum;
   DevBuf<float4> xh, xl, nrm;
   DevBuf<double> up, farx;
   DevBuf<float2> part, m, z;
@@ -506,9 +512,9 @@ struct HMat {
     d.start = start.p, d.end = end.p, d.right = right.p, d.parent = parent.p, d.leaves = leaves.p;
     d.chain_off = chain_off.p, d.chain = chain.p;
     d.far_ptr = far_ptr.p, d.far_col = far_col.p, d.far_coef = far_coef.p;
-    d.xh = xh.p, d.xl = xl.p, d.nrm = nrm.p, d.node_farA = node_farA.p;
+    d.xh = xh.p, d.xl = xl.p, d.nrm = nrm.p, d.leaf_farA = leaf_farA.p;
     d.colidx = colidx.p, d.items = items.p, d.item_off = item_off.p;
-    d.up = up.p, d.farx = farx.p, d.part = part.p, d.count = count.p;
+    d.up = up.p, d.farx = farx.p, d.part = part.p, d.count = count.p, d.leafsum = leafsum.p;
     d.m = m.p, d.z = z.p;
     d.n_nodes = (int)tree.n_nodes(), d.n_leaves = (int)tree.leaves.size(), d.n_el = (int)n_el;
     d.n_items = (int)n_items;
@@ -523,6 +529,7 @@ struct HMat {
   void reserve(int C_) {
     size_t nn = tree.n_nodes();
     if ((size_t)C_ * nn > up.n) up.alloc((size_t)C_ * nn), farx.alloc((size_t)C_ * nn);
+    if ((size_t)C_ * tree.leaves.size() > leafsum.n) leafsum.alloc((size_t)C_ * tree.leaves.size());
     if ((size_t)C_ * n_el > m.n) m.alloc((size_t)C_ * n_el), z.alloc((size_t)C_ * n_el);
     if (n_items * 8 * (size_t)C_ > part.n) part.alloc(std::max<size_t>(n_items * 8 * (size_t)C_, 1));
   }
@@ -552,6 +559,10 @@ struct HMat {
     prof.begin(s, kind == FACE ? "metric_far" : "vfrac_far");
     hm_far_kernel<SEL, CC><<<nblk(nn * 32, 256), 256, 0, s>>>(d);
     RSG_LAUNCHED(ctx, "hm_far");
+    if (SEL != ONES) {
+      hm_chain_sum_kernel<CC><<<nblk(nl * CC, 256), 256, 0, s>>>(d, d.farx, d.leafsum);
+      RSG_LAUNCHED(ctx, "hm_chain_sum");
+    }
     prof.end(s);
   }
 
@@ -656,7 +667,6 @@ struct HMat {
                                                    xh.p, xl.p, kind == FACE ? nrm.p : nullptr);
     RSG_LAUNCHED(ctx, "hm_pack");
     // far part of H~a: upward over psi = a (m = 1, 2 channels) and far sums per node
-    node_farA.alloc(nn);
     reserve(4);
     std::vector<float2> ones(2 * n_el, make_float2(1.f, 0.f));
     DevBuf<float2> mm;
@@ -664,7 +674,9 @@ struct HMat {
     HDev d = dev(2);
     d.m = mm.p;
     upward_far<ONES, 2>(d);
-    RSG_CUDA("upload", cudaMemcpyAsync(node_farA.p, farx.p, nn * sizeof(double2), cudaMemcpyDeviceToDevice, s));
+    leaf_farA.alloc(std::max<size_t>(nl, 1));
+    hm_chain_sum_kernel<2><<<nblk(nl * 2, 256), 256, 0, s>>>(d, farx.p, reinterpret_cast<double *>(leaf_farA.p));
+    RSG_LAUNCHED(ctx, "hm_chain_sum");
     RSG_CUDA("upload", cudaStreamSynchronize(s));
   }
 
@@ -1074,7 +1086,8 @@ inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 size_t noalloc_bytes(const HMat &h, int C) {
   size_t nn = h.tree.n_nodes();
   return 2 * align256(nn * C * sizeof(double)) + 2 * align256(h.n_el * C * sizeof(float2)) +
-         align256(std::max<size_t>(h.n_items, 1) * 8 * C * sizeof(float2)) + align256(64 * sizeof(unsigned long long));
+         align256(std::max<size_t>(h.n_items, 1) * 8 * C * sizeof(float2)) +
+         align256(h.tree.leaves.size() * C * sizeof(double)) + align256(64 * sizeof(unsigned long long));
 }
 
 HDev noalloc_dev(const HMat &h, int C, unsigned char *base) {
@@ -1090,6 +1103,7 @@ HDev noalloc_dev(const HMat &h, int C, unsigned char *base) {
   d.m = reinterpret_cast<const float2 *>(take(h.n_el * C * sizeof(float2)));
   d.z = reinterpret_cast<float2 *>(take(h.n_el * C * sizeof(float2)));
   d.part = reinterpret_cast<float2 *>(take(std::max<size_t>(h.n_items, 1) * 8 * C * sizeof(float2)));
+  d.leafsum = reinterpret_cast<double *>(take(h.tree.leaves.size() * C * sizeof(double)));
   return d;
 }
 

@@ -107,17 +107,17 @@ __global__ void mu_kernel(const double *__restrict__ s1, const double *__restric
 // AMG layout [v][3 nb] <- r_q[3 v + k] - c_v mu_{q, g(v), k}
 __global__ void to_mg_kernel(const double *__restrict__ r, size_t ld, int nb, int nv,
                              const uint32_t *__restrict__ group, const double *__restrict__ c,
-                             const double *__restrict__ mu, int G, double *__restrict__ out) {
+                             const double *__restrict__ mu, int G, mgreal *__restrict__ out) {
   size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (t >= (size_t)nv * 3 * nb) return;
   size_t v = t / (3 * nb);
   int col = (int)(t % (3 * nb)), q = col / 3, k = col % 3;
   double sub = mu ? c[v] * mu[(size_t)q * 3 * G + 3 * group[v] + k] : 0.0;
-  out[t] = r[q * ld + 3 * v + k] - sub;
+  out[t] = (mgreal)(r[q * ld + 3 * v + k] - sub);
 }
 
 // y_q[3 v + k] = yy[v][3 q + k] + shift_{q, g(v), k}, y_q[nd + 3 g + k] = mu (multipliers).
-__global__ void from_mg_kernel(const double *__restrict__ yy, double *__restrict__ y, size_t ld,
+__global__ void from_mg_kernel(const mgreal *__restrict__ yy, double *__restrict__ y, size_t ld,
                                int nb, int nv, const uint32_t *__restrict__ group, int G,
                                const double *__restrict__ shift, const double *__restrict__ mu,
                                const double *__restrict__ add) {
@@ -130,7 +130,7 @@ __global__ void from_mg_kernel(const double *__restrict__ yy, double *__restrict
   if (i < nd) {
     size_t v = i / 3;
     int k = (int)(i % 3);
-    val = yy[v * 3 * nb + 3 * q + k] + shift[(size_t)q * 3 * G + 3 * group[v] + k];
+    val = (double)yy[v * 3 * nb + 3 * q + k] + shift[(size_t)q * 3 * G + 3 * group[v] + k];
   } else {
     val = mu[(size_t)q * 3 * G + (i - nd)];
   }
@@ -183,7 +183,8 @@ struct rs_solver {
   std::vector<uint32_t> group_h;
   AmgDevice amg;
   DevBuf<uint32_t> group;
-  DevBuf<double> c, eps_area, part, s1, mu, cy, shift, mg_in, mg_out, mg_tmp, tmp, tmp2, ky;
+  DevBuf<double> c, eps_area, part, s1, mu, cy, shift, tmp, tmp2;
+  DevBuf<mgreal> mg_in, mg_out;  // right-hand sides and solutions on the multigrid layout
   std::vector<GmresReport> last;
   Operator op, prec;
 
@@ -203,7 +204,7 @@ struct rs_solver {
     size_t K = (size_t)3 * G * nb;
     if (s1.n < K) s1.alloc(K), mu.alloc(K), cy.alloc(K), shift.alloc(K);
     size_t m = (size_t)nv * 3 * nb;
-    if (mg_in.n < m) mg_in.alloc(m), mg_out.alloc(m), mg_tmp.alloc(m), ky.alloc(m);
+    if (mg_in.n < m) mg_in.alloc(m), mg_out.alloc(m);
     if (tmp.n < (size_t)nb * n) tmp.alloc((size_t)nb * n), tmp2.alloc((size_t)nb * n);
   }
 
@@ -310,7 +311,7 @@ __global__ void add_kernel(size_t m, const double *x, double *y) {
   if (i < m) y[i] += x[i];
 }
 // cy[q][3g + k] = sum_{v in g} c_v yy[v][3q + k]  (weighted group sums on the multigrid layout)
-__global__ void mg_group_partial(const double *__restrict__ yy, int nb, int nv,
+__global__ void mg_group_partial(const mgreal *__restrict__ yy, int nb, int nv,
                                  const uint32_t *__restrict__ group, const double *__restrict__ c,
                                  int G, double *part) {
   const int K = 3 * G * nb;
@@ -321,7 +322,7 @@ __global__ void mg_group_partial(const double *__restrict__ yy, int nb, int nv,
     int q = i / (3 * G), g = (i % (3 * G)) / 3, k = i % 3;
     double acc = 0.0;
     for (size_t v = v0 + threadIdx.x; v < v1; v += blockDim.x)
-      if ((int)group[v] == g) acc += c[v] * yy[v * 3 * nb + 3 * q + k];
+      if ((int)group[v] == g) acc += c[v] * (double)yy[v * 3 * nb + 3 * q + k];
     for (int m = 16; m >= 1; m >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, m);
     if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = acc;
     __syncthreads();

@@ -33,6 +33,7 @@ thread_local bool g_topology_trusted = false;
 
 TrustedTopology::TrustedTopology() : prev(g_topology_trusted) { g_topology_trusted = true; }
 TrustedTopology::~TrustedTopology() { g_topology_trusted = prev; }
+bool topology_trusted() { return g_topology_trusted; }
 
 void validate_topology(int nv, int nf, const uint32_t *faces) {
   if (g_topology_trusted) return;

@@ -21,6 +21,9 @@ struct TrustedTopology {
   TrustedTopology &operator=(const TrustedTopology &) = delete;
   bool prev;
 };
+// Whether this thread runs under a TrustedTopology (a worker thread takes its caller's trust
+// over by making its own).
+bool topology_trusted();
 // Surface::validate_positions (RS/src/surface.rs:513-541).
 void validate_positions(int nv, int nf, const uint32_t *faces, const double *pos);
 

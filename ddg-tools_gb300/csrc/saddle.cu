@@ -16,7 +16,9 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <future>
 #include <memory>
+#include <optional>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -480,11 +482,50 @@ int rs_solver_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const do
     for (int v = 0; v < nv; ++v) ch[v] = S->vmass[v] / garea[S->group_h[v]];
     S->n = S->nd + 3 * (size_t)S->G;
     bool multi = !per_comp && ncomp > 1;  // translations_fixed_per_component (precond.rs:96-124)
-    double eps = 0.0;
+    auto secs = [](clk::time_point a, clk::time_point b) { return std::chrono::duration<double>(b - a).count(); };
+    // Three independent parts run side by side: the metric's face tree and blocks (this
+    // thread), the vertex fractional tree, and the Laplacian block with its multigrid set-up
+    // (host only). A worker keeps the caller's trust in the face list.
+    const bool trusted = topology_trusted();
+    const double sexp = (beta - 2.0) / alpha;
+    double eps = 0.0, t_lap = 0.0, t_amg = 0.0, t_vf = 0.0;
+    auto amg_task = std::async(std::launch::async, [&, trusted] {
+      std::optional<TrustedTopology> tt;
+      if (trusted) tt.emplace();
+      auto t0 = clk::now();
+      Csr K = laplacian_block(nv, nf, faces, positions_host, S->vmass, multi ? o->eps_multi_rel : o->eps_rel,
+                              o->clamp_laplacian != 0, eps);
+      auto t1 = clk::now();
+      AmgHost h = amg_setup(K);
+      t_lap = secs(t0, t1), t_amg = secs(t1, clk::now());
+      return h;
+    });
+    std::unique_ptr<rs_vfrac, void (*)(rs_vfrac *)> vf(nullptr, rs_vfrac_free);
+    auto vf_task = std::async(std::launch::async, [&, trusted] {
+      std::optional<TrustedTopology> tt;
+      if (trusted) tt.emplace();
+      auto t0 = clk::now();
+      rs_vfrac *v = nullptr;
+      int rc = rs_vfrac_build(ctx, nv, positions_host, S->vmass.data(), 2.0 - sexp, o->chi, o->leaf_size,
+                              o->leaf_pairs, &v);
+      vf.reset(v);
+      t_vf = secs(t0, clk::now());
+      return std::make_pair(rc, rc ? std::string(rs_last_error()) : std::string());
+    });
+    auto t_m0 = clk::now();
+    std::unique_ptr<rs_metric, void (*)(rs_metric *)> m(nullptr, rs_metric_free);
+    rs_metric *mp = nullptr;
+    int rc_m = rs_metric_build(ctx, nv, nf, faces, positions_host, alpha, beta, o->chi, o->leaf_size,
+                               o->leaf_pairs, &mp);
+    m.reset(mp);
+    std::string err_m = rc_m ? rs_last_error() : "";
+    S->build_times[0] = secs(t_m0, clk::now());
+    auto [rc_v, err_v] = vf_task.get();
+    AmgHost amg_h = amg_task.get();
+    if (rc_m) fail(rc_m, "Gpu", "solver", "metric: " + err_m);
+    if (rc_v) fail(rc_v, "Gpu", "solver", "fractional tree: " + err_v);
+    S->build_times[1] = t_vf, S->build_times[2] = t_lap, S->build_times[3] = t_amg;
     t_ph = clk::now();
-    Csr K = laplacian_block(nv, nf, faces, positions_host, S->vmass, multi ? o->eps_multi_rel : o->eps_rel,
-                            o->clamp_laplacian != 0, eps);
-    double t_lap = std::chrono::duration<double>(clk::now() - t_ph).count();
     S->eps = eps;
     std::vector<double> ea(S->G);
     for (int g = 0; g < S->G; ++g) ea[g] = eps * garea[g];
@@ -492,27 +533,9 @@ int rs_solver_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const do
     S->group.upload(S->group_h, s);
     S->c.upload(ch, s);
     S->eps_area.upload(ea, s);
-    // metric and fractional factor
-    t_ph = clk::now();
-    rs_metric *m = nullptr;
-    int rc = rs_metric_build(ctx, nv, nf, faces, positions_host, alpha, beta, o->chi, o->leaf_size,
-                             o->leaf_pairs, &m);
-    if (rc) fail(rc, "Gpu", "solver", std::string("metric: ") + rs_last_error());
-    S->metric = m;
-    lap(S->build_times[0]);
     S->w_hi = o->tp_weight;
     S->w_lo = o->tp_weight * (o->low_order ? 1.0 : 0.0);
-    double sexp = (beta - 2.0) / alpha;
-    rs_vfrac *vf = nullptr;
-    rc = rs_vfrac_build(ctx, nv, positions_host, S->vmass.data(), 2.0 - sexp, o->chi, o->leaf_size,
-                        o->leaf_pairs, &vf);
-    if (rc) fail(rc, "Gpu", "solver", std::string("fractional tree: ") + rs_last_error());
-    S->vfrac = vf;
-    lap(S->build_times[1]);
-    S->build_times[2] = t_lap;
     S->frac_scale = 1.0 / (o->tp_weight * symbol_ratio(sexp));  // FractionalScale::Symbol
-    AmgHost amg_h = amg_setup(K);
-    lap(S->build_times[3]);
     S->amg.upload(amg_h, s);
     S->vcycles = std::max(1, o->vcycles);
     S->use_prec = o->preconditioner != 0;
@@ -529,6 +552,7 @@ int rs_solver_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const do
     RSG_CUDA("solver", cudaStreamSynchronize(s));
     lap(S->build_times[4]);
     S->build_times[5] = std::chrono::duration<double>(clk::now() - t_all).count();
+    S->metric = m.release(), S->vfrac = vf.release();
     ctx_retain(ctx);
     *out = S.release();
   });

@@ -190,6 +190,24 @@ __global__ void hm_far_kernel(HDev d) {
     if (lane == (c & 31)) o[c] = acc[c];
 }
 
+// One column of a near tile as the rows kernel reads it: position (hi, lo; w = weight),
+// normal, and the CC channel values (hi, lo pairs) of the pass.
+template <int CC>
+struct alignas(16) RowsCol {
+  float4 h, l, n;
+  float4 m[CC / 2];
+};
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
 // Near sums of one work item (a slice of the flattened near columns of a leaf's root-to-leaf
 // chain) in difference form: sum_q w_pq (m_p - m_q) for channels [c0, c0 + CC) of the row's
 // element p. One warp per item; the leaf's ns rows (3 to 8) each take G = 32 / ns lanes
@@ -200,12 +218,20 @@ __global__ void hm_far_kernel(HDev d) {
 // by error-free additions (two_sum), whose errors gather with the low parts in a second
 // float. (Kahan summation would leave an error of eps times each lane's partial sum, a
 // first-order quantity.) The G partial sums of a row are then added in lane order as float
-// pairs (through shared memory). For a smooth input the terms are first-order quantities
+// pairs (through shared memory). The columns of an item pass through shared memory in tiles
+// of 32 (one column per lane, copied by cp.async while the previous tile is being used), so
+// that the loads of a column's record are issued together and overlap the arithmetic.
+// For a smooth input the terms are first-order quantities
 // that cancel to a second-order result, and the output stage (M^T, a discrete divergence)
 // cancels once more, so plain FP32 sums of H~a m and H~(a m) would lose about four digits.
 template <int KIND, int CC>
 __global__ void __launch_bounds__(128, 5) hm_rows_kernel(HDev d, int c0) {
-  __shared__ float2 red[4][32][CC];
+  static_assert(CC <= 12 && CC % 2 == 0, "at most twelve channels per pass");
+  // per warp: two tiles of 32 columns (double buffer, filled by cp.async) and their indices;
+  // the lane-sum table of the end reuses the warp's tiles
+  __shared__ RowsCol<CC> tiles[4][2][32];
+  __shared__ uint32_t qs[4][2][32];
+  static_assert(sizeof(tiles[0]) >= 32 * CC * sizeof(float2), "reduction table fits a warp's tiles");
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (w >= d.n_items) return;
@@ -230,50 +256,82 @@ __global__ void __launch_bounds__(128, 5) hm_rows_kernel(HDev d, int c0) {
   }
 #pragma unroll
   for (int c = 0; c < CC; ++c) ks[c] = 0.f, kc[c] = 0.f;
-  if (act)
-    for (uint32_t idx = it.y + j; idx < it.z; idx += G) {
-      const uint32_t q = d.colidx[idx];
-      if (q == p) continue;
-      const float4 qh = d.xh[q], ql = d.xl[q];
-      const float d0 = (ph.x - qh.x) + (pl.x - ql.x);
-      const float d1 = (ph.y - qh.y) + (pl.y - ql.y);
-      const float d2 = (ph.z - qh.z) + (pl.z - ql.z);
-      float k0, k1;
-      near_kernel<KIND>(d, d0, d1, d2, np, KIND == FACE ? d.nrm[q] : np, k0, k1);
-      const float w0 = k0 * qh.w, w1 = k1 * qh.w;
+  const uint32_t ncol = it.z - it.y, ntiles = (ncol + 31) / 32;
+  // lane l copies column t0 + l of the item into buffer `buf` (16-byte async copies)
+  auto stage = [&](int buf, uint32_t t0) {
+    if ((uint32_t)lane < ncol - t0) {
+      const uint32_t q = d.colidx[it.y + t0 + lane];
+      qs[wib][buf][lane] = q;
+      RowsCol<CC> &cl = tiles[wib][buf][lane];
+      cp_async16(&cl.h, d.xh + q);
+      cp_async16(&cl.l, d.xl + q);
+      if (KIND == FACE) cp_async16(&cl.n, d.nrm + q);
       const float4 *mq = reinterpret_cast<const float4 *>(d.m + (size_t)q * C + c0);
 #pragma unroll
-      for (int c2 = 0; c2 < CC / 2; ++c2) {
-        const float4 v = mq[c2];
+      for (int c2 = 0; c2 < CC / 2; ++c2) cp_async16(&cl.m[c2], mq + c2);
+    }
+    cp_async_commit();
+  };
+  if (ntiles > 0) stage(0, 0);
+  for (uint32_t ti = 0; ti < ntiles; ++ti) {
+    const int buf = ti & 1;
+    if (ti + 1 < ntiles) {
+      stage(buf ^ 1, (ti + 1) * 32);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncwarp();
+    const uint32_t t0 = ti * 32, nt = min(32u, ncol - t0);
+    // lane j of a row takes the item's columns j, j + G, ... (in order): here the local
+    // indices k with (t0 + k) = j mod G
+    if (act)
+      for (uint32_t k = ((uint32_t)j + (uint32_t)G - t0 % (uint32_t)G) % (uint32_t)G; k < nt; k += G) {
+        const uint32_t q = qs[wib][buf][k];
+        if (q == p) continue;
+        const RowsCol<CC> &cl = tiles[wib][buf][k];
+        const float4 qh = cl.h, ql = cl.l;
+        const float d0 = (ph.x - qh.x) + (pl.x - ql.x);
+        const float d1 = (ph.y - qh.y) + (pl.y - ql.y);
+        const float d2 = (ph.z - qh.z) + (pl.z - ql.z);
+        float k0, k1;
+        near_kernel<KIND>(d, d0, d1, d2, np, KIND == FACE ? cl.n : np, k0, k1);
+        const float w0 = k0 * qh.w, w1 = k1 * qh.w;
 #pragma unroll
-        for (int e = 0; e < 2; ++e) {
-          const int c = 2 * c2 + e;
-          const float qhv = e ? v.z : v.x, qlv = e ? v.w : v.y;
-          const float wk = (KIND == FACE && c >= 9) ? w1 : w0;
-          // w (m_p - m_q) = pr + pe + w dl up to eps^2 terms: dh = mh_p - mh_q is exact (the
-          // hi parts share a grid), dl = ml_p - ml_q, w dh = pr + pe (FMA), so no rounding that
-          // depends on the input reaches the sum above eps^2
-          const float dh = mh[c] - qhv;
-          const float dl = ml[c] - qlv;
-          const float pr = wk * dh;
-          const float lo = fmaf(wk, dl, fmaf(wk, dh, -pr));
-          float sn, se;
-          two_sum(ks[c], pr, sn, se);
-          ks[c] = sn;
-          kc[c] += se + lo;
+        for (int c2 = 0; c2 < CC / 2; ++c2) {
+          const float4 v = cl.m[c2];
+#pragma unroll
+          for (int e = 0; e < 2; ++e) {
+            const int c = 2 * c2 + e;
+            const float qhv = e ? v.z : v.x, qlv = e ? v.w : v.y;
+            const float wk = (KIND == FACE && c >= 9) ? w1 : w0;
+            // w (m_p - m_q) = pr + pe + w dl up to eps^2 terms: dh = mh_p - mh_q is exact (the
+            // hi parts share a grid), dl = ml_p - ml_q, w dh = pr + pe (FMA), so no rounding
+            // that depends on the input reaches the sum above eps^2
+            const float dh = mh[c] - qhv;
+            const float dl = ml[c] - qlv;
+            const float pr = wk * dh;
+            const float lo = fmaf(wk, dl, fmaf(wk, dh, -pr));
+            float sn, se;
+            two_sum(ks[c], pr, sn, se);
+            ks[c] = sn;
+            kc[c] += se + lo;
+          }
         }
       }
-    }
+    __syncwarp();
+  }
   // the G lanes of a row: partial sums (s, t) added in lane order as float pairs
+  float2(*red)[CC] = reinterpret_cast<float2(*)[CC]>(&tiles[wib][0][0]);
 #pragma unroll
-  for (int c = 0; c < CC; ++c) red[wib][lane][c] = make_float2(ks[c], kc[c]);
+  for (int c = 0; c < CC; ++c) red[lane][c] = make_float2(ks[c], kc[c]);
   __syncwarp();
   if (!act || j != 0) return;
   float2 *o = d.part + ((size_t)w * 8 + r) * C + c0;
 #pragma unroll
   for (int c = 0; c < CC; ++c) {
-    float h = red[wib][lane][c].x, l = red[wib][lane][c].y;
-    for (int g = 1; g < G; ++g) pair_add(h, l, red[wib][lane + g][c].x, red[wib][lane + g][c].y);
+    float h = red[lane][c].x, l = red[lane][c].y;
+    for (int g = 1; g < G; ++g) pair_add(h, l, red[lane + g][c].x, red[lane + g][c].y);
     o[c] = make_float2(h, l);
   }
 }

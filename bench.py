@@ -206,9 +206,10 @@ def _lumped_interactions(bh) -> int:
 
 
 FLOW_METRIC = "Hs-flow steps/s @204,800 faces (plain preconditioner, rel.res 1e-6)"
-# Near-field work of the metric per near entry and vector when the near field is recomputed on
-# the fly (kernel 20 FLOP + 2 per channel, C = 12 channels per vector).
-NEAR_FLOP_PER_ENTRY = 44
+# Near-field work of the metric per near entry and vector: w (m_p - m_q) added up, 3 FLOP per
+# channel, C = 12 channels per vector (the near weights w are evaluated once per set-up, not per
+# product; the compensated arithmetic executes about four times this count).
+NEAR_FLOP_PER_ENTRY = 36
 # Operator applications per step assumed by the CPU reference arm (which has no preconditioned
 # solver of its own): the GPU arm's mean on this workload, GMRES iterations of the three
 # right-hand sides.

@@ -25,6 +25,7 @@
 #include <mutex>
 #include <numeric>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "block_tree.hpp"
@@ -55,7 +56,8 @@ struct HDev {
   const double2 *leaf_farA;  // per leaf: far sums of psi = a (k_0, k_1) along its chain, the far part of H~a
   double *leafsum;           // per leaf: C channel far sums along its chain
   const uint32_t *colidx;    // near columns of every leaf's chain, flattened, leaf by leaf
-  const uint4 *items;        // per work item: leaf ordinal, column-range begin / end, -
+  const uint4 *items;        // per work item: leaf ordinal, column-range begin / end, weight base
+  const void *wts;           // near weights per item: rows x (columns padded to 32), see NearW
   const uint32_t *item_off;  // per leaf: its work items [item_off[k], item_off[k + 1])
   double *up;                // per node: C channel sums of a m (FP64)
   double *farx;              // per node: C channel far sums (FP64)
@@ -164,38 +166,96 @@ __global__ void hm_upward_kernel(HDev d) {
 }
 
 // farx[a][c] = sum over the far blocks (a, b) of h(a, b)[kernel(c)] up[b][c] (block_tree.rs:
-// 564-578), FP64; one warp per node, lanes strided over the node's far blocks, each summing
-// all CC channels, then a fixed butterfly over the lanes.
+// 564-578), FP64. One warp per (node, group of at most twelve channels): lane = sub CG + c
+// holds channel c of the group and takes the node's far blocks sub, sub + 2, ... (sub = 0, 1);
+// the two partial sums are then added. The order of the operations does not depend on the
+// channel count, so the pass over psi = a (two channels) and a product pass add the same
+// terms in the same order.
 template <int SEL, int CC>
 __global__ void hm_far_kernel(HDev d) {
-  int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
+  constexpr int CG = CC < 12 ? CC : 12;
+  static_assert(CC % CG == 0 && 2 * CG <= 32, "channel groups");
+  constexpr int NG = CC / CG;
+  const int wg = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int a = wg / NG, grp = wg - a * NG;
   if (a >= d.n_nodes) return;
-  double acc[CC];
+  const int lane = threadIdx.x & 31, sub = lane / CG, c = lane - sub * CG;
+  const int ch = grp * CG + c;
+  double acc = 0.0;
+  if (sub < 2) {
+    const bool k1 = uses_k1<SEL>(ch);
+    const uint32_t q1 = d.far_ptr[a + 1];
+    uint32_t q = d.far_ptr[a] + sub;
+    // four of the lane's blocks at a time: loads first, then the additions in order
+    for (; q + 6 < q1; q += 8) {
+      double kk[4], u[4];
 #pragma unroll
-  for (int c = 0; c < CC; ++c) acc[c] = 0.0;
-  for (uint32_t q = d.far_ptr[a] + lane; q < d.far_ptr[a + 1]; q += 32) {
-    const double2 k = d.far_coef[q];
-    const double *u = d.up + (size_t)d.far_col[q] * CC;
+      for (int i = 0; i < 4; ++i) {
+        const double2 k = d.far_coef[q + 2 * i];
+        kk[i] = k1 ? k.y : k.x;
+        u[i] = d.up[(size_t)d.far_col[q + 2 * i] * CC + ch];
+      }
 #pragma unroll
-    for (int c = 0; c < CC; ++c) acc[c] = fma(uses_k1<SEL>(c) ? k.y : k.x, u[c], acc[c]);
+      for (int i = 0; i < 4; ++i) acc = fma(kk[i], u[i], acc);
+    }
+    for (; q < q1; q += 2) {
+      const double2 k = d.far_coef[q];
+      acc = fma(k1 ? k.y : k.x, d.up[(size_t)d.far_col[q] * CC + ch], acc);
+    }
   }
-#pragma unroll
-  for (int c = 0; c < CC; ++c)
-#pragma unroll
-    for (int m = 16; m >= 1; m >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], m);
-  double *o = d.farx + (size_t)a * CC;
-#pragma unroll
-  for (int c = 0; c < CC; ++c)
-    if (lane == (c & 31)) o[c] = acc[c];
+  acc += __shfl_down_sync(0xffffffffu, acc, CG);
+  if (sub == 0) d.farx[(size_t)a * CC + ch] = acc;
 }
 
-// One column of a near tile as the rows kernel reads it: position (hi, lo; w = weight),
-// normal, and the CC channel values (hi, lo pairs) of the pass.
-template <int CC>
-struct alignas(16) RowsCol {
-  float4 h, l, n;
-  float4 m[CC / 2];
+// Near weights of an element pair as the rows kernel applies them: faces (w_0, w_1) =
+// a_q (k_0, k_1), vertices w_0 = a_q k_0; zero on the diagonal (q = p). Stored per work item
+// as [row][column], rows padded to a multiple of 32 columns so that each 32-column slice
+// starts on a 128-byte boundary.
+template <int KIND>
+using NearW = typename std::conditional<KIND == FACE, float2, float>::type;
+constexpr int kTileW = 36;  // shared-memory row stride of a weight tile (bank spread)
+
+template <int KIND>
+__global__ void hm_weights_kernel(HDev d, size_t total) {
+  // one warp per (item, row); lanes strided over the item's columns
+  const size_t wr = (blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (wr >= (size_t)d.n_items * 8) return;
+  const uint32_t w = (uint32_t)(wr >> 3), r = (uint32_t)(wr & 7);
+  const uint4 it = d.items[w];
+  const uint32_t leaf = d.leaves[it.x];
+  const uint32_t s0 = d.start[leaf], ns = d.end[leaf] - s0;
+  if (r >= ns) return;
+  const uint32_t p = s0 + r, ncol = it.z - it.y, npad = (ncol + 31) & ~31u;
+  const float4 ph = d.xh[p], pl = d.xl[p];
+  const float4 np = KIND == FACE ? d.nrm[p] : make_float4(0.f, 0.f, 0.f, 0.f);
+  NearW<KIND> *out = reinterpret_cast<NearW<KIND> *>(const_cast<void *>(d.wts)) + it.w + (size_t)r * npad;
+  for (uint32_t k = lane; k < npad; k += 32) {
+    float w0 = 0.f, w1 = 0.f;
+    if (k < ncol) {
+      const uint32_t q = d.colidx[it.y + k];
+      if (q != p) {
+        const float4 qh = d.xh[q], ql = d.xl[q];
+        const float d0 = (ph.x - qh.x) + (pl.x - ql.x);
+        const float d1 = (ph.y - qh.y) + (pl.y - ql.y);
+        const float d2 = (ph.z - qh.z) + (pl.z - ql.z);
+        float k0, k1;
+        near_kernel<KIND>(d, d0, d1, d2, np, KIND == FACE ? d.nrm[q] : np, k0, k1);
+        w0 = k0 * qh.w, w1 = k1 * qh.w;
+      }
+    }
+    if constexpr (KIND == FACE) out[k] = make_float2(w0, w1);
+    else out[k] = w0;
+  }
+  (void)total;
+}
+
+// One tile of a work item in shared memory: the channel values (hi, lo pairs) of 32 columns
+// and the near weights of up to 8 rows x 32 columns.
+template <int KIND, int CC>
+struct alignas(16) RowsTile {
+  float4 m[32][CC / 2];
+  NearW<KIND> w[8][kTileW];
 };
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
@@ -212,38 +272,38 @@ __device__ __forceinline__ void cp_async_wait() {
 // chain) in difference form: sum_q w_pq (m_p - m_q) for channels [c0, c0 + CC) of the row's
 // element p. One warp per item; the leaf's ns rows (3 to 8) each take G = 32 / ns lanes
 // (lane = r G + j), lane j of a row taking every G-th column, so that small leaves keep the
-// warp busy. The kernel values of a column are evaluated once per row and applied to the CC
-// channels. m_p - m_q is formed exactly from the float pairs (their hi parts share a grid), each product
-// w (m_p - m_q) is split exactly too, and the terms are summed as float pairs: the high parts
-// by error-free additions (two_sum), whose errors gather with the low parts in a second
-// float. (Kahan summation would leave an error of eps times each lane's partial sum, a
-// first-order quantity.) The G partial sums of a row are then added in lane order as float
-// pairs (through shared memory). The columns of an item pass through shared memory in tiles
-// of 32 (one column per lane, copied by cp.async while the previous tile is being used), so
-// that the loads of a column's record are issued together and overlap the arithmetic.
-// For a smooth input the terms are first-order quantities
-// that cancel to a second-order result, and the output stage (M^T, a discrete divergence)
-// cancels once more, so plain FP32 sums of H~a m and H~(a m) would lose about four digits.
+// warp busy. The weights w_pq were evaluated once per set-up (hm_weights_kernel) and are
+// applied to the CC channels. m_p - m_q is formed exactly from the float pairs (their hi
+// parts share a grid), each product w (m_p - m_q) is split exactly too, and the terms are
+// summed as float pairs: the high parts by error-free additions (two_sum), whose errors gather
+// with the low parts in a second float. (Kahan summation would leave an error of eps times
+// each lane's partial sum, a first-order quantity.) The G partial sums of a row are then added
+// in lane order as float pairs (through shared memory). The columns of an item pass through
+// shared memory in tiles of 32 (channel values and the weights of the tile, copied by cp.async
+// while the previous tile is being used). For a smooth input the terms are first-order
+// quantities that cancel to a second-order result, and the output stage (M^T, a discrete
+// divergence) cancels once more, so plain FP32 sums of H~a m and H~(a m) would lose about
+// four digits.
 template <int KIND, int CC>
 __global__ void __launch_bounds__(128, 5) hm_rows_kernel(HDev d, int c0) {
   static_assert(CC <= 12 && CC % 2 == 0, "at most twelve channels per pass");
-  // per warp: two tiles of 32 columns (double buffer, filled by cp.async) and their indices;
-  // the lane-sum table of the end reuses the warp's tiles
-  __shared__ RowsCol<CC> tiles[4][2][32];
-  __shared__ uint32_t qs[4][2][32];
+  using WT = NearW<KIND>;
+  constexpr int kChunkW = 16 / (int)sizeof(WT);   // weights per 16-byte copy
+  constexpr int kChunksRow = 32 / kChunkW;         // copies per 32-column weight row
+  // per warp: two tiles (double buffer filled by cp.async); the lane-sum table of the end
+  // reuses the warp's tiles
+  __shared__ RowsTile<KIND, CC> tiles[4][2];
   static_assert(sizeof(tiles[0]) >= 32 * CC * sizeof(float2), "reduction table fits a warp's tiles");
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (w >= d.n_items) return;
-  const uint4 it = d.items[w];  // leaf ordinal, flat column range [y, z)
+  const uint4 it = d.items[w];  // leaf ordinal, flat column range [y, z), weight base
   const uint32_t leaf = d.leaves[it.x];
   const uint32_t s0 = d.start[leaf], ns = d.end[leaf] - s0;
   const int G = 32 / (int)ns;
   const int r = lane / G, j = lane - r * G;
   const bool act = (uint32_t)r < ns;
   const uint32_t p = s0 + (act ? r : 0);
-  const float4 ph = d.xh[p], pl = d.xl[p];
-  const float4 np = KIND == FACE ? d.nrm[p] : make_float4(0.f, 0.f, 0.f, 0.f);
   const int C = d.C;
   float mh[CC], ml[CC], ks[CC], kc[CC];
   {
@@ -256,19 +316,21 @@ __global__ void __launch_bounds__(128, 5) hm_rows_kernel(HDev d, int c0) {
   }
 #pragma unroll
   for (int c = 0; c < CC; ++c) ks[c] = 0.f, kc[c] = 0.f;
-  const uint32_t ncol = it.z - it.y, ntiles = (ncol + 31) / 32;
-  // lane l copies column t0 + l of the item into buffer `buf` (16-byte async copies)
+  const uint32_t ncol = it.z - it.y, ntiles = (ncol + 31) / 32, npad = ntiles * 32;
+  const WT *wg = reinterpret_cast<const WT *>(d.wts) + it.w;
+  // lane l copies the channel values of column t0 + l and its share of the weight rows
   auto stage = [&](int buf, uint32_t t0) {
+    RowsTile<KIND, CC> &tl = tiles[wib][buf];
     if ((uint32_t)lane < ncol - t0) {
       const uint32_t q = d.colidx[it.y + t0 + lane];
-      qs[wib][buf][lane] = q;
-      RowsCol<CC> &cl = tiles[wib][buf][lane];
-      cp_async16(&cl.h, d.xh + q);
-      cp_async16(&cl.l, d.xl + q);
-      if (KIND == FACE) cp_async16(&cl.n, d.nrm + q);
       const float4 *mq = reinterpret_cast<const float4 *>(d.m + (size_t)q * C + c0);
 #pragma unroll
-      for (int c2 = 0; c2 < CC / 2; ++c2) cp_async16(&cl.m[c2], mq + c2);
+      for (int c2 = 0; c2 < CC / 2; ++c2) cp_async16(&tl.m[lane][c2], mq + c2);
+    }
+#pragma unroll
+    for (int i = 0; i < 8 * kChunksRow / 32; ++i) {
+      const int id = lane + 32 * i, row = id / kChunksRow, ch = id - row * kChunksRow;
+      if ((uint32_t)row < ns) cp_async16(&tl.w[row][ch * kChunkW], wg + (size_t)row * npad + t0 + ch * kChunkW);
     }
     cp_async_commit();
   };
@@ -283,23 +345,21 @@ __global__ void __launch_bounds__(128, 5) hm_rows_kernel(HDev d, int c0) {
     }
     __syncwarp();
     const uint32_t t0 = ti * 32, nt = min(32u, ncol - t0);
+    const RowsTile<KIND, CC> &tl = tiles[wib][buf];
     // lane j of a row takes the item's columns j, j + G, ... (in order): here the local
     // indices k with (t0 + k) = j mod G
     if (act)
       for (uint32_t k = ((uint32_t)j + (uint32_t)G - t0 % (uint32_t)G) % (uint32_t)G; k < nt; k += G) {
-        const uint32_t q = qs[wib][buf][k];
-        if (q == p) continue;
-        const RowsCol<CC> &cl = tiles[wib][buf][k];
-        const float4 qh = cl.h, ql = cl.l;
-        const float d0 = (ph.x - qh.x) + (pl.x - ql.x);
-        const float d1 = (ph.y - qh.y) + (pl.y - ql.y);
-        const float d2 = (ph.z - qh.z) + (pl.z - ql.z);
-        float k0, k1;
-        near_kernel<KIND>(d, d0, d1, d2, np, KIND == FACE ? cl.n : np, k0, k1);
-        const float w0 = k0 * qh.w, w1 = k1 * qh.w;
+        float w0, w1;
+        if constexpr (KIND == FACE) {
+          const float2 ww = tl.w[r][k];
+          w0 = ww.x, w1 = ww.y;
+        } else {
+          w0 = w1 = tl.w[r][k];
+        }
 #pragma unroll
         for (int c2 = 0; c2 < CC / 2; ++c2) {
-          const float4 v = cl.m[c2];
+          const float4 v = tl.m[k][c2];
 #pragma unroll
           for (int e = 0; e < 2; ++e) {
             const int c = 2 * c2 + e;
@@ -322,7 +382,7 @@ __global__ void __launch_bounds__(128, 5) hm_rows_kernel(HDev d, int c0) {
     __syncwarp();
   }
   // the G lanes of a row: partial sums (s, t) added in lane order as float pairs
-  float2(*red)[CC] = reinterpret_cast<float2(*)[CC]>(&tiles[wib][0][0]);
+  float2(*red)[CC] = reinterpret_cast<float2(*)[CC]>(&tiles[wib][0]);
 #pragma unroll
   for (int c = 0; c < CC; ++c) red[lane][c] = make_float2(ks[c], kc[c]);
   __syncwarp();
@@ -556,6 +616,8 @@ struct HMat {
   DevBuf<uint32_t> far_ptr, far_col, count;
   DevBuf<uint32_t> colidx;
   DevBuf<uint4> items;
+  DevBuf<unsigned char> wts;  // near weights (NearW per entry), see hm_weights_kernel
+  size_t n_wts = 0;
   DevBuf<double2> far_coef, leaf_farA;
   DevBuf<double> leafsum;
   DevBuf<float4> xh, xl, nrm;
@@ -571,7 +633,7 @@ struct HMat {
     d.chain_off = chain_off.p, d.chain = chain.p;
     d.far_ptr = far_ptr.p, d.far_col = far_col.p, d.far_coef = far_coef.p;
     d.xh = xh.p, d.xl = xl.p, d.nrm = nrm.p, d.leaf_farA = leaf_farA.p;
-    d.colidx = colidx.p, d.items = items.p, d.item_off = item_off.p;
+    d.colidx = colidx.p, d.items = items.p, d.item_off = item_off.p, d.wts = wts.p;
     d.up = up.p, d.farx = farx.p, d.part = part.p, d.count = count.p, d.leafsum = leafsum.p;
     d.m = m.p, d.z = z.p;
     d.n_nodes = (int)tree.n_nodes(), d.n_leaves = (int)tree.leaves.size(), d.n_el = (int)n_el;
@@ -615,7 +677,7 @@ struct HMat {
     RSG_LAUNCHED(ctx, "hm_upward");
     prof.end(s);
     prof.begin(s, kind == FACE ? "metric_far" : "vfrac_far");
-    hm_far_kernel<SEL, CC><<<nblk(nn * 32, 256), 256, 0, s>>>(d);
+    hm_far_kernel<SEL, CC><<<nblk(nn * (CC < 12 ? 1 : CC / 12) * 32, 256), 256, 0, s>>>(d);
     RSG_LAUNCHED(ctx, "hm_far");
     if (SEL != ONES) {
       hm_chain_sum_kernel<CC><<<nblk(nl * CC, 256), 256, 0, s>>>(d, d.farx, d.leafsum);
@@ -685,6 +747,14 @@ struct HMat {
       }
     });
     n_items = items_h.size();
+    // weight base of every item: its rows times its columns padded to 32
+    n_wts = 0;
+    for (uint4 &it : items_h) {
+      const uint32_t leaf = T.leaves[it.x];
+      it.w = (uint32_t)n_wts;
+      n_wts += (size_t)(T.end[leaf] - T.start[leaf]) * ((it.z - it.y + 31) & ~31u);
+      if (n_wts > UINT32_MAX) fail(RS_INVALID_OPTION, "InvalidOption", "upload", "near field too large");
+    }
     up_vec(start, T.start, s), up_vec(end, T.end, s), up_vec(right, T.right, s);
     up_vec(parent, parent_h, s), up_vec(leaves, T.leaves, s), up_vec(chain_off, coff, s);
     up_vec(chain, chain_h, s), up_vec(colidx, cols_h, s), up_vec(items, items_h, s), up_vec(item_off, ioff, s);
@@ -724,6 +794,15 @@ struct HMat {
     hm_pack_kernel<<<nblk(n_el, 256), 256, 0, s>>>(dp.p, dw.p, nrm64 ? dn.p : nullptr, ord.p, (int)n_el,
                                                    xh.p, xl.p, kind == FACE ? nrm.p : nullptr);
     RSG_LAUNCHED(ctx, "hm_pack");
+    // near weights of every work item, evaluated once; the product passes read them
+    wts.alloc(std::max<size_t>(n_wts * (kind == FACE ? sizeof(float2) : sizeof(float)), 16));
+    {
+      const HDev dw0 = dev(0);
+      const unsigned g = nblk(n_items * 8 * 32, 256);
+      if (kind == FACE) hm_weights_kernel<FACE><<<g, 256, 0, s>>>(dw0, n_wts);
+      else hm_weights_kernel<VERTEX><<<g, 256, 0, s>>>(dw0, n_wts);
+      RSG_LAUNCHED(ctx, "hm_weights");
+    }
     // far part of H~a: upward over psi = a (m = 1, 2 channels) and far sums per node
     reserve(4);
     std::vector<float2> ones(2 * n_el, make_float2(1.f, 0.f));

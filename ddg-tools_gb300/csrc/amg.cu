@@ -164,10 +164,25 @@ __global__ void __launch_bounds__(128) cg_dots_kernel(int n, const mgreal *__res
   __syncthreads();
   if (!last) return;
   __threadfence();
+  // the last block: the partials strided over its threads, then the same tree
+  double tp[C];
+#pragma unroll
+  for (int c = 0; c < C; ++c) tp[c] = 0.0;
+  for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+#pragma unroll
+    for (int c = 0; c < C; ++c) tp[c] += __ldcg(part + (size_t)b * C + c);
+#pragma unroll
+  for (int c = 0; c < C; ++c) sh[c][threadIdx.x] = tp[c];
+  __syncthreads();
+  for (int st = blockDim.x / 2; st > 0; st >>= 1) {
+    if ((int)threadIdx.x < st)
+#pragma unroll
+      for (int c = 0; c < C; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + st];
+    __syncthreads();
+  }
   const int c = threadIdx.x;
   if (c < C) {
-    double t = 0.0;
-    for (unsigned b = 0; b < gridDim.x; ++b) t += __ldcg(part + (size_t)b * C + c);
+    const double t = sh[c][0];
     if (mode == 0) {
       s[C + c] = (t > 0.0 && s[c] > 0.0) ? s[c] / t : 0.0;
     } else if (mode == 1) {

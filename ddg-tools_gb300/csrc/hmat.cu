@@ -250,11 +250,13 @@ __global__ void hm_weights_kernel(HDev d, size_t total) {
   (void)total;
 }
 
-// One tile of a work item in shared memory: the channel values (hi, lo pairs) of 32 columns
-// and the near weights of up to 8 rows x 32 columns.
+// One tile of a work item in shared memory: the channel values (hi, lo pairs) of 32 columns,
+// channel pair major (consecutive columns in consecutive 16-byte slots, so that the lanes of a
+// load phase reading up to 8 columns meet no bank twice), and the near weights of up to
+// 8 rows x 32 columns.
 template <int KIND, int CC>
 struct alignas(16) RowsTile {
-  float4 m[32][CC / 2];
+  float4 m[CC / 2][32];
   NearW<KIND> w[8][kTileW];
 };
 
@@ -325,7 +327,7 @@ __global__ void __launch_bounds__(128, 5) hm_rows_kernel(HDev d, int c0) {
       const uint32_t q = d.colidx[it.y + t0 + lane];
       const float4 *mq = reinterpret_cast<const float4 *>(d.m + (size_t)q * C + c0);
 #pragma unroll
-      for (int c2 = 0; c2 < CC / 2; ++c2) cp_async16(&tl.m[lane][c2], mq + c2);
+      for (int c2 = 0; c2 < CC / 2; ++c2) cp_async16(&tl.m[c2][lane], mq + c2);
     }
 #pragma unroll
     for (int i = 0; i < 8 * kChunksRow / 32; ++i) {
@@ -359,7 +361,7 @@ __global__ void __launch_bounds__(128, 5) hm_rows_kernel(HDev d, int c0) {
         }
 #pragma unroll
         for (int c2 = 0; c2 < CC / 2; ++c2) {
-          const float4 v = tl.m[k][c2];
+          const float4 v = tl.m[c2][k];
 #pragma unroll
           for (int e = 0; e < 2; ++e) {
             const int c = 2 * c2 + e;

@@ -127,40 +127,53 @@ __device__ __forceinline__ void near_kernel(const HDev &d, float d0, float d1, f
   }
 }
 
-// Bottom-up channel sums in FP64: one thread per leaf sums its elements in registers, then
-// climbs; at every parent the second child to arrive adds left + right (fixed order, no
-// waiting). The far field is FP64 end to end (upward, far sums, chain push-down): its sums
+// Bottom-up channel sums in FP64: one warp per leaf (lanes over the channels) sums its
+// elements in registers, then climbs; at every parent the second child to arrive adds
+// left + right (fixed order, no waiting). The far field is FP64 end to end (upward, far sums, chain push-down): its sums
 // cancel against m_p H~a for a smooth input just as the near sums do, and at O(nodes) and
 // O(far blocks) work the FP64 rate costs little.
 template <int CC>
 __global__ void hm_upward_kernel(HDev d) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  // one warp per leaf, lane l holding channels l, l + 32, ...
+  constexpr int NPL = (CC + 31) / 32;
+  const int k = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
   if (k >= d.n_leaves) return;
-  uint32_t leaf = d.leaves[k];
-  double u[CC];
+  const uint32_t leaf = d.leaves[k];
+  double u[NPL];
 #pragma unroll
-  for (int c = 0; c < CC; ++c) u[c] = 0.0;
+  for (int i = 0; i < NPL; ++i) u[i] = 0.0;
   for (uint32_t p = d.start[leaf]; p < d.end[leaf]; ++p) {
     const double a = d.xh[p].w;
     const float2 *mp = d.m + (size_t)p * CC;
 #pragma unroll
-    for (int c = 0; c < CC; ++c) u[c] = fma(a, (double)mp[c].x + (double)mp[c].y, u[c]);
+    for (int i = 0; i < NPL; ++i) {
+      const int c = lane + 32 * i;
+      if (c < CC) u[i] = fma(a, (double)mp[c].x + (double)mp[c].y, u[i]);
+    }
   }
   double *o = d.up + (size_t)leaf * CC;
 #pragma unroll
-  for (int c = 0; c < CC; ++c) o[c] = u[c];
+  for (int i = 0; i < NPL; ++i)
+    if (lane + 32 * i < CC) o[lane + 32 * i] = u[i];
   uint32_t n = leaf;
   while (n != 0) {
-    uint32_t par = d.parent[n];
-    __threadfence();
-    unsigned old = atomicAdd(&d.count[par], 1u);
-    if ((old & 1u) == 0u) return;
+    const uint32_t par = d.parent[n];
+    __threadfence();  // this warp's sums of n, before the arrival is counted
+    __syncwarp();
+    unsigned old = 0u;
+    if (lane == 0) old = atomicAdd(&d.count[par], 1u);
+    old = __shfl_sync(0xffffffffu, old, 0);
+    if ((old & 1u) == 0u) return;  // first child to arrive: the sibling's warp adds
     __threadfence();
     const double *l = d.up + (size_t)(par + 1) * CC;
     const double *r = d.up + (size_t)d.right[par] * CC;
     double *op = d.up + (size_t)par * CC;
 #pragma unroll
-    for (int c = 0; c < CC; ++c) op[c] = __ldcg(l + c) + __ldcg(r + c);
+    for (int i = 0; i < NPL; ++i) {
+      const int c = lane + 32 * i;
+      if (c < CC) op[c] = __ldcg(l + c) + __ldcg(r + c);
+    }
     n = par;
   }
 }
@@ -410,48 +423,32 @@ __global__ void hm_chain_sum_kernel(HDev d, const double *__restrict__ src, doub
   dst[t] = s;
 }
 
-// Per leaf (thread per row): z = near + (m_p H~a_far - H~(a m)_far), the near sums of the
+// Per (row, channel): z = near + (m_p H~a_far - H~(a m)_far), the near sums of the leaf's
 // items (in item order, as float pairs) plus the leaf's chain sums of the far field (FP64,
 // hm_chain_sum_kernel). The far part of H~a was summed with the same operations from psi = a,
-// so m = 1 gives z = 0 exactly. Channels are taken twelve at a time to bound the registers.
+// so m = 1 gives z = 0 exactly.
 template <int SEL, int CC>
 __global__ void hm_epilogue_kernel(HDev d) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  int k = t >> 3, r = t & 7;
-  if (k >= d.n_leaves) return;
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t row = t / CC;
+  const int c = (int)(t - row * CC);
+  const uint32_t k = (uint32_t)(row >> 3), r = (uint32_t)(row & 7);
+  if (k >= (uint32_t)d.n_leaves) return;
   const uint32_t leaf = d.leaves[k];
   const uint32_t s0 = d.start[leaf];
-  if ((uint32_t)r >= d.end[leaf] - s0) return;
+  if (r >= d.end[leaf] - s0) return;
   const uint32_t p = s0 + r;
-  constexpr int G = CC < 12 ? CC : 12;
-  static_assert(CC % G == 0, "channel groups");
-  const double2 fa = d.leaf_farA[k];
-  const double fa0 = fa.x, fa1 = fa.y;
-  const float2 *mp = d.m + (size_t)p * CC;
-  float2 *zp = d.z + (size_t)p * CC;
-#pragma unroll 1
-  for (int c0 = 0; c0 < CC; c0 += G) {
-    float nh[G], nl[G];
-    double fx[G];
-#pragma unroll
-    for (int c = 0; c < G; ++c) nh[c] = 0.f, nl[c] = 0.f, fx[c] = d.leafsum[(size_t)k * CC + c0 + c];
-    for (uint32_t i = d.item_off[k]; i < d.item_off[k + 1]; ++i) {
-      const float2 *o = d.part + ((size_t)i * 8 + r) * CC + c0;
-#pragma unroll
-      for (int c = 0; c < G; ++c) {
-        const float2 v = o[c];
-        pair_add(nh[c], nl[c], v.x, v.y);
-      }
-    }
-#pragma unroll
-    for (int c = 0; c < G; ++c) {
-      const float2 mv = mp[c0 + c];
-      const double far = ((double)mv.x + (double)mv.y) * (uses_k1<SEL>(c0 + c) ? fa1 : fa0) - fx[c];
-      const double zz = ((double)nh[c] + (double)nl[c]) + far;
-      const float zh = (float)zz;
-      zp[c0 + c] = make_float2(zh, (float)(zz - (double)zh));
-    }
+  float nh = 0.f, nl = 0.f;
+  for (uint32_t i = d.item_off[k]; i < d.item_off[k + 1]; ++i) {
+    const float2 v = d.part[((size_t)i * 8 + r) * CC + c];
+    pair_add(nh, nl, v.x, v.y);
   }
+  const double2 fa = d.leaf_farA[k];
+  const float2 mv = d.m[(size_t)p * CC + c];
+  const double far = ((double)mv.x + (double)mv.y) * (uses_k1<SEL>(c) ? fa.y : fa.x) - d.leafsum[(size_t)k * CC + c];
+  const double zz = ((double)nh + (double)nl) + far;
+  const float zh = (float)zz;
+  d.z[(size_t)p * CC + c] = make_float2(zh, (float)(zz - (double)zh));
 }
 
 // ------------------------------------------------------------------ face prologue / epilogue
@@ -471,25 +468,31 @@ struct FaceOps {
 // Channel values as float pairs on a common grid per channel: hi = k Q with Q = 2^(e - 22) for
 // the channel's largest magnitude 2^e <= max < 2^(e+1), so |k| < 2^24 and the difference of two
 // hi values is exact in FP32; lo = v - hi (|lo| <= Q / 2) rounded to FP32. The near field then
-// forms m_p - m_q with two plain subtractions. qmax holds the channels' largest |v| as the bit
-// patterns of non-negative doubles (ordered like the integers).
+// forms m_p - m_q with two plain subtractions. Only the exponent of the largest magnitude
+// matters: qmax holds, per channel, the largest high word (sign, exponent, leading mantissa
+// bits) of |v| among the channel's values, shifted into the high half of a 64-bit word (the
+// bit pattern of a non-negative double, ordered like the integers). Q is a power of two, so
+// v / Q is the exact product v 2^(22 - e).
+__device__ __forceinline__ double pow2(int k) {  // 2^k, from the bits when it is a normal number
+  return (k >= -1022 && k <= 1023) ? __longlong_as_double((long long)(k + 1023) << 52) : ldexp(1.0, k);
+}
 __device__ __forceinline__ float2 split_q(double v, unsigned long long qbits) {
-  const double mx = __longlong_as_double((long long)qbits);
-  if (!(mx > 0.0)) return make_float2(0.f, 0.f);
-  const double Q = ldexp(1.0, ilogb(mx) - 22);
-  const double hi = rint(v / Q) * Q;
+  const unsigned hw = (unsigned)(qbits >> 32);
+  if (hw == 0u) return make_float2(0.f, 0.f);
+  const int ef = (int)((hw >> 20) & 0x7ffu);
+  const int e = ef ? ef - 1023 : ilogb(__longlong_as_double((long long)qbits));
+  const double hi = rint(v * pow2(22 - e)) * pow2(e - 22);
   return make_float2((float)hi, (float)(v - hi));
 }
 
-// pass 0: the channels' largest magnitudes (a warp maximum, then one atomic per warp and
-// channel; every lane of the warp takes part, `act` false contributing 0); pass 1: the split
-// values
+// pass 0: the channels' largest magnitudes (a warp maximum of the high words, then one atomic
+// per warp and channel; every lane of the warp takes part, `act` false contributing 0);
+// pass 1: the split values
 __device__ __forceinline__ void emit(float2 *mp, int c, double v, unsigned long long *qmax, int pass, bool act) {
   if (pass == 0) {
-    double a = act ? fabs(v) : 0.0;
-#pragma unroll
-    for (int m = 16; m >= 1; m >>= 1) a = fmax(a, __shfl_xor_sync(0xffffffffu, a, m));
-    if ((threadIdx.x & 31) == 0 && a > 0.0) atomicMax(qmax + c, (unsigned long long)__double_as_longlong(a));
+    unsigned a = act ? (unsigned)((unsigned long long)__double_as_longlong(fabs(v)) >> 32) : 0u;
+    a = __reduce_max_sync(0xffffffffu, a);
+    if ((threadIdx.x & 31) == 0 && a != 0u) atomicMax(qmax + c, (unsigned long long)a << 32);
   } else if (act) {
     mp[c] = split_q(v, qmax[c]);
   }
@@ -497,7 +500,9 @@ __device__ __forceinline__ void emit(float2 *mp, int c, double v, unsigned long 
 
 // m per face in BVH order (FaceMetricTree::product, hierarchical.rs:711-746), in FP64 and
 // stored as float pairs; vector q owns channels 12q + (3k + r) = sum_c x[3 t_c + k] g_c[r]
-// (gradient) and 12q + 9 + k = (x_0 + x_1 + x_2)/3 for axis k (average).
+// (gradient) and 12q + 9 + k = (x_0 + x_1 + x_2)/3 for axis k (average; the division by 3 is
+// a product with the rounded 1/3, within an FP64 unit of the quotient, far below the float
+// pairs' resolution).
 __global__ void face_m_kernel(FaceOps o, const double *__restrict__ xs, size_t ldx, int nb, int C,
                               float2 *m, unsigned long long *qmax, int pass) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -512,7 +517,7 @@ __global__ void face_m_kernel(FaceOps o, const double *__restrict__ xs, size_t l
       const double x0 = x[3 * (size_t)t[0] + k], x1 = x[3 * (size_t)t[1] + k], x2 = x[3 * (size_t)t[2] + k];
       for (int r = 0; r < 3; ++r)
         emit(mp, 12 * q + 3 * k + r, x0 * g[r] + x1 * g[3 + r] + x2 * g[6 + r], qmax, pass, act);
-      emit(mp, 12 * q + 9 + k, ((x0 + x1) + x2) / 3.0, qmax, pass, act);
+      emit(mp, 12 * q + 9 + k, ((x0 + x1) + x2) * (1.0 / 3.0), qmax, pass, act);
     }
   }
   if (pass == 1 && act)
@@ -675,7 +680,7 @@ struct HMat {
     size_t nn = tree.n_nodes(), nl = tree.leaves.size();
     cudaStream_t s = st();
     prof.begin(s, kind == FACE ? "metric_upward" : "vfrac_upward");
-    hm_upward_kernel<CC><<<nblk(nl, 128), 128, 0, s>>>(d);
+    hm_upward_kernel<CC><<<nblk(nl * 32, 128), 128, 0, s>>>(d);
     RSG_LAUNCHED(ctx, "hm_upward");
     prof.end(s);
     prof.begin(s, kind == FACE ? "metric_far" : "vfrac_far");
@@ -823,7 +828,6 @@ struct HMat {
   template <int K, int CC>
   void product_cc(int nb) {
     cudaStream_t s = st();
-    size_t nl = tree.leaves.size();
     HDev d = dev(CC);
     constexpr int SEL = K == FACE ? FACE_CH : VERTEX_CH;
     upward_far<SEL, CC>(d);
@@ -839,9 +843,15 @@ struct HMat {
     }
     prof.end(s);
     prof.begin(s, K == FACE ? "metric_epilogue" : "vfrac_epilogue");
-    hm_epilogue_kernel<SEL, CC><<<nblk(nl * 8, 128), 128, 0, s>>>(d);
-    RSG_LAUNCHED(ctx, "hm_epilogue");
+    epilogue<SEL, CC>(d);
     prof.end(s);
+  }
+
+  // z from the near partial sums and the far chain sums (one thread per row and channel)
+  template <int SEL, int CC>
+  void epilogue(const HDev &d) {
+    hm_epilogue_kernel<SEL, CC><<<nblk(tree.leaves.size() * 8 * CC, 256), 256, 0, st()>>>(d);
+    RSG_LAUNCHED(ctx, "hm_epilogue");
   }
 
   void product(int nb) {
@@ -1269,8 +1279,7 @@ void noalloc_face_group(rs_metric *M, const HDev &d, unsigned long long *qmax, i
     hm_rows_kernel<FACE, 12><<<nblk(h.n_items * 32, 128), 128, 0, s>>>(d, 12 * q);
     RSG_LAUNCHED(h.ctx, "hm_rows");
   }
-  hm_epilogue_kernel<FACE_CH, CC><<<nblk(h.tree.leaves.size() * 8, 128), 128, 0, s>>>(d);
-  RSG_LAUNCHED(h.ctx, "hm_epilogue");
+  h.epilogue<FACE_CH, CC>(d);
   face_gather_kernel<<<nblk(M->nv, 128), 128, 0, s>>>(M->ops(), d.z, k, CC, w_hi, w_lo, ys, ldy);
   RSG_LAUNCHED(h.ctx, "face_gather");
 }

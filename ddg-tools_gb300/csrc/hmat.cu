@@ -49,7 +49,10 @@ __device__ __forceinline__ bool uses_k1(int c) {
 struct HDev {
   const uint32_t *start, *end, *right, *parent, *leaves, *chain_off, *chain;
   const uint32_t *far_ptr, *far_col;
-  const double2 *far_coef;   // per far block: (k_0, k_1)
+  const uint4 *far_items;       // per far work item: node, block range [y, z) (at most kFarChunk), -
+  const uint32_t *far_item_off; // per node: its far items [far_item_off[a], far_item_off[a + 1])
+  float2 *fpart;                // per far item: C channel partial sums (float pairs)
+  const float4 *far_coef;    // per far block: (k_0, k_1) as float pairs (k_0 hi, k_0 lo, k_1 hi, k_1 lo)
   const float4 *xh;          // per BVH position: position hi (xyz), weight a (w)
   const float4 *xl;          // per BVH position: position lo (xyz): X = hi + lo to ~48 bits
   const float4 *nrm;         // per BVH position: normal (faces only)
@@ -60,12 +63,13 @@ struct HDev {
   const void *wts;           // near weights per item: rows x (columns padded to 32), see NearW
   const uint32_t *item_off;  // per leaf: its work items [item_off[k], item_off[k + 1])
   double *up;                // per node: C channel sums of a m (FP64)
+  float2 *up2;               // the same sums as float pairs (hi, lo), read by the far sums
   double *farx;              // per node: C channel far sums (FP64)
   float2 *part;              // per work item: 8 rows x C near sums as float pairs
   uint32_t *count;           // per node: arrival counter of the upward pass
   const float2 *m;           // [n][C] channel values as float pairs (hi, lo)
   float2 *z;                 // [n][C] results as float pairs
-  int n_nodes, n_leaves, n_el, n_items, C;
+  int n_nodes, n_leaves, n_el, n_items, n_far_items, C;
   float neg_s;               // kernel exponent e applied to r^2: r2^e
   int pw_mode, pw_k;         // e = pw_k / pw_mode for pw_mode 2 or 3 (exact roots), else powf
 };
@@ -78,6 +82,12 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &t) {
 }
 
 // (h, l) += (oh, ol) for float pairs.
+// v as a float pair: hi = v rounded to FP32, lo = the rest rounded
+__device__ __forceinline__ float2 to_pair(double v) {
+  const float h = (float)v;
+  return make_float2(h, (float)(v - (double)h));
+}
+
 __device__ __forceinline__ void pair_add(float &h, float &l, float oh, float ol) {
   float s, t;
   two_sum(h, oh, s, t);
@@ -153,9 +163,10 @@ __global__ void hm_upward_kernel(HDev d) {
     }
   }
   double *o = d.up + (size_t)leaf * CC;
+  float2 *o2 = d.up2 + (size_t)leaf * CC;
 #pragma unroll
   for (int i = 0; i < NPL; ++i)
-    if (lane + 32 * i < CC) o[lane + 32 * i] = u[i];
+    if (lane + 32 * i < CC) o[lane + 32 * i] = u[i], o2[lane + 32 * i] = to_pair(u[i]);
   uint32_t n = leaf;
   while (n != 0) {
     const uint32_t par = d.parent[n];
@@ -169,55 +180,92 @@ __global__ void hm_upward_kernel(HDev d) {
     const double *l = d.up + (size_t)(par + 1) * CC;
     const double *r = d.up + (size_t)d.right[par] * CC;
     double *op = d.up + (size_t)par * CC;
+    float2 *op2 = d.up2 + (size_t)par * CC;
 #pragma unroll
     for (int i = 0; i < NPL; ++i) {
       const int c = lane + 32 * i;
-      if (c < CC) op[c] = __ldcg(l + c) + __ldcg(r + c);
+      if (c < CC) {
+        const double v = __ldcg(l + c) + __ldcg(r + c);
+        op[c] = v, op2[c] = to_pair(v);
+      }
     }
     n = par;
   }
 }
 
 // farx[a][c] = sum over the far blocks (a, b) of h(a, b)[kernel(c)] up[b][c] (block_tree.rs:
-// 564-578), FP64. One warp per (node, group of at most twelve channels): lane = sub CG + c
-// holds channel c of the group and takes the node's far blocks sub, sub + 2, ... (sub = 0, 1);
-// the two partial sums are then added. The order of the operations does not depend on the
-// channel count, so the pass over psi = a (two channels) and a product pass add the same
-// terms in the same order.
+// 564-578) in double-float arithmetic: the coefficients and the node sums are float pairs
+// (about 48 bits), each product is formed exactly to that width (FMA) and added by error-free
+// transformations; the result is handed on in FP64. GB300 issues FP32 at many times its FP64
+// rate. One warp per (node, group of at most twelve channels): lane = sub CG + c holds channel
+// c of the group and takes the node's far blocks sub, sub + 2, ... (sub = 0, 1); the two
+// partial sums are then added. The operations do not depend on the channel count, so the pass
+// over psi = a (two channels) and a product pass add the same terms in the same order.
+__device__ __forceinline__ void df_fma(float &ah, float &al, float kh, float kl, float uh, float ul) {
+  const float ph = kh * uh;
+  float pe = fmaf(kh, uh, -ph);
+  pe = fmaf(kh, ul, pe);
+  pe = fmaf(kl, uh, pe);
+  float sh, se;
+  two_sum(ah, ph, sh, se);
+  se += al + pe;
+  ah = sh + se;
+  al = se - (ah - sh);
+}
+
 template <int SEL, int CC>
 __global__ void hm_far_kernel(HDev d) {
   constexpr int CG = CC < 12 ? CC : 12;
   static_assert(CC % CG == 0 && 2 * CG <= 32, "channel groups");
   constexpr int NG = CC / CG;
   const int wg = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
-  const int a = wg / NG, grp = wg - a * NG;
-  if (a >= d.n_nodes) return;
+  const int w = wg / NG, grp = wg - w * NG;
+  if (w >= d.n_far_items) return;
+  const uint4 it = d.far_items[w];
   const int lane = threadIdx.x & 31, sub = lane / CG, c = lane - sub * CG;
   const int ch = grp * CG + c;
-  double acc = 0.0;
+  float ah = 0.f, al = 0.f;
   if (sub < 2) {
     const bool k1 = uses_k1<SEL>(ch);
-    const uint32_t q1 = d.far_ptr[a + 1];
-    uint32_t q = d.far_ptr[a] + sub;
+    uint32_t q = it.y + sub;
     // four of the lane's blocks at a time: loads first, then the additions in order
-    for (; q + 6 < q1; q += 8) {
-      double kk[4], u[4];
+    for (; q + 6 < it.z; q += 8) {
+      float4 kk[4];
+      float2 u[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        const double2 k = d.far_coef[q + 2 * i];
-        kk[i] = k1 ? k.y : k.x;
-        u[i] = d.up[(size_t)d.far_col[q + 2 * i] * CC + ch];
+        kk[i] = d.far_coef[q + 2 * i];
+        u[i] = d.up2[(size_t)d.far_col[q + 2 * i] * CC + ch];
       }
 #pragma unroll
-      for (int i = 0; i < 4; ++i) acc = fma(kk[i], u[i], acc);
+      for (int i = 0; i < 4; ++i)
+        df_fma(ah, al, k1 ? kk[i].z : kk[i].x, k1 ? kk[i].w : kk[i].y, u[i].x, u[i].y);
     }
-    for (; q < q1; q += 2) {
-      const double2 k = d.far_coef[q];
-      acc = fma(k1 ? k.y : k.x, d.up[(size_t)d.far_col[q] * CC + ch], acc);
+    for (; q < it.z; q += 2) {
+      const float4 k = d.far_coef[q];
+      const float2 u = d.up2[(size_t)d.far_col[q] * CC + ch];
+      df_fma(ah, al, k1 ? k.z : k.x, k1 ? k.w : k.y, u.x, u.y);
     }
   }
-  acc += __shfl_down_sync(0xffffffffu, acc, CG);
-  if (sub == 0) d.farx[(size_t)a * CC + ch] = acc;
+  const float oh = __shfl_down_sync(0xffffffffu, ah, CG), ol = __shfl_down_sync(0xffffffffu, al, CG);
+  pair_add(ah, al, oh, ol);
+  if (sub == 0) d.fpart[(size_t)w * CC + ch] = make_float2(ah, al);
+}
+
+// farx[a][c]: the node's item partials added in item order as float pairs, handed on in FP64
+// (zero for a node without far blocks); one thread per (node, channel)
+template <int CC>
+__global__ void hm_far_final_kernel(HDev d) {
+  const size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= (size_t)d.n_nodes * CC) return;
+  const size_t a = t / CC;
+  const int c = (int)(t - a * CC);
+  float h = 0.f, l = 0.f;
+  for (uint32_t i = d.far_item_off[a]; i < d.far_item_off[a + 1]; ++i) {
+    const float2 v = d.fpart[(size_t)i * CC + c];
+    pair_add(h, l, v.x, v.y);
+  }
+  d.farx[t] = (double)h + (double)l;
 }
 
 // Near weights of an element pair as the rows kernel applies them: faces (w_0, w_1) =
@@ -226,7 +274,8 @@ __global__ void hm_far_kernel(HDev d) {
 // starts on a 128-byte boundary.
 template <int KIND>
 using NearW = typename std::conditional<KIND == FACE, float2, float>::type;
-constexpr int kTileW = 36;  // shared-memory row stride of a weight tile (bank spread)
+constexpr int kTileW = 36;          // shared-memory row stride of a weight tile (bank spread)
+constexpr uint32_t kFarChunk = 64;  // far blocks per far work item
 
 template <int KIND>
 __global__ void hm_weights_kernel(HDev d, size_t total) {
@@ -620,15 +669,20 @@ struct HMat {
   size_t n_el = 0, n_items = 0;
   double neg_s = 0;
   DevBuf<uint32_t> start, end, right, parent, leaves, chain_off, chain, item_off;
-  DevBuf<uint32_t> far_ptr, far_col, count;
+  DevBuf<uint32_t> far_ptr, far_col, count, far_item_off;
+  DevBuf<uint4> far_items;
+  size_t n_far_items = 0;
+  DevBuf<float2> fpart;
   DevBuf<uint32_t> colidx;
   DevBuf<uint4> items;
   DevBuf<unsigned char> wts;  // near weights (NearW per entry), see hm_weights_kernel
   size_t n_wts = 0;
-  DevBuf<double2> far_coef, leaf_farA;
+  DevBuf<float4> far_coef;
+  DevBuf<double2> leaf_farA;
   DevBuf<double> leafsum;
   DevBuf<float4> xh, xl, nrm;
   DevBuf<double> up, farx;
+  DevBuf<float2> up2;
   DevBuf<float2> part, m, z;
   DevBuf<unsigned long long> qmax;  // per channel: largest |m| (see split_q)
   int pw_mode = 0, pw_k = 0;
@@ -639,9 +693,11 @@ struct HMat {
     d.start = start.p, d.end = end.p, d.right = right.p, d.parent = parent.p, d.leaves = leaves.p;
     d.chain_off = chain_off.p, d.chain = chain.p;
     d.far_ptr = far_ptr.p, d.far_col = far_col.p, d.far_coef = far_coef.p;
+    d.far_items = far_items.p, d.far_item_off = far_item_off.p, d.fpart = fpart.p;
+    d.n_far_items = (int)n_far_items;
     d.xh = xh.p, d.xl = xl.p, d.nrm = nrm.p, d.leaf_farA = leaf_farA.p;
     d.colidx = colidx.p, d.items = items.p, d.item_off = item_off.p, d.wts = wts.p;
-    d.up = up.p, d.farx = farx.p, d.part = part.p, d.count = count.p, d.leafsum = leafsum.p;
+    d.up = up.p, d.up2 = up2.p, d.farx = farx.p, d.part = part.p, d.count = count.p, d.leafsum = leafsum.p;
     d.m = m.p, d.z = z.p;
     d.n_nodes = (int)tree.n_nodes(), d.n_leaves = (int)tree.leaves.size(), d.n_el = (int)n_el;
     d.n_items = (int)n_items;
@@ -655,7 +711,8 @@ struct HMat {
   // Channel scratch for C channels.
   void reserve(int C_) {
     size_t nn = tree.n_nodes();
-    if ((size_t)C_ * nn > up.n) up.alloc((size_t)C_ * nn), farx.alloc((size_t)C_ * nn);
+    if ((size_t)C_ * nn > up.n) up.alloc((size_t)C_ * nn), up2.alloc((size_t)C_ * nn), farx.alloc((size_t)C_ * nn);
+    if ((size_t)C_ * n_far_items > fpart.n) fpart.alloc(std::max<size_t>((size_t)C_ * n_far_items, 1));
     if ((size_t)C_ * tree.leaves.size() > leafsum.n) leafsum.alloc((size_t)C_ * tree.leaves.size());
     if ((size_t)C_ * n_el > m.n) m.alloc((size_t)C_ * n_el), z.alloc((size_t)C_ * n_el);
     if (n_items * 8 * (size_t)C_ > part.n) part.alloc(std::max<size_t>(n_items * 8 * (size_t)C_, 1));
@@ -684,8 +741,12 @@ struct HMat {
     RSG_LAUNCHED(ctx, "hm_upward");
     prof.end(s);
     prof.begin(s, kind == FACE ? "metric_far" : "vfrac_far");
-    hm_far_kernel<SEL, CC><<<nblk(nn * (CC < 12 ? 1 : CC / 12) * 32, 256), 256, 0, s>>>(d);
-    RSG_LAUNCHED(ctx, "hm_far");
+    if (n_far_items > 0) {  // chi = 0 (all near) has none
+      hm_far_kernel<SEL, CC><<<nblk(n_far_items * (CC < 12 ? 1 : CC / 12) * 32, 256), 256, 0, s>>>(d);
+      RSG_LAUNCHED(ctx, "hm_far");
+    }
+    hm_far_final_kernel<CC><<<nblk(nn * CC, 256), 256, 0, s>>>(d);
+    RSG_LAUNCHED(ctx, "hm_far_final");
     if (SEL != ONES) {
       hm_chain_sum_kernel<CC><<<nblk(nl * CC, 256), 256, 0, s>>>(d, d.farx, d.leafsum);
       RSG_LAUNCHED(ctx, "hm_chain_sum");
@@ -766,10 +827,22 @@ struct HMat {
     up_vec(parent, parent_h, s), up_vec(leaves, T.leaves, s), up_vec(chain_off, coff, s);
     up_vec(chain, chain_h, s), up_vec(colidx, cols_h, s), up_vec(items, items_h, s), up_vec(item_off, ioff, s);
     up_vec(far_ptr, blocks.far_ptr, s), up_vec(far_col, blocks.far_col, s);
+    {
+      std::vector<uint4> fi;
+      std::vector<uint32_t> fo(nn + 1, 0);
+      for (size_t a = 0; a < nn; ++a) {
+        for (uint32_t q0 = blocks.far_ptr[a]; q0 < blocks.far_ptr[a + 1]; q0 += kFarChunk)
+          fi.push_back(make_uint4((uint32_t)a, q0, std::min(q0 + kFarChunk, blocks.far_ptr[a + 1]), 0));
+        fo[a + 1] = (uint32_t)fi.size();
+      }
+      n_far_items = fi.size();
+      up_vec(far_items, fi, s), up_vec(far_item_off, fo, s);
+    }
     count.alloc(nn);
     RSG_CUDA("upload", cudaMemsetAsync(count.p, 0, nn * sizeof(uint32_t), s));
     // far coefficients on the host in FP64 (kernel.far, hierarchical.rs:210-220 / 980-984)
-    std::vector<double2> coef(blocks.far_col.size());
+    std::vector<float4> coef(blocks.far_col.size());  // (k_0, k_1) as float pairs
+    auto fpair = [](double v, float &h, float &l) { h = (float)v, l = (float)(v - (double)h); };
     auto qf = [&](size_t n, const double *d) {
       const double *p = proj6 + 6 * n;
       return p[0] * d[0] * d[0] + p[3] * d[1] * d[1] + p[5] * d[2] * d[2] +
@@ -785,7 +858,9 @@ struct HMat {
           double h = std::pow(r2, neg_s);
           double h1 = h;
           if (kind == FACE) h1 = 0.5 * (qf(lo, d) + qf(hi, d)) / (r2 * r2) * h;
-          coef[q] = make_double2(h, h1);
+          float4 k;
+          fpair(h, k.x, k.y), fpair(h1, k.z, k.w);
+          coef[q] = k;
         }
     }, 256);
     up_vec(far_coef, coef, s);
@@ -1234,9 +1309,11 @@ inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 // Scratch bytes of one tree pass with C channels (the layout carved below).
 size_t noalloc_bytes(const HMat &h, int C) {
   size_t nn = h.tree.n_nodes();
-  return 2 * align256(nn * C * sizeof(double)) + 2 * align256(h.n_el * C * sizeof(float2)) +
+  return 2 * align256(nn * C * sizeof(double)) + align256(nn * C * sizeof(float2)) +
+         2 * align256(h.n_el * C * sizeof(float2)) +
          align256(std::max<size_t>(h.n_items, 1) * 8 * C * sizeof(float2)) +
-         align256(h.tree.leaves.size() * C * sizeof(double)) + align256(64 * sizeof(unsigned long long));
+         align256(h.tree.leaves.size() * C * sizeof(double)) +
+         align256(std::max<size_t>(h.n_far_items, 1) * C * sizeof(float2)) + align256(64 * sizeof(unsigned long long));
 }
 
 HDev noalloc_dev(const HMat &h, int C, unsigned char *base) {
@@ -1248,11 +1325,13 @@ HDev noalloc_dev(const HMat &h, int C, unsigned char *base) {
     return p;
   };
   d.up = reinterpret_cast<double *>(take(nn * C * sizeof(double)));
+  d.up2 = reinterpret_cast<float2 *>(take(nn * C * sizeof(float2)));
   d.farx = reinterpret_cast<double *>(take(nn * C * sizeof(double)));
   d.m = reinterpret_cast<const float2 *>(take(h.n_el * C * sizeof(float2)));
   d.z = reinterpret_cast<float2 *>(take(h.n_el * C * sizeof(float2)));
   d.part = reinterpret_cast<float2 *>(take(std::max<size_t>(h.n_items, 1) * 8 * C * sizeof(float2)));
   d.leafsum = reinterpret_cast<double *>(take(h.tree.leaves.size() * C * sizeof(double)));
+  d.fpart = reinterpret_cast<float2 *>(take(std::max<size_t>(h.n_far_items, 1) * C * sizeof(float2)));
   return d;
 }
 

@@ -17,33 +17,65 @@ constexpr int RB = 256;  // reduction blocks of the dot products (fixed: determi
 inline unsigned nb_(size_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
 
 // Partial sums of v_i . w over a fixed row split: block b owns rows [b c, (b+1) c).
-__global__ void dots_partial_kernel(const double *const *vs, int nvec, const double *__restrict__ w,
-                                    size_t n, double *partial) {
-  __shared__ double sh[256];
+constexpr int kDotVecs = 8;  // vectors per pass over w
+
+// out[i] = v_i . w (sqrt of it with `root`) for i < nvec, v_i = vs[i] (or v1 when given, nvec =
+// 1). Each block takes a fixed row range and up to kDotVecs vectors per pass over it (w read
+// once per pass), reduces by warp shuffles and then over the warps in order, and writes its
+// partials; the last block to finish (a ticket counter, reset by that block) adds the
+// partials of every vector in block order, a warp per vector. Deterministic: the grid, the
+// row ranges and every reduction order are fixed.
+__global__ void __launch_bounds__(256) dots_kernel(const double *const *vs, const double *v1, int nvec,
+                                                   const double *__restrict__ w, size_t n, double *part,
+                                                   unsigned *ticket, double *out, int root) {
+  __shared__ double sh[8][kDotVecs];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const size_t chunk = (n + gridDim.x - 1) / gridDim.x;
   const size_t r0 = blockIdx.x * chunk, r1 = min(n, r0 + chunk);
-  for (int i = 0; i < nvec; ++i) {
-    const double *v = vs[i];
-    double acc = 0.0;
-    for (size_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) acc = fma(v[r], w[r], acc);
-    sh[threadIdx.x] = acc;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-      if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
-      __syncthreads();
+  for (int i0 = 0; i0 < nvec; i0 += kDotVecs) {
+    const double *vp[kDotVecs];
+    double acc[kDotVecs];
+#pragma unroll
+    for (int j = 0; j < kDotVecs; ++j) {
+      vp[j] = (i0 + j < nvec) ? (v1 ? v1 : vs[i0 + j]) : nullptr;
+      acc[j] = 0.0;
     }
-    if (threadIdx.x == 0) partial[(size_t)blockIdx.x * nvec + i] = sh[0];
+    for (size_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+      const double wr = w[r];
+#pragma unroll
+      for (int j = 0; j < kDotVecs; ++j)
+        if (vp[j]) acc[j] = fma(vp[j][r], wr, acc[j]);
+    }
+#pragma unroll
+    for (int j = 0; j < kDotVecs; ++j) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], o);
+      if (lane == 0) sh[wid][j] = acc[j];
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < kDotVecs && i0 + (int)threadIdx.x < nvec) {
+      double t = 0.0;
+      for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sh[k][threadIdx.x];
+      part[(size_t)blockIdx.x * nvec + i0 + threadIdx.x] = t;
+    }
     __syncthreads();
   }
-}
-
-__global__ void dots_final_kernel(const double *partial, int nblocks, int nvec, double *out,
-                                  const double *add) {
-  int i = threadIdx.x;
-  if (i >= nvec) return;
-  double s = 0.0;
-  for (int b = 0; b < nblocks; ++b) s += partial[(size_t)b * nvec + i];
-  out[i] = add ? s + add[i] : s;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int i = wid; i < nvec; i += (int)(blockDim.x >> 5)) {
+    double t = 0.0;
+    for (unsigned b = lane; b < gridDim.x; b += 32) t += __ldcg(part + (size_t)b * nvec + i);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) out[i] = root ? sqrt(t) : t;
+  }
+  if (threadIdx.x == 0) *ticket = 0u;
 }
 
 // w -= sum_i h_i v_i (sign = -1) or x += sum_i h_i v_i (sign = +1).
@@ -71,18 +103,20 @@ __global__ void sub_kernel(const double *a, const double *b, double *y, size_t n
     y[r] = a[r] - b[r];
 }
 
-__global__ void sqrt_kernel(double *x) { *x = sqrt(*x); }
 
 }  // namespace
 
 void dev_dots(rs_ctx *ctx, const double *const *vs, int nvec, const double *w, size_t n,
-              double *out_dev) {
+              double *out_dev, const double *v1, bool root) {
   static thread_local DevBuf<double> partial;
-  if (partial.n < (size_t)RB * 64) partial.alloc((size_t)RB * 64);
-  dots_partial_kernel<<<RB, 256, 0, ctx->stream>>>(vs, nvec, w, n, partial.p);
-  RSG_LAUNCHED(ctx, "dots_partial");
-  dots_final_kernel<<<1, 64, 0, ctx->stream>>>(partial.p, RB, nvec, out_dev, nullptr);
-  RSG_LAUNCHED(ctx, "dots_final");
+  static thread_local DevBuf<unsigned> ticket;
+  if (nvec < 1 || nvec > 64) fail(RS_INTERNAL, "Internal", "gmres", "1 to 64 vectors per dot-product launch");
+  if (partial.n < (size_t)RB * 64) {
+    partial.alloc((size_t)RB * 64), ticket.alloc(1);
+    RSG_CUDA("gmres", cudaMemsetAsync(ticket.p, 0, sizeof(unsigned), ctx->stream));
+  }
+  dots_kernel<<<RB, 256, 0, ctx->stream>>>(vs, v1, nvec, w, n, partial.p, ticket.p, out_dev, root ? 1 : 0);
+  RSG_LAUNCHED(ctx, "dots");
 }
 
 namespace {
@@ -90,7 +124,7 @@ namespace {
 // Per right-hand side: the device basis, the host Hessenberg / Givens state.
 struct Rhs {
   DevBuf<double> V, Z, w, r, h;           // V: (m+1) n, Z: m n, h: 2 (m+2) scratch
-  DevBuf<const double *> vptr, zptr, wptr;  // pointer tables for the multi-vector kernels
+  DevBuf<const double *> vptr, zptr;  // pointer tables for the multi-vector kernels
   std::vector<double> H, cs, sn, g, hcol;
   double bnorm = 0, beta = 0;
   int j = 0;
@@ -114,13 +148,7 @@ void gmres_batch(rs_ctx *ctx, const Operator &A, const Operator *P, int nb, cons
   DevBuf<double> xbuf((size_t)nb * n), ybuf((size_t)nb * n);  // batched operator in/out
   DevBuf<double> norm2(1);
   // one norm: dots of w with itself, then sqrt
-  auto norm_dev = [&](Rhs &q, const double *v, double *out) {
-    const double *ptrs[1] = {v};
-    RSG_CUDA("gmres", rsg::copy_async(q.wptr.p, ptrs, sizeof(ptrs), cudaMemcpyHostToDevice, s));
-    dev_dots(ctx, q.wptr.p, 1, v, n, out);
-    sqrt_kernel<<<1, 1, 0, s>>>(out);
-    RSG_LAUNCHED(ctx, "sqrt");
-  };
+  auto norm_dev = [&](Rhs &, const double *v, double *out) { dev_dots(ctx, nullptr, 1, v, n, out, v, true); };
   auto host_value = [&](const double *dev) {
     double v;
     RSG_CUDA("gmres", rsg::copy_async(&v, dev, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -135,7 +163,7 @@ void gmres_batch(rs_ctx *ctx, const Operator &A, const Operator *P, int nb, cons
     Q.w.alloc(n);
     Q.r.alloc(n);
     Q.h.alloc(2 * (size_t)(m + 2) + 2);
-    Q.vptr.alloc(m + 1), Q.zptr.alloc(m), Q.wptr.alloc(1);
+    Q.vptr.alloc(m + 1), Q.zptr.alloc(m);
     std::vector<const double *> vp(m + 1), zp(m);
     for (int i = 0; i <= m; ++i) vp[i] = Q.V.p + (size_t)i * n;
     for (int i = 0; i < m; ++i) zp[i] = Q.Z.p + (size_t)i * n;
@@ -339,11 +367,8 @@ void gmres_batch(rs_ctx *ctx, const Operator &A, const Operator *P, int nb, cons
 }
 
 double dev_norm(rs_ctx *ctx, const double *w, size_t n) {
-  DevBuf<const double *> p(1);
   DevBuf<double> out(1);
-  const double *ptrs[1] = {w};
-  RSG_CUDA("gmres", rsg::copy_async(p.p, ptrs, sizeof(ptrs), cudaMemcpyHostToDevice, ctx->stream));
-  dev_dots(ctx, p.p, 1, w, n, out.p);
+  dev_dots(ctx, nullptr, 1, w, n, out.p, w, false);
   double v;
   RSG_CUDA("gmres", rsg::copy_async(&v, out.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   RSG_CUDA("gmres", cudaStreamSynchronize(ctx->stream));

@@ -42,8 +42,10 @@ void gmres_batch(rs_ctx *ctx, const Operator &A, const Operator *P, int nb, cons
                  double *x, const GmresOptions &opt, std::vector<GmresReport> &reports);
 
 // FP64 helpers (deterministic: fixed grid, fixed reduction trees).
+// out[i] = v_i . w for v_i = vs[i], or for the single vector v1 when given (nvec = 1); root:
+// out = sqrt of it
 void dev_dots(rs_ctx *ctx, const double *const *vs, int nvec, const double *w, size_t n,
-              double *out_dev);  // out[i] = v_i . w
+              double *out_dev, const double *v1 = nullptr, bool root = false);
 double dev_norm(rs_ctx *ctx, const double *w, size_t n);
 
 }  // namespace rsg

@@ -38,11 +38,34 @@ namespace {
 inline unsigned nblk(size_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
 constexpr int GB = 128;  // reduction blocks of the group sums
 
+// The end of a group-sum launch: the block's K partials are in part; the last block to finish
+// (a ticket counter, reset by that block) adds every entry's partials in block order, a warp
+// per entry with the lanes strided over the blocks, and writes out.
+__device__ __forceinline__ void finish_group_sums(const double *part, int K, unsigned *ticket, double *out) {
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const int lane = threadIdx.x & 31;
+  for (int i = threadIdx.x >> 5; i < K; i += (int)(blockDim.x >> 5)) {
+    double t = 0.0;
+    for (unsigned b = lane; b < gridDim.x; b += 32) t += __ldcg(part + (size_t)b * K + i);
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) out[i] = t;
+  }
+  if (threadIdx.x == 0) *ticket = 0u;
+}
+
 // part[b][q][3 g + k] = sum over the block's vertices v of group g of wgt_v x_q[3 v + k]
 // (wgt = null: weight 1). x has leading dimension ld; G groups.
 __global__ void group_sums_partial(const double *__restrict__ x, size_t ld, int nb, int nv,
                                    const uint32_t *__restrict__ group, const double *__restrict__ wgt,
-                                   int G, double *part) {
+                                   int G, double *part, unsigned *ticket, double *out) {
   extern __shared__ double sh[];  // 3 G nb per block
   const int K = 3 * G * nb;
   for (int i = threadIdx.x; i < K; i += blockDim.x) sh[i] = 0.0;
@@ -69,15 +92,9 @@ __global__ void group_sums_partial(const double *__restrict__ x, size_t ld, int 
         __syncthreads();
       }
   for (int i = threadIdx.x; i < K; i += blockDim.x) part[(size_t)blockIdx.x * K + i] = sh[i];
+  finish_group_sums(part, K, ticket, out);
 }
 
-__global__ void group_sums_final(const double *part, int nblocks, int K, double *out) {
-  int i = threadIdx.x + blockIdx.x * blockDim.x;
-  if (i >= K) return;
-  double s = 0.0;
-  for (int b = 0; b < nblocks; ++b) s += part[(size_t)b * K + i];
-  out[i] = s;
-}
 
 // Operator tail: y_pos += c_v l_{g(v)} and y_mult = C_Q x (from the group sums `cx`).
 __global__ void cq_apply_kernel(const double *__restrict__ x, double *__restrict__ y, size_t ld,
@@ -186,6 +203,7 @@ struct rs_solver {
   AmgDevice amg;
   DevBuf<uint32_t> group;
   DevBuf<double> c, eps_area, part, s1, mu, cy, shift, tmp, tmp2;
+  DevBuf<unsigned> gs_ticket;  // blocks done in the current group-sum launch (0 between launches)
   DevBuf<mgreal> mg_in, mg_out;  // right-hand sides and solutions on the multigrid layout
   std::vector<GmresReport> last;
   Operator op, prec;
@@ -196,10 +214,9 @@ struct rs_solver {
   void group_sums(const double *x, size_t ld, int nb, const double *wgt, double *out) {
     int K = 3 * G * nb;
     if (part.n < (size_t)GB * K) part.alloc((size_t)GB * K);
-    group_sums_partial<<<GB, 256, (size_t)K * sizeof(double), st()>>>(x, ld, nb, nv, group.p, wgt, G, part.p);
+    group_sums_partial<<<GB, 256, (size_t)K * sizeof(double), st()>>>(x, ld, nb, nv, group.p, wgt, G, part.p,
+                                                                      gs_ticket.p, out);
     RSG_LAUNCHED(ctx, "group_sums");
-    group_sums_final<<<nblk(K, 128), 128, 0, st()>>>(part.p, GB, K, out);
-    RSG_LAUNCHED(ctx, "group_sums_final");
   }
 
   void reserve(int nb) {
@@ -315,7 +332,7 @@ __global__ void add_kernel(size_t m, const double *x, double *y) {
 // cy[q][3g + k] = sum_{v in g} c_v yy[v][3q + k]  (weighted group sums on the multigrid layout)
 __global__ void mg_group_partial(const mgreal *__restrict__ yy, int nb, int nv,
                                  const uint32_t *__restrict__ group, const double *__restrict__ c,
-                                 int G, double *part) {
+                                 int G, double *part, unsigned *ticket, double *out) {
   const int K = 3 * G * nb;
   const size_t chunk = (nv + gridDim.x - 1) / gridDim.x;
   const size_t v0 = blockIdx.x * chunk, v1 = min((size_t)nv, v0 + chunk);
@@ -335,6 +352,7 @@ __global__ void mg_group_partial(const mgreal *__restrict__ yy, int nb, int nv,
     }
     __syncthreads();
   }
+  finish_group_sums(part, K, ticket, out);
 }
 
 }  // namespace
@@ -351,10 +369,8 @@ void rs_solver::add_into(size_t m, const double *x, double *y) {
 void rs_solver::pos_copy_weighted(int nb) {
   int K = 3 * G * nb;
   if (part.n < (size_t)GB * K) part.alloc((size_t)GB * K);
-  mg_group_partial<<<GB, 256, 0, st()>>>(mg_out.p, nb, nv, group.p, c.p, G, part.p);
+  mg_group_partial<<<GB, 256, 0, st()>>>(mg_out.p, nb, nv, group.p, c.p, G, part.p, gs_ticket.p, cy.p);
   RSG_LAUNCHED(ctx, "mg_group");
-  group_sums_final<<<nblk(K, 128), 128, 0, st()>>>(part.p, GB, K, cy.p);
-  RSG_LAUNCHED(ctx, "group_sums_final");
 }
 
 namespace rsg {
@@ -531,6 +547,8 @@ int rs_solver_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const do
     for (int g = 0; g < S->G; ++g) ea[g] = eps * garea[g];
     cudaStream_t s = ctx->stream;
     S->group.upload(S->group_h, s);
+    S->gs_ticket.alloc(1);
+    RSG_CUDA("solver", cudaMemsetAsync(S->gs_ticket.p, 0, sizeof(unsigned), s));
     S->c.upload(ch, s);
     S->eps_area.upload(ea, s);
     S->w_hi = o->tp_weight;

@@ -20,6 +20,7 @@
 // H~a is formed with the same operations as H~(a m) for m = 1, so L 1 = 0 exactly (the
 // reference's null-space property, hierarchical.rs:13-16).
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <memory>
 #include <mutex>
@@ -687,6 +688,7 @@ struct HMat {
   DevBuf<unsigned long long> qmax;  // per channel: largest |m| (see split_q)
   int pw_mode = 0, pw_k = 0;
   Profiler prof;
+  double setup_times[3] = {0, 0, 0};  // seconds: work items, far coefficients, device part
 
   HDev dev(int C_) const {
     HDev d;
@@ -758,6 +760,13 @@ struct HMat {
   // the far coefficients; computes the far part of H~a. pts/wt/nrm64 are per element
   // (original order), FP64.
   void setup(const double *pts, const double *wt, const double *nrm64, const double *proj6) {
+    using clk = std::chrono::steady_clock;
+    auto t_ph = clk::now();
+    auto lap = [&](double &slot) {
+      const auto now = clk::now();
+      slot = std::chrono::duration<double>(now - t_ph).count();
+      t_ph = now;
+    };
     cudaStream_t s = st();
     const Tree &T = tree;
     size_t nn = T.n_nodes(), nl = T.leaves.size();
@@ -815,6 +824,7 @@ struct HMat {
       }
     });
     n_items = items_h.size();
+    lap(setup_times[0]);
     // weight base of every item: its rows times its columns padded to 32
     n_wts = 0;
     for (uint4 &it : items_h) {
@@ -863,6 +873,7 @@ struct HMat {
           coef[q] = k;
         }
     }, 256);
+    lap(setup_times[1]);
     up_vec(far_coef, coef, s);
     // element records
     DevBuf<double> dp, dw, dn;
@@ -897,6 +908,7 @@ struct HMat {
     hm_chain_sum_kernel<2><<<nblk(nl * 2, 256), 256, 0, s>>>(d, farx.p, reinterpret_cast<double *>(leaf_farA.p));
     RSG_LAUNCHED(ctx, "hm_chain_sum");
     RSG_CUDA("upload", cudaStreamSynchronize(s));
+    lap(setup_times[2]);
   }
 
   // z for the C-channel m already in `m` (faces: C = 12 nb, vertices: C = 4 nb).
@@ -965,6 +977,9 @@ void check_exponents(double alpha, double beta) {
 struct rs_metric {
   HMat h;
   int nv = 0, nf = 0;
+  // build phases in seconds: geometry, tree, projectors, blocks, face records, work items,
+  // far coefficients, device part (uploads, element records, weights, far part of H~a)
+  double build_times[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   FaceGeom geom;
   DevBuf<uint32_t> faces, order, position, inc_off, inc;
   DevBuf<double> g, area;
@@ -995,9 +1010,18 @@ void metric_setup(rs_metric *M, rs_ctx *ctx, int nv, int nf, const uint32_t *fac
   validate_topology(nv, nf, faces);
   validate_positions(nv, nf, faces, pos);
   ctx->use();
+  using clk = std::chrono::steady_clock;
+  auto t_ph = clk::now();
+  auto lap = [&](int slot) {
+    const auto now = clk::now();
+    M->build_times[slot] = std::chrono::duration<double>(now - t_ph).count();
+    t_ph = now;
+  };
   M->nv = nv, M->nf = nf;
   M->geom = face_geometry(nf, faces, pos);
+  lap(0);
   Tree T = build_face_tree(nf, faces, pos, M->geom, leaf_size);
+  lap(1);
   M->h.kind = FACE;
   M->h.n_el = nf;
   M->h.set_exponent(-(beta - 2.0) / alpha);
@@ -1019,7 +1043,9 @@ void metric_setup(rs_metric *M, rs_ctx *ctx, int nv, int nf, const uint32_t *fac
     }
     for (int k = 0; k < 6; ++k) proj[6 * i + k] = o[k + 1] / o[0];
   }
+  lap(2);
   M->h.build_common(ctx, std::move(T), chi, leaf_pairs);
+  lap(3);
   cudaStream_t s = M->h.st();
   // df coefficients (RS/src/metric/mod.rs:120-131) in FP64
   std::vector<double> gh(9 * (size_t)nf), ah(nf);
@@ -1054,7 +1080,9 @@ void metric_setup(rs_metric *M, rs_ctx *ctx, int nv, int nf, const uint32_t *fac
   }
   up_vec(M->faces, fh, s), up_vec(M->order, M->h.tree.order, s), up_vec(M->position, posn, s);
   up_vec(M->g, gh, s), up_vec(M->area, ah, s), up_vec(M->inc_off, ioff, s), up_vec(M->inc, inc, s);
+  lap(4);
   M->h.setup(M->geom.bary.data(), M->geom.area.data(), M->geom.normal.data(), proj.data());
+  for (int i = 0; i < 3; ++i) M->build_times[5 + i] = M->h.setup_times[i];
 }
 
 }  // namespace
@@ -1166,6 +1194,10 @@ int rs_metric_apply_device(rs_metric *M, double w_hi, double w_lo, int nb, const
     M->h.ctx->use();
     metric_apply_strided(M, w_hi, w_lo, nb, xs_dev, 3 * (size_t)M->nv, ys_dev, 3 * (size_t)M->nv);
   });
+}
+
+int rs_metric_build_times(rs_metric *M, double *out8) {
+  return guard([&] { std::copy(M->build_times, M->build_times + 8, out8); });
 }
 
 int rs_metric_stats(rs_metric *M, int64_t *o) {

@@ -107,6 +107,7 @@ def load_library(path: str | os.PathLike | None = None):
         "rs_metric_apply": [_vp, C.c_double, C.c_double, C.c_int, _f64p, _f64p],
         "rs_metric_apply_device": [_vp, C.c_double, C.c_double, C.c_int, _vp, _vp],
         "rs_metric_stats": [_vp, _i64p],
+        "rs_metric_build_times": [_vp, _f64p],
         "rs_metric_blocks": [_vp, _u32p, _u32p, _u32p, _u32p],
         "rs_metric_profile": [_vp, C.c_double, C.c_double, C.c_int, C.c_int, C.c_char_p, C.c_int,
                               _f64p, C.c_int, C.POINTER(C.c_int)],
@@ -485,6 +486,13 @@ class FaceMetricTree:
         o = np.zeros(5, np.int64)
         _check(_lib.rs_metric_stats(self._h, o))
         return dict(zip(["far_blocks", "near_blocks", "near_entries", "depth", "nodes"], map(int, o)))
+
+    def build_times(self) -> dict:
+        """Seconds spent in the phases of the build."""
+        o = np.zeros(8)
+        _check(_lib.rs_metric_build_times(self._h, o))
+        return dict(zip(["geometry", "tree", "projectors", "blocks", "face_records", "work_items",
+                         "far_coefficients", "device"], map(float, o)))
 
     def blocks(self) -> dict:
         s = self.stats()

@@ -193,6 +193,9 @@ int rs_metric_apply_device_noalloc(rs_metric *m, double w_hi, double w_lo, int n
                                    const double *xs_dev, double *ys_dev);
 /* BctStats (far blocks, near blocks, near entries, depth, nodes). */
 int rs_metric_stats(rs_metric *m, int64_t *out5);
+// Seconds spent in the phases of rs_metric_build: geometry, tree, projectors, blocks, face
+// records, work items, far coefficients, device part. No crate counterpart (diagnostics).
+int rs_metric_build_times(rs_metric *m, double *out8);
 /* The blocks grouped by row node: far_ptr [nodes+1], far_col, near_ptr [nodes+1], near_col. */
 int rs_metric_blocks(rs_metric *m, uint32_t *far_ptr, uint32_t *far_col, uint32_t *near_ptr,
                      uint32_t *near_col);

@@ -27,28 +27,47 @@ Csr transpose(const Csr &A) {
   return T;
 }
 
-// C = A B (Gustavson, rows in order, columns sorted).
+// C = A B (Gustavson, columns sorted), rows in parallel: a pass that counts each row's
+// columns, then a pass that fills the rows at their prefix offsets. Every row is formed
+// exactly as a sequential pass would form it.
 Csr spgemm(const Csr &A, const Csr &B) {
   Csr C;
   C.n = A.n, C.m = B.m;
   C.ptr.assign(C.n + 1, 0);
-  std::vector<double> acc(B.m, 0.0);
-  std::vector<int> mark(B.m, -1), cols;
-  for (int i = 0; i < A.n; ++i) {
-    cols.clear();
-    for (int p = A.ptr[i]; p < A.ptr[i + 1]; ++p) {
-      int k = A.col[p];
-      double a = A.val[p];
-      for (int q = B.ptr[k]; q < B.ptr[k + 1]; ++q) {
-        int j = B.col[q];
-        if (mark[j] != i) mark[j] = i, acc[j] = 0.0, cols.push_back(j);
-        acc[j] += a * B.val[q];
+  parallel_for((size_t)A.n, [&](size_t i0, size_t i1) {
+    std::vector<int> mark(B.m, -1);
+    for (size_t i = i0; i < i1; ++i) {
+      int cnt = 0;
+      for (int p = A.ptr[i]; p < A.ptr[i + 1]; ++p) {
+        const int k = A.col[p];
+        for (int q = B.ptr[k]; q < B.ptr[k + 1]; ++q)
+          if (mark[B.col[q]] != (int)i) mark[B.col[q]] = (int)i, ++cnt;
       }
+      C.ptr[i + 1] = cnt;
     }
-    std::sort(cols.begin(), cols.end());
-    for (int j : cols) C.col.push_back(j), C.val.push_back(acc[j]);
-    C.ptr[i + 1] = (int)C.col.size();
-  }
+  }, 2048);
+  for (int i = 0; i < C.n; ++i) C.ptr[i + 1] += C.ptr[i];
+  C.col.resize(C.ptr[C.n]);
+  C.val.resize(C.ptr[C.n]);
+  parallel_for((size_t)A.n, [&](size_t i0, size_t i1) {
+    std::vector<double> acc(B.m, 0.0);
+    std::vector<int> mark(B.m, -1), cols;
+    for (size_t i = i0; i < i1; ++i) {
+      cols.clear();
+      for (int p = A.ptr[i]; p < A.ptr[i + 1]; ++p) {
+        const int k = A.col[p];
+        const double a = A.val[p];
+        for (int q = B.ptr[k]; q < B.ptr[k + 1]; ++q) {
+          const int j = B.col[q];
+          if (mark[j] != (int)i) mark[j] = (int)i, acc[j] = 0.0, cols.push_back(j);
+          acc[j] += a * B.val[q];
+        }
+      }
+      std::sort(cols.begin(), cols.end());
+      int o = C.ptr[i];
+      for (int j : cols) C.col[o] = j, C.val[o] = acc[j], ++o;
+    }
+  }, 2048);
   return C;
 }
 
@@ -77,37 +96,43 @@ double spectral_radius(const Csr &A, const std::vector<double> &d) {
 // leftovers to a neighbouring aggregate, then group whatever remains.
 std::vector<int> aggregate(const Csr &A, const std::vector<double> &d, int &n_agg) {
   const double theta = 0.08;
-  std::vector<std::vector<int>> S(A.n);
-  for (int i = 0; i < A.n; ++i)
-    for (int p = A.ptr[i]; p < A.ptr[i + 1]; ++p) {
-      int j = A.col[p];
-      if (j != i && std::fabs(A.val[p]) >= theta * std::sqrt(std::fabs(d[i] * d[j]))) S[i].push_back(j);
-    }
+  // strong[p]: entry p of A is a strong connection (off the diagonal); computed in parallel,
+  // read in A's column order by the sequential greedy passes
+  std::vector<unsigned char> strong(A.col.size(), 0);
+  parallel_for((size_t)A.n, [&](size_t i0, size_t i1) {
+    for (size_t i = i0; i < i1; ++i)
+      for (int p = A.ptr[i]; p < A.ptr[i + 1]; ++p) {
+        const int j = A.col[p];
+        strong[p] = j != (int)i && std::fabs(A.val[p]) >= theta * std::sqrt(std::fabs(d[i] * d[j]));
+      }
+  });
   std::vector<int> agg(A.n, -1);
   n_agg = 0;
   for (int i = 0; i < A.n; ++i) {
     if (agg[i] != -1) continue;
-    bool free_ = true;
-    for (int j : S[i]) free_ = free_ && agg[j] == -1;
-    if (!free_ || S[i].empty()) continue;
+    bool free_ = true, any = false;
+    for (int p = A.ptr[i]; p < A.ptr[i + 1]; ++p)
+      if (strong[p]) free_ = free_ && agg[A.col[p]] == -1, any = true;
+    if (!free_ || !any) continue;
     agg[i] = n_agg;
-    for (int j : S[i]) agg[j] = n_agg;
+    for (int p = A.ptr[i]; p < A.ptr[i + 1]; ++p)
+      if (strong[p]) agg[A.col[p]] = n_agg;
     ++n_agg;
   }
   std::vector<int> first = agg;
   for (int i = 0; i < A.n; ++i) {
     if (agg[i] != -1) continue;
-    for (int j : S[i])
-      if (first[j] != -1) {
-        agg[i] = first[j];
+    for (int p = A.ptr[i]; p < A.ptr[i + 1]; ++p)
+      if (strong[p] && first[A.col[p]] != -1) {
+        agg[i] = first[A.col[p]];
         break;
       }
   }
   for (int i = 0; i < A.n; ++i) {
     if (agg[i] != -1) continue;
     agg[i] = n_agg;
-    for (int j : S[i])
-      if (agg[j] == -1) agg[j] = n_agg;
+    for (int p = A.ptr[i]; p < A.ptr[i + 1]; ++p)
+      if (strong[p] && agg[A.col[p]] == -1) agg[A.col[p]] = n_agg;
     ++n_agg;
   }
   return agg;
@@ -178,21 +203,34 @@ AmgHost amg_setup(const Csr &A0, int coarse_max, int max_levels) {
     Csr P;
     P.n = A.n, P.m = na;
     P.ptr.assign(A.n + 1, 0);
-    for (int i = 0; i < A.n; ++i) {
-      // merge Pt row (one entry) with -omega/d_i AP row
-      int pc = Pt.col[i];
-      double pv = Pt.val[i];
-      bool done = false;
-      for (int q = AP.ptr[i]; q < AP.ptr[i + 1]; ++q) {
-        int j = AP.col[q];
-        double v = -omega / d[i] * AP.val[q];
-        if (!done && pc < j) P.col.push_back(pc), P.val.push_back(pv), done = true;
-        if (j == pc) v += pv, done = true;
-        P.col.push_back(j), P.val.push_back(v);
+    // merge the Pt row (one entry) with the -omega/d_i AP row: the row has AP's columns plus
+    // Pt's when AP lacks it
+    parallel_for((size_t)A.n, [&](size_t i0, size_t i1) {
+      for (size_t i = i0; i < i1; ++i) {
+        const int pc = Pt.col[i];
+        const int *b = AP.col.data() + AP.ptr[i], *e = AP.col.data() + AP.ptr[i + 1];
+        P.ptr[i + 1] = (int)(e - b) + (std::binary_search(b, e, pc) ? 0 : 1);
       }
-      if (!done) P.col.push_back(pc), P.val.push_back(pv);
-      P.ptr[i + 1] = (int)P.col.size();
-    }
+    });
+    for (int i = 0; i < A.n; ++i) P.ptr[i + 1] += P.ptr[i];
+    P.col.resize(P.ptr[A.n]);
+    P.val.resize(P.ptr[A.n]);
+    parallel_for((size_t)A.n, [&](size_t i0, size_t i1) {
+      for (size_t i = i0; i < i1; ++i) {
+        const int pc = Pt.col[i];
+        const double pv = Pt.val[i];
+        int o = P.ptr[i];
+        bool done = false;
+        for (int q = AP.ptr[i]; q < AP.ptr[i + 1]; ++q) {
+          const int j = AP.col[q];
+          double v = -omega / d[i] * AP.val[q];
+          if (!done && pc < j) P.col[o] = pc, P.val[o] = pv, ++o, done = true;
+          if (j == pc) v += pv, done = true;
+          P.col[o] = j, P.val[o] = v, ++o;
+        }
+        if (!done) P.col[o] = pc, P.val[o] = pv;
+      }
+    });
     Csr R = transpose(P);
     Csr Ac = spgemm(R, spgemm(A, P));
     std::vector<double> dinv(A.n);

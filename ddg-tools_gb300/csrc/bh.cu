@@ -13,10 +13,12 @@
 #include <cub/device/device_radix_sort.cuh>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <memory>
 #include <numeric>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "bh_kernels.cuh"
@@ -147,58 +149,172 @@ __device__ __forceinline__ bool admissible(const ListsDev &L, const double *lb, 
   return __dmul_rn(h, h) < __dmul_rn(L.theta2, d2);
 }
 
-// Depth-first traversal from the root, left child first (barnes_hut.rs:752-766). FILL=false
-// counts, FILL=true writes the entries at the offsets computed from the counts.
-template <bool FILL>
-__global__ void lists_kernel(BhDev d, ListsDev L, uint32_t *cnt_lum, uint32_t *cnt_ex,
-                             uint32_t *cnt_partner, unsigned long long *pairs,
-                             unsigned long long *lum_inter, uint32_t *lumped, uint32_t *exact,
-                             uint32_t *partner_off, const uint32_t *partner_base,
-                             unsigned int *overflow) {
-  int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= d.n_leaves) return;
-  uint32_t leaf = d.leaves[k];
-  double lb[6];
+// The lists of a leaf: a depth-first traversal from the root, left child first
+// (barnes_hut.rs:752-766): an admissible node is lumped, an inadmissible leaf is exact, any
+// other node is opened. The traversal is cut into ordered segments so that it runs in
+// parallel: lists_top_kernel walks the tree down to depth kTopDepth and records, in traversal
+// order, the entries met there and the depth-kTopDepth nodes it has to open (subtree roots);
+// lists_seg_kernel runs the traversal of each segment, counting (FILL=false) or writing at the
+// segment's offsets (FILL=true): one thread per slot for the single entries, one thread per
+// subtree from a compact work list for the rest (so that the warps that walk subtrees are full;
+// most segments are single entries); lists_scan_kernel turns a leaf's segment counts into
+// offsets. The concatenated segments are the sequential traversal's lists, entry for entry.
+constexpr int kTopDepth = 5;
+constexpr int kSegs = 64;  // at most one segment per node of depth <= kTopDepth: 63
+constexpr uint32_t kSegNode = 0x3fffffffu;
+
+struct LeafBox {
+  double lb[6], lr;
+  uint32_t leaf, ns;
+};
+__device__ __forceinline__ LeafBox leaf_box(const BhDev &d, const ListsDev &L, uint32_t k) {
+  LeafBox b;
+  b.leaf = d.leaves[k];
 #pragma unroll
-  for (int i = 0; i < 6; ++i) lb[i] = L.box[6 * (size_t)leaf + i];
-  double lr = L.radius[leaf];
-  uint32_t ns = d.node_end[leaf] - d.node_start[leaf];
-  uint32_t stack[kMaxDepth];
-  int sp = 0;
-  stack[sp++] = 0;
+  for (int i = 0; i < 6; ++i) b.lb[i] = L.box[6 * (size_t)b.leaf + i];
+  b.lr = L.radius[b.leaf];
+  b.ns = d.node_end[b.leaf] - d.node_start[b.leaf];
+  return b;
+}
+
+// seg[k][i] = node | kind << 30 (0 lumped node, 1 exact leaf, 2 opened node of depth
+// kTopDepth: its subtree's traversal), nseg[k] of them; the kind-2 slots k kSegs + i are also
+// appended to the work list `heavy` (in any order: each slot's results have their own place)
+__global__ void lists_top_kernel(BhDev d, ListsDev L, uint32_t *seg, uint32_t *nseg, uint32_t *heavy,
+                                 uint32_t *n_heavy, unsigned int *overflow) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= (uint32_t)d.n_leaves) return;
+  const LeafBox B = leaf_box(d, L, k);
+  uint32_t st[2 * kTopDepth + 4];
+  int sd[2 * kTopDepth + 4];
+  int sp = 0, n = 0;
+  st[sp] = 0, sd[sp++] = 0;
+  uint32_t *out = seg + (size_t)k * kSegs;
+  while (sp > 0) {
+    --sp;
+    const uint32_t c = st[sp];
+    const int dep = sd[sp];
+    uint32_t code;
+    if (admissible(L, B.lb, B.lr, c)) {
+      code = c;
+    } else if (d.node_right[c] == 0) {
+      code = c | (1u << 30);
+    } else if (dep == kTopDepth) {
+      code = c | (2u << 30);
+    } else {
+      st[sp] = d.node_right[c], sd[sp++] = dep + 1;
+      st[sp] = c + 1, sd[sp++] = dep + 1;
+      continue;
+    }
+    if (n == kSegs) {
+      atomicExch(overflow, 1u);
+      break;
+    }
+    if ((code >> 30) == 2u) heavy[atomicAdd(n_heavy, 1u)] = k * kSegs + (uint32_t)n;
+    out[n++] = code;
+  }
+  nseg[k] = (uint32_t)n;
+}
+
+// HEAVY = false: one thread per slot, the single-entry segments (kinds 0, 1); HEAVY = true:
+// one thread per work-list entry, the subtree traversals (kind 2).
+template <bool FILL, bool HEAVY>
+__global__ void lists_seg_kernel(BhDev d, ListsDev L, const uint32_t *seg, const uint32_t *nseg,
+                                 const uint32_t *heavy, const uint32_t *n_heavy, uint32_t *s_lum, uint32_t *s_ex,
+                                 uint32_t *s_par, unsigned long long *s_pr, uint32_t *lumped, uint32_t *exact,
+                                 uint32_t *partner_off, const uint32_t *partner_base, unsigned int *overflow) {
+  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (HEAVY) {
+    if (t >= *n_heavy) return;
+    t = heavy[t];
+  }
+  const uint32_t k = (uint32_t)(t / kSegs), i = (uint32_t)(t % kSegs);
+  if (k >= (uint32_t)d.n_leaves || i >= nseg[k]) return;
+  if (HEAVY != ((seg[t] >> 30) == 2u)) return;
+  const LeafBox B = leaf_box(d, L, k);
   uint32_t nl = 0, ne = 0, np = 0;
   unsigned long long pr = 0;
-  uint32_t lo = FILL ? d.lumped_off[k] : 0, eo = FILL ? d.exact_off[k] : 0;
-  uint32_t pb = FILL ? partner_base[k] : 0;
-  while (sp > 0) {
-    uint32_t c = stack[--sp];
-    if (admissible(L, lb, lr, c)) {
-      if (FILL) lumped[lo + nl] = c;
-      ++nl;
-    } else if (d.node_right[c] == 0) {
-      uint32_t nc = d.node_end[c] - d.node_start[c];
-      if (FILL) {
-        exact[eo + ne] = c;
-        partner_off[eo + ne] = pb + np;
+  const uint32_t lo = FILL ? d.lumped_off[k] + s_lum[t] : 0, eo = FILL ? d.exact_off[k] + s_ex[t] : 0;
+  const uint32_t pb = FILL ? partner_base[k] + s_par[t] : 0;
+  auto lump = [&](uint32_t c) {
+    if (FILL) lumped[lo + nl] = c;
+    ++nl;
+  };
+  auto exact_leaf = [&](uint32_t c) {
+    const uint32_t nc = d.node_end[c] - d.node_start[c];
+    if (FILL) {
+      exact[eo + ne] = c;
+      partner_off[eo + ne] = pb + np;
+    }
+    ++ne;
+    np += nc;
+    pr += (c == B.leaf) ? (unsigned long long)B.ns * (B.ns - 1) : (unsigned long long)B.ns * nc;
+  };
+  const uint32_t code = seg[t], c0 = code & kSegNode, kind = code >> 30;
+  if (kind == 0) {
+    lump(c0);
+  } else if (kind == 1) {
+    exact_leaf(c0);
+  } else {
+    uint32_t stack[kMaxDepth];
+    int sp = 0;
+    stack[sp++] = d.node_right[c0];  // c0 was tested (inadmissible, not a leaf): open it
+    stack[sp++] = c0 + 1;
+    while (sp > 0) {
+      const uint32_t c = stack[--sp];
+      if (admissible(L, B.lb, B.lr, c)) {
+        lump(c);
+      } else if (d.node_right[c] == 0) {
+        exact_leaf(c);
+      } else {
+        if (sp + 2 > kMaxDepth) {
+          atomicExch(overflow, 1u);
+          break;
+        }
+        stack[sp++] = d.node_right[c];
+        stack[sp++] = c + 1;
       }
-      ++ne;
-      np += nc;
-      pr += (c == leaf) ? (unsigned long long)ns * (ns - 1) : (unsigned long long)ns * nc;
-    } else {
-      if (sp + 2 > kMaxDepth) {
-        atomicExch(overflow, 1u);
-        break;
-      }
-      stack[sp++] = d.node_right[c];
-      stack[sp++] = c + 1;
     }
   }
-  if (!FILL) {
-    cnt_lum[k] = nl;
-    cnt_ex[k] = ne;
-    cnt_partner[k] = np;
-    pairs[k] = pr;
-    lum_inter[k] = (unsigned long long)nl * ns;
+  if (!FILL) s_lum[t] = nl, s_ex[t] = ne, s_par[t] = np, s_pr[t] = pr;
+}
+
+// One warp per leaf: the segment counts become exclusive offsets within the leaf (in place),
+// the leaf's totals go to the per-leaf arrays (pairs: exact element pairs; lum_inter: lumped
+// nodes x the leaf's faces).
+__global__ void lists_scan_kernel(BhDev d, const uint32_t *nseg, uint32_t *s_lum, uint32_t *s_ex, uint32_t *s_par,
+                                  const unsigned long long *s_pr, uint32_t *cnt_lum, uint32_t *cnt_ex,
+                                  uint32_t *cnt_partner, unsigned long long *pairs, unsigned long long *lum_inter) {
+  const uint32_t k = (uint32_t)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (k >= (uint32_t)d.n_leaves) return;
+  static_assert(kSegs == 64, "two segments per lane");
+  const uint32_t n = nseg[k];
+  const size_t b = (size_t)k * kSegs + 2 * lane;
+  const bool v0 = 2u * lane < n, v1 = 2u * lane + 1 < n;
+  uint32_t *arr[3] = {s_lum, s_ex, s_par};
+  uint32_t tot[3];
+  for (int a = 0; a < 3; ++a) {
+    const uint32_t x0 = v0 ? arr[a][b] : 0u, x1 = v1 ? arr[a][b + 1] : 0u;
+    uint32_t inc = x0 + x1;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += y;
+    }
+    const uint32_t exc = inc - (x0 + x1);
+    if (v0) arr[a][b] = exc;
+    if (v1) arr[a][b + 1] = exc + x0;
+    tot[a] = __shfl_sync(0xffffffffu, inc, 31);
+  }
+  unsigned long long p = (v0 ? s_pr[b] : 0ull) + (v1 ? s_pr[b + 1] : 0ull);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) p += __shfl_xor_sync(0xffffffffu, p, o);
+  if (lane == 0) {
+    const uint32_t leaf = d.leaves[k], ns = d.node_end[leaf] - d.node_start[leaf];
+    cnt_lum[k] = tot[0], cnt_ex[k] = tot[1], cnt_partner[k] = tot[2];
+    pairs[k] = p;
+    lum_inter[k] = (unsigned long long)tot[0] * ns;
   }
 }
 
@@ -700,6 +816,9 @@ using namespace rsg;
 struct rs_bh {
   rs_ctx *ctx = nullptr;
   int nv = 0, nf = 0, leaf_size = 8;
+  // build phases in seconds: geometry, tree, topology, list counts, list fill, list finish
+  // (transposes, chunks, schedule), refit
+  double build_times[7] = {0, 0, 0, 0, 0, 0, 0};
   double theta = 0.5;
   Tree tree;
   std::vector<uint32_t> faces_h;
@@ -972,6 +1091,14 @@ void finish_lists(rs_bh *h, const std::vector<uint32_t> &lo, const std::vector<u
 }
 
 void build_lists_device(rs_bh *h) {
+  using clk = std::chrono::steady_clock;
+  auto t_ph = clk::now();
+  auto lap = [&] {
+    const auto now = clk::now();
+    const double d = std::chrono::duration<double>(now - t_ph).count();
+    t_ph = now;
+    return d;
+  };
   cudaStream_t s = h->st();
   const Tree &T = h->tree;
   size_t nl = T.leaves.size();
@@ -983,10 +1110,25 @@ void build_lists_device(rs_bh *h) {
   DevBuf<unsigned int> overflow(1);
   RSG_CUDA("upload", cudaMemsetAsync(overflow.p, 0, sizeof(unsigned), s));
   BhDev d = h->dev();
-  lists_kernel<false><<<blocks(nl, 128), 128, 0, s>>>(d, L, c_lum.p, c_ex.p, c_par.p, pairs.p,
-                                                       linter.p, nullptr, nullptr, nullptr, nullptr,
-                                                       overflow.p);
-  RSG_LAUNCHED(h->ctx, "lists_count");
+  const size_t nsl = nl * (size_t)kSegs;
+  DevBuf<uint32_t> seg(nsl), nseg(nl), s_lum(nsl), s_ex(nsl), s_par(nsl), heavy(nsl), n_heavy(1);
+  DevBuf<unsigned long long> s_pr(nsl);
+  RSG_CUDA("upload", cudaMemsetAsync(n_heavy.p, 0, sizeof(uint32_t), s));
+  lists_top_kernel<<<blocks(nl, 128), 128, 0, s>>>(d, L, seg.p, nseg.p, heavy.p, n_heavy.p, overflow.p);
+  RSG_LAUNCHED(h->ctx, "lists_top");
+  auto seg_pass = [&](auto fill, uint32_t *lum, uint32_t *ex, uint32_t *po, const uint32_t *pbase) {
+    constexpr bool F = decltype(fill)::value;
+    lists_seg_kernel<F, false><<<blocks(nsl, 128), 128, 0, s>>>(d, L, seg.p, nseg.p, heavy.p, n_heavy.p, s_lum.p,
+                                                                s_ex.p, s_par.p, s_pr.p, lum, ex, po, pbase, overflow.p);
+    RSG_LAUNCHED(h->ctx, F ? "lists_fill" : "lists_count");
+    lists_seg_kernel<F, true><<<blocks(nsl, 128), 128, 0, s>>>(d, L, seg.p, nseg.p, heavy.p, n_heavy.p, s_lum.p,
+                                                               s_ex.p, s_par.p, s_pr.p, lum, ex, po, pbase, overflow.p);
+    RSG_LAUNCHED(h->ctx, F ? "lists_fill" : "lists_count");
+  };
+  seg_pass(std::false_type{}, nullptr, nullptr, nullptr, nullptr);
+  lists_scan_kernel<<<blocks(nl * 32, 128), 128, 0, s>>>(d, nseg.p, s_lum.p, s_ex.p, s_par.p, s_pr.p, c_lum.p, c_ex.p,
+                                                          c_par.p, pairs.p, linter.p);
+  RSG_LAUNCHED(h->ctx, "lists_scan");
   std::vector<uint32_t> hl(nl), he(nl), hp(nl);
   std::vector<unsigned long long> hpr(nl), hli(nl);
   unsigned ovf = 0;
@@ -997,6 +1139,7 @@ void build_lists_device(rs_bh *h) {
   linter.download(hli.data(), nl, s);
   overflow.download(&ovf, 1, s);
   RSG_CUDA("upload", cudaStreamSynchronize(s));
+  h->build_times[3] = lap();
   if (ovf) fail(RS_INTERNAL, "Internal", "upload", "traversal stack overflow");
   std::vector<uint32_t> lo(nl + 1, 0), eo(nl + 1, 0), pb(nl, 0);
   uint64_t tl = 0, te = 0, tp = 0;
@@ -1020,15 +1163,14 @@ void build_lists_device(rs_bh *h) {
   h->exact.alloc(std::max<size_t>(te, 1));
   h->partner_off.alloc(te + 1);
   d = h->dev();
-  lists_kernel<true><<<blocks(nl, 128), 128, 0, s>>>(d, L, nullptr, nullptr, nullptr, nullptr,
-                                                      nullptr, h->lumped.p, h->exact.p,
-                                                      h->partner_off.p, pbase.p, overflow.p);
-  RSG_LAUNCHED(h->ctx, "lists_fill");
+  seg_pass(std::true_type{}, h->lumped.p, h->exact.p, h->partner_off.p, pbase.p);
   uint32_t tp32 = (uint32_t)tp;
   RSG_CUDA("upload", rsg::copy_async(h->partner_off.p + te, &tp32, sizeof(uint32_t),
                                      cudaMemcpyHostToDevice, s));
   RSG_CUDA("upload", cudaStreamSynchronize(s));
+  h->build_times[4] = lap();
   finish_lists(h, lo, eo);
+  h->build_times[5] = lap();
 }
 
 void refit_device(rs_bh *h) {
@@ -1156,13 +1298,25 @@ int rs_bh_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const double
     h->ctx = ctx;
     h->nv = nv, h->nf = nf, h->theta = theta, h->leaf_size = leaf_size;
     h->faces_h.assign(faces, faces + 3 * (size_t)nf);
+    using clk = std::chrono::steady_clock;
+    auto t_ph = clk::now();
+    auto lap = [&](int slot) {
+      const auto now = clk::now();
+      h->build_times[slot] = std::chrono::duration<double>(now - t_ph).count();
+      t_ph = now;
+    };
     FaceGeom g = face_geometry(nf, faces, positions_host);
+    lap(0);
     h->tree = build_face_tree(nf, faces, positions_host, g, leaf_size);
+    lap(1);
     upload_topology(h.get());
+    lap(2);
     build_lists_device(h.get());
+    t_ph = clk::now();
     h->pos.upload(positions_host, 3 * (size_t)nv, h->st());
     refit_device(h.get());
     RSG_CUDA("upload", cudaStreamSynchronize(h->st()));
+    lap(6);
     ctx_retain(ctx);
     *out = h.release();
   });
@@ -1330,6 +1484,10 @@ int rs_bh_energy_and_differential_device(rs_bh *h, double alpha, double beta, do
     h->ctx->use();
     evaluate(h, pw, is_fast(alpha, beta), true, energy_dev, differential_dev);
   });
+}
+
+int rs_bh_build_times(rs_bh *h, double *out7) {
+  return guard([&] { std::copy(h->build_times, h->build_times + 7, out7); });
 }
 
 int rs_bh_sizes(rs_bh *h, int64_t *o) {

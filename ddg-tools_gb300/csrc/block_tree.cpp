@@ -1,8 +1,8 @@
 // Block classification of the block cluster tree (see block_tree.hpp). Level by level, worker
 // threads classify contiguous slices of the level's pairs; the slices' outputs are kept in
 // slice order (never concatenated), so the blocks come out in exactly the sequential level
-// order. The CSR grouping by row node is split by row ranges: each worker owns a range of rows
-// and reads the slices in order, so every row keeps its level order too.
+// order. The CSR grouping by row node is a parallel stable counting sort of that sequence, so
+// every row keeps its level order too.
 #include "block_tree.hpp"
 
 #include <algorithm>
@@ -16,20 +16,27 @@ namespace rsg {
 
 namespace {
 
+// What the classification reads of a node, in one cache line.
+struct alignas(64) NodeRec {
+  double box[6];  // min xyz, max xyz
+  double radius;
+  uint32_t right;  // 0 for a leaf
+  uint32_t len;    // elements
+};
+
 // box_distance_sq (RS/src/spatial/mod.rs:131-138) and separated (hierarchical.rs:116-123).
 // The boxes and radii are finite, so plain comparisons give fmax / fmin's values (a zero's
 // sign aside, which the squares remove).
 inline double mx(double a, double b) { return a < b ? b : a; }
 inline double mn(double a, double b) { return b < a ? b : a; }
-inline bool separated(const Tree &T, uint32_t a, uint32_t b, double chi) {
+inline bool separated(const NodeRec &A, const NodeRec &B, double chi) {
   if (!(chi > 0.0)) return false;
-  const double *ba = &T.box[6 * (size_t)a], *bb = &T.box[6 * (size_t)b];
   double d2 = 0.0;
   for (int k = 0; k < 3; ++k) {
-    double d = mx(mx(ba[k], bb[k]) - mn(ba[3 + k], bb[3 + k]), 0.0);
+    double d = mx(mx(A.box[k], B.box[k]) - mn(A.box[3 + k], B.box[3 + k]), 0.0);
     d2 += d * d;
   }
-  double h = mx(T.radius[a], T.radius[b]);
+  double h = mx(A.radius, B.radius);
   return d2 > 0.0 && h * h <= chi * chi * d2;
 }
 
@@ -104,43 +111,74 @@ struct Slices {
     v.push_back(std::move(s));
   }
   size_t size() const { return off.back(); }
-  // calls f(pair) for the elements [b, e) in order
-  template <class F>
-  void each(size_t b, size_t e, F f) const {
+  // calls f(pair) for the elements [b, e) in order, and ahead(pair) for the element kAhead
+  // positions further on within the same slice (to prefetch what f will read)
+  template <class F, class A>
+  void each(size_t b, size_t e, F f, A ahead) const {
+    constexpr size_t kAhead = 16;
     size_t s = std::upper_bound(off.begin(), off.end(), b) - off.begin() - 1;
-    for (size_t i = b; i < e; ++s)
-      for (size_t j = i - off[s]; j < v[s].size() && i < e; ++j, ++i) f(v[s][j]);
+    for (size_t i = b; i < e; ++s) {
+      const std::vector<Pair> &x = v[s];
+      for (size_t j = i - off[s]; j < x.size() && i < e; ++j, ++i) {
+        if (j + kAhead < x.size()) ahead(x[j + kAhead]);
+        f(x[j]);
+      }
+    }
   }
 };
 
-// CSR by row (pair.first) of the levels' pairs in order: counts per row range, then each
-// worker fills its rows (a range balanced by entries) from all slices in order.
+// CSR by row (pair.first) of the levels' pairs in order, a stable counting sort: the ordered
+// sequence of all slices is cut into nt contiguous parts; each part counts its rows, every
+// part's write offset per row follows from the counts (row start + the counts of the parts
+// before it), and each part scatters its pairs in order. `weight(pair)` is summed on the way.
+template <class Wt>
 void group(const std::vector<Slices> &levels, size_t n, Workers &W, int nt, std::vector<uint32_t> &ptr,
-           std::vector<uint32_t> &col) {
-  ptr.assign(n + 1, 0);
+           std::vector<uint32_t> &col, Wt weight, uint64_t &total) {
+  std::vector<const std::vector<Pair> *> sl;
+  std::vector<size_t> off{0};
+  for (const Slices &L : levels)
+    for (const auto &s : L.v) sl.push_back(&s), off.push_back(off.back() + s.size());
+  const size_t m = off.back();
+  auto range = [&](int t, auto f) {  // f(pair) over part t in order
+    const size_t b = m * t / nt, e = m * (t + 1) / nt;
+    size_t s = std::upper_bound(off.begin(), off.end(), b) - off.begin() - 1;
+    for (size_t i = b; i < e; ++s)
+      for (size_t j = i - off[s]; j < sl[s]->size() && i < e; ++j, ++i) f((*sl[s])[j]);
+  };
+  std::vector<std::vector<uint32_t>> cnt(nt);
+  std::vector<uint64_t> tot(nt, 0);
   W.run(nt, [&](int t) {
-    const size_t r0 = n * t / nt, r1 = n * (t + 1) / nt;
-    for (const Slices &L : levels)
-      for (const auto &s : L.v)
-        for (const Pair &p : s)
-          if (p.first >= r0 && p.first < r1) ptr[p.first + 1]++;
+    std::vector<uint32_t> &c = cnt[t];
+    c.assign(n, 0);
+    uint64_t w = 0;
+    range(t, [&](const Pair &p) { ++c[p.first], w += weight(p); });
+    tot[t] = w;
   });
-  for (size_t i = 0; i < n; ++i) ptr[i + 1] += ptr[i];
-  col.resize(ptr[n]);
-  // row ranges balanced by entries
-  std::vector<size_t> cut(nt + 1, n);
-  cut[0] = 0;
-  for (int t = 1; t < nt; ++t)
-    cut[t] = std::lower_bound(ptr.begin(), ptr.end(), (uint32_t)((uint64_t)ptr[n] * t / nt)) - ptr.begin();
-  for (int t = 1; t <= nt; ++t) cut[t] = std::max(cut[t], cut[t - 1]);
+  total = 0;
+  for (uint64_t w : tot) total += w;
+  ptr.assign(n + 1, 0);
+  W.run(nt, [&](int t) {  // rows split over the workers: row sums, then per-part offsets
+    for (size_t r = n * t / nt; r < n * (t + 1) / nt; ++r) {
+      uint32_t sum = 0;
+      for (int k = 0; k < nt; ++k) sum += cnt[k][r];
+      ptr[r + 1] = sum;
+    }
+  });
+  for (size_t r = 0; r < n; ++r) ptr[r + 1] += ptr[r];
   W.run(nt, [&](int t) {
-    const size_t r0 = cut[t], r1 = cut[t + 1];
-    if (r0 >= r1) return;
-    std::vector<uint32_t> fill(ptr.begin() + r0, ptr.begin() + r1);
-    for (const Slices &L : levels)
-      for (const auto &s : L.v)
-        for (const Pair &p : s)
-          if (p.first >= r0 && p.first < r1) col[fill[p.first - r0]++] = p.second;
+    for (size_t r = n * t / nt; r < n * (t + 1) / nt; ++r) {
+      uint32_t o = ptr[r];
+      for (int k = 0; k < nt; ++k) {
+        const uint32_t c = cnt[k][r];
+        cnt[k][r] = o;
+        o += c;
+      }
+    }
+  });
+  col.resize(ptr[n]);
+  W.run(nt, [&](int t) {
+    std::vector<uint32_t> &o = cnt[t];
+    range(t, [&](const Pair &p) { col[o[p.first]++] = p.second; });
   });
 }
 
@@ -148,10 +186,17 @@ void group(const std::vector<Slices> &levels, size_t n, Workers &W, int nt, std:
 
 Blocks classify_blocks(const Tree &T, double chi, size_t leaf_pairs, int threads) {
   const size_t nn = T.n_nodes();
-  auto leaf = [&](uint32_t a) { return T.right[a] == 0; };
   auto len = [&](uint32_t a) { return (size_t)(T.end[a] - T.start[a]); };
   const int nt = threads > 0 ? threads : (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
   Workers W(nt);
+  std::vector<NodeRec> rec(nn);
+  W.run(nt, [&](int t) {
+    for (size_t a = nn * t / nt; a < nn * (t + 1) / nt; ++a) {
+      NodeRec &r = rec[a];
+      for (int k = 0; k < 6; ++k) r.box[k] = T.box[6 * a + k];
+      r.radius = T.radius[a], r.right = T.right[a], r.len = T.end[a] - T.start[a];
+    }
+  });
   Blocks B;
   std::vector<Slices> far, near;
   Slices level;
@@ -165,17 +210,22 @@ Blocks classify_blocks(const Tree &T, double chi, size_t leaf_pairs, int threads
       std::vector<Pair> &fa = of[t], &ne = on[t], &nx = ox[t];
       level.each(n * t / parts, n * (t + 1) / parts, [&](const Pair &pr) {
         const uint32_t a = pr.first, c = pr.second;
-        if (a != c && separated(T, a, c, chi))
+        const NodeRec &A = rec[a], &Cn = rec[c];
+        const bool la = A.right == 0, lc = Cn.right == 0;
+        if (a != c && separated(A, Cn, chi))
           fa.push_back(pr);
-        else if ((leaf(a) && leaf(c)) || len(a) * len(c) <= leaf_pairs)
+        else if ((la && lc) || (size_t)A.len * Cn.len <= leaf_pairs)
           ne.push_back(pr);
         else {
-          uint32_t ka[2] = {leaf(a) ? a : a + 1, T.right[a]};
-          uint32_t kc[2] = {leaf(c) ? c : c + 1, T.right[c]};
-          int na = leaf(a) ? 1 : 2, nc = leaf(c) ? 1 : 2;
+          uint32_t ka[2] = {la ? a : a + 1, A.right};
+          uint32_t kc[2] = {lc ? c : c + 1, Cn.right};
+          int na = la ? 1 : 2, nc = lc ? 1 : 2;
           for (int x = 0; x < na; ++x)
             for (int y = 0; y < nc; ++y) nx.push_back({ka[x], kc[y]});
         }
+      }, [&](const Pair &pr) {
+        __builtin_prefetch(&rec[pr.first]);
+        __builtin_prefetch(&rec[pr.second]);
       });
     });
     Slices fl, nl, next;
@@ -188,14 +238,12 @@ Blocks classify_blocks(const Tree &T, double chi, size_t leaf_pairs, int threads
     near.push_back(std::move(nl));
     level = std::move(next);
   }
-  for (const Slices &L : near)
-    for (const auto &s : L.v)
-      for (auto [a, c] : s) B.near_entries += a == c ? len(a) * (len(a) - 1) : len(a) * len(c);
-  for (const Slices &L : far)
-    for (const auto &s : L.v)
-      for (auto [a, c] : s) B.far_pairs += len(a) * len(c);
-  group(far, nn, W, nt, B.far_ptr, B.far_col);
-  group(near, nn, W, nt, B.near_ptr, B.near_col);
+  uint64_t fp = 0, ne = 0;
+  group(far, nn, W, nt, B.far_ptr, B.far_col, [&](const Pair &p) { return (uint64_t)len(p.first) * len(p.second); }, fp);
+  group(near, nn, W, nt, B.near_ptr, B.near_col, [&](const Pair &p) {
+    return p.first == p.second ? (uint64_t)len(p.first) * (len(p.first) - 1) : (uint64_t)len(p.first) * len(p.second);
+  }, ne);
+  B.far_pairs = fp, B.near_entries = ne;
   return B;
 }
 

@@ -269,6 +269,34 @@ __global__ void hm_far_final_kernel(HDev d) {
   d.farx[t] = (double)h + (double)l;
 }
 
+// Far coefficients (k_0, k_1) of every far block, FP64, as float pairs (hi, lo): d the centroid
+// difference of the pair (lower node index first), h = r2^e, and for faces
+// k_1 = (q_lo(d) + q_hi(d)) / 2 / r2^2 h with q the node's area-weighted projector form
+// (proj = null: vertices, k_1 = k_0). One warp per far work item, lanes over its blocks.
+__global__ void hm_far_coef_kernel(const uint4 *__restrict__ items, int n_items, const uint32_t *__restrict__ far_col,
+                                   const double *__restrict__ cen, const double *__restrict__ proj, double e,
+                                   float4 *__restrict__ coef) {
+  const int w = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+  if (w >= n_items) return;
+  const uint4 it = items[w];
+  const uint32_t a = it.x;
+  auto qf = [&](uint32_t n, const double *d) {
+    const double *p = proj + 6 * (size_t)n;
+    return p[0] * d[0] * d[0] + p[3] * d[1] * d[1] + p[5] * d[2] * d[2] +
+           2.0 * (p[1] * d[0] * d[1] + p[2] * d[0] * d[2] + p[4] * d[1] * d[2]);
+  };
+  for (uint32_t q = it.y + lane; q < it.z; q += 32) {
+    const uint32_t b = far_col[q], lo = min(a, b), hi = max(a, b);
+    const double d[3] = {cen[3 * (size_t)lo] - cen[3 * (size_t)hi], cen[3 * (size_t)lo + 1] - cen[3 * (size_t)hi + 1],
+                         cen[3 * (size_t)lo + 2] - cen[3 * (size_t)hi + 2]};
+    const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    const double h = pow(r2, e);
+    const double h1 = proj ? 0.5 * (qf(lo, d) + qf(hi, d)) / (r2 * r2) * h : h;
+    const float2 k0 = to_pair(h), k1 = to_pair(h1);
+    coef[q] = make_float4(k0.x, k0.y, k1.x, k1.y);
+  }
+}
+
 // Near weights of an element pair as the rows kernel applies them: faces (w_0, w_1) =
 // a_q (k_0, k_1), vertices w_0 = a_q k_0; zero on the diagonal (q = p). Stored per work item
 // as [row][column], rows padded to a multiple of 32 columns so that each 32-column slice
@@ -850,31 +878,21 @@ struct HMat {
     }
     count.alloc(nn);
     RSG_CUDA("upload", cudaMemsetAsync(count.p, 0, nn * sizeof(uint32_t), s));
-    // far coefficients on the host in FP64 (kernel.far, hierarchical.rs:210-220 / 980-984)
-    std::vector<float4> coef(blocks.far_col.size());  // (k_0, k_1) as float pairs
-    auto fpair = [](double v, float &h, float &l) { h = (float)v, l = (float)(v - (double)h); };
-    auto qf = [&](size_t n, const double *d) {
-      const double *p = proj6 + 6 * n;
-      return p[0] * d[0] * d[0] + p[3] * d[1] * d[1] + p[5] * d[2] * d[2] +
-             2.0 * (p[1] * d[0] * d[1] + p[2] * d[0] * d[2] + p[4] * d[1] * d[2]);
-    };
-    parallel_for(nn, [&](size_t a0, size_t a1) {
-      for (size_t a = a0; a < a1; ++a)
-        for (uint32_t q = blocks.far_ptr[a]; q < blocks.far_ptr[a + 1]; ++q) {
-          size_t b = blocks.far_col[q], lo = std::min(a, b), hi = std::max(a, b);
-          double d[3] = {T.centroid[3 * lo] - T.centroid[3 * hi], T.centroid[3 * lo + 1] - T.centroid[3 * hi + 1],
-                         T.centroid[3 * lo + 2] - T.centroid[3 * hi + 2]};
-          double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-          double h = std::pow(r2, neg_s);
-          double h1 = h;
-          if (kind == FACE) h1 = 0.5 * (qf(lo, d) + qf(hi, d)) / (r2 * r2) * h;
-          float4 k;
-          fpair(h, k.x, k.y), fpair(h1, k.z, k.w);
-          coef[q] = k;
-        }
-    }, 256);
+    // far coefficients (kernel.far, hierarchical.rs:210-220 / 980-984) in FP64 on the device
+    // from the node centroids (and, for faces, the node projectors)
+    {
+      DevBuf<double> cen, pj;
+      cen.upload(T.centroid.data(), 3 * nn, s);
+      if (kind == FACE) pj.upload(proj6, 6 * nn, s);
+      far_coef.alloc(std::max<size_t>(blocks.far_col.size(), 1));
+      if (n_far_items > 0) {
+        hm_far_coef_kernel<<<nblk(n_far_items * 32, 256), 256, 0, s>>>(
+            far_items.p, (int)n_far_items, far_col.p, cen.p, kind == FACE ? pj.p : nullptr, neg_s, far_coef.p);
+        RSG_LAUNCHED(ctx, "hm_far_coef");
+      }
+      RSG_CUDA("upload", cudaStreamSynchronize(s));  // before the staging buffers go
+    }
     lap(setup_times[1]);
-    up_vec(far_coef, coef, s);
     // element records
     DevBuf<double> dp, dw, dn;
     dp.upload(pts, 3 * n_el, s);

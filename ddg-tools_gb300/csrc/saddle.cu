@@ -379,42 +379,81 @@ namespace {
 // cotan stiffness W (RS/src/geometry.rs:217-249), scalar |V| x |V|, plus eps M on the diagonal.
 Csr laplacian_block(int nv, int nf, const uint32_t *faces, const double *pos, const std::vector<double> &mass,
                     double eps_rel, bool clamp, double &eps_out) {
-  std::vector<std::vector<std::pair<int, double>>> rows(nv);
-  auto add = [&](int i, int j, double v) { rows[i].push_back({j, v}); };
-  for (int f = 0; f < nf; ++f) {
-    const uint32_t *t = faces + 3 * (size_t)f;
-    for (int c = 0; c < 3; ++c) {
-      const double *p = pos + 3 * (size_t)t[c];
-      const double *p1 = pos + 3 * (size_t)t[(c + 1) % 3];
-      const double *p2 = pos + 3 * (size_t)t[(c + 2) % 3];
-      double u[3] = {p1[0] - p[0], p1[1] - p[1], p1[2] - p[2]};
-      double w[3] = {p2[0] - p[0], p2[1] - p[1], p2[2] - p[2]};
-      double cr[3] = {u[1] * w[2] - u[2] * w[1], u[2] * w[0] - u[0] * w[2], u[0] * w[1] - u[1] * w[0]};
-      double cot = (u[0] * w[0] + u[1] * w[1] + u[2] * w[2]) /
-                   std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
-      double h = 0.5 * cot;
-      int a = (int)t[(c + 1) % 3], b = (int)t[(c + 2) % 3];
-      add(a, b, -h), add(b, a, -h), add(a, a, h), add(b, b, h);
+  // cotangent half-weights per face corner c (the edge opposite it: t[c+1], t[c+2])
+  std::vector<double> hc(3 * (size_t)nf);
+  parallel_for((size_t)nf, [&](size_t f0, size_t f1) {
+    for (size_t f = f0; f < f1; ++f) {
+      const uint32_t *t = faces + 3 * f;
+      for (int c = 0; c < 3; ++c) {
+        const double *p = pos + 3 * (size_t)t[c];
+        const double *p1 = pos + 3 * (size_t)t[(c + 1) % 3];
+        const double *p2 = pos + 3 * (size_t)t[(c + 2) % 3];
+        double u[3] = {p1[0] - p[0], p1[1] - p[1], p1[2] - p[2]};
+        double w[3] = {p2[0] - p[0], p2[1] - p[1], p2[2] - p[2]};
+        double cr[3] = {u[1] * w[2] - u[2] * w[1], u[2] * w[0] - u[0] * w[2], u[0] * w[1] - u[1] * w[0]};
+        double cot = (u[0] * w[0] + u[1] * w[1] + u[2] * w[2]) /
+                     std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+        hc[3 * f + c] = 0.5 * cot;
+      }
     }
+  });
+  // vertex -> incident faces, ascending
+  std::vector<uint32_t> ioff((size_t)nv + 1, 0), inc(3 * (size_t)nf);
+  for (size_t e = 0; e < 3 * (size_t)nf; ++e) ioff[faces[e] + 1]++;
+  for (int v = 0; v < nv; ++v) ioff[v + 1] += ioff[v];
+  {
+    std::vector<uint32_t> fill(ioff.begin(), ioff.end() - 1);
+    for (size_t f = 0; f < (size_t)nf; ++f)
+      for (int c = 0; c < 3; ++c) inc[fill[faces[3 * f + c]]++] = (uint32_t)f;
   }
-  double trw = 0.0, trm = 0.0;
+  // row i: the terms (i, b, -h), (i, i, h) of every face corner whose opposite edge touches i,
+  // in face, corner, slot order; sorted by column (stable), equal columns added in that order
+  auto row = [&](int i, std::vector<std::pair<int, double>> &r) {
+    r.clear();
+    for (uint32_t e = ioff[i]; e < ioff[i + 1]; ++e) {
+      const uint32_t f = inc[e], *t = faces + 3 * (size_t)f;
+      for (int c = 0; c < 3; ++c) {
+        const int a = (int)t[(c + 1) % 3], b = (int)t[(c + 2) % 3];
+        const double h = hc[3 * (size_t)f + c];
+        if (a == i) r.push_back({b, -h});
+        if (b == i) r.push_back({a, -h});
+        if (a == i) r.push_back({i, h});
+        if (b == i) r.push_back({i, h});
+      }
+    }
+    std::stable_sort(r.begin(), r.end(), [](const auto &x, const auto &y) { return x.first < y.first; });
+  };
   Csr K;
   K.n = K.m = nv;
   K.ptr.assign(nv + 1, 0);
-  for (int i = 0; i < nv; ++i) {
-    auto &r = rows[i];
-    std::sort(r.begin(), r.end(), [](auto &x, auto &y) { return x.first < y.first; });
-    for (size_t p = 0; p < r.size();) {
-      size_t q = p;
-      double v = 0.0;
-      while (q < r.size() && r[q].first == r[p].first) v += r[q++].second;
-      K.col.push_back(r[p].first);
-      K.val.push_back(v);
-      p = q;
+  parallel_for((size_t)nv, [&](size_t v0, size_t v1) {
+    std::vector<std::pair<int, double>> r;
+    for (size_t i = v0; i < v1; ++i) {
+      row((int)i, r);
+      int cnt = 0;
+      for (size_t p = 0; p < r.size(); ++p) cnt += (p == 0 || r[p].first != r[p - 1].first);
+      K.ptr[i + 1] = cnt;
     }
-    K.ptr[i + 1] = (int)K.col.size();
-    trm += mass[i];
-  }
+  });
+  for (int i = 0; i < nv; ++i) K.ptr[i + 1] += K.ptr[i];
+  K.col.resize(K.ptr[nv]);
+  K.val.resize(K.ptr[nv]);
+  parallel_for((size_t)nv, [&](size_t v0, size_t v1) {
+    std::vector<std::pair<int, double>> r;
+    for (size_t i = v0; i < v1; ++i) {
+      row((int)i, r);
+      int o = K.ptr[i];
+      for (size_t p = 0; p < r.size();) {
+        size_t q = p;
+        double v = 0.0;
+        while (q < r.size() && r[q].first == r[p].first) v += r[q++].second;
+        K.col[o] = r[p].first, K.val[o] = v, ++o;
+        p = q;
+      }
+    }
+  });
+  double trw = 0.0, trm = 0.0;
+  for (int i = 0; i < nv; ++i) trm += mass[i];
   for (int i = 0; i < nv; ++i) {
     int dp = -1;
     for (int p = K.ptr[i]; p < K.ptr[i + 1]; ++p)

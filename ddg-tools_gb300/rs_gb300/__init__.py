@@ -98,6 +98,7 @@ def load_library(path: str | os.PathLike | None = None):
         "rs_bh_energy_and_differential_device": [_vp, C.c_double, C.c_double, _vp, _vp],
         "rs_bh_face_partials": [_vp, C.c_double, C.c_double, _dp, _f64p],
         "rs_bh_sizes": [_vp, _i64p],
+        "rs_bh_build_times": [_vp, _f64p],
         "rs_bh_export": [_vp, _u32p, _u32p, _u32p, _u32p, _i64p, _u32p, _i64p, _u32p],
         "rs_bh_culprit": [_vp, _i64p],
         "rs_bh_profile": [_vp, C.c_double, C.c_double, C.c_int, C.c_char_p, C.c_int, _f64p,
@@ -371,6 +372,13 @@ class BhTree:
         p = np.empty((self.n_faces, 7))
         _check(_lib.rs_bh_face_partials(self._h, e.alpha, e.beta, C.byref(out), p.ravel()))
         return out.value, p
+
+    def build_times(self) -> dict:
+        """Seconds spent in the phases of the build."""
+        o = np.zeros(7)
+        _check(_lib.rs_bh_build_times(self._h, o))
+        return dict(zip(["geometry", "tree", "topology", "list_counts", "list_fill", "list_finish", "refit"],
+                        map(float, o)))
 
     def sizes(self) -> dict:
         o = np.zeros(7, np.int64)

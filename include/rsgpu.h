@@ -148,6 +148,9 @@ int rs_bh_face_partials(rs_bh *bh, double alpha, double beta, double *energy,
  * out[0..7] = n_nodes, n_leaves, n_lumped, n_exact, n_partner_slots, pairs_exact,
  *             lumped_interactions (sum over lumped entries of the leaf's face count). */
 int rs_bh_sizes(rs_bh *bh, int64_t *out7);
+// Seconds spent in the phases of rs_bh_build: geometry, tree, topology, list counts, list
+// fill, list finish, refit. No crate counterpart (diagnostics).
+int rs_bh_build_times(rs_bh *bh, double *out7);
 /* The tree and lists (for parity checks): arrays sized by rs_bh_sizes. */
 int rs_bh_export(rs_bh *bh, uint32_t *node_start, uint32_t *node_end, uint32_t *node_right,
                  uint32_t *order, int64_t *lumped_off, uint32_t *lumped, int64_t *exact_off,

@@ -83,6 +83,54 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &t) {
 }
 
 // (h, l) += (oh, ol) for float pairs.
+// Layout of the channel values m: per element, C channels as float pairs (hi, lo), stored by
+// channel pairs as (hi_2i, hi_2i+1, lo_2i, lo_2i+1) so that the near field reads the hi parts
+// (and the lo parts) of two channels as one packed operand.
+__device__ __forceinline__ int m_hi(int c) { return (c >> 1) * 4 + (c & 1); }
+__device__ __forceinline__ float2 m_get(const float2 *row, int c) {
+  const float *f = reinterpret_cast<const float *>(row);
+  return make_float2(f[m_hi(c)], f[m_hi(c) + 2]);
+}
+__device__ __forceinline__ void m_set(float2 *row, int c, float2 v) {
+  float *f = reinterpret_cast<float *>(row);
+  f[m_hi(c)] = v.x, f[m_hi(c) + 2] = v.y;
+}
+
+// Two FP32 values in one 64-bit register (first in the low half) and the packed FP32 pair
+// arithmetic of sm_100 and later (each half rounded to nearest, as the scalar operations).
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 f2_pack(float a, float b) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ float2 f2_unpack(f32x2 v) {
+  float2 r;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+  return r;
+}
+__device__ __forceinline__ f32x2 f2_add(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 f2_sub(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 f2_mul(f32x2 a, f32x2 b) {
+  f32x2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f32x2 f2_fma(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+constexpr f32x2 kF2Sign = 0x8000000080000000ull;  // both halves' sign bits
+
 // v as a float pair: hi = v rounded to FP32, lo = the rest rounded
 __device__ __forceinline__ float2 to_pair(double v) {
   const float h = (float)v;
@@ -160,7 +208,10 @@ __global__ void hm_upward_kernel(HDev d) {
 #pragma unroll
     for (int i = 0; i < NPL; ++i) {
       const int c = lane + 32 * i;
-      if (c < CC) u[i] = fma(a, (double)mp[c].x + (double)mp[c].y, u[i]);
+      if (c < CC) {
+        const float2 v = m_get(mp, c);
+        u[i] = fma(a, (double)v.x + (double)v.y, u[i]);
+      }
     }
   }
   double *o = d.up + (size_t)leaf * CC;
@@ -341,8 +392,8 @@ __global__ void hm_weights_kernel(HDev d, size_t total) {
   (void)total;
 }
 
-// One tile of a work item in shared memory: the channel values (hi, lo pairs) of 32 columns,
-// channel pair major (consecutive columns in consecutive 16-byte slots, so that the lanes of a
+// One tile of a work item in shared memory: the channel values of 32 columns (per channel
+// pair the 16 bytes (hi, hi, lo, lo) of the paired layout), channel pair major (consecutive columns in consecutive 16-byte slots, so that the lanes of a
 // load phase reading up to 8 columns meet no bank twice), and the near weights of up to
 // 8 rows x 32 columns.
 template <int KIND, int CC>
@@ -398,17 +449,16 @@ __global__ void __launch_bounds__(128, 5) hm_rows_kernel(HDev d, int c0) {
   const bool act = (uint32_t)r < ns;
   const uint32_t p = s0 + (act ? r : 0);
   const int C = d.C;
-  float mh[CC], ml[CC], ks[CC], kc[CC];
+  // channel pairs c2: hi parts mh, lo parts ml of the row, sums (ks, kc)
+  f32x2 mh[CC / 2], ml[CC / 2], ks[CC / 2], kc[CC / 2];
   {
-    const float4 *mp = reinterpret_cast<const float4 *>(d.m + (size_t)p * C + c0);
+    const ulonglong2 *mp = reinterpret_cast<const ulonglong2 *>(d.m + (size_t)p * C + c0);
 #pragma unroll
     for (int c2 = 0; c2 < CC / 2; ++c2) {
-      const float4 v = mp[c2];
-      mh[2 * c2] = v.x, ml[2 * c2] = v.y, mh[2 * c2 + 1] = v.z, ml[2 * c2 + 1] = v.w;
+      const ulonglong2 v = mp[c2];
+      mh[c2] = v.x, ml[c2] = v.y, ks[c2] = 0ull, kc[c2] = 0ull;
     }
   }
-#pragma unroll
-  for (int c = 0; c < CC; ++c) ks[c] = 0.f, kc[c] = 0.f;
   const uint32_t ncol = it.z - it.y, ntiles = (ncol + 31) / 32, npad = ntiles * 32;
   const WT *wg = reinterpret_cast<const WT *>(d.wts) + it.w;
   // lane l copies the channel values of column t0 + l and its share of the weight rows
@@ -443,33 +493,35 @@ __global__ void __launch_bounds__(128, 5) hm_rows_kernel(HDev d, int c0) {
     // indices k with (t0 + k) = j mod G
     if (act)
       for (uint32_t k = ((uint32_t)j + (uint32_t)G - t0 % (uint32_t)G) % (uint32_t)G; k < nt; k += G) {
-        float w0, w1;
+        // packed weights of the channel pairs: (w0, w0), (w0, w1) (the pair of channels 8, 9),
+        // (w1, w1), and their negatives
+        f32x2 W[3];
         if constexpr (KIND == FACE) {
-          const float2 ww = tl.w[r][k];
-          w0 = ww.x, w1 = ww.y;
+          const f32x2 ww = *reinterpret_cast<const f32x2 *>(&tl.w[r][k]);
+          const float2 wf = f2_unpack(ww);
+          W[0] = f2_pack(wf.x, wf.x), W[1] = ww, W[2] = f2_pack(wf.y, wf.y);
         } else {
-          w0 = w1 = tl.w[r][k];
+          const float w0 = tl.w[r][k];
+          W[0] = W[1] = W[2] = f2_pack(w0, w0);
         }
 #pragma unroll
         for (int c2 = 0; c2 < CC / 2; ++c2) {
-          const float4 v = tl.m[c2][k];
-#pragma unroll
-          for (int e = 0; e < 2; ++e) {
-            const int c = 2 * c2 + e;
-            const float qhv = e ? v.z : v.x, qlv = e ? v.w : v.y;
-            const float wk = (KIND == FACE && c >= 9) ? w1 : w0;
-            // w (m_p - m_q) = pr + pe + w dl up to eps^2 terms: dh = mh_p - mh_q is exact (the
-            // hi parts share a grid), dl = ml_p - ml_q, w dh = pr + pe (FMA), so no rounding
-            // that depends on the input reaches the sum above eps^2
-            const float dh = mh[c] - qhv;
-            const float dl = ml[c] - qlv;
-            const float pr = wk * dh;
-            const float lo = fmaf(wk, dl, fmaf(wk, dh, -pr));
-            float sn, se;
-            two_sum(ks[c], pr, sn, se);
-            ks[c] = sn;
-            kc[c] += se + lo;
-          }
+          const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(&tl.m[c2][k]);  // (hi pair, lo pair)
+          const int wi = KIND == FACE ? (2 * c2 + 1 < 9 ? 0 : (2 * c2 >= 9 ? 2 : 1)) : 0;
+          const f32x2 w = W[wi], wn = W[wi] ^ kF2Sign;
+          // w (m_p - m_q) = pr + pe + w dl up to eps^2 terms: dh = mh_p - mh_q is exact (the
+          // hi parts share a grid), dl = ml_p - ml_q, w dh = pr + pe (FMA), so no rounding that
+          // depends on the input reaches the sum above eps^2. npr = -pr (exact); the
+          // error-free sum ks + pr = s + err: bb = s - ks, err = (ks - (s - bb)) + (pr - bb).
+          const f32x2 dh = f2_sub(mh[c2], v.x);
+          const f32x2 dl = f2_sub(ml[c2], v.y);
+          const f32x2 npr = f2_mul(wn, dh);
+          const f32x2 lo = f2_fma(w, dl, f2_fma(w, dh, npr));
+          const f32x2 sn = f2_sub(ks[c2], npr);
+          const f32x2 bb = f2_sub(sn, ks[c2]);
+          const f32x2 err = f2_sub(f2_sub(ks[c2], f2_sub(sn, bb)), f2_add(npr, bb));
+          ks[c2] = sn;
+          kc[c2] = f2_add(kc[c2], f2_add(err, lo));
         }
       }
     __syncwarp();
@@ -477,7 +529,10 @@ __global__ void __launch_bounds__(128, 5) hm_rows_kernel(HDev d, int c0) {
   // the G lanes of a row: partial sums (s, t) added in lane order as float pairs
   float2(*red)[CC] = reinterpret_cast<float2(*)[CC]>(&tiles[wib][0]);
 #pragma unroll
-  for (int c = 0; c < CC; ++c) red[lane][c] = make_float2(ks[c], kc[c]);
+  for (int c2 = 0; c2 < CC / 2; ++c2) {
+    const float2 s2 = f2_unpack(ks[c2]), k2 = f2_unpack(kc[c2]);
+    red[lane][2 * c2] = make_float2(s2.x, k2.x), red[lane][2 * c2 + 1] = make_float2(s2.y, k2.y);
+  }
   __syncwarp();
   if (!act || j != 0) return;
   float2 *o = d.part + ((size_t)w * 8 + r) * C + c0;
@@ -522,7 +577,7 @@ __global__ void hm_epilogue_kernel(HDev d) {
     pair_add(nh, nl, v.x, v.y);
   }
   const double2 fa = d.leaf_farA[k];
-  const float2 mv = d.m[(size_t)p * CC + c];
+  const float2 mv = m_get(d.m + (size_t)p * CC, c);
   const double far = ((double)mv.x + (double)mv.y) * (uses_k1<SEL>(c) ? fa.y : fa.x) - d.leafsum[(size_t)k * CC + c];
   const double zz = ((double)nh + (double)nl) + far;
   const float zh = (float)zz;
@@ -572,7 +627,7 @@ __device__ __forceinline__ void emit(float2 *mp, int c, double v, unsigned long 
     a = __reduce_max_sync(0xffffffffu, a);
     if ((threadIdx.x & 31) == 0 && a != 0u) atomicMax(qmax + c, (unsigned long long)a << 32);
   } else if (act) {
-    mp[c] = split_q(v, qmax[c]);
+    m_set(mp, c, split_q(v, qmax[c]));
   }
 }
 
@@ -599,7 +654,7 @@ __global__ void face_m_kernel(FaceOps o, const double *__restrict__ xs, size_t l
     }
   }
   if (pass == 1 && act)
-    for (int c = 12 * nb; c < C; ++c) mp[c] = make_float2(0.f, 0.f);
+    for (int c = 12 * nb; c < C; ++c) m_set(mp, c, make_float2(0.f, 0.f));
 }
 
 // y_v = 2 sum_{S ni v} a_S (w_hi g_c . z_hi + w_lo z_lo / 3) in FP64 (hierarchical.rs:779-811).
@@ -640,7 +695,7 @@ __global__ void vertex_m_kernel(const uint32_t *order, const double *__restrict_
   const uint32_t v = act ? order[p] : 0;
   float2 *mp = m + (size_t)(act ? p : 0) * C;
   if (pass == 1 && act)
-    for (int c = 0; c < C; ++c) mp[c] = make_float2(0.f, 0.f);
+    for (int c = 0; c < C; ++c) m_set(mp, c, make_float2(0.f, 0.f));
   for (int q = 0; q < nb; ++q)
     for (int k = 0; k < 3; ++k) emit(mp, 4 * q + k, xs[q * ldx + 3 * (size_t)v + k], qmax, pass, act);
 }
@@ -916,7 +971,9 @@ struct HMat {
     }
     // far part of H~a: upward over psi = a (m = 1, 2 channels) and far sums per node
     reserve(4);
-    std::vector<float2> ones(2 * n_el, make_float2(1.f, 0.f));
+    // m = 1 in both channels: hi parts (1, 1), lo parts (0, 0) in the paired layout
+    std::vector<float2> ones(2 * n_el);
+    for (size_t i = 0; i < n_el; ++i) ones[2 * i] = make_float2(1.f, 1.f), ones[2 * i + 1] = make_float2(0.f, 0.f);
     DevBuf<float2> mm;
     mm.upload(ones.data(), ones.size(), s);
     HDev d = dev(2);

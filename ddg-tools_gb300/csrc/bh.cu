@@ -1305,9 +1305,15 @@ int rs_bh_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const double
       h->build_times[slot] = std::chrono::duration<double>(now - t_ph).count();
       t_ph = now;
     };
-    FaceGeom g = face_geometry(nf, faces, positions_host);
-    lap(0);
-    h->tree = build_face_tree(nf, faces, positions_host, g, leaf_size);
+    const SharedFaceTree *sh = shared_face_tree(faces, positions_host, nf, leaf_size);
+    if (!sh) {
+      FaceGeom g = face_geometry(nf, faces, positions_host);
+      lap(0);
+      h->tree = build_face_tree(nf, faces, positions_host, g, leaf_size);
+    } else {
+      lap(0);
+      h->tree = sh->tree;
+    }
     lap(1);
     upload_topology(h.get());
     lap(2);

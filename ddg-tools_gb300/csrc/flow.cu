@@ -18,7 +18,9 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <future>
 #include <memory>
+#include <optional>
 #include <string>
 #include <thread>
 #include <vector>
@@ -233,8 +235,18 @@ int rs_flow_step(rs_flow *F, double *report) {
     int w_code = 0;
     std::string w_kind, w_op, w_msg;
     double t_solver = 0.0;
+    // one face BVH for the Barnes-Hut lists and the metric's block cluster tree (when both ask
+    // for the same leaf size), built here while the solver's other parts (vertex tree,
+    // Laplacian, multigrid) start on the worker; the metric's build waits for it
+    FaceGeom g_sh;
+    Tree t_sh;
+    const bool share = F->o.leaf_size == F->o.solver.leaf_size;
+    std::promise<void> tree_ready;
+    std::shared_future<void> tree_fut = tree_ready.get_future().share();
     std::thread worker([&] {
       TrustedTopology trusted_here;
+      std::optional<SharedFaceTree> sh;
+      if (share) sh.emplace(g_sh, t_sh, faces, F->pos.data(), nf, F->o.leaf_size, &tree_fut);
       auto t0 = clk::now();
       int c = rs_solver_build(ctx, nv, nf, faces, F->pos.data(), F->o.alpha, F->o.beta, &F->o.solver, &sv.p);
       if (c == 0 && F->lmodel) {
@@ -244,7 +256,23 @@ int rs_flow_step(rs_flow *F, double *report) {
       if (c != 0) w_code = c, w_kind = rs_last_error_kind(), w_op = rs_last_error_operation(), w_msg = rs_last_error();
       t_solver = since(t0);
     });
-    const int b_code = rs_bh_build(ctx, nv, nf, faces, F->pos.data(), F->o.theta, F->o.leaf_size, &bh.p);
+    int b_code = 0;
+    try {
+      if (share) {
+        g_sh = face_geometry(nf, faces, F->pos.data());
+        t_sh = build_face_tree(nf, faces, F->pos.data(), g_sh, F->o.leaf_size);
+      }
+      tree_ready.set_value();
+    } catch (...) {
+      tree_ready.set_exception(std::current_exception());
+      worker.join();
+      throw;
+    }
+    {
+      std::optional<SharedFaceTree> sh_main;
+      if (share) sh_main.emplace(g_sh, t_sh, faces, F->pos.data(), nf, F->o.leaf_size, nullptr);
+      b_code = rs_bh_build(ctx, nv, nf, faces, F->pos.data(), F->o.theta, F->o.leaf_size, &bh.p);
+    }
     rep[9] = since(t);
     worker.join();
     check(b_code, "flow (tree)");

@@ -1093,9 +1093,10 @@ void metric_setup(rs_metric *M, rs_ctx *ctx, int nv, int nf, const uint32_t *fac
     t_ph = now;
   };
   M->nv = nv, M->nf = nf;
-  M->geom = face_geometry(nf, faces, pos);
+  const SharedFaceTree *sh = shared_face_tree(faces, pos, nf, leaf_size);
+  M->geom = sh ? sh->geom : face_geometry(nf, faces, pos);
   lap(0);
-  Tree T = build_face_tree(nf, faces, pos, M->geom, leaf_size);
+  Tree T = sh ? sh->tree : build_face_tree(nf, faces, pos, M->geom, leaf_size);
   lap(1);
   M->h.kind = FACE;
   M->h.n_el = nf;

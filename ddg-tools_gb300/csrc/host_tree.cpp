@@ -29,6 +29,23 @@ static std::string s(size_t x) { return std::to_string(x); }
 
 namespace {
 thread_local bool g_topology_trusted = false;
+thread_local const SharedFaceTree *g_shared_tree = nullptr;
+}
+
+SharedFaceTree::SharedFaceTree(const FaceGeom &g, const Tree &t, const uint32_t *faces_, const double *pos_, int nf_,
+                               int leaf_size_, const std::shared_future<void> *ready_)
+    : geom(g), tree(t), faces(faces_), pos(pos_), nf(nf_), leaf_size(leaf_size_), ready(ready_),
+      prev(g_shared_tree) {
+  g_shared_tree = this;
+}
+SharedFaceTree::~SharedFaceTree() { g_shared_tree = prev; }
+const SharedFaceTree *shared_face_tree(const uint32_t *faces, const double *pos, int nf, int leaf_size) {
+  for (const SharedFaceTree *s = g_shared_tree; s; s = s->prev)
+    if (s->faces == faces && s->pos == pos && s->nf == nf && s->leaf_size == leaf_size) {
+      if (s->ready) s->ready->get();
+      return s;
+    }
+  return nullptr;
 }
 
 TrustedTopology::TrustedTopology() : prev(g_topology_trusted) { g_topology_trusted = true; }

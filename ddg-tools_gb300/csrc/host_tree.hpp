@@ -4,6 +4,7 @@
 #pragma once
 #include <array>
 #include <cstdint>
+#include <future>
 #include <vector>
 
 namespace rsg {
@@ -60,5 +61,28 @@ Tree build_tree(size_t n, const double *pts, const double *ebox, const double *m
 // vertices, area.
 Tree build_face_tree(int nf, const uint32_t *faces, const double *pos, const FaceGeom &g,
                      int leaf_size);
+
+// A face geometry and face tree built once and offered, on the threads that hold one of these,
+// to the builders that would build the same ones: the flow step builds its BVH once for the
+// Barnes-Hut lists and the metric's block cluster tree. A builder asks with its faces and
+// positions (the same arrays, compared by address), face count and leaf size.
+struct SharedFaceTree {
+  // ready (optional): completed when geom and tree are built; a lookup waits for it and
+  // rethrows the builder's exception
+  SharedFaceTree(const FaceGeom &g, const Tree &t, const uint32_t *faces, const double *pos, int nf,
+                 int leaf_size, const std::shared_future<void> *ready);
+  ~SharedFaceTree();
+  SharedFaceTree(const SharedFaceTree &) = delete;
+  SharedFaceTree &operator=(const SharedFaceTree &) = delete;
+  const FaceGeom &geom;
+  const Tree &tree;
+  const uint32_t *faces;
+  const double *pos;
+  int nf, leaf_size;
+  const std::shared_future<void> *ready;
+  const SharedFaceTree *prev;
+};
+// The shared tree on this thread for these arguments, or null.
+const SharedFaceTree *shared_face_tree(const uint32_t *faces, const double *pos, int nf, int leaf_size);
 
 }  // namespace rsg

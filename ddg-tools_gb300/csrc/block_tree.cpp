@@ -207,26 +207,34 @@ Blocks classify_blocks(const Tree &T, double chi, size_t leaf_pairs, int threads
     const int parts = (n < 4096) ? 1 : nt;
     std::vector<std::vector<Pair>> of(parts), on(parts), ox(parts);
     W.run(parts, [&](int t) {
+      // branch-free: every pair's far and near entries and its (up to four) children are
+      // written at the current ends and the ends advance by the pair's class; the buffers hold
+      // the worst case (one far or near entry, four children per pair)
+      const size_t b = n * t / parts, e = n * (t + 1) / parts;
       std::vector<Pair> &fa = of[t], &ne = on[t], &nx = ox[t];
-      level.each(n * t / parts, n * (t + 1) / parts, [&](const Pair &pr) {
+      fa.resize(e - b), ne.resize(e - b), nx.resize(4 * (e - b));
+      Pair *pf = fa.data(), *pn = ne.data(), *px = nx.data();
+      level.each(b, e, [&](const Pair &pr) {
         const uint32_t a = pr.first, c = pr.second;
         const NodeRec &A = rec[a], &Cn = rec[c];
         const bool la = A.right == 0, lc = Cn.right == 0;
-        if (a != c && separated(A, Cn, chi))
-          fa.push_back(pr);
-        else if ((la && lc) || (size_t)A.len * Cn.len <= leaf_pairs)
-          ne.push_back(pr);
-        else {
-          uint32_t ka[2] = {la ? a : a + 1, A.right};
-          uint32_t kc[2] = {lc ? c : c + 1, Cn.right};
-          int na = la ? 1 : 2, nc = lc ? 1 : 2;
-          for (int x = 0; x < na; ++x)
-            for (int y = 0; y < nc; ++y) nx.push_back({ka[x], kc[y]});
-        }
+        const bool far_ = a != c && separated(A, Cn, chi);
+        const bool near_ = !far_ && ((la && lc) || (size_t)A.len * Cn.len <= leaf_pairs);
+        const bool split = !far_ && !near_;
+        *pf = pr, pf += far_;
+        *pn = pr, pn += near_;
+        // children (x, y) for x < na, y < nc in order; na = 1 or nc = 1 gives two of them
+        const uint32_t a0 = la ? a : a + 1, a1 = A.right, c0 = lc ? c : c + 1, c1 = Cn.right;
+        px[0] = {a0, c0};
+        px[1] = lc ? Pair{a1, c0} : Pair{a0, c1};
+        px[2] = {a1, c0};
+        px[3] = {a1, c1};
+        px += split ? (la || lc ? 2 : 4) : 0;
       }, [&](const Pair &pr) {
         __builtin_prefetch(&rec[pr.first]);
         __builtin_prefetch(&rec[pr.second]);
       });
+      fa.resize(pf - fa.data()), ne.resize(pn - ne.data()), nx.resize(px - nx.data());
     });
     Slices fl, nl, next;
     for (int t = 0; t < parts; ++t) {

@@ -238,6 +238,37 @@ inline int64_t tkey(double x) {
   return b ^ (int64_t)(((uint64_t)(b >> 63)) >> 1);
 }
 
+// Indices 0..n-1 ordered by (key, index): a stable least-significant-digit radix sort of the
+// keys made unsigned (sign bit flipped), 8 bits per pass, starting from index order; passes
+// whose digit is the same for every key are skipped.
+std::vector<uint32_t> sort_by_key(const std::vector<int64_t> &key) {
+  const size_t n = key.size();
+  std::vector<uint64_t> k0(n), k1(n);
+  std::vector<uint32_t> i0(n), i1(n);
+  std::vector<size_t> hist(8 * 256, 0);
+  for (size_t i = 0; i < n; ++i) {
+    const uint64_t u = (uint64_t)key[i] ^ (1ull << 63);
+    k0[i] = u, i0[i] = (uint32_t)i;
+    for (int d = 0; d < 8; ++d) hist[256 * d + ((u >> (8 * d)) & 255u)]++;
+  }
+  for (int d = 0; d < 8; ++d) {
+    size_t *h = hist.data() + 256 * d;
+    if (*std::max_element(h, h + 256) == n) continue;
+    size_t off = 0;
+    for (int b = 0; b < 256; ++b) {
+      const size_t c = h[b];
+      h[b] = off;
+      off += c;
+    }
+    for (size_t i = 0; i < n; ++i) {
+      const size_t o = h[(k0[i] >> (8 * d)) & 255u]++;
+      k1[o] = k0[i], i1[o] = i0[i];
+    }
+    k0.swap(k1), i0.swap(i1);
+  }
+  return i0;
+}
+
 }  // namespace
 
 namespace {
@@ -342,13 +373,9 @@ Tree build_tree(size_t n, const double *pts, const double *ebox, const double *m
   std::vector<uint32_t> srt[3];
   {
     auto presort = [&](int a) {
-      srt[a].resize(n);
       std::vector<int64_t> key(n);
       for (size_t i = 0; i < n; ++i) key[i] = tkey(pts[3 * i + a]);
-      std::iota(srt[a].begin(), srt[a].end(), 0u);
-      std::sort(srt[a].begin(), srt[a].end(), [&](uint32_t x, uint32_t y) {
-        return key[x] != key[y] ? key[x] < key[y] : x < y;
-      });
+      srt[a] = sort_by_key(key);
     };
     if (n > 65536) {
       auto f1 = std::async(std::launch::async, presort, 1);

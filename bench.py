@@ -14,8 +14,11 @@ is N(0, 0.001) per coordinate: the specified N(0, 0.01) exceeds the torus' minor
   move gigabytes, far above L2).
 * ``e2e``: the same through the public call with the positions read back to the host after
   every step, on the wall clock; h2d/d2h bytes from the library's copy counters.
-* ``roofline``: the dominant kernel of the step, the metric's near-field kernel (hm_rows),
-  FP32-bound, against the measured FP32 FMA peak; the pair kernel is reported beside it.
+* ``roofline``: the dominant kernel of the step, the metric's near-field kernel (hm_rows):
+  the bytes it must move per launch (the stored FP32 near weights and the channel values)
+  against the measured HBM copy bandwidth, with its FP32 view (``compute``: counted FLOP
+  against the measured FP32 FMA peak; the compensated arithmetic keeps it at the FP32 issue
+  limit, far below HBM); the pair kernel is reported beside it.
 * ``cpu_baseline`` / ``--impl reference``: the FP64 C++ restatement of the reference (the
   oracle; the Rust crate cannot be built here) on the host cores: one BH energy + differential
   and one metric product of the same mesh, combined with the step's measured GMRES iteration
@@ -210,6 +213,36 @@ FLOW_METRIC = "Hs-flow steps/s @204,800 faces (plain preconditioner, rel.res 1e-
 # channel, C = 12 channels per vector (the near weights w are evaluated once per set-up, not per
 # product; the compensated arithmetic executes about four times this count).
 NEAR_FLOP_PER_ENTRY = 36
+# Algorithmic bytes of one near-field launch (one vector, 12 channels): the stored FP32 weight
+# pair of every near entry (8 B) and the channel values of every face as float pairs (96 B).
+NEAR_BYTES_PER_ENTRY, NEAR_BYTES_PER_FACE = 8, 96
+
+
+def hbm_peak():
+    """The measured copy bandwidth of the GB300s (GB/s), else the stated fallback."""
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback (6.8 TB/s)"
+
+
+def near_roofline(near_entries, n_faces, t_rows_ms, fp32_peak, traffic, kernel_ms):
+    """The near-field kernel against HBM (the bytes it must move per launch), with its FP32
+    view beside it (it executes the compensated difference form at the FP32 issue limit)."""
+    algo = NEAR_BYTES_PER_ENTRY * near_entries + NEAR_BYTES_PER_FACE * n_faces
+    peak, src = hbm_peak()
+    gbs = algo / (t_rows_ms * 1e-3) / 1e9 if t_rows_ms else None
+    tflops = NEAR_FLOP_PER_ENTRY * near_entries / (t_rows_ms * 1e-3) / 1e12 if t_rows_ms else None
+    return {"bound": "hbm", "kernel": "hm_rows (metric near field, one vector)", "achieved": gbs, "peak": peak,
+            "unit": "GB/s", "frac": (gbs / peak) if gbs else None, "peak_source": src,
+            "work": f"{NEAR_BYTES_PER_ENTRY} B x {near_entries} near entries + {NEAR_BYTES_PER_FACE} B x "
+                    f"{n_faces} faces per launch ({algo} B)",
+            "traffic": traffic, "kernel_ms": kernel_ms,
+            "compute": {"bound": "fp32", "achieved": tflops, "peak": fp32_peak, "unit": "TFLOP/s",
+                        "frac": (tflops / fp32_peak) if tflops else None,
+                        "peak_source": "measured FP32 FMA throughput (rs_fp32_peak)",
+                        "work": f"{NEAR_FLOP_PER_ENTRY} FLOP x {near_entries} near entries per launch"}}
 # Operator applications per step assumed by the CPU reference arm (which has no preconditioned
 # solver of its own): the GPU arm's mean on this workload, GMRES iterations of the three
 # right-hand sides.
@@ -367,8 +400,6 @@ def bench_flow(args, rank, world, local):
     mprof = m.profile(1, 5)
     t_rows = mprof.get("metric_rows")
     peak = ctx.fp32_peak_tflops()
-    rows_flop = NEAR_FLOP_PER_ENTRY * mst["near_entries"]
-    achieved = rows_flop / (t_rows * 1e-3) / 1e12 if t_rows else None
     # the pair kernel on the same surface
     bh = R.BhTree.build(F, Q, R.BhOptions(theta, 8), ctx)
     bs = bh.sizes()
@@ -411,14 +442,8 @@ def bench_flow(args, rank, world, local):
         "e2e": {"value": e2e, "unit": "steps/s",
                 "h2d_bytes_per_step": int((c1[0] - c0[0]) / args.steps),
                 "d2h_bytes_per_step": int((c1[1] - c0[1]) / args.steps)},
-        "roofline": {"bound": "fp32", "kernel": "hm_rows (metric near field, one vector)",
-                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": (achieved / peak) if achieved else None,
-                     "peak_source": "measured FP32 FMA throughput (rs_fp32_peak); "
-                                    "MEASURED_PEAKS.json has no FP32 figure",
-                     "work": f"{NEAR_FLOP_PER_ENTRY} FLOP x {mst['near_entries']} near entries per launch",
-                     "traffic": _scaled_traffic("hm_rows", "matvec", mst["near_entries"], 103578780),
-                     "kernel_ms": mprof},
+        "roofline": near_roofline(mst["near_entries"], len(F), t_rows, peak,
+                                  _scaled_traffic("hm_rows", "matvec", mst["near_entries"], 103578780), mprof),
         "pair_kernel": {"gflops": FLOP_PER_INTERACTION * n_int / (t_pair * 1e-3) / 1e9 if t_pair else None,
                         "interactions": n_int, "ms": t_pair,
                         "frac": (FLOP_PER_INTERACTION * n_int / (t_pair * 1e-3) / 1e12 / peak) if t_pair else None},
@@ -499,7 +524,6 @@ def bench_matvec(args, rank, world, local):
     prof = m.profile(1, 5)
     peak = ctx.fp32_peak_tflops()
     t_rows = prof.get("metric_rows")
-    achieved = NEAR_FLOP_PER_ENTRY * st["near_entries"] / (t_rows * 1e-3) / 1e12 if t_rows else None
     if world > 1:
         import torch.distributed as dist
 
@@ -517,11 +541,8 @@ def bench_matvec(args, rank, world, local):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": world * args.steps / t_e2e, "unit": "products/s",
                 "h2d_bytes_per_step": int(xh.nbytes), "d2h_bytes_per_step": int(xh.nbytes)},
-        "roofline": {"bound": "fp32", "kernel": "hm_rows (metric near field, one vector)", "achieved": achieved,
-                     "peak": peak, "unit": "TFLOP/s", "frac": (achieved / peak) if achieved else None,
-                     "peak_source": "measured FP32 FMA throughput (rs_fp32_peak)",
-                     "work": f"{NEAR_FLOP_PER_ENTRY} FLOP x {st['near_entries']} near entries per launch",
-                     "traffic": traffic_from_profiles("hm_rows", "matvec"), "kernel_ms": prof},
+        "roofline": near_roofline(st["near_entries"], len(F), t_rows, peak, traffic_from_profiles("hm_rows", "matvec"),
+                                  prof),
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }

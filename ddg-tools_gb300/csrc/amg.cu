@@ -44,10 +44,12 @@ __device__ __forceinline__ void row_product(int i, int sub, const int *__restric
 
 // y = A x (accumulate: y += A x); C columns per row, a compile-time width so that the
 // accumulators stay in registers.
+// With t_out (and ACC false) also t_out = dinv y: the first Jacobi sweep from x = 0 of the level
+// whose right-hand side y is (a restriction that starts the next level's pre-smoothing).
 template <int TPR, bool ACC, int C>
 __global__ void spmv_c_kernel(int n, const int *__restrict__ ap, const int *__restrict__ ac,
                               const mgreal *__restrict__ av, const mgreal *__restrict__ x,
-                              mgreal *__restrict__ y) {
+                              mgreal *__restrict__ y, const mgreal *__restrict__ dinv, mgreal *__restrict__ t_out) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = t / TPR, sub = t % TPR;
   if (i >= n) return;
@@ -56,6 +58,11 @@ __global__ void spmv_c_kernel(int n, const int *__restrict__ ap, const int *__re
   if (sub != 0) return;
 #pragma unroll
   for (int c = 0; c < C; ++c) y[(size_t)i * C + c] = ACC ? y[(size_t)i * C + c] + acc[c] : acc[c];
+  if (!ACC && t_out) {
+    const mgreal d = dinv[i];
+#pragma unroll
+    for (int c = 0; c < C; ++c) t_out[(size_t)i * C + c] = d * acc[c];
+  }
 }
 
 // out = x + dinv (b - A x)
@@ -196,13 +203,17 @@ __global__ void __launch_bounds__(128) cg_dots_kernel(int n, const mgreal *__res
 }
 
 // x += alpha p, r -= alpha q (per column)
+// With t0: also t0 = dinv r (the next V-cycle's first sweep on level 0).
 __global__ void cg_update(int n, int C, const double *__restrict__ s, const mgreal *__restrict__ p,
-                          const mgreal *__restrict__ q, mgreal *__restrict__ x, mgreal *__restrict__ r) {
+                          const mgreal *__restrict__ q, mgreal *__restrict__ x, mgreal *__restrict__ r,
+                          const mgreal *__restrict__ dinv, mgreal *__restrict__ t0) {
   size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (t >= (size_t)n * C) return;
   const mgreal a = (mgreal)s[C + t % C];
   x[t] = fma(a, p[t], x[t]);
-  r[t] = fma(-a, q[t], r[t]);
+  const mgreal rn = fma(-a, q[t], r[t]);
+  r[t] = rn;
+  if (t0) t0[t] = dinv[t / C] * rn;
 }
 
 // p = z + beta p
@@ -245,9 +256,9 @@ int lanes_per_row(const Csr &A) {
 
 template <bool ACC, int C>
 void spmv_launch(int tpr, int n, const int *ap, const int *ac, const mgreal *av, const mgreal *x, mgreal *y,
-                 cudaStream_t s) {
+                 cudaStream_t s, const mgreal *dinv = nullptr, mgreal *t_out = nullptr) {
   const unsigned g = nblk((size_t)n * tpr, 128);
-#define RSG_CALL(T) spmv_c_kernel<T, ACC, C><<<g, 128, 0, s>>>(n, ap, ac, av, x, y)
+#define RSG_CALL(T) spmv_c_kernel<T, ACC, C><<<g, 128, 0, s>>>(n, ap, ac, av, x, y, dinv, t_out)
   RSG_TPR(tpr, RSG_CALL)
 #undef RSG_CALL
 }
@@ -314,7 +325,7 @@ void AmgDevice::spmv0_t(rs_ctx *ctx, const mgreal *x, mgreal *y) {
 }
 
 template <int CC>
-void AmgDevice::vcycle_t(rs_ctx *ctx, const mgreal *b, mgreal *x) {
+void AmgDevice::vcycle_t(rs_ctx *ctx, const mgreal *b, mgreal *x, bool pre0) {
   cudaStream_t s = ctx->stream;
   const int nl = (int)L.size();
   // `count` Jacobi sweeps that alternate between x_l and the level's scratch t, starting from
@@ -329,21 +340,26 @@ void AmgDevice::vcycle_t(rs_ctx *ctx, const mgreal *b, mgreal *x) {
     if (cur != xl)
       RSG_CUDA("preconditioner", cudaMemcpyAsync(xl, cur, (size_t)v.n * CC * sizeof(mgreal), cudaMemcpyDeviceToDevice, s));
   };
-  // down: level l solves A_l x_l = b_l (b_0 = b), x_l starts at 0
+  // down: level l solves A_l x_l = b_l (b_0 = b), x_l starts at 0. Pre-smoothing: the first
+  // sweep from x = 0 is dinv b, written where the remaining sweeps end in x_l (t for an even
+  // sweep count); below level 0 the restriction that forms b_l writes it, on level 0 the caller
+  // may have (pre0)
+  const bool odd = (sweeps - 1) % 2 == 1;
   const mgreal *bl = b;
   for (int l = 0; l < nl - 1; ++l) {
     Level &v = L[l];
     mgreal *xl = (l == 0) ? x : v.x.p;
-    // pre-smoothing: the first sweep from x = 0 is dinv b, written where the remaining sweeps
-    // end in x_l
-    const bool odd = (sweeps - 1) % 2 == 1;
-    jacobi0_kernel<CC><<<nblk((size_t)v.n * CC, 256), 256, 0, s>>>(v.n, v.dinv.p, bl, odd ? v.t.p : xl);
-    RSG_LAUNCHED(ctx, "amg_jacobi");
+    if (l == 0 && !pre0) {
+      jacobi0_kernel<CC><<<nblk((size_t)v.n * CC, 256), 256, 0, s>>>(v.n, v.dinv.p, bl, odd ? v.t.p : xl);
+      RSG_LAUNCHED(ctx, "amg_jacobi");
+    }
     smooth(v, bl, xl, odd, sweeps - 1);
     residual_launch<CC>(v.tpr_a, v.n, v.ap.p, v.ac.p, v.av.p, bl, xl, v.r.p, s);
     RSG_LAUNCHED(ctx, "amg_residual");
     Level &w = L[l + 1];
-    spmv_launch<false, CC>(v.tpr_r, w.n, v.rp.p, v.rc.p, v.rv.p, v.r.p, w.b.p, s);
+    const bool coarsest = l + 1 == nl - 1;  // solved densely, no sweep
+    spmv_launch<false, CC>(v.tpr_r, w.n, v.rp.p, v.rc.p, v.rv.p, v.r.p, w.b.p, s, coarsest ? nullptr : w.dinv.p,
+                           coarsest ? nullptr : (odd ? w.t.p : w.x.p));
     RSG_LAUNCHED(ctx, "amg_restrict");
     bl = w.b.p;
   }
@@ -379,9 +395,9 @@ void AmgDevice::spmv0(rs_ctx *ctx, const mgreal *x, mgreal *y, int C_) {
 #undef RSG_CALL
 }
 
-void AmgDevice::vcycle(rs_ctx *ctx, const mgreal *b, mgreal *x, int C_) {
+void AmgDevice::vcycle(rs_ctx *ctx, const mgreal *b, mgreal *x, int C_, bool pre0) {
   reserve(C_);
-#define RSG_CALL(W) vcycle_t<W>(ctx, b, x)
+#define RSG_CALL(W) vcycle_t<W>(ctx, b, x, pre0)
   RSG_AMG_WIDTH(RSG_CALL)
 #undef RSG_CALL
 }
@@ -406,10 +422,14 @@ void AmgDevice::pcg_body(rs_ctx *ctx, const mgreal *b, mgreal *x, int C_, int it
   for (int it = 0; it < iters; ++it) {
     spmv0(ctx, cg_p.p, cg_q.p, C_);
     dots(cg_p.p, cg_q.p, 0);
-    cg_update<<<g, 256, 0, s>>>(n, C_, cg_s.p, cg_p.p, cg_q.p, x, cg_r.p);
+    // the update also writes the next V-cycle's first level-0 sweep (none after the last step)
+    const bool more = it + 1 < iters;
+    const bool odd = (sweeps - 1) % 2 == 1;
+    cg_update<<<g, 256, 0, s>>>(n, C_, cg_s.p, cg_p.p, cg_q.p, x, cg_r.p, L[0].dinv.p,
+                                more ? (odd ? L[0].t.p : cg_z.p) : nullptr);
     RSG_LAUNCHED(ctx, "cg_update");
-    if (it + 1 == iters) break;
-    vcycle(ctx, cg_r.p, cg_z.p, C_);
+    if (!more) break;
+    vcycle(ctx, cg_r.p, cg_z.p, C_, true);
     dots(cg_r.p, cg_z.p, 1);
     cg_direction<<<g, 256, 0, s>>>(n, C_, cg_s.p, cg_z.p, cg_p.p);
     RSG_LAUNCHED(ctx, "cg_direction");

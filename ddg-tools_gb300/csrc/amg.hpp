@@ -51,7 +51,8 @@ struct AmgDevice {
   void upload(const AmgHost &h, cudaStream_t s);
   void reserve(int C_);
   // x = V-cycle(b) on level 0; b and x are n_0 x C device arrays (x overwritten).
-  void vcycle(rs_ctx *ctx, const mgreal *b, mgreal *x, int C_);
+  // pre0: the first Jacobi sweep of level 0 (dinv b) is already in place.
+  void vcycle(rs_ctx *ctx, const mgreal *b, mgreal *x, int C_, bool pre0 = false);
   // y = A_0 x for C columns.
   void spmv0(rs_ctx *ctx, const mgreal *x, mgreal *y, int C_);
   // x ~ A_0^-1 b by `iters` steps of conjugate gradients per column, preconditioned by one
@@ -77,7 +78,7 @@ struct AmgDevice {
 
  private:
   template <int CC>
-  void vcycle_t(rs_ctx *ctx, const mgreal *b, mgreal *x);
+  void vcycle_t(rs_ctx *ctx, const mgreal *b, mgreal *x, bool pre0);
   template <int CC>
   void spmv0_t(rs_ctx *ctx, const mgreal *x, mgreal *y);
   void pcg_body(rs_ctx *ctx, const mgreal *b, mgreal *x, int C_, int iters);

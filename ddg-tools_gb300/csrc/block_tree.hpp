@@ -3,8 +3,8 @@
 // (RS/src/spatial/block_tree.rs:159-247): level by level from (root, root); a pair of distinct
 // nodes is far when separated (max(r_a, r_b)^2 <= chi^2 d_box^2, d_box > 0;
 // RS/src/metric/hierarchical.rs:116-123), near when both are leaves or |a||b| <= leaf_pairs,
-// else both non-leaf sides are split. The near entries are not stored: the device evaluates
-// them in every product.
+// else both non-leaf sides are split. classify_blocks_device (block_tree_gpu.cu) runs the
+// classification on the device, in the same order as the crate's sequential pass.
 #pragma once
 #include <cstdint>
 #include <vector>
@@ -21,6 +21,6 @@ struct Blocks {
   size_t depth = 0;
 };
 
-Blocks classify_blocks(const Tree &T, double chi, size_t leaf_pairs, int threads = 0);
+Blocks classify_blocks_device(const Tree &T, double chi, size_t leaf_pairs);
 
 }  // namespace rsg

@@ -1036,7 +1036,7 @@ struct HMat {
     if (!(std::isfinite(chi) && chi >= 0.0))
       fail(RS_INVALID_OPTION, "InvalidOption", "upload", "chi must be a finite number >= 0");
     if (leaf_pairs < 0) fail(RS_INVALID_OPTION, "InvalidOption", "upload", "leaf_pairs must be >= 0");
-    blocks = classify_blocks(tree, chi, (size_t)leaf_pairs);
+    blocks = classify_blocks_device(tree, chi, (size_t)leaf_pairs);
   }
 };
 

@@ -50,6 +50,20 @@ sys.path.insert(0, str(ROOT / "ddg-tools_gb300"))
 FLOP_PER_INTERACTION = 61  # energy + gradient, SURVEY's count (FMA = 2, Kahan not counted)
 
 
+def replica_rate(units, seconds, world, device=None):
+    """(rate, seconds) of `world` replicas that each processed `units` in their own `seconds`:
+    all ranks' units over the slowest rank's time, from an all-reduce (max) of the times over
+    the initialised process group (NCCL on the GPUs, gloo in the CPU tests)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        tt = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        seconds = float(tt.item())
+    return world * units / seconds, seconds
+
+
 def workload(name: str):
     from rs_gb300 import generators as gen
 
@@ -330,12 +344,7 @@ def bench_flow(args, rank, world, local):
         stream.synchronize()
     launches = ctx.launch_count() - l0
     ms = [a.elapsed_time(b) for a, b in evs]
-    t_total = sum(ms) / 1e3
-    if world > 1:
-        tt = torch.tensor([t_total], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_total = float(tt.item())
-    value = world * args.steps / t_total
+    value, t_total = replica_rate(args.steps, sum(ms) / 1e3, world, dev)
 
     # e2e: the public call with host positions read back after every step, wall clock
     if world > 1:
@@ -346,13 +355,8 @@ def bench_flow(args, rank, world, local):
     for _ in range(args.steps):
         e2e_reps.append(flow.step())
         Q = flow.positions()
-    t_e2e = time.perf_counter() - t0
     c1 = R.copy_counters()
-    if world > 1:
-        tt = torch.tensor([t_e2e], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(tt.item())
-    e2e = world * args.steps / t_e2e
+    e2e, t_e2e = replica_rate(args.steps, time.perf_counter() - t0, world, dev)
 
     # the learned preconditioner on the same flow (continuing from here), plain as its fallback
     learned = None
@@ -509,18 +513,13 @@ def bench_matvec(args, rank, world, local):
                 b.record(stream)
             stream.synchronize()
         launches = ctx.launch_count() - l0
-    t_total = sum(a.elapsed_time(b) for a, b in evs) / 1e3
-    if world > 1:
-        tt = torch.tensor([t_total], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_total = float(tt.item())
-    value = world * args.steps / t_total
+    value, t_total = replica_rate(args.steps, sum(a.elapsed_time(b) for a, b in evs) / 1e3, world, dev)
     xh = np.random.default_rng(1).standard_normal(3 * len(P))
     m.apply(xh)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         yh = m.apply(xh)
-    t_e2e = time.perf_counter() - t0
+    e2e, _ = replica_rate(args.steps, time.perf_counter() - t0, world, dev)
     prof = m.profile(1, 5)
     peak = ctx.fp32_peak_tflops()
     t_rows = prof.get("metric_rows")
@@ -539,7 +538,7 @@ def bench_matvec(args, rank, world, local):
         "config": {"workload": f"matvec: {desc}", "chi": 0.5, "alpha": 6, "beta": 12, "leaf_size": 8,
                    "leaf_pairs": 64, **st, "l2": "flushed (256 MiB) between steps",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "e2e": {"value": world * args.steps / t_e2e, "unit": "products/s",
+        "e2e": {"value": e2e, "unit": "products/s",
                 "h2d_bytes_per_step": int(xh.nbytes), "d2h_bytes_per_step": int(xh.nbytes)},
         "roofline": near_roofline(st["near_entries"], len(F), t_rows, peak, traffic_from_profiles("hm_rows", "matvec"),
                                   prof),
@@ -641,12 +640,7 @@ def main() -> int:
         launches = ctx.launch_count() - l0
         torch.cuda.synchronize(dev)
     ms = [a.elapsed_time(b) for a, b in evs]
-    t_total = sum(ms) / 1e3
-    if world > 1:
-        tt = torch.tensor([t_total], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_total = float(tt.item())
-    value = world * flop * args.steps / t_total / 1e9
+    value, t_total = replica_rate(flop * args.steps / 1e9, sum(ms) / 1e3, world, dev)
     energy = float(e_dev.item())
 
     # ---- e2e: public C-ABI entry points with host buffers
@@ -658,12 +652,7 @@ def main() -> int:
     for _ in range(args.steps):
         tree.refit(P)
         E2, dE2 = tree.energy_and_differential(ex)
-    t_e2e = time.perf_counter() - t0
-    if world > 1:
-        tt = torch.tensor([t_e2e], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(tt.item())
-    e2e = world * flop * args.steps / t_e2e / 1e9
+    e2e, _ = replica_rate(flop * args.steps / 1e9, time.perf_counter() - t0, world, dev)
 
     # ---- roofline of the pair kernel (events around each launch on the library stream)
     prof = tree.profile(ex, reps=max(3, min(args.steps, 10)))

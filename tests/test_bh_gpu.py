@@ -206,3 +206,22 @@ def test_full_size_c3_identities(ctx):
     euler = np.sum((P - c) * g)
     assert abs(euler - (4 + 6 - 12) * E) <= 1e-5 * np.abs((P - c) * g).sum()
     assert t.try_energy() == E
+
+
+def test_build_phase_times(ctx):
+    """rs_bh_build_times / rs_metric_build_times: every phase non-negative, and the phases
+    together within the build's wall time."""
+    import time
+
+    P, F = gen.config_c2(level=4)
+    t0 = time.perf_counter()
+    t = R.BhTree.build(F, P, R.BhOptions(0.25), ctx)
+    wall = time.perf_counter() - t0
+    bt = t.build_times()
+    assert set(bt) == {"geometry", "tree", "topology", "list_counts", "list_fill", "list_finish", "refit"}
+    assert all(v >= 0.0 for v in bt.values()) and sum(bt.values()) <= wall
+    t0 = time.perf_counter()
+    m = R.FaceMetricTree(F, P, R.Exponents(), R.ClusterTreeOptions(chi=0.5), ctx)
+    wall = time.perf_counter() - t0
+    mt = m.build_times()
+    assert len(mt) == 8 and all(v >= 0.0 for v in mt.values()) and sum(mt.values()) <= wall

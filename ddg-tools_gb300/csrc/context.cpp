@@ -62,6 +62,25 @@ const char *rs_last_error(void) { return rsg::last_detail(); }
 const char *rs_last_error_operation(void) { return rsg::last_operation(); }
 const char *rs_last_error_kind(void) { return rsg::last_kind(); }
 
+int rs_device_info(int ordinal, char *name, int name_len, int *cc_major, int *cc_minor,
+                   uint64_t *memory_bytes) {
+  return rsg::guard([&] {
+    int n = 0;
+    RSG_CUDA("context", cudaGetDeviceCount(&n));
+    if (ordinal < 0 || ordinal >= n)
+      rsg::fail(RS_INVALID_OPTION, "InvalidOption", "context", "cuda_ordinal " + std::to_string(ordinal) +
+                " is not below the device count " + std::to_string(n));
+    cudaDeviceProp p;
+    RSG_CUDA("context", cudaGetDeviceProperties(&p, ordinal));
+    if (name && name_len > 0) {
+      std::strncpy(name, p.name, (size_t)name_len - 1);
+      name[name_len - 1] = 0;
+    }
+    *cc_major = p.major, *cc_minor = p.minor;
+    *memory_bytes = (uint64_t)p.totalGlobalMem;
+  });
+}
+
 int rs_device_count(int *count) {
   return rsg::guard([&] {
     int n = 0;

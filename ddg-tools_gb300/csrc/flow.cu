@@ -299,8 +299,12 @@ int rs_flow_step(rs_flow *F, double *report) {
     RSG_CUDA("flow", cudaStreamSynchronize(s));
     rep[10] = since(t);
     if (!std::isfinite(E0)) fail(RS_NONFINITE_ENERGY, "NonFiniteEnergy", "flow", "non-finite energy");
-    for (double x : g)
+    double gsq = 0.0;
+    for (double x : g) {
       if (!std::isfinite(x)) fail(RS_NONFINITE_ENERGY, "NonFiniteEnergy", "flow", "non-finite differential");
+      gsq += x * x;
+    }
+    rep[21] = std::sqrt(gsq);
     // C_N rows
     std::vector<std::vector<double>> cn(k, std::vector<double>(nd));
     for (int i = 0; i < k; ++i) {
@@ -399,6 +403,8 @@ int rs_flow_step(rs_flow *F, double *report) {
     // 4. Armijo backtracking on the frozen lists
     t = clk::now();
     double tau = F->last_tau > 0.0 ? 2.0 * F->last_tau : F->l0 / maxdisp;
+    rep[22] = tau;
+    rep[23] = xinf;
     const double tau_min = 1e-12 * F->l0 / xinf;
     std::vector<double> trial(nd);
     double E1 = E0;
@@ -422,7 +428,10 @@ int rs_flow_step(rs_flow *F, double *report) {
     // 5. projection
     t = clk::now();
     double cres = 0.0;
+    int newton_rounds = 0;
+    bool proj_converged = true;
     if (accepted) {
+      proj_converged = k == 0;
       for (int round = 0; round < F->o.newton_max && k > 0; ++round) {
         std::vector<double> phi(k);
         double worst_rel = 0.0;
@@ -432,7 +441,11 @@ int rs_flow_step(rs_flow *F, double *report) {
           phi[i] = val - tgt;
           worst_rel = std::max(worst_rel, std::fabs(phi[i]) / std::max(1.0, std::fabs(tgt)));
         }
-        if (worst_rel <= 1e-12) break;
+        if (worst_rel <= 1e-12) {
+          proj_converged = true;
+          break;
+        }
+        ++newton_rounds;
         std::vector<double> cc = solve_n(phi);
         for (size_t r = 0; r < nd; ++r) {
           double h = 0.0;
@@ -449,6 +462,14 @@ int rs_flow_step(rs_flow *F, double *report) {
         double tgt = rows[i] == 0 ? F->area0 : F->vol0;
         cres = std::max(cres, std::fabs(val - tgt) / std::max(1.0, std::fabs(tgt)));
       }
+      if (cres <= 1e-12) proj_converged = true;
+      // F after the projection, on the same lists (StepReport::energy_after, session.rs:155-156)
+      double Ea = NAN;
+      check(rs_bh_refit(bh.p, trial.data()), "flow (energy)");
+      check(rs_bh_energy(bh.p, F->o.alpha, F->o.beta, &Ea), "flow (energy)");
+      if (!std::isfinite(Ea)) fail(RS_NONFINITE_ENERGY, "NonFiniteEnergy", "flow", "non-finite energy after the projection");
+      rep[26] = E1;
+      E1 = Ea;
       F->pos = trial;
       F->last_tau = tau;
       F->iteration++;
@@ -459,12 +480,15 @@ int rs_flow_step(rs_flow *F, double *report) {
       check(rs_solver_learned_counts(sv.p, &ls, &lf), "flow");
       rep[19] = (double)ls, rep[20] = (double)lf;
     }
+    if (!accepted) rep[26] = E0;
     rep[0] = E0;
     rep[1] = E1;
     rep[2] = accepted ? tau : 0.0;
     rep[3] = halvings;
     rep[15] = accepted ? 1.0 : 0.0;
     rep[17] = cres;
+    rep[24] = newton_rounds;
+    rep[25] = proj_converged ? 0.0 : 1.0;
     rep[8] = since(t_step);
     if (report) std::memcpy(report, rep, sizeof(rep));
   });

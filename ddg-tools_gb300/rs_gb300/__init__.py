@@ -78,6 +78,8 @@ def load_library(path: str | os.PathLike | None = None):
         getattr(L, name).restype = C.c_char_p
     sig = {
         "rs_device_count": [C.POINTER(C.c_int)],
+        "rs_device_info": [C.c_int, C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                           C.POINTER(C.c_uint64)],
         "rs_ctx_create": [C.c_int, C.POINTER(_vp)],
         "rs_ctx_stream": [_vp, C.POINTER(_vp)],
         "rs_ctx_synchronize": [_vp],
@@ -183,6 +185,16 @@ def device_count() -> int:
     n = C.c_int()
     _check(load_library().rs_device_count(C.byref(n)))
     return n.value
+
+
+def device_info(ordinal: int = 0) -> dict:
+    """Name, compute capability and memory of one device, without creating a context
+    (gpu::devices, RS/src/gpu/mod.rs:89-100)."""
+    name = C.create_string_buffer(256)
+    ma, mi, mem = C.c_int(), C.c_int(), C.c_uint64()
+    _check(load_library().rs_device_info(int(ordinal), name, 256, C.byref(ma), C.byref(mi), C.byref(mem)))
+    return {"ordinal": int(ordinal), "name": name.value.decode(), "compute_capability": f"{ma.value}.{mi.value}",
+            "memory_bytes": int(mem.value)}
 
 
 class Context:
@@ -673,7 +685,8 @@ FLOW_REPORT_KEYS = ["energy_before", "energy_after", "tau", "halvings", "gmres_a
                     "gmres_direction", "relative_residual", "seconds", "seconds_tree", "seconds_energy",
                     "seconds_solver_build", "seconds_solve", "seconds_line_search", "seconds_projection",
                     "accepted", "slope", "constraint_residual", "fallbacks", "learned_solves",
-                    "learned_fallbacks"]
+                    "learned_fallbacks", "gradient_norm", "tau0", "direction_max", "newton_steps",
+                    "projection_max_rounds", "energy_trial"]
 
 
 class Flow:

@@ -62,6 +62,11 @@ const char *rs_last_error_kind(void);
 
 /* Number of CUDA devices (gpu::device_count, RS/src/gpu/mod.rs:89-100). */
 int rs_device_count(int *count);
+/* Name, compute capability and memory of device `ordinal`, without creating a context
+ * (gpu::devices, RS/src/gpu/mod.rs:89-100, as gpu_info lists them:
+ * crates/ddg-py/src/repulsive_surfaces.rs:1899-1938). */
+int rs_device_info(int ordinal, char *name, int name_len, int *cc_major, int *cc_minor,
+                   uint64_t *memory_bytes);
 
 /* A context on device `ordinal` with its own non-blocking stream
  * (GpuContext::new, RS/src/gpu/mod.rs:102-127; cuda.rs:100-119). */
@@ -349,16 +354,22 @@ int rs_solver_set_learned(rs_solver *s, rs_learned *model, rs_lgraph *graph, int
 /* Learned solves and how many of them fell back to the plain preconditioner. */
 int rs_solver_learned_counts(rs_solver *s, int64_t *solves, int64_t *fallbacks);
 
-#define RS_FLOW_REPORT_LEN 21
+#define RS_FLOW_REPORT_LEN 27
 /* Session::step (session.rs:724-747): one step. report[RS_FLOW_REPORT_LEN]:
- *  0 energy before, 1 energy after, 2 accepted tau (0: refused), 3 halvings,
+ *  0 energy before, 1 energy after the projection (on the step's lists; the energy before
+ *  when refused), 2 accepted tau (0: refused), 3 halvings,
  *  4..6 GMRES iterations of the solves (area row, volume row, direction),
  *  7 worst true relative residual, 8 seconds of the step, 9 tree and lists, 10 energy,
  *  11 solver build, 12 solves, 13 line search, 14 projection, 15 accepted (1/0),
  *  16 slope g.x, 17 relative nonlinear-constraint residual after the projection,
  *  18 fallbacks: solves repeated with restart 60 and the larger iteration cap after GMRES
  *     ended above the divergence threshold (RobustHierarchical, direction.rs:269-379),
- *  19 learned-preconditioner solves, 20 of them repeated with the plain preconditioner. */
+ *  19 learned-preconditioner solves, 20 of them repeated with the plain preconditioner,
+ *  21 gradient norm |dE|_2 over the 3V coordinates (StepReport::gradient_norm, session.rs:161-162),
+ *  22 the first trial's step size (tau0), 23 |x|_inf, the largest coordinate of the direction,
+ *  24 Newton rounds of the projection, 25 projection status (0 converged: every held row within
+ *     1e-12 relative, or no held rows; 1 the rounds were used up: ProjectionStatus::MaxRounds,
+ *     solve/schur.rs:450-461), 26 energy at the accepted trial, before the projection. */
 int rs_flow_step(rs_flow *f, double *report);
 /* The current positions (V x 3). */
 int rs_flow_positions(rs_flow *f, double *positions_host);

@@ -1,0 +1,585 @@
+// Continuous collision detection of a mesh moving against itself, on the GPU: first_contact of
+// RS/src/ccd.rs:762-884 (no obstacles, no exempt band) with its windows (ccd.rs:887-1045), the
+// conservative advancement (ccd.rs:529-592) and the distances of RC/src/ccd.rs:237-319.
+//
+// This file is compiled with -fmad=false: every FP64 operation rounds as the reference's host
+// code does (Rust never contracts a multiply-add), so tau_max is bitwise the reference's.
+//
+// Per window [lo, hi]:
+//   1. swept boxes: per vertex the hull of its positions at lo and hi; per face and per edge the
+//      union of its vertices' boxes, inflated by h = gap/2 (1 + 1e-6);
+//   2. a box tree per primitive kind, as the reference builds it: boxes sorted along a Morton
+//      curve of their centres, blocks of 8 united, blocks merged pairwise up to one root;
+//   3. one thread per query (a vertex against the face tree, an edge against the edge tree)
+//      walks the tree and runs the narrow phase on every element whose own box overlaps the
+//      query box (so the candidate pairs are exactly those of the reference, whatever the
+//      tree's shape), keeping the earliest contact in one global atomic minimum.
+// A pair's contact time does not depend on the horizon it is given (see advance()), so the
+// global minimum used as horizon only skips pairs that cannot lower the result.
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <vector>
+
+#include "common.hpp"
+
+namespace rsg {
+namespace {
+
+struct DBox {
+  double lo[3], hi[3];
+};
+
+__device__ __forceinline__ double3 at3(double3 p, double3 u, double t) {
+  return make_double3(p.x + t * u.x, p.y + t * u.y, p.z + t * u.z);
+}
+__device__ __forceinline__ double3 sub3(double3 a, double3 b) { return make_double3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ double3 add3(double3 a, double3 b) { return make_double3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ double3 scale3(double3 a, double s) { return make_double3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ double dot3(double3 a, double3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ double3 cross3(double3 a, double3 b) {
+  return make_double3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ double norm3(double3 a) { return sqrt(dot3(a, a)); }
+// f64::clamp(0, 1): a NaN stays NaN
+__device__ __forceinline__ double clamp01(double x) {
+  if (x < 0.0) x = 0.0;
+  if (x > 1.0) x = 1.0;
+  return x;
+}
+
+__device__ double point_segment_distance(double3 p, double3 a, double3 b) {  // RC/src/ccd.rs:237-247
+  const double3 ab = sub3(b, a), ap = sub3(p, a);
+  const double e = dot3(ab, ab);
+  const double t = e > 0.0 ? clamp01(dot3(ap, ab) / e) : 0.0;
+  return norm3(sub3(ap, scale3(ab, t)));
+}
+
+__device__ double segment_segment_distance(double3 p1, double3 q1, double3 p2, double3 q2) {  // ccd.rs:266-291
+  double best = fmin(fmin(fmin(point_segment_distance(p1, p2, q2), point_segment_distance(q1, p2, q2)),
+                          point_segment_distance(p2, p1, q1)),
+                     point_segment_distance(q2, p1, q1));
+  const double3 d1 = sub3(q1, p1), d2 = sub3(q2, p2);
+  const double a = dot3(d1, d1), e = dot3(d2, d2);
+  const double3 n = cross3(d1, d2);
+  const double nn = dot3(n, n);
+  if (a > 0.0 && e > 0.0 && nn > 0.0) {
+    const double3 r = sub3(p1, p2);
+    const double b = dot3(d1, d2), c = dot3(d1, r), f = dot3(d2, r);
+    double s = clamp01(dot3(cross3(sub3(p2, p1), d2), n) / nn);
+    const double t = clamp01((b * s + f) / e);
+    s = clamp01((b * t - c) / a);
+    best = fmin(best, norm3(sub3(add3(p1, scale3(d1, s)), add3(p2, scale3(d2, t)))));
+  }
+  return best;
+}
+
+__device__ double point_triangle_distance(double3 p, double3 a, double3 b, double3 c) {  // ccd.rs:298-319
+  const double edges =
+      fmin(fmin(point_segment_distance(p, a, b), point_segment_distance(p, b, c)), point_segment_distance(p, c, a));
+  const double3 ab = sub3(b, a), ac = sub3(c, a);
+  const double3 n = cross3(ab, ac);
+  const double nn = dot3(n, n);
+  if (nn <= 0.0) return edges;
+  const double3 ap = sub3(p, a);
+  const double v = dot3(cross3(ap, ac), n) / nn;
+  const double w = dot3(cross3(ab, ap), n) / nn;
+  if (v >= 0.0 && w >= 0.0 && v + w <= 1.0) return fmin(edges, fabs(dot3(ap, n)) / sqrt(nn));
+  return edges;
+}
+
+struct Tally {
+  unsigned long long pairs = 0, close = 0, touching = 0, evals = 0;
+};
+
+// Conservative advancement of one pair on [lo, hz] (advance, RS/src/ccd.rs:529-592); returns
+// the contact time or -1 for none. When a step would pass hz with the cheap bound, the
+// reference retries with the refined bound l' and takes min(l, l'); that step is at least as
+// long, so it passes hz too and the pair has no contact before hz. The retry is therefore
+// left out: the result is the same. Every iterate that stays below hz is the reference's, so
+// a contact time below the horizon does not depend on the horizon.
+template <class Dist>
+__device__ double advance(const Dist &dist, double l, double gap_abs, int max_iterations, double close_factor,
+                          double lo, double hz, Tally &tally) {
+  const double d0 = dist(0.0);
+  tally.pairs += 1;
+  tally.evals += 1;
+  if (lo == 0.0) {
+    if (d0 <= 1e-12 * gap_abs) {
+      tally.touching += 1;
+      return -1.0;
+    }
+    if (d0 < gap_abs) tally.close += 1;
+  } else if (d0 <= 1e-12 * gap_abs) {
+    return -1.0;
+  }
+  const double target = d0 > gap_abs ? gap_abs : close_factor * d0;
+  const double slack = 1e-9 * d0;
+  double tau = lo;
+  double d = d0;
+  if (lo != 0.0) {
+    d = dist(lo);
+    tally.evals += 1;
+  }
+  for (int it = 0; it < max_iterations; ++it) {
+    if (isnan(d) || d - target <= slack) return tau;
+    const double next = tau + (d - target) / l;
+    if (next >= hz || isnan(next)) return -1.0;
+    tau = next;
+    d = dist(tau);
+    tally.evals += 1;
+  }
+  return tau;
+}
+
+__device__ __forceinline__ bool overlaps(const DBox &a, const DBox &b) {  // ccd.rs:258-261
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    if (!(a.lo[k] <= b.hi[k] && b.lo[k] <= a.hi[k])) return false;
+  return true;
+}
+
+__device__ __forceinline__ DBox inflate(DBox b, double h) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) b.lo[k] = b.lo[k] - h, b.hi[k] = b.hi[k] + h;
+  return b;
+}
+
+__device__ __forceinline__ DBox unite(DBox a, const DBox &b) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) a.lo[k] = fmin(a.lo[k], b.lo[k]), a.hi[k] = fmax(a.hi[k], b.hi[k]);
+  return a;
+}
+
+__global__ void speed_kernel(int nv, const double3 *vel, double *speed) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < nv) speed[v] = norm3(vel[v]);
+}
+
+// hull of the positions at lo and hi (Aabb::empty grown by both points)
+__global__ void vbox_kernel(int nv, const double3 *start, const double3 *vel, double lo, double hi, DBox *vbox) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= nv) return;
+  const double3 a = at3(start[v], vel[v], lo), b = at3(start[v], vel[v], hi);
+  DBox r;
+  r.lo[0] = fmin(fmin(INFINITY, a.x), b.x), r.hi[0] = fmax(fmax(-INFINITY, a.x), b.x);
+  r.lo[1] = fmin(fmin(INFINITY, a.y), b.y), r.hi[1] = fmax(fmax(-INFINITY, a.y), b.y);
+  r.lo[2] = fmin(fmin(INFINITY, a.z), b.z), r.hi[2] = fmax(fmax(-INFINITY, a.z), b.z);
+  vbox[v] = r;
+}
+
+// Inflated primitive boxes and 30-bit Morton keys of their centres (the order only shapes the
+// tree; it does not change the candidate pairs).
+template <int K>
+__global__ void prim_box_kernel(int n, const uint32_t *verts, const DBox *vbox, double h, double3 blo,
+                                double3 bscale, DBox *box, uint32_t *key, uint32_t *idx) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  DBox b = vbox[verts[K * i]];
+#pragma unroll
+  for (int k = 1; k < K; ++k) b = unite(b, vbox[verts[K * i + k]]);
+  b = inflate(b, h);
+  box[i] = b;
+  auto q = [](double c, double l, double s) {
+    double x = (c - l) * s;
+    x = x < 0.0 ? 0.0 : (x > 1023.0 ? 1023.0 : x);
+    uint32_t u = (uint32_t)x;
+    u = (u | (u << 16)) & 0x030000FFu;
+    u = (u | (u << 8)) & 0x0300F00Fu;
+    u = (u | (u << 4)) & 0x030C30C3u;
+    u = (u | (u << 2)) & 0x09249249u;
+    return u;
+  };
+  key[i] = q(0.5 * (b.lo[0] + b.hi[0]), blo.x, bscale.x) | (q(0.5 * (b.lo[1] + b.hi[1]), blo.y, bscale.y) << 1) |
+           (q(0.5 * (b.lo[2] + b.hi[2]), blo.z, bscale.z) << 2);
+  idx[i] = (uint32_t)i;
+}
+
+__global__ void gather_boxes_kernel(int n, const uint32_t *order, const DBox *box, DBox *sbox) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) sbox[i] = box[order[i]];
+}
+
+// level 0: unions of blocks of `leaf` sorted boxes; level k: unions of pairs of level k - 1
+__global__ void level_kernel(int n_out, const DBox *in, int n_in, int group, DBox *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_out) return;
+  DBox r;
+  for (int k = 0; k < 3; ++k) r.lo[k] = INFINITY, r.hi[k] = -INFINITY;
+  const int b = i * group, e = min(b + group, n_in);
+  for (int j = b; j < e; ++j) r = unite(r, in[j]);
+  out[i] = r;
+}
+
+struct Tree {
+  const DBox *sbox;      // sorted element boxes
+  const uint32_t *order; // sorted position -> element
+  const DBox *levels;    // all levels, level 0 first
+  const int *lvl_off;    // offset of each level in `levels`
+  const int *lvl_len;
+  int n, n_levels, leaf;
+};
+
+constexpr int kStack = 64;
+
+// Calls f(element) for every element whose box overlaps q (query, ccd.rs:359-389). Returns
+// false if the stack would overflow (not reachable: a depth-first walk of a tree of n_levels
+// <= 62 levels holds at most n_levels + 1 entries).
+template <class F>
+__device__ bool query(const Tree &t, const DBox &q, F &&f) {
+  int2 stack[kStack];
+  int sp = 0;
+  stack[sp++] = make_int2(t.n_levels - 1, 0);
+  while (sp > 0) {
+    const int2 e = stack[--sp];
+    if (!overlaps(t.levels[t.lvl_off[e.x] + e.y], q)) continue;
+    if (e.x == 0) {
+      const int b = e.y * t.leaf, end = min(b + t.leaf, t.n);
+      for (int pos = b; pos < end; ++pos)
+        if (overlaps(t.sbox[pos], q)) f(t.order[pos]);
+    } else {
+      if (sp + 2 > kStack) return false;
+      stack[sp++] = make_int2(e.x - 1, 2 * e.y);
+      if (2 * e.y + 1 < t.lvl_len[e.x - 1]) stack[sp++] = make_int2(e.x - 1, 2 * e.y + 1);
+    }
+  }
+  return true;
+}
+
+struct Params {
+  const double3 *start, *vel;
+  const double *speed;
+  const uint32_t *faces;  // 3 per face
+  const uint32_t *edges;  // 2 per edge
+  const DBox *vbox;
+  const DBox *ebox;       // inflated, element order
+  int nv, ne, max_iterations;
+  double gap_abs, close_factor, h, lo, hi;
+  unsigned long long *best;   // bits of the earliest contact time (+inf: none)
+  unsigned long long *tally;  // pairs, close, touching, evaluations
+  int *overflow;
+};
+
+constexpr double kMargin = 1.0 + 1e-12;  // ccd.rs:498-499
+
+__device__ __forceinline__ double horizon(const Params &P) {
+  const double b = __longlong_as_double((long long)*(volatile unsigned long long *)P.best);
+  return fmin(b, P.hi);
+}
+
+__device__ void flush_tally(const Params &P, const Tally &t) {
+  unsigned long long v[4] = {t.pairs, t.close, t.touching, t.evals};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    unsigned long long x = v[k];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0 && x) atomicAdd(P.tally + k, x);
+  }
+}
+
+// vertex against triangle, one thread per vertex (ccd.rs:937-985)
+__global__ void __launch_bounds__(128) vt_kernel(Params P, Tree ft) {
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  Tally tally;
+  if (v < P.nv) {
+    const DBox q = inflate(P.vbox[v], P.h);
+    const double3 p = P.start[v], u = P.vel[v];
+    const double sv = P.speed[v];
+    const bool ok = query(ft, q, [&](uint32_t f) {
+      const uint32_t a = P.faces[3 * f], b = P.faces[3 * f + 1], c = P.faces[3 * f + 2];
+      if (a == (uint32_t)v || b == (uint32_t)v || c == (uint32_t)v) return;
+      const double3 ta = at3(P.start[a], P.vel[a], 0.0), tb = at3(P.start[b], P.vel[b], 0.0),
+                    tc = at3(P.start[c], P.vel[c], 0.0);
+      const double3 ua = P.vel[a], ub = P.vel[b], uc = P.vel[c];
+      const double lc = (sv + fmax(fmax(P.speed[a], P.speed[b]), P.speed[c])) * kMargin;
+      auto dist = [&](double t) {
+        return point_triangle_distance(at3(p, u, t), at3(ta, ua, t), at3(tb, ub, t), at3(tc, uc, t));
+      };
+      const double r = advance(dist, lc, P.gap_abs, P.max_iterations, P.close_factor, P.lo, horizon(P), tally);
+      if (r >= 0.0) atomicMin(P.best, (unsigned long long)__double_as_longlong(r));
+    });
+    if (!ok) atomicExch(P.overflow, 1);
+  }
+  flush_tally(P, tally);
+}
+
+// edge against edge, one thread per edge e, partners e2 > e without a common vertex
+// (ccd.rs:987-1038)
+__global__ void __launch_bounds__(128) ee_kernel(Params P, Tree et) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  Tally tally;
+  if (e < P.ne) {
+    const DBox q = P.ebox[e];
+    const uint32_t a = P.edges[2 * e], b = P.edges[2 * e + 1];
+    const double3 pa = P.start[a], pb = P.start[b], ua = P.vel[a], ub = P.vel[b];
+    const double sab = fmax(P.speed[a], P.speed[b]);
+    const bool ok = query(et, q, [&](uint32_t e2) {
+      if (e2 <= (uint32_t)e) return;
+      const uint32_t c = P.edges[2 * e2], d = P.edges[2 * e2 + 1];
+      if (c == a || c == b || d == a || d == b) return;
+      const double3 pc = P.start[c], pd = P.start[d], uc = P.vel[c], ud = P.vel[d];
+      const double lc = (sab + fmax(P.speed[c], P.speed[d])) * kMargin;
+      auto dist = [&](double t) {
+        return segment_segment_distance(at3(pa, ua, t), at3(pb, ub, t), at3(pc, uc, t), at3(pd, ud, t));
+      };
+      const double r = advance(dist, lc, P.gap_abs, P.max_iterations, P.close_factor, P.lo, horizon(P), tally);
+      if (r >= 0.0) atomicMin(P.best, (unsigned long long)__double_as_longlong(r));
+    });
+    if (!ok) atomicExch(P.overflow, 1);
+  }
+  flush_tally(P, tally);
+}
+
+// best = +inf (no contact), the four counters = 0
+__global__ void reset_kernel(unsigned long long *best, unsigned long long *tally) {
+  if (threadIdx.x == 0) *best = 0x7FF0000000000000ull;
+  if (threadIdx.x < 4) tally[threadIdx.x] = 0;
+}
+
+inline unsigned blocks(long long n, int t) { return (unsigned)((n + t - 1) / t); }
+
+// A box tree's device storage, rebuilt per window.
+struct TreeBufs {
+  int n = 0;
+  DevBuf<DBox> box, sbox, levels;
+  DevBuf<uint32_t> key, key_sorted, idx, order;
+  DevBuf<int> lvl_off, lvl_len;
+  std::vector<int> off, len;
+  void init(int n_, cudaStream_t s) {
+    n = n_;
+    box.alloc(n), sbox.alloc(n), key.alloc(n), key_sorted.alloc(n), idx.alloc(n), order.alloc(n);
+    off.clear(), len.clear();
+    int total = 0, m = (n + 7) / 8;
+    for (;;) {
+      off.push_back(total), len.push_back(m);
+      total += m;
+      if (m <= 1) break;
+      m = (m + 1) / 2;
+    }
+    if (off.size() > 62) fail(RS_INTERNAL, "Internal", "ccd", "box tree deeper than 62 levels");
+    levels.alloc(total);
+    lvl_off.upload(off, s), lvl_len.upload(len, s);
+  }
+  Tree view() const {
+    return Tree{sbox.p, order.p, levels.p, lvl_off.p, lvl_len.p, n, (int)off.size(), 8};
+  }
+};
+
+}  // namespace
+}  // namespace rsg
+
+using namespace rsg;
+
+struct rs_ccd {
+  rs_ctx *ctx = nullptr;
+  int nv = 0, nf = 0, ne = 0;
+  std::vector<uint32_t> edges_h;  // sorted (min, max) pairs: the Surface's edge order
+  DevBuf<uint32_t> faces, edges;
+  DevBuf<double3> start, vel;
+  DevBuf<double> speed;
+  DevBuf<DBox> vbox;
+  TreeBufs ft, et;
+  DevBuf<unsigned char> cub_tmp;
+  DevBuf<unsigned long long> scratch;  // best, 4 tally counters, overflow flag
+  double last_seconds = 0.0;
+};
+
+extern "C" {
+
+rs_ccd_options rs_ccd_options_default(void) {
+  rs_ccd_options o;
+  o.gap = 0.05;
+  o.reference_length = 0.0;
+  o.max_iterations = 100;
+  o.close_factor = 0.5;
+  return o;
+}
+
+int rs_ccd_create(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, rs_ccd **out) {
+  *out = nullptr;
+  return guard([&] {
+    if (nv <= 0 || nf <= 0) fail(RS_INVALID_OPTION, "InvalidOption", "ccd", "a surface has vertices and faces");
+    ctx->use();
+    cudaStream_t s = ctx->stream;
+    auto c = std::make_unique<rs_ccd>();
+    c->ctx = ctx;
+    c->nv = nv, c->nf = nf;
+    std::vector<std::pair<uint32_t, uint32_t>> e;
+    e.reserve(3 * (size_t)nf);
+    for (int f = 0; f < nf; ++f)
+      for (int k = 0; k < 3; ++k) {
+        const uint32_t a = faces[3 * f + k], b = faces[3 * f + (k + 1) % 3];
+        if (a >= (uint32_t)nv || b >= (uint32_t)nv)
+          fail(RS_INVALID_OPTION, "InvalidOption", "ccd", "face index out of range");
+        e.push_back({std::min(a, b), std::max(a, b)});
+      }
+    std::sort(e.begin(), e.end());
+    e.erase(std::unique(e.begin(), e.end()), e.end());
+    c->ne = (int)e.size();
+    c->edges_h.resize(2 * e.size());
+    for (size_t i = 0; i < e.size(); ++i) c->edges_h[2 * i] = e[i].first, c->edges_h[2 * i + 1] = e[i].second;
+    c->faces.upload(faces, 3 * (size_t)nf, s);
+    c->edges.upload(c->edges_h, s);
+    c->start.alloc(nv), c->vel.alloc(nv), c->speed.alloc(nv), c->vbox.alloc(nv);
+    c->ft.init(nf, s), c->et.init(c->ne, s);
+    size_t t1 = 0, t2 = 0;
+    RSG_CUDA("ccd", cub::DeviceRadixSort::SortPairs(nullptr, t1, c->ft.key.p, c->ft.key_sorted.p, c->ft.idx.p,
+                                                    c->ft.order.p, nf, 0, 30, s));
+    RSG_CUDA("ccd", cub::DeviceRadixSort::SortPairs(nullptr, t2, c->et.key.p, c->et.key_sorted.p, c->et.idx.p,
+                                                    c->et.order.p, c->ne, 0, 30, s));
+    c->cub_tmp.alloc(std::max<size_t>(std::max(t1, t2), 16));
+    c->scratch.alloc(8);
+    RSG_CUDA("ccd", cudaStreamSynchronize(s));
+    ctx_retain(ctx);
+    *out = c.release();
+  });
+}
+
+void rs_ccd_free(rs_ccd *c) {
+  if (!c) return;
+  rs_ctx *ctx = c->ctx;
+  delete c;
+  ctx_release(ctx);
+}
+
+int rs_ccd_first_contact(rs_ccd *c, const double *start, const double *velocity, double tau_end,
+                         const rs_ccd_options *opts, double *tau_max, int64_t *report6) {
+  return guard([&] {
+    auto t_begin = std::chrono::steady_clock::now();
+    const rs_ccd_options o = opts ? *opts : rs_ccd_options_default();
+    // CcdOptions::validate (ccd.rs:126-153) and first_contact's checks (ccd.rs:820-835)
+    if (!(std::isfinite(o.gap) && o.gap > 0.0))
+      fail(RS_INVALID_OPTION, "InvalidOption", "ccd", "ccd.gap must be finite and positive");
+    if (!(std::isfinite(o.reference_length) && o.reference_length >= 0.0))
+      fail(RS_INVALID_OPTION, "InvalidOption", "ccd",
+           "ccd.reference_length must be finite and positive (0: the mean edge length of start)");
+    if (o.max_iterations < 1) fail(RS_INVALID_OPTION, "InvalidOption", "ccd", "ccd.max_iterations must be at least 1");
+    if (!(o.close_factor >= 0.0 && o.close_factor < 1.0))
+      fail(RS_INVALID_OPTION, "InvalidOption", "ccd", "ccd.close_factor must be in [0, 1)");
+    if (!(std::isfinite(tau_end) && tau_end >= 0.0))
+      fail(RS_INVALID_OPTION, "InvalidOption", "ccd", "tau_end must be finite and non-negative");
+    const int nv = c->nv;
+    for (size_t i = 0; i < 3 * (size_t)nv; ++i) {
+      if (!std::isfinite(start[i])) fail(RS_INVALID_OPTION, "InvalidOption", "ccd", "positions must be finite");
+      if (!std::isfinite(velocity[i]))
+        fail(RS_INVALID_OPTION, "InvalidOption", "ccd", "velocity must have finite components");
+    }
+    rs_ctx *ctx = c->ctx;
+    ctx->use();
+    cudaStream_t s = ctx->stream;
+    // host scalars, in the reference's order: the mean edge length over the sorted edges,
+    // the largest speed, the box bounds of the sweep (these only place the Morton grid)
+    double sum = 0.0;
+    for (int i = 0; i < c->ne; ++i) {
+      const double *x = start + 3 * (size_t)c->edges_h[2 * i], *y = start + 3 * (size_t)c->edges_h[2 * i + 1];
+      const double d0 = x[0] - y[0], d1 = x[1] - y[1], d2 = x[2] - y[2];
+      sum += std::sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+    }
+    const double mel = sum / (double)c->ne;
+    const double ell = o.reference_length > 0.0 ? o.reference_length : mel;
+    const double gap_abs = o.gap * ell;
+    double vmax = 0.0;
+    double blo[3] = {INFINITY, INFINITY, INFINITY}, bhi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int v = 0; v < nv; ++v) {
+      const double *u = velocity + 3 * (size_t)v, *p = start + 3 * (size_t)v;
+      vmax = std::fmax(vmax, std::sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]));
+      for (int k = 0; k < 3; ++k) blo[k] = std::fmin(blo[k], p[k]), bhi[k] = std::fmax(bhi[k], p[k]);
+    }
+    const double t1 = vmax > 0.0 ? mel / vmax : INFINITY;
+    c->start.upload(reinterpret_cast<const double3 *>(start), nv, s);
+    c->vel.upload(reinterpret_cast<const double3 *>(velocity), nv, s);
+    speed_kernel<<<blocks(nv, 256), 256, 0, s>>>(nv, c->vel.p, c->speed.p);
+    RSG_LAUNCHED(ctx, "ccd speed");
+    const double h = 0.5 * gap_abs * (1.0 + 1e-6);
+    unsigned long long *best = c->scratch.p, *tally = c->scratch.p + 1;
+    int *overflow = reinterpret_cast<int *>(c->scratch.p + 5);
+    RSG_CUDA("ccd", cudaMemsetAsync(c->scratch.p, 0, 8 * sizeof(unsigned long long), s));
+    unsigned long long tally_h[4] = {0, 0, 0, 0};
+    int64_t windows = 0, pairs_total = 0, close = 0, touching = 0, evals = 0, contact = 0;
+    double tau = tau_end, lo = 0.0, hi = std::fmin(t1, tau_end);
+    const unsigned long long kInf = 0x7FF0000000000000ull;
+    for (;;) {
+      if (vmax == 0.0) hi = 0.0;
+      windows += 1;
+      reset_kernel<<<1, 32, 0, s>>>(best, tally);
+      RSG_LAUNCHED(ctx, "ccd reset");
+      vbox_kernel<<<blocks(nv, 256), 256, 0, s>>>(nv, c->start.p, c->vel.p, lo, hi, c->vbox.p);
+      RSG_LAUNCHED(ctx, "ccd boxes");
+      // the Morton grid spans the sweep of the window (any grid gives the same pairs)
+      double3 gl, gs;
+      {
+        const double ext = vmax * hi + h;
+        double l3[3], s3[3];
+        for (int k = 0; k < 3; ++k) {
+          l3[k] = blo[k] - ext;
+          const double w = (bhi[k] + ext) - l3[k];
+          s3[k] = w > 0.0 ? 1023.0 / w : 0.0;
+        }
+        gl = make_double3(l3[0], l3[1], l3[2]);
+        gs = make_double3(s3[0], s3[1], s3[2]);
+      }
+      for (int kind = 0; kind < 2; ++kind) {
+        TreeBufs &T = kind == 0 ? c->ft : c->et;
+        const int n = T.n;
+        if (kind == 0)
+          prim_box_kernel<3><<<blocks(n, 256), 256, 0, s>>>(n, c->faces.p, c->vbox.p, h, gl, gs, T.box.p, T.key.p,
+                                                            T.idx.p);
+        else
+          prim_box_kernel<2><<<blocks(n, 256), 256, 0, s>>>(n, c->edges.p, c->vbox.p, h, gl, gs, T.box.p, T.key.p,
+                                                            T.idx.p);
+        RSG_LAUNCHED(ctx, "ccd primitive boxes");
+        size_t tb = c->cub_tmp.n;
+        RSG_CUDA("ccd", cub::DeviceRadixSort::SortPairs(c->cub_tmp.p, tb, T.key.p, T.key_sorted.p, T.idx.p,
+                                                        T.order.p, n, 0, 30, s));
+        ctx->launches++;
+        gather_boxes_kernel<<<blocks(n, 256), 256, 0, s>>>(n, T.order.p, T.box.p, T.sbox.p);
+        RSG_LAUNCHED(ctx, "ccd gather");
+        for (size_t k = 0; k < T.off.size(); ++k) {
+          const DBox *in = k == 0 ? T.sbox.p : T.levels.p + T.off[k - 1];
+          const int n_in = k == 0 ? n : T.len[k - 1];
+          level_kernel<<<blocks(T.len[k], 128), 128, 0, s>>>(T.len[k], in, n_in, k == 0 ? 8 : 2, T.levels.p + T.off[k]);
+          RSG_LAUNCHED(ctx, "ccd tree level");
+        }
+      }
+      Params P{c->start.p, c->vel.p, c->speed.p, c->faces.p, c->edges.p, c->vbox.p, c->et.box.p,
+               nv, c->ne, o.max_iterations, gap_abs, o.close_factor, h, lo, hi, best, tally, overflow};
+      vt_kernel<<<blocks(nv, 128), 128, 0, s>>>(P, c->ft.view());
+      RSG_LAUNCHED(ctx, "ccd vertex-triangle");
+      ee_kernel<<<blocks(c->ne, 128), 128, 0, s>>>(P, c->et.view());
+      RSG_LAUNCHED(ctx, "ccd edge-edge");
+      unsigned long long res[8];
+      c->scratch.download(res, 8, s);
+      RSG_CUDA("ccd", cudaStreamSynchronize(s));
+      if (reinterpret_cast<int *>(res + 5)[0]) fail(RS_INTERNAL, "Internal", "ccd", "box tree stack overflow");
+      for (int k = 0; k < 4; ++k) tally_h[k] = res[1 + k];
+      pairs_total += (int64_t)tally_h[0];
+      evals += (int64_t)tally_h[3];
+      if (lo == 0.0) close = (int64_t)tally_h[1], touching = (int64_t)tally_h[2];
+      if (res[0] != kInf) {
+        double b;
+        std::memcpy(&b, &res[0], sizeof(b));
+        tau = b;
+        contact = 1;
+        break;
+      }
+      if (hi >= tau_end || vmax == 0.0) break;
+      lo = hi;
+      hi = std::fmin(std::fmax(2.0 * hi, hi + t1), tau_end);
+      if (hi <= lo) break;
+    }
+    *tau_max = tau;
+    if (report6) {
+      report6[0] = contact, report6[1] = windows, report6[2] = pairs_total;
+      report6[3] = close, report6[4] = touching, report6[5] = evals;
+    }
+    c->last_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_begin).count();
+  });
+}
+
+int rs_ccd_last_seconds(rs_ccd *c, double *seconds) {
+  return guard([&] { *seconds = c->last_seconds; });
+}
+
+}  // extern "C"

@@ -150,6 +150,8 @@ struct rs_flow {
   rs_learned *lmodel = nullptr;
   int l_cheap = 2, l_cap = 0;
   int iteration = 0;
+  rs_ccd *ccd = nullptr;  // the surface's topology for the collision cap (ccd on)
+  ~rs_flow() { rs_ccd_free(ccd); }
 };
 
 extern "C" {
@@ -168,6 +170,10 @@ rs_flow_options rs_flow_options_default(void) {
   o.armijo_c = 1e-2;
   o.max_halvings = 30;
   o.newton_max = 5;
+  o.ccd = 0;
+  o.ccd_gap = 0.05;
+  o.ccd_max_iterations = 100;
+  o.ccd_close_factor = 0.5;
   return o;
 }
 
@@ -187,6 +193,7 @@ int rs_flow_create(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const dou
     F->area0 = total_area(nf, faces, positions_host);
     F->vol0 = total_volume(nf, faces, positions_host);
     barycenter(nv, nf, faces, positions_host, F->bary0);
+    if (F->o.ccd) check(rs_ccd_create(ctx, nv, nf, faces, &F->ccd), "flow (ccd)");
     ctx_retain(ctx);
     *out = F.release();
   });
@@ -403,6 +410,22 @@ int rs_flow_step(rs_flow *F, double *report) {
     // 4. Armijo backtracking on the frozen lists
     t = clk::now();
     double tau = F->last_tau > 0.0 ? 2.0 * F->last_tau : F->l0 / maxdisp;
+    // the collision cap (session.rs:927-955): the largest safe time of x - t d, two thirds of it
+    rep[27] = NAN;
+    if (F->ccd && std::isfinite(tau) && tau > 0.0) {
+      auto tc = clk::now();
+      std::vector<double> vel(nd);
+      for (size_t r = 0; r < nd; ++r) vel[r] = -x[r];
+      rs_ccd_options co = rs_ccd_options_default();
+      co.gap = F->o.ccd_gap, co.reference_length = F->l0;
+      co.max_iterations = F->o.ccd_max_iterations, co.close_factor = F->o.ccd_close_factor;
+      double tmax = 0.0;
+      int64_t cr[6] = {0, 0, 0, 0, 0, 0};
+      check(rs_ccd_first_contact(F->ccd, F->pos.data(), vel.data(), tau, &co, &tmax, cr), "flow (ccd)");
+      if (cr[0]) tau = std::min(tau, 2.0 / 3.0 * tmax);
+      rep[27] = tmax;
+      rep[28] = since(tc);
+    }
     rep[22] = tau;
     rep[23] = xinf;
     const double tau_min = 1e-12 * F->l0 / xinf;

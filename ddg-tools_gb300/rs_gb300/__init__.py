@@ -50,7 +50,16 @@ class FlowOptions(C.Structure):
     _fields_ = [("alpha", C.c_double), ("beta", C.c_double), ("theta", C.c_double),
                 ("leaf_size", C.c_int), ("solver", SolverOptions), ("hold_area", C.c_int),
                 ("hold_volume", C.c_int), ("armijo_c", C.c_double), ("max_halvings", C.c_int),
-                ("newton_max", C.c_int)]
+                ("newton_max", C.c_int), ("ccd", C.c_int), ("ccd_gap", C.c_double),
+                ("ccd_max_iterations", C.c_int), ("ccd_close_factor", C.c_double)]
+
+
+class CcdOptions(C.Structure):
+    """rs_ccd_options of include/rsgpu.h (CcdOptions, RS/src/ccd.rs:86-111): gap 0.05 of the
+    reference length (0: the mean edge length of the start), 100 advances, close factor 0.5."""
+
+    _fields_ = [("gap", C.c_double), ("reference_length", C.c_double), ("max_iterations", C.c_int),
+                ("close_factor", C.c_double)]
 
 
 class RsError(RuntimeError):
@@ -78,6 +87,9 @@ def load_library(path: str | os.PathLike | None = None):
         getattr(L, name).restype = C.c_char_p
     sig = {
         "rs_device_count": [C.POINTER(C.c_int)],
+        "rs_ccd_create": [_vp, C.c_int, C.c_int, _u32p, C.POINTER(_vp)],
+        "rs_ccd_first_contact": [_vp, _f64p, _f64p, C.c_double, C.POINTER(CcdOptions), _dp, _i64p],
+        "rs_ccd_last_seconds": [_vp, _dp],
         "rs_device_info": [C.c_int, C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                            C.POINTER(C.c_uint64)],
         "rs_ctx_create": [C.c_int, C.POINTER(_vp)],
@@ -164,6 +176,10 @@ def load_library(path: str | os.PathLike | None = None):
     L.rs_flow_options_default.argtypes = []
     L.rs_flow_free.argtypes = [_vp]
     L.rs_flow_free.restype = None
+    L.rs_ccd_options_default.restype = CcdOptions
+    L.rs_ccd_options_default.argtypes = []
+    L.rs_ccd_free.argtypes = [_vp]
+    L.rs_ccd_free.restype = None
     for name in ("rs_learned_free", "rs_lgraph_free"):
         getattr(L, name).argtypes = [_vp]
         getattr(L, name).restype = None
@@ -686,7 +702,7 @@ FLOW_REPORT_KEYS = ["energy_before", "energy_after", "tau", "halvings", "gmres_a
                     "seconds_solver_build", "seconds_solve", "seconds_line_search", "seconds_projection",
                     "accepted", "slope", "constraint_residual", "fallbacks", "learned_solves",
                     "learned_fallbacks", "gradient_norm", "tau0", "direction_max", "newton_steps",
-                    "projection_max_rounds", "energy_trial"]
+                    "projection_max_rounds", "energy_trial", "tau_ccd", "seconds_ccd"]
 
 
 class Flow:
@@ -721,6 +737,52 @@ class Flow:
         out = np.empty((self.n_vertices, 3))
         _check(_lib.rs_flow_positions(self._h, out.ravel()))
         return out
+
+
+def ccd_options(**kw) -> CcdOptions:
+    """The library defaults (rs_ccd_options_default) with the given fields replaced."""
+    o = load_library().rs_ccd_options_default()
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class CcdSurface:
+    """Continuous collision detection of one surface against itself (first_contact,
+    RS/src/ccd.rs:762-884, without obstacles and without the exempt band): the topology lives
+    on the device, each ``first_contact`` call sweeps one linear motion."""
+
+    REPORT_KEYS = ["contact", "windows", "pairs_tested", "close_pairs", "touching_pairs", "evaluations"]
+
+    def __init__(self, faces, n_vertices: int, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        faces = np.ascontiguousarray(faces, dtype=np.uint32).reshape(-1, 3)
+        self.n_vertices = int(n_vertices)
+        h = _vp()
+        _check(_lib.rs_ccd_create(self.ctx.handle, self.n_vertices, len(faces), faces.ravel(), C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.rs_ccd_free(self._h)
+            self._h = None
+
+    def first_contact(self, start, velocity, tau_end: float, options: CcdOptions | None = None) -> dict:
+        start = np.ascontiguousarray(start, dtype=np.float64).reshape(-1, 3)
+        vel = np.ascontiguousarray(velocity, dtype=np.float64).reshape(-1, 3)
+        if len(start) != self.n_vertices or len(vel) != self.n_vertices:
+            raise RsError(1, "InvalidOption", "ccd", "start and velocity need one vector per vertex")
+        o = options or ccd_options()
+        tau = C.c_double()
+        rep = np.zeros(6, np.int64)
+        _check(_lib.rs_ccd_first_contact(self._h, start.ravel(), vel.ravel(), float(tau_end), C.byref(o),
+                                         C.byref(tau), rep))
+        return {"tau_max": tau.value, **{k: int(v) for k, v in zip(self.REPORT_KEYS, rep)}}
+
+    def last_seconds(self) -> float:
+        t = C.c_double()
+        _check(_lib.rs_ccd_last_seconds(self._h, C.byref(t)))
+        return t.value
 
 
 def copy_counters() -> tuple[int, int]:

@@ -21,6 +21,9 @@ BUILD = ROOT / "_build"
 INCLUDE = ROOT.parent / "include"
 LIB = PKG / "librsgpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Device code that must round like the reference's FP64 host code, operation for operation:
+# no multiply-add contraction.
+NO_FMAD = {"ccd.cu"}
 
 
 def _cuda_home() -> Path:
@@ -57,6 +60,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
         if src.suffix == ".cu":
             cmd = [nvcc, *ARCH, "-lineinfo", *common, "-Xcompiler", "-fPIC",
                    "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr",
+                   *(["-fmad=false"] if src.name in NO_FMAD else []),
                    "-c", str(src), "-o", str(obj)]
         else:
             cmd = [os.environ.get("CXX", "g++"), *common, "-fPIC", "-ffp-contract=off",

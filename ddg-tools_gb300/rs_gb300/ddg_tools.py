@@ -14,9 +14,10 @@ Positions are any buffer or (nested) sequence of 3 reals per vertex, faces 3 ind
 results are ``array('d')`` / ``array('i')``. Every option name of the reference is known. The
 values this library runs are the GPU hot path of one Hs step: the tangent-point energy
 (Barnes-Hut or exact), the Sobolev metric with the hierarchical solver and right-preconditioned
-GMRES, projected gradient descent with the standard Armijo line search, and the barycenter,
-total-area and total-volume constraints held at their initial values. A value outside that path
-(remeshing, collision detection, penalties, obstacles, pins, schedules, the other energies,
+GMRES, projected gradient descent with the standard Armijo line search and its continuous
+collision detection cap, and the barycenter, total-area and total-volume constraints held at
+their initial values. A value outside that path (remeshing, penalties, obstacles, pins,
+schedules, the other energies,
 metrics, back ends and methods, ``device="cpu"``) raises ``RepulsiveSurfaceInputError`` naming
 the option, as the reference does for a value outside an option's domain. There is no CPU
 fallback.
@@ -77,7 +78,7 @@ REMESH_OPS = ["split", "collapse", "flip", "smooth"]
 # Every option of the reference (OPTION_NAMES, crates/ddg-py/src/repulsive_surfaces.rs:684-753)
 # with this library's default. The defaults equal the reference's except where the reference's
 # default is outside the GPU path: device "cuda" (reference "cpu"), backend "hierarchical"
-# (reference "auto", dense below 1000 faces), ccd False and remesh False (reference True).
+# (reference "auto", dense below 1000 faces) and remesh False (reference True).
 _DEFAULTS = {
     "alpha": 6.0, "beta": 12.0, "energy": "tangent_point", "coulomb_alpha": None, "tp_weight": 1.0,
     "metric": "sobolev", "low_order": True, "l2_kind": "mass", "backend": "hierarchical",
@@ -89,7 +90,7 @@ _DEFAULTS = {
     "pins": None, "pin_targets": None, "pin_move": None, "pin_move_steps": None,
     "schedule_timing": "before_projection", "penalties": None, "ccd_obstacles": None,
     "armijo": "standard", "armijo_c": 1e-2, "start": "grow_previous", "start_lengths": 1.0,
-    "start_factor": 2.0, "start_tau": None, "tau_min_rel": 1e-12, "max_halvings": None, "ccd": False,
+    "start_factor": 2.0, "start_tau": None, "tau_min_rel": 1e-12, "max_halvings": None, "ccd": True,
     "ccd_gap": 0.05, "ccd_max_iterations": 100, "ccd_close_factor": 0.5, "newton_steps": None,
     "newton_max": 5, "remesh": False, "remesh_split": 1.5, "remesh_collapse": 0.5, "remesh_rounds": 5,
     "remesh_rho": 0.5, "remesh_flip_cap": 100, "remesh_order": "flip_then_smooth",
@@ -103,7 +104,7 @@ OPTION_NAMES = tuple(_DEFAULTS)
 _FIXED = {
     "energy": "tangent_point", "metric": "sobolev", "gmres_side": "right", "method": "projected_gradient",
     "barycenter_shift": False, "armijo": "standard", "start": "grow_previous", "start_lengths": 1.0,
-    "start_factor": 2.0, "tau_min_rel": 1e-12, "ccd": False, "remesh": False, "reference_compat": False,
+    "start_factor": 2.0, "tau_min_rel": 1e-12, "remesh": False, "reference_compat": False,
 }
 _ABSENT = ("pins", "pin_targets", "pin_move", "pin_move_steps", "penalties", "ccd_obstacles",
            "newton_steps", "start_tau")
@@ -219,6 +220,13 @@ class _Options:
             raise _bad("barycenter_mode", f"'per_component' {_OFF_PATH}: the global barycenter is held")
         if o["barycenter"] is False:
             raise _bad("barycenter", f"False {_OFF_PATH}: the global barycenter is always held")
+        if o["ccd"]:
+            if not (o["ccd_gap"] > 0):
+                raise _bad("ccd_gap", f"{o['ccd_gap']} must be finite and positive")
+            if o["ccd_max_iterations"] < 1:
+                raise _bad("ccd_max_iterations", "must be at least 1")
+            if not (0.0 <= o["ccd_close_factor"] < 1.0):
+                raise _bad("ccd_close_factor", f"{o['ccd_close_factor']} must be in [0, 1)")
         if o["time_limit"] is not None and o["time_limit"] < 0:
             raise _bad("time_limit", f"{o['time_limit']} must be finite and >= 0 seconds")
         if not (o["tp_weight"] > 0):
@@ -264,7 +272,8 @@ class _Options:
                           leaf_size=o["leaf_size"], hold_area=int(self.hold_area),
                           hold_volume=int(self.hold_volume), armijo_c=o["armijo_c"],
                           max_halvings=10_000 if o["max_halvings"] is None else o["max_halvings"],
-                          newton_max=o["newton_max"])
+                          newton_max=o["newton_max"], ccd=int(o["ccd"]), ccd_gap=o["ccd_gap"],
+                          ccd_max_iterations=o["ccd_max_iterations"], ccd_close_factor=o["ccd_close_factor"])
         s = fo.solver
         s.chi, s.leaf_size = o["chi"], o["cluster_leaf_size"]
         s.restart, s.tolerance, s.max_iterations = o["gmres_restart"], o["gmres_tolerance"], o["gmres_max_iterations"]
@@ -387,7 +396,9 @@ class RepulsiveSurfaceSession:
     Each step is ``rs_flow_step`` on the GPU: Barnes-Hut energy and differential, the
     hierarchical Hs solve, the Armijo line search on frozen lists and the projection. The
     session adds the reference's outer loop: stop rules, ``stuck_limit``, ``max_iterations``,
-    ``time_limit``, ``cancel`` and ``reset``. ``step`` and ``run`` release the GIL inside the
+    ``time_limit``, ``cancel`` and ``reset``. With ``ccd`` (the default) the first trial of the
+    line search is capped at two thirds of the first contact time of the motion
+    (RS/src/ccd.rs:762-884, on the GPU). ``step`` and ``run`` release the GIL inside the
     library; ``snapshot`` and the getters never wait for a running step; ``cancel`` is safe from
     any thread and takes effect before the next step (a step in progress completes). There is
     no remeshing: the faces, ``face_origin`` (the identity) and ``pinned`` (empty) never change.
@@ -532,7 +543,7 @@ class RepulsiveSurfaceSession:
             "energy_before": r["energy_before"], "energy_after": r["energy_after"],
             "tangent_point_after": r["energy_after"], "penalties_after": [],
             "gradient_norm": r["gradient_norm"], "sobolev_norm_sq": slope,
-            "tau": r["tau"], "tau0": r["tau0"], "tau_ccd": None,
+            "tau": r["tau"], "tau0": r["tau0"], "tau_ccd": None if math.isnan(r["tau_ccd"]) else r["tau_ccd"],
             "halvings": int(r["halvings"]), "newton_steps": int(r["newton_steps"]),
             "projection": "maxrounds" if r["projection_max_rounds"] > 0 else "converged",
             "max_violation": r["constraint_residual"], "dropped_rows": [],
@@ -541,7 +552,7 @@ class RepulsiveSurfaceSession:
             "remesh": None,
             "seconds": {"bvh": r["seconds_tree"], "energy": r["seconds_energy"],
                         "factor": r["seconds_solver_build"], "solve": r["seconds_solve"],
-                        "line_search": r["seconds_line_search"], "ccd": 0.0,
+                        "line_search": r["seconds_line_search"], "ccd": r["seconds_ccd"],
                         "projection": r["seconds_projection"], "remesh": 0.0, "total": r["seconds"]},
         }
         with self._snap_lock:

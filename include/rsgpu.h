@@ -308,6 +308,10 @@ typedef struct rs_flow_options {
   double armijo_c;           /* ArmijoRule::Standard c (1e-2) */
   int max_halvings;          /* line-search halvings before a step is refused (30) */
   int newton_max;            /* NewtonSteps::UntilTolerance max (5) */
+  int ccd;                   /* cap the first trial by continuous collision detection (0) */
+  double ccd_gap;            /* CcdOptions: gap relative to the initial mean edge length (0.05), */
+  int ccd_max_iterations;    /* advances per pair and window (100), */
+  double ccd_close_factor;   /* closing fraction of pairs closer than the gap (0.5) */
 } rs_flow_options;
 
 rs_flow_options rs_flow_options_default(void);
@@ -354,7 +358,37 @@ int rs_solver_set_learned(rs_solver *s, rs_learned *model, rs_lgraph *graph, int
 /* Learned solves and how many of them fell back to the plain preconditioner. */
 int rs_solver_learned_counts(rs_solver *s, int64_t *solves, int64_t *fallbacks);
 
-#define RS_FLOW_REPORT_LEN 27
+/* ---- Continuous collision detection (RS/src/ccd.rs) ---------------------------------- */
+
+typedef struct rs_ccd rs_ccd;
+/* CcdOptions (RS/src/ccd.rs:86-111): gap relative to the reference length (0.05), the
+ * reference length (0: the mean edge length of the start positions), advances per pair and
+ * window (100), the fraction of its initial distance a pair closer than the gap may close to
+ * (0.5). The broad-phase leaf size is 8. */
+typedef struct rs_ccd_options {
+  double gap;
+  double reference_length;
+  int max_iterations;
+  double close_factor;
+} rs_ccd_options;
+rs_ccd_options rs_ccd_options_default(void);
+/* The surface's topology (faces, its sorted edge list) on the device, for repeated queries. */
+int rs_ccd_create(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, rs_ccd **out);
+void rs_ccd_free(rs_ccd *c);
+/* first_contact (RS/src/ccd.rs:762-884) of the mesh moving as start + t velocity (host arrays,
+ * V x 3) on [0, tau_end], against itself: the largest tau_max <= tau_end that keeps every
+ * vertex-triangle pair (vertex not in the triangle) and every edge-edge pair without a common
+ * vertex at distance >= gap (pairs closer at t = 0: >= close_factor times their distance;
+ * touching pairs unconstrained). No obstacles and no exempt band of self-intersecting inputs.
+ * tau_max is bitwise the crate's. report6 (may be NULL): contact found (0/1), windows,
+ * candidate pairs tested, close pairs, touching pairs, distance evaluations (the last
+ * depends on the order pairs are met and is not the crate's count). */
+int rs_ccd_first_contact(rs_ccd *c, const double *start, const double *velocity, double tau_end,
+                         const rs_ccd_options *o, double *tau_max, int64_t *report6);
+/* Wall seconds of the last rs_ccd_first_contact. No counterpart in the crate. */
+int rs_ccd_last_seconds(rs_ccd *c, double *seconds);
+
+#define RS_FLOW_REPORT_LEN 29
 /* Session::step (session.rs:724-747): one step. report[RS_FLOW_REPORT_LEN]:
  *  0 energy before, 1 energy after the projection (on the step's lists; the energy before
  *  when refused), 2 accepted tau (0: refused), 3 halvings,
@@ -366,10 +400,15 @@ int rs_solver_learned_counts(rs_solver *s, int64_t *solves, int64_t *fallbacks);
  *     ended above the divergence threshold (RobustHierarchical, direction.rs:269-379),
  *  19 learned-preconditioner solves, 20 of them repeated with the plain preconditioner,
  *  21 gradient norm |dE|_2 over the 3V coordinates (StepReport::gradient_norm, session.rs:161-162),
- *  22 the first trial's step size (tau0), 23 |x|_inf, the largest coordinate of the direction,
+ *  22 the first trial's step size (tau0, after the collision cap), 23 |x|_inf, the largest
+ *     coordinate of the direction,
  *  24 Newton rounds of the projection, 25 projection status (0 converged: every held row within
  *     1e-12 relative, or no held rows; 1 the rounds were used up: ProjectionStatus::MaxRounds,
- *     solve/schur.rs:450-461), 26 energy at the accepted trial, before the projection. */
+ *     solve/schur.rs:450-461), 26 energy at the accepted trial, before the projection,
+ *  27 tau_max of the collision detection (NaN when it is off), 28 its seconds.
+ * With ccd on, the first trial is min(tau0, 2/3 tau_max) when the motion x -> x - t d meets a
+ * contact before tau0 (session.rs:927-955; reference length the initial mean edge length).
+ * The exempt band of a self-intersecting start and the projection guard are not applied. */
 int rs_flow_step(rs_flow *f, double *report);
 /* The current positions (V x 3). */
 int rs_flow_positions(rs_flow *f, double *positions_host);

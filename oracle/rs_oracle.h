@@ -125,6 +125,17 @@ int rso_vfrac_stats(const rso_vfrac *h, int64_t *out5);
 /* y = L^V_tau x = 2 (a . H~a . x - a . H~(a . x)) per axis (hierarchical.rs:1313-1345). */
 int rso_vfrac_apply(const rso_vfrac *h, int nb, const double *xs, double *ys);
 
+/* first_contact of a mesh moving against itself, start + t velocity on [0, tau_end]
+ * (RS/src/ccd.rs:762-884; no obstacles, no exempt band). gap, max_iterations and close_factor
+ * are CcdOptions (ccd.rs:86-111); reference_length 0 takes the mean edge length of start.
+ * out5: contact found (0/1), windows, candidate pairs tested, close pairs, touching pairs. */
+int rso_ccd_first_contact(int nv, const double *start, int nf, const uint32_t *faces,
+                          const double *velocity, double tau_end, double gap, double reference_length,
+                          int max_iterations, double close_factor, double *tau_max, int64_t *out5);
+const char *rso_ccd_last_error(void);
+/* The smallest vertex-triangle / edge-edge distance over the pairs CCD constrains. */
+int rso_ccd_min_distance(int nv, const double *pos, int nf, const uint32_t *faces, double *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -293,3 +293,37 @@ class VertexFractionalTree:
         ys = np.empty_like(xs)
         _mcheck(_metric_lib().rso_vfrac_apply(self._h, len(xs), xs.ravel(), ys.ravel()))
         return ys.reshape(x.shape)
+
+
+def ccd_first_contact(faces, start, velocity, tau_end, gap=0.05, reference_length=0.0, max_iterations=100,
+                      close_factor=0.5) -> dict:
+    """first_contact of the mesh moving as start + t velocity on [0, tau_end], against itself
+    (RS/src/ccd.rs:762-884; no obstacles, no exempt band). reference_length 0: the mean edge
+    length of start."""
+    start, faces = _mesh(start, faces)
+    vel = np.ascontiguousarray(velocity, dtype=np.float64).reshape(-1, 3)
+    L = lib()
+    L.rso_ccd_first_contact.argtypes = [C.c_int, _f64p, C.c_int, _u32p, _f64p, C.c_double, C.c_double,
+                                        C.c_double, C.c_int, C.c_double, C.POINTER(C.c_double), _i64p]
+    L.rso_ccd_last_error.restype = C.c_char_p
+    tau = C.c_double()
+    out = np.zeros(5, np.int64)
+    code = L.rso_ccd_first_contact(len(start), start.ravel(), len(faces), faces.ravel(), vel.ravel(),
+                                   float(tau_end), float(gap), float(reference_length), int(max_iterations),
+                                   float(close_factor), C.byref(tau), out)
+    if code != 0:
+        raise OracleError(code, L.rso_ccd_last_error().decode())
+    keys = ["contact", "windows", "pairs_tested", "close_pairs", "touching_pairs"]
+    return {"tau_max": tau.value, **{k: int(v) for k, v in zip(keys, out)}}
+
+
+def ccd_min_distance(pos, faces) -> float:
+    """The smallest distance over the vertex-triangle and edge-edge pairs CCD constrains."""
+    pos, faces = _mesh(pos, faces)
+    L = lib()
+    L.rso_ccd_min_distance.argtypes = [C.c_int, _f64p, C.c_int, _u32p, C.POINTER(C.c_double)]
+    d = C.c_double()
+    code = L.rso_ccd_min_distance(len(pos), pos.ravel(), len(faces), faces.ravel(), C.byref(d))
+    if code != 0:
+        raise OracleError(code, L.rso_ccd_last_error().decode())
+    return d.value

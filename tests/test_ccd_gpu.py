@@ -1,0 +1,85 @@
+"""Continuous collision detection on the GPU against the oracle: tau_max bitwise, and the
+window, candidate-pair, close-pair and touching-pair counts equal, on the reference's
+known-answer scenes, seeded random soups, sphere pairs and a torus sweep over several windows
+(first_contact, RS/src/ccd.rs:762-884)."""
+import numpy as np
+import pytest
+
+import ccd_scenes as S
+import rs_gb300 as R
+import rs_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+KEYS = ("tau_max", "contact", "windows", "pairs_tested", "close_pairs", "touching_pairs")
+
+
+def _both(f, p, v, tau_end, ell, **kw):
+    o = O.ccd_first_contact(f, p, v, tau_end, reference_length=ell, **kw)
+    g = R.CcdSurface(f, len(p)).first_contact(p, v, tau_end, R.ccd_options(reference_length=ell, **kw))
+    return o, g
+
+
+def _same(o, g):
+    assert {k: g[k] for k in KEYS} == {k: o[k] for k in KEYS}, (o, g)
+
+
+@pytest.mark.parametrize("name", list(S.known_answer_scenes()))
+def test_known_answer_scenes_bitwise(name):
+    f, p, v, tau_end, ell, *_ = S.known_answer_scenes()[name]
+    _same(*_both(f, p, v, tau_end, ell))
+
+
+def test_random_soups_bitwise():
+    contacts = 0
+    for seed in range(40):
+        f, p, v, tau_end, ell = S.random_soup(1000 + seed)
+        o, g = _both(f, p, v, tau_end, ell)
+        _same(o, g)
+        contacts += o["contact"]
+    assert contacts >= 3
+
+
+def test_sphere_pairs_bitwise():
+    for seed in range(6):
+        _same(*_both(*S.sphere_pair(77 + seed, level=2)))
+
+
+@pytest.mark.parametrize("reach", [0.5, 3.0, 12.0])
+def test_torus_sweep_bitwise(reach):
+    f, p, v, tau_end, ell = S.torus_sweep(48, 24, reach=reach)
+    o, g = _both(f, p, v, tau_end, ell)
+    _same(o, g)
+    assert g["pairs_tested"] > 0 and g["evaluations"] >= g["pairs_tested"]
+
+
+def test_options_change_the_result_as_in_the_oracle():
+    f, p, v, tau_end, ell = S.torus_sweep(24, 12, reach=3.0)
+    for kw in ({"gap": 0.2}, {"max_iterations": 2}, {"close_factor": 0.0}):
+        _same(*_both(f, p, v, tau_end, ell, **kw))
+
+
+def test_repeated_calls_reuse_the_topology():
+    f, p, v, tau_end, ell = S.torus_sweep(24, 12, reach=3.0)
+    c = R.CcdSurface(f, len(p))
+    a = c.first_contact(p, v, tau_end)
+    b = c.first_contact(p, v, tau_end)
+    assert a == b
+    o = O.ccd_first_contact(f, p, v, tau_end)
+    assert a["tau_max"] == o["tau_max"]
+    assert c.last_seconds() > 0.0
+
+
+def test_errors_are_invalid_option():
+    f, p, v, *_ = S.known_answer_scenes()["stationary"]
+    c = R.CcdSurface(f, len(p))
+    for kw in ({"gap": 0.0}, {"max_iterations": 0}, {"close_factor": 1.0}, {"reference_length": -1.0}):
+        with pytest.raises(R.RsError) as e:
+            c.first_contact(p, v, 1.0, R.ccd_options(**kw))
+        assert e.value.kind == "InvalidOption"
+    bad = v.copy()
+    bad[2, 1] = np.nan
+    with pytest.raises(R.RsError):
+        c.first_contact(p, bad, 1.0)
+    with pytest.raises(R.RsError):
+        c.first_contact(p, v, -1.0)

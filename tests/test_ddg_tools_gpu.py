@@ -197,3 +197,21 @@ def test_bad_inputs_and_device_errors():
         D.RepulsiveSurfaceSession(P, bad)
     with pytest.raises(D.RepulsiveSurfaceInputError):
         D.surface_energy(P, bad)
+
+
+def test_collision_cap_in_the_flow():
+    """With ccd the first trial is min(tau0, 2/3 tau_max) when the motion meets a contact before
+    tau0, and unchanged otherwise (session.rs:927-955)."""
+    P, F = _torus()
+    a = D.RepulsiveSurfaceSession(P, F, ccd=False).step()
+    assert a["tau_ccd"] is None and a["seconds"]["ccd"] == 0.0
+    t0 = a["tau0"]
+    for gap in (0.05, 1.0, 3.0):
+        b = D.RepulsiveSurfaceSession(P, F, ccd=True, ccd_gap=gap).step()
+        assert b["tau_ccd"] is not None and b["tau_ccd"] <= t0
+        assert b["seconds"]["ccd"] > 0.0
+        if b["tau_ccd"] == t0:  # no contact before the first trial: nothing changes
+            assert b["tau0"] == t0 and b["energy_after"] == a["energy_after"]
+        else:
+            assert b["tau0"] == min(t0, 2.0 / 3.0 * b["tau_ccd"])
+        assert b["energy_after"] < b["energy_before"]

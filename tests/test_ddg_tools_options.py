@@ -38,8 +38,9 @@ def test_defaults_are_the_references_on_the_path():
     assert (d["gmres_restart"], d["gmres_tolerance"], d["gmres_max_iterations"]) == (60, 1e-3, 200)
     assert (d["armijo_c"], d["newton_max"], d["stop_relative"], d["stop_window"]) == (1e-2, 5, 1e-7, 10)
     assert (d["max_iterations"], d["stuck_limit"], d["tau_min_rel"]) == (1000, 5, 1e-12)
-    # the defaults that differ: the GPU path has no CPU device, remeshing or collision detection
-    assert (d["device"], d["backend"], d["remesh"], d["ccd"]) == ("cuda", "hierarchical", False, False)
+    # the defaults that differ: the GPU path has no CPU device and no remeshing
+    assert (d["device"], d["backend"], d["remesh"]) == ("cuda", "hierarchical", False)
+    assert (d["ccd"], d["ccd_gap"], d["ccd_max_iterations"], d["ccd_close_factor"]) == (True, 0.05, 100, 0.5)
 
 
 def _fields(st):
@@ -65,6 +66,11 @@ def test_options_map_onto_the_flow():
     s = f.solver
     assert (s.chi, s.leaf_size, s.restart, s.tolerance, s.max_iterations) == (0.25, 12, 30, 1e-6, 77)
     assert (s.tp_weight, s.low_order) == (2.0, 0)
+    assert (f.ccd, f.ccd_gap, f.ccd_max_iterations, f.ccd_close_factor) == (1, 0.05, 100, 0.5)
+    f = D._Options(dict(ccd=False)).flow_options()
+    assert f.ccd == 0
+    f = D._Options(dict(ccd_gap=0.1, ccd_max_iterations=7, ccd_close_factor=0.25)).flow_options()
+    assert (f.ccd_gap, f.ccd_max_iterations, f.ccd_close_factor) == (0.1, 7, 0.25)
     # exact evaluation is Barnes-Hut with theta 0 (no node is admissible)
     assert D._Options({"energy_eval": "exact", "theta": 0.7}).flow_options().theta == 0.0
     # no halving cap by default: the search stops at tau_min
@@ -85,6 +91,9 @@ def test_options_map_onto_the_flow():
     ({"remesh_ops": ["split", "twist"]}, "remesh_ops"),
     ({"time_limit": -1.0}, "time_limit"),
     ({"tp_weight": 0.0}, "tp_weight"),
+    ({"ccd_gap": 0.0}, "ccd_gap"),
+    ({"ccd_max_iterations": 0}, "ccd_max_iterations"),
+    ({"ccd_close_factor": 1.0}, "ccd_close_factor"),
     ({"theta": None}, "theta"),
 ])
 def test_bad_values_are_named(kw, name):
@@ -96,7 +105,6 @@ def test_bad_values_are_named(kw, name):
 
 @pytest.mark.parametrize("kw, name", [
     ({"remesh": True}, "remesh"),
-    ({"ccd": True}, "ccd"),
     ({"device": "cpu"}, "device"),
     ({"backend": "dense"}, "backend"),
     ({"method": "aqp"}, "method"),

@@ -564,6 +564,79 @@ def bench_matvec(args, rank, world, local):
     return 0
 
 
+def ccd_motion(P, F, reach=2.0, seed=5):
+    """A smooth seeded velocity field on the surface, scaled so that the fastest vertex moves
+    `reach` mean edge lengths by t = 1 (a line-search trial of the flow moves it one to two)."""
+    rng = np.random.default_rng(seed)
+    k = rng.normal(size=(4, 3))
+    ph = rng.uniform(0, 2 * np.pi, (4, 3))
+    vel = sum(np.sin(P @ k[i][:, None] * 2.0 + ph[i]) for i in range(4))
+    e = np.concatenate([F[:, [0, 1]], F[:, [1, 2]], F[:, [2, 0]]]).astype(np.int64)
+    e = np.unique(np.sort(e, axis=1), axis=0)
+    mel = np.linalg.norm(P[e[:, 0]] - P[e[:, 1]], axis=1).mean()
+    return np.ascontiguousarray(vel * (reach * mel / np.linalg.norm(vel, axis=1).max()))
+
+
+def bench_ccd(args, rank, world, local):
+    """Continuous collision detection of the 204,800-face torus against itself along a smooth
+    motion (rs_ccd_first_contact: host arrays in, tau_max out; one call per step)."""
+    import torch
+
+    import rs_gb300 as R
+
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    warmup = max(3, args.warmup)
+    P, F, _, desc = workload("flow")
+    V = ccd_motion(P, F)
+    ctx = R.Context(local)
+    c = R.CcdSurface(F, len(P), ctx)
+    for _ in range(warmup):
+        r = c.first_contact(P, V, 1.0)
+    if world > 1:
+        torch.distributed.barrier()
+    l0 = ctx.launch_count()
+    ms = []
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            r = c.first_contact(P, V, 1.0)
+            ms.append((time.perf_counter() - t0) * 1e3)
+    launches = ctx.launch_count() - l0
+    value, t_total = replica_rate(args.steps, sum(ms) / 1e3, world, torch.device(f"cuda:{local}"))
+    if world > 1:
+        torch.distributed.barrier()
+        if rank != 0:
+            torch.distributed.destroy_process_group()
+            return 0
+    line = {
+        "metric": "CCD first_contact calls/s @204,800 faces (self contacts, gap 0.05 of the mean edge)",
+        "value": value, "unit": "calls/s", "n_gpus": world, "steps": args.steps, "warmup": warmup,
+        "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded mesh generator and motion)",
+        "config": {"workload": f"ccd: {desc}; smooth seeded velocity, fastest vertex 2 mean edges by t = 1",
+                   "tau_end": 1.0, **{k: r[k] for k in ("tau_max", "contact", "windows", "pairs_tested",
+                                                      "close_pairs", "touching_pairs", "evaluations")},
+                   "l2": "inputs uploaded from the host in every call",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": value, "unit": "calls/s", "h2d_bytes_per_step": int(P.nbytes + V.nbytes),
+                "d2h_bytes_per_step": 64 * int(r["windows"])},
+        "pairs_per_s": r["pairs_tested"] * value, "evaluations_per_s": r["evaluations"] * value,
+        "roofline": None,
+        "roofline_note": ("FP64 distance evaluations behind a tree walk per query: latency-bound "
+                          "(no FP64 peak is measured on this pool); see the launch list"),
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 METRIC = "pair GFLOP/s, Barnes-Hut energy+differential (61 FLOP/interaction)"
 
 
@@ -573,7 +646,7 @@ def main() -> int:
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="flow", choices=["flow", "flow-spec", "matvec", "c2", "c3"])
+    ap.add_argument("--workload", default="flow", choices=["flow", "flow-spec", "matvec", "c2", "c3", "ccd"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.steps is None:
@@ -582,6 +655,12 @@ def main() -> int:
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
+        if args.workload == "ccd":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": (
+                    "the CCD oracle enumerates pairs by brute force (quadratic in the faces): "
+                    "no timed CPU arm at 204,800 faces")}), flush=True)
+            return 0
         if args.workload.startswith("flow"):
             return run_reference_flow(args, rank)
         return run_reference(args, rank)
@@ -589,6 +668,8 @@ def main() -> int:
         return bench_flow(args, rank, world, local)
     if args.workload == "matvec":
         return bench_matvec(args, rank, world, local)
+    if args.workload == "ccd":
+        return bench_ccd(args, rank, world, local)
 
     import torch
 

@@ -202,21 +202,55 @@ __global__ void gather_boxes_kernel(int n, const uint32_t *order, const DBox *bo
   if (i < n) sbox[i] = box[order[i]];
 }
 
-// level 0: unions of blocks of `leaf` sorted boxes; level k: unions of pairs of level k - 1
-__global__ void level_kernel(int n_out, const DBox *in, int n_in, int group, DBox *out) {
+// Node boxes of the walk in FP32, rounded outward: a node box contains the FP64 union of its
+// elements' boxes, so the walk visits every leaf block the FP64 tree would (it may visit more;
+// the element test below is exact).
+struct FBox {
+  float lo[3], hi[3];
+};
+
+__device__ __forceinline__ FBox outward(const DBox &b) {
+  FBox r;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) r.lo[k] = __double2float_rd(b.lo[k]), r.hi[k] = __double2float_ru(b.hi[k]);
+  return r;
+}
+
+__device__ __forceinline__ bool overlaps_f(const FBox &a, const FBox &b) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    if (!(a.lo[k] <= b.hi[k] && b.lo[k] <= a.hi[k])) return false;
+  return true;
+}
+
+// level 0: unions of blocks of 8 sorted element boxes (FP64, then rounded outward)
+__global__ void level0_kernel(int n_out, const DBox *in, int n_in, FBox *out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_out) return;
   DBox r;
   for (int k = 0; k < 3; ++k) r.lo[k] = INFINITY, r.hi[k] = -INFINITY;
-  const int b = i * group, e = min(b + group, n_in);
+  const int b = i * 8, e = min(b + 8, n_in);
   for (int j = b; j < e; ++j) r = unite(r, in[j]);
+  out[i] = outward(r);
+}
+
+// level k: unions of pairs of level k - 1 (min / max of floats are exact)
+__global__ void level_kernel(int n_out, const FBox *in, int n_in, FBox *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_out) return;
+  FBox r = in[2 * i];
+  if (2 * i + 1 < n_in) {
+    const FBox &o = in[2 * i + 1];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r.lo[k] = fminf(r.lo[k], o.lo[k]), r.hi[k] = fmaxf(r.hi[k], o.hi[k]);
+  }
   out[i] = r;
 }
 
 struct Tree {
-  const DBox *sbox;      // sorted element boxes
+  const DBox *sbox;      // sorted element boxes (FP64, the exact test)
   const uint32_t *order; // sorted position -> element
-  const DBox *levels;    // all levels, level 0 first
+  const FBox *levels;    // all levels, level 0 first
   const int *lvl_off;    // offset of each level in `levels`
   const int *lvl_len;
   int n, n_levels, leaf;
@@ -224,17 +258,18 @@ struct Tree {
 
 constexpr int kStack = 64;
 
-// Calls f(element) for every element whose box overlaps q (query, ccd.rs:359-389). Returns
-// false if the stack would overflow (not reachable: a depth-first walk of a tree of n_levels
-// <= 62 levels holds at most n_levels + 1 entries).
+// Calls f(element) for every element whose FP64 box overlaps q (query, ccd.rs:359-389).
+// Returns false if the stack would overflow (not reachable: a depth-first walk of a tree of
+// n_levels <= 62 levels holds at most n_levels + 1 entries).
 template <class F>
 __device__ bool query(const Tree &t, const DBox &q, F &&f) {
+  const FBox qf = outward(q);
   int2 stack[kStack];
   int sp = 0;
   stack[sp++] = make_int2(t.n_levels - 1, 0);
   while (sp > 0) {
     const int2 e = stack[--sp];
-    if (!overlaps(t.levels[t.lvl_off[e.x] + e.y], q)) continue;
+    if (!overlaps_f(t.levels[t.lvl_off[e.x] + e.y], qf)) continue;
     if (e.x == 0) {
       const int b = e.y * t.leaf, end = min(b + t.leaf, t.n);
       for (int pos = b; pos < end; ++pos)
@@ -279,55 +314,70 @@ __device__ void flush_tally(const Params &P, const Tally &t) {
   }
 }
 
-// vertex against triangle, one thread per vertex (ccd.rs:937-985)
-__global__ void __launch_bounds__(128) vt_kernel(Params P, Tree ft) {
-  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+// Broad phase, one thread per query: KIND 0 a vertex against the face tree (the vertex not in
+// the face, ccd.rs:937-985), KIND 1 an edge against the edge tree (partners e2 > e without a
+// common vertex, ccd.rs:987-1038). FILL 0 counts each query's candidates; FILL 1 writes them
+// as (query, element) from the query's offset, in the walk's order.
+template <int KIND, bool FILL>
+__global__ void __launch_bounds__(128) walk_kernel(Params P, Tree t, unsigned long long *count,
+                                                   const unsigned long long *off, uint2 *pairs) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nq = KIND == 0 ? P.nv : P.ne;
+  if (q >= nq) return;
+  const DBox qb = KIND == 0 ? inflate(P.vbox[q], P.h) : P.ebox[q];
+  uint32_t a = 0, b = 0;
+  if (KIND == 1) a = P.edges[2 * q], b = P.edges[2 * q + 1];
+  unsigned long long w = FILL ? off[q] : 0;
+  uint32_t n = 0;
+  const bool ok = query(t, qb, [&](uint32_t el) {
+    if (KIND == 0) {
+      if (P.faces[3 * el] == (uint32_t)q || P.faces[3 * el + 1] == (uint32_t)q || P.faces[3 * el + 2] == (uint32_t)q)
+        return;
+    } else {
+      if (el <= (uint32_t)q) return;
+      const uint32_t c = P.edges[2 * el], d = P.edges[2 * el + 1];
+      if (c == a || c == b || d == a || d == b) return;
+    }
+    if (FILL) pairs[w++] = make_uint2((uint32_t)q, el);
+    ++n;
+  });
+  if (!ok) atomicExch(P.overflow, 1);
+  if (!FILL) count[q] = n;
+}
+
+// Narrow phase, one thread per candidate pair: the lanes of a warp evaluate their distances
+// together. KIND 0: (vertex, face); KIND 1: (edge, edge).
+template <int KIND>
+__global__ void __launch_bounds__(128) narrow_kernel(Params P, const uint2 *pairs, unsigned long long n) {
+  const unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
   Tally tally;
-  if (v < P.nv) {
-    const DBox q = inflate(P.vbox[v], P.h);
-    const double3 p = P.start[v], u = P.vel[v];
-    const double sv = P.speed[v];
-    const bool ok = query(ft, q, [&](uint32_t f) {
+  if (i < n) {
+    const uint2 pr = pairs[i];
+    double r;
+    if (KIND == 0) {
+      const uint32_t v = pr.x, f = pr.y;
       const uint32_t a = P.faces[3 * f], b = P.faces[3 * f + 1], c = P.faces[3 * f + 2];
-      if (a == (uint32_t)v || b == (uint32_t)v || c == (uint32_t)v) return;
+      const double3 p = P.start[v], u = P.vel[v];
       const double3 ta = at3(P.start[a], P.vel[a], 0.0), tb = at3(P.start[b], P.vel[b], 0.0),
                     tc = at3(P.start[c], P.vel[c], 0.0);
       const double3 ua = P.vel[a], ub = P.vel[b], uc = P.vel[c];
-      const double lc = (sv + fmax(fmax(P.speed[a], P.speed[b]), P.speed[c])) * kMargin;
+      const double lc = (P.speed[v] + fmax(fmax(P.speed[a], P.speed[b]), P.speed[c])) * kMargin;
       auto dist = [&](double t) {
         return point_triangle_distance(at3(p, u, t), at3(ta, ua, t), at3(tb, ub, t), at3(tc, uc, t));
       };
-      const double r = advance(dist, lc, P.gap_abs, P.max_iterations, P.close_factor, P.lo, horizon(P), tally);
-      if (r >= 0.0) atomicMin(P.best, (unsigned long long)__double_as_longlong(r));
-    });
-    if (!ok) atomicExch(P.overflow, 1);
-  }
-  flush_tally(P, tally);
-}
-
-// edge against edge, one thread per edge e, partners e2 > e without a common vertex
-// (ccd.rs:987-1038)
-__global__ void __launch_bounds__(128) ee_kernel(Params P, Tree et) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  Tally tally;
-  if (e < P.ne) {
-    const DBox q = P.ebox[e];
-    const uint32_t a = P.edges[2 * e], b = P.edges[2 * e + 1];
-    const double3 pa = P.start[a], pb = P.start[b], ua = P.vel[a], ub = P.vel[b];
-    const double sab = fmax(P.speed[a], P.speed[b]);
-    const bool ok = query(et, q, [&](uint32_t e2) {
-      if (e2 <= (uint32_t)e) return;
-      const uint32_t c = P.edges[2 * e2], d = P.edges[2 * e2 + 1];
-      if (c == a || c == b || d == a || d == b) return;
+      r = advance(dist, lc, P.gap_abs, P.max_iterations, P.close_factor, P.lo, horizon(P), tally);
+    } else {
+      const uint32_t a = P.edges[2 * pr.x], b = P.edges[2 * pr.x + 1];
+      const uint32_t c = P.edges[2 * pr.y], d = P.edges[2 * pr.y + 1];
+      const double3 pa = P.start[a], pb = P.start[b], ua = P.vel[a], ub = P.vel[b];
       const double3 pc = P.start[c], pd = P.start[d], uc = P.vel[c], ud = P.vel[d];
-      const double lc = (sab + fmax(P.speed[c], P.speed[d])) * kMargin;
+      const double lc = (fmax(P.speed[a], P.speed[b]) + fmax(P.speed[c], P.speed[d])) * kMargin;
       auto dist = [&](double t) {
         return segment_segment_distance(at3(pa, ua, t), at3(pb, ub, t), at3(pc, uc, t), at3(pd, ud, t));
       };
-      const double r = advance(dist, lc, P.gap_abs, P.max_iterations, P.close_factor, P.lo, horizon(P), tally);
-      if (r >= 0.0) atomicMin(P.best, (unsigned long long)__double_as_longlong(r));
-    });
-    if (!ok) atomicExch(P.overflow, 1);
+      r = advance(dist, lc, P.gap_abs, P.max_iterations, P.close_factor, P.lo, horizon(P), tally);
+    }
+    if (r >= 0.0) atomicMin(P.best, (unsigned long long)__double_as_longlong(r));
   }
   flush_tally(P, tally);
 }
@@ -343,7 +393,8 @@ inline unsigned blocks(long long n, int t) { return (unsigned)((n + t - 1) / t);
 // A box tree's device storage, rebuilt per window.
 struct TreeBufs {
   int n = 0;
-  DevBuf<DBox> box, sbox, levels;
+  DevBuf<DBox> box, sbox;
+  DevBuf<FBox> levels;
   DevBuf<uint32_t> key, key_sorted, idx, order;
   DevBuf<int> lvl_off, lvl_len;
   std::vector<int> off, len;
@@ -381,6 +432,9 @@ struct rs_ccd {
   DevBuf<double> speed;
   DevBuf<DBox> vbox;
   TreeBufs ft, et;
+  DevBuf<unsigned long long> count;   // candidates per query (vertices, then edges)
+  DevBuf<unsigned long long> offs;    // their exclusive sums: nv + 1, then ne + 1
+  DevBuf<uint2> pairs;                // the window's candidate pairs, vertex-face then edge-edge
   DevBuf<unsigned char> cub_tmp;
   DevBuf<unsigned long long> scratch;  // best, 4 tally counters, overflow flag
   double last_seconds = 0.0;
@@ -429,7 +483,11 @@ int rs_ccd_create(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, rs_ccd **o
                                                     c->ft.order.p, nf, 0, 30, s));
     RSG_CUDA("ccd", cub::DeviceRadixSort::SortPairs(nullptr, t2, c->et.key.p, c->et.key_sorted.p, c->et.idx.p,
                                                     c->et.order.p, c->ne, 0, 30, s));
-    c->cub_tmp.alloc(std::max<size_t>(std::max(t1, t2), 16));
+    c->count.alloc((size_t)nv + c->ne + 2);
+    c->offs.alloc((size_t)nv + c->ne + 2);
+    size_t t3 = 0;
+    RSG_CUDA("ccd", cub::DeviceScan::ExclusiveSum(nullptr, t3, c->count.p, c->offs.p, std::max(nv, c->ne) + 1, s));
+    c->cub_tmp.alloc(std::max<size_t>(std::max(std::max(t1, t2), t3), 16));
     c->scratch.alloc(8);
     RSG_CUDA("ccd", cudaStreamSynchronize(s));
     ctx_retain(ctx);
@@ -536,19 +594,50 @@ int rs_ccd_first_contact(rs_ccd *c, const double *start, const double *velocity,
         ctx->launches++;
         gather_boxes_kernel<<<blocks(n, 256), 256, 0, s>>>(n, T.order.p, T.box.p, T.sbox.p);
         RSG_LAUNCHED(ctx, "ccd gather");
-        for (size_t k = 0; k < T.off.size(); ++k) {
-          const DBox *in = k == 0 ? T.sbox.p : T.levels.p + T.off[k - 1];
-          const int n_in = k == 0 ? n : T.len[k - 1];
-          level_kernel<<<blocks(T.len[k], 128), 128, 0, s>>>(T.len[k], in, n_in, k == 0 ? 8 : 2, T.levels.p + T.off[k]);
+        level0_kernel<<<blocks(T.len[0], 128), 128, 0, s>>>(T.len[0], T.sbox.p, n, T.levels.p);
+        RSG_LAUNCHED(ctx, "ccd tree level");
+        for (size_t k = 1; k < T.off.size(); ++k) {
+          level_kernel<<<blocks(T.len[k], 128), 128, 0, s>>>(T.len[k], T.levels.p + T.off[k - 1], T.len[k - 1],
+                                                               T.levels.p + T.off[k]);
           RSG_LAUNCHED(ctx, "ccd tree level");
         }
       }
       Params P{c->start.p, c->vel.p, c->speed.p, c->faces.p, c->edges.p, c->vbox.p, c->et.box.p,
                nv, c->ne, o.max_iterations, gap_abs, o.close_factor, h, lo, hi, best, tally, overflow};
-      vt_kernel<<<blocks(nv, 128), 128, 0, s>>>(P, c->ft.view());
-      RSG_LAUNCHED(ctx, "ccd vertex-triangle");
-      ee_kernel<<<blocks(c->ne, 128), 128, 0, s>>>(P, c->et.view());
-      RSG_LAUNCHED(ctx, "ccd edge-edge");
+      // broad phase: count the candidates of every query, offsets by an exclusive sum
+      unsigned long long *cnt_vt = c->count.p, *cnt_ee = c->count.p + nv + 1;
+      unsigned long long *off_vt = c->offs.p, *off_ee = c->offs.p + nv + 1;
+      RSG_CUDA("ccd", cudaMemsetAsync(c->count.p, 0, c->count.bytes(), s));
+      walk_kernel<0, false><<<blocks(nv, 128), 128, 0, s>>>(P, c->ft.view(), cnt_vt, nullptr, nullptr);
+      RSG_LAUNCHED(ctx, "ccd walk");
+      walk_kernel<1, false><<<blocks(c->ne, 128), 128, 0, s>>>(P, c->et.view(), cnt_ee, nullptr, nullptr);
+      RSG_LAUNCHED(ctx, "ccd walk");
+      for (int kind = 0; kind < 2; ++kind) {
+        size_t tb = c->cub_tmp.n;
+        const int nq = kind == 0 ? nv : c->ne;
+        RSG_CUDA("ccd", cub::DeviceScan::ExclusiveSum(c->cub_tmp.p, tb, kind == 0 ? cnt_vt : cnt_ee,
+                                                      kind == 0 ? off_vt : off_ee, nq + 1, s));
+        ctx->launches++;
+      }
+      unsigned long long tot[2];
+      RSG_CUDA("ccd", rsg::copy_async(&tot[0], off_vt + nv, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+      RSG_CUDA("ccd", rsg::copy_async(&tot[1], off_ee + c->ne, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+      RSG_CUDA("ccd", cudaStreamSynchronize(s));
+      const unsigned long long n_vt = tot[0], n_ee = tot[1];
+      if (n_vt + n_ee > c->pairs.n) c->pairs.alloc((size_t)((n_vt + n_ee) * 5 / 4 + 1024));
+      walk_kernel<0, true><<<blocks(nv, 128), 128, 0, s>>>(P, c->ft.view(), nullptr, off_vt, c->pairs.p);
+      RSG_LAUNCHED(ctx, "ccd walk");
+      walk_kernel<1, true><<<blocks(c->ne, 128), 128, 0, s>>>(P, c->et.view(), nullptr, off_ee, c->pairs.p + n_vt);
+      RSG_LAUNCHED(ctx, "ccd walk");
+      // narrow phase, one thread per candidate pair
+      if (n_vt) {
+        narrow_kernel<0><<<blocks((long long)n_vt, 128), 128, 0, s>>>(P, c->pairs.p, n_vt);
+        RSG_LAUNCHED(ctx, "ccd vertex-triangle");
+      }
+      if (n_ee) {
+        narrow_kernel<1><<<blocks((long long)n_ee, 128), 128, 0, s>>>(P, c->pairs.p + n_vt, n_ee);
+        RSG_LAUNCHED(ctx, "ccd edge-edge");
+      }
       unsigned long long res[8];
       c->scratch.download(res, 8, s);
       RSG_CUDA("ccd", cudaStreamSynchronize(s));

@@ -90,6 +90,28 @@ __device__ double point_triangle_distance(double3 p, double3 a, double3 b, doubl
   return edges;
 }
 
+// ---- static queries (RS/src/ccd.rs:1153-1191) ----
+
+__device__ __forceinline__ double orient(double3 a, double3 b, double3 c, double3 d) {
+  return dot3(cross3(sub3(b, a), sub3(c, a)), sub3(d, a));
+}
+
+__device__ bool segment_meets_triangle(double3 p, double3 q, double3 a, double3 b, double3 c) {  // ccd.rs:1158-1186
+  const double d1 = orient(a, b, c, p), d2 = orient(a, b, c, q);
+  if ((d1 > 0.0 && d2 > 0.0) || (d1 < 0.0 && d2 < 0.0)) return false;
+  const double n = norm3(cross3(sub3(b, a), sub3(c, a)));
+  const double len = fmax(fmax(fmax(norm3(sub3(q, p)), norm3(sub3(b, a))), norm3(sub3(c, a))), norm3(sub3(c, b)));
+  const double flat = 1e-12 * n * len;
+  if (fabs(d1) <= flat && fabs(d2) <= flat) {
+    const double eps = 1e-14 * (norm3(sub3(b, a)) + norm3(sub3(c, a)));
+    return point_triangle_distance(p, a, b, c) <= eps || point_triangle_distance(q, a, b, c) <= eps ||
+           segment_segment_distance(p, q, a, b) <= eps || segment_segment_distance(p, q, b, c) <= eps ||
+           segment_segment_distance(p, q, c, a) <= eps;
+  }
+  const double s1 = orient(p, q, a, b), s2 = orient(p, q, b, c), s3 = orient(p, q, c, a);
+  return (s1 >= 0.0 && s2 >= 0.0 && s3 >= 0.0) || (s1 <= 0.0 && s2 <= 0.0 && s3 <= 0.0);
+}
+
 struct Tally {
   unsigned long long pairs = 0, close = 0, touching = 0, evals = 0;
 };
@@ -290,10 +312,12 @@ struct Params {
   const uint32_t *edges;  // 2 per edge
   const DBox *vbox;
   const DBox *ebox;       // inflated, element order
-  int nv, ne, max_iterations;
+  const DBox *fbox;       // face boxes, element order (the band's face-face walk)
+  const uint8_t *band;    // exempt band per vertex, or null
+  int nv, ne, nf, max_iterations;
   double gap_abs, close_factor, h, lo, hi;
   unsigned long long *best;   // bits of the earliest contact time (+inf: none)
-  unsigned long long *tally;  // pairs, close, touching, evaluations
+  unsigned long long *tally;  // pairs, close, touching, evaluations, exempt
   int *overflow;
 };
 
@@ -318,31 +342,104 @@ __device__ void flush_tally(const Params &P, const Tally &t) {
 // the face, ccd.rs:937-985), KIND 1 an edge against the edge tree (partners e2 > e without a
 // common vertex, ccd.rs:987-1038). FILL 0 counts each query's candidates; FILL 1 writes them
 // as (query, element) from the query's offset, in the walk's order.
+// KIND 2 (the band): a face against the face tree of the static hulls, partners g > f
+// (intersecting_pairs, ccd.rs:1229-1279); the intersection test runs per pair afterwards.
+// A pair whose two elements both have a vertex in the band is exempt (ccd.rs:947-950,
+// 1001-1004): it is not a candidate, and the count pass tallies it.
 template <int KIND, bool FILL>
 __global__ void __launch_bounds__(128) walk_kernel(Params P, Tree t, unsigned long long *count,
                                                    const unsigned long long *off, uint2 *pairs) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nq = KIND == 0 ? P.nv : P.ne;
+  const int nq = KIND == 0 ? P.nv : (KIND == 1 ? P.ne : P.nf);
   if (q >= nq) return;
-  const DBox qb = KIND == 0 ? inflate(P.vbox[q], P.h) : P.ebox[q];
+  const DBox qb = KIND == 0 ? inflate(P.vbox[q], P.h) : (KIND == 1 ? P.ebox[q] : P.fbox[q]);
   uint32_t a = 0, b = 0;
   if (KIND == 1) a = P.edges[2 * q], b = P.edges[2 * q + 1];
+  const bool qband = P.band && (KIND == 0 ? P.band[q] : (KIND == 1 ? (P.band[a] || P.band[b]) : false));
   unsigned long long w = FILL ? off[q] : 0;
-  uint32_t n = 0;
+  uint32_t n = 0, exempt = 0;
   const bool ok = query(t, qb, [&](uint32_t el) {
     if (KIND == 0) {
-      if (P.faces[3 * el] == (uint32_t)q || P.faces[3 * el + 1] == (uint32_t)q || P.faces[3 * el + 2] == (uint32_t)q)
+      const uint32_t fa = P.faces[3 * el], fb = P.faces[3 * el + 1], fc = P.faces[3 * el + 2];
+      if (fa == (uint32_t)q || fb == (uint32_t)q || fc == (uint32_t)q) return;
+      if (qband && (P.band[fa] || P.band[fb] || P.band[fc])) {
+        ++exempt;
         return;
-    } else {
+      }
+    } else if (KIND == 1) {
       if (el <= (uint32_t)q) return;
       const uint32_t c = P.edges[2 * el], d = P.edges[2 * el + 1];
       if (c == a || c == b || d == a || d == b) return;
+      if (qband && (P.band[c] || P.band[d])) {
+        ++exempt;
+        return;
+      }
+    } else {
+      if (el <= (uint32_t)q) return;
     }
     if (FILL) pairs[w++] = make_uint2((uint32_t)q, el);
     ++n;
   });
   if (!ok) atomicExch(P.overflow, 1);
-  if (!FILL) count[q] = n;
+  if (!FILL) {
+    count[q] = n;
+    if (exempt) atomicAdd(P.tally + 4, (unsigned long long)exempt);
+  }
+}
+
+// The intersection test of one candidate face pair (f, g), f < g (ccd.rs:1247-1270): faces
+// without a common vertex that meet, or faces with one common vertex whose opposite edge meets
+// the other face; faces that share an edge are not tested.
+__global__ void isect_kernel(Params P, const uint2 *pairs, unsigned long long n, uint8_t *hit) {
+  const unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t f = pairs[i].x, g = pairs[i].y;
+  uint32_t A[3] = {P.faces[3 * f], P.faces[3 * f + 1], P.faces[3 * f + 2]};
+  uint32_t B[3] = {P.faces[3 * g], P.faces[3 * g + 1], P.faces[3 * g + 2]};
+  int common[3], nc = 0;
+  for (int k = 0; k < 3; ++k)
+    if (B[0] == A[k] || B[1] == A[k] || B[2] == A[k]) common[nc++] = k;
+  const double3 a0 = P.start[A[0]], a1 = P.start[A[1]], a2 = P.start[A[2]];
+  const double3 b0 = P.start[B[0]], b1 = P.start[B[1]], b2 = P.start[B[2]];
+  bool h = false;
+  if (nc == 0) {
+    // triangles_intersect (ccd.rs:1188-1191): each edge of one against the other, in order
+    const double3 ta[3] = {a0, a1, a2}, tb[3] = {b0, b1, b2};
+    for (int k = 0; k < 3 && !h; ++k) h = segment_meets_triangle(ta[k], ta[(k + 1) % 3], b0, b1, b2);
+    for (int k = 0; k < 3 && !h; ++k) h = segment_meets_triangle(tb[k], tb[(k + 1) % 3], a0, a1, a2);
+  } else if (nc == 1) {
+    const int k = common[0];
+    int j = 0;
+    while (B[j] != A[k]) ++j;
+    h = segment_meets_triangle(P.start[A[(k + 1) % 3]], P.start[A[(k + 2) % 3]], b0, b1, b2) ||
+        segment_meets_triangle(P.start[B[(j + 1) % 3]], P.start[B[(j + 2) % 3]], a0, a1, a2);
+  }
+  hit[i] = h ? 1 : 0;
+}
+
+// IntersectionBand::new (ccd.rs:1292-1319): the vertices of the intersecting faces (core) ...
+__global__ void core_kernel(Params P, const uint2 *pairs, const uint8_t *hit, unsigned long long n, uint8_t *core,
+                            unsigned long long *n_hits) {
+  const unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !hit[i]) return;
+  const uint32_t f = pairs[i].x, g = pairs[i].y;
+  for (int k = 0; k < 3; ++k) core[P.faces[3 * f + k]] = 1, core[P.faces[3 * g + k]] = 1;
+  atomicAdd(n_hits, 1ull);
+}
+
+// ... widened by one ring: both ends of every edge with an end in the core
+__global__ void ring_kernel(Params P, const uint8_t *core, uint8_t *band) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= P.ne) return;
+  const uint32_t a = P.edges[2 * e], b = P.edges[2 * e + 1];
+  if (core[a] || core[b]) band[a] = 1, band[b] = 1;
+}
+
+__global__ void count_flags_kernel(int n, const uint8_t *flag, unsigned long long *count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool f = i < n && flag[i];
+  const unsigned m = __ballot_sync(0xffffffffu, f);
+  if ((threadIdx.x & 31) == 0 && m) atomicAdd(count, (unsigned long long)__popc(m));
 }
 
 // Narrow phase, one thread per candidate pair: the lanes of a warp evaluate their distances
@@ -382,10 +479,10 @@ __global__ void __launch_bounds__(128) narrow_kernel(Params P, const uint2 *pair
   flush_tally(P, tally);
 }
 
-// best = +inf (no contact), the four counters = 0
+// best = +inf (no contact), the five counters = 0
 __global__ void reset_kernel(unsigned long long *best, unsigned long long *tally) {
   if (threadIdx.x == 0) *best = 0x7FF0000000000000ull;
-  if (threadIdx.x < 4) tally[threadIdx.x] = 0;
+  if (threadIdx.x < 5) tally[threadIdx.x] = 0;
 }
 
 inline unsigned blocks(long long n, int t) { return (unsigned)((n + t - 1) / t); }
@@ -432,13 +529,133 @@ struct rs_ccd {
   DevBuf<double> speed;
   DevBuf<DBox> vbox;
   TreeBufs ft, et;
-  DevBuf<unsigned long long> count;   // candidates per query (vertices, then edges)
-  DevBuf<unsigned long long> offs;    // their exclusive sums: nv + 1, then ne + 1
-  DevBuf<uint2> pairs;                // the window's candidate pairs, vertex-face then edge-edge
+  DevBuf<unsigned long long> count;   // candidates per query
+  DevBuf<unsigned long long> offs;    // their exclusive sums
+  DevBuf<uint2> pairs;                // candidate pairs of a window (or of the band's walk)
+  DevBuf<uint8_t> hit, core, band;    // the band: intersection flags per candidate, per vertex
+  bool has_band = false;
   DevBuf<unsigned char> cub_tmp;
-  DevBuf<unsigned long long> scratch;  // best, 4 tally counters, overflow flag
+  DevBuf<unsigned long long> scratch;  // best, 5 tally counters, overflow flag, band hits
   double last_seconds = 0.0;
 };
+
+namespace {
+
+// The element boxes of one kind, sorted along the Morton curve, and the tree levels over them.
+void build_tree(rs_ccd *c, TreeBufs &T, int kind, double h, double3 gl, double3 gs, cudaStream_t s) {
+  rs_ctx *ctx = c->ctx;
+  const int n = T.n;
+  if (kind == 0)
+    prim_box_kernel<3><<<blocks(n, 256), 256, 0, s>>>(n, c->faces.p, c->vbox.p, h, gl, gs, T.box.p, T.key.p, T.idx.p);
+  else
+    prim_box_kernel<2><<<blocks(n, 256), 256, 0, s>>>(n, c->edges.p, c->vbox.p, h, gl, gs, T.box.p, T.key.p, T.idx.p);
+  RSG_LAUNCHED(ctx, "ccd primitive boxes");
+  size_t tb = c->cub_tmp.n;
+  RSG_CUDA("ccd", cub::DeviceRadixSort::SortPairs(c->cub_tmp.p, tb, T.key.p, T.key_sorted.p, T.idx.p, T.order.p, n,
+                                                  0, 30, s));
+  ctx->launches++;
+  gather_boxes_kernel<<<blocks(n, 256), 256, 0, s>>>(n, T.order.p, T.box.p, T.sbox.p);
+  RSG_LAUNCHED(ctx, "ccd gather");
+  level0_kernel<<<blocks(T.len[0], 128), 128, 0, s>>>(T.len[0], T.sbox.p, n, T.levels.p);
+  RSG_LAUNCHED(ctx, "ccd tree level");
+  for (size_t k = 1; k < T.off.size(); ++k) {
+    level_kernel<<<blocks(T.len[k], 128), 128, 0, s>>>(T.len[k], T.levels.p + T.off[k - 1], T.len[k - 1],
+                                                       T.levels.p + T.off[k]);
+    RSG_LAUNCHED(ctx, "ccd tree level");
+  }
+}
+
+// The Morton grid over the start positions widened by `ext` (any grid gives the same pairs).
+void morton_grid(const double *start, int nv, double ext, double3 &gl, double3 &gs) {
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int v = 0; v < nv; ++v)
+    for (int k = 0; k < 3; ++k) lo[k] = std::fmin(lo[k], start[3 * (size_t)v + k]), hi[k] = std::fmax(hi[k], start[3 * (size_t)v + k]);
+  double l3[3], s3[3];
+  for (int k = 0; k < 3; ++k) {
+    l3[k] = lo[k] - ext;
+    const double w = (hi[k] + ext) - l3[k];
+    s3[k] = w > 0.0 ? 1023.0 / w : 0.0;
+  }
+  gl = make_double3(l3[0], l3[1], l3[2]);
+  gs = make_double3(s3[0], s3[1], s3[2]);
+}
+
+// Candidate pairs of one kind: count, exclusive sum, fill at c->pairs + base. Returns their
+// number (the caller has synchronised nothing; this reads the total back).
+template <int KIND>
+unsigned long long collect(rs_ccd *c, const Params &P, const Tree &t, int nq, unsigned long long base,
+                           bool grow_keep, cudaStream_t s) {
+  rs_ctx *ctx = c->ctx;
+  RSG_CUDA("ccd", cudaMemsetAsync(c->count.p, 0, ((size_t)nq + 1) * sizeof(unsigned long long), s));
+  walk_kernel<KIND, false><<<blocks(nq, 128), 128, 0, s>>>(P, t, c->count.p, nullptr, nullptr);
+  RSG_LAUNCHED(ctx, "ccd walk");
+  size_t tb = c->cub_tmp.n;
+  RSG_CUDA("ccd", cub::DeviceScan::ExclusiveSum(c->cub_tmp.p, tb, c->count.p, c->offs.p, nq + 1, s));
+  ctx->launches++;
+  unsigned long long tot = 0;
+  RSG_CUDA("ccd", rsg::copy_async(&tot, c->offs.p + nq, sizeof(tot), cudaMemcpyDeviceToHost, s));
+  RSG_CUDA("ccd", cudaStreamSynchronize(s));
+  if (base + tot > c->pairs.n) {
+    DevBuf<uint2> bigger((size_t)((base + tot) * 5 / 4 + 1024));
+    if (grow_keep && base)
+      RSG_CUDA("ccd", cudaMemcpyAsync(bigger.p, c->pairs.p, base * sizeof(uint2), cudaMemcpyDeviceToDevice, s));
+    c->pairs = std::move(bigger);
+  }
+  if (tot) {
+    walk_kernel<KIND, true><<<blocks(nq, 128), 128, 0, s>>>(P, t, nullptr, c->offs.p, c->pairs.p + base);
+    RSG_LAUNCHED(ctx, "ccd walk");
+  }
+  return tot;
+}
+
+Params make_params(rs_ccd *c, double gap_abs, double close_factor, int max_iterations, double h, double lo,
+                   double hi, const uint8_t *band) {
+  Params P;
+  P.start = c->start.p, P.vel = c->vel.p, P.speed = c->speed.p, P.faces = c->faces.p, P.edges = c->edges.p;
+  P.vbox = c->vbox.p, P.ebox = c->et.box.p, P.fbox = c->ft.box.p, P.band = band;
+  P.nv = c->nv, P.ne = c->ne, P.nf = c->nf, P.max_iterations = max_iterations;
+  P.gap_abs = gap_abs, P.close_factor = close_factor, P.h = h, P.lo = lo, P.hi = hi;
+  P.best = c->scratch.p, P.tally = c->scratch.p + 1;
+  P.overflow = reinterpret_cast<int *>(c->scratch.p + 6);
+  return P;
+}
+
+void check_overflow(rs_ccd *c, cudaStream_t s) {
+  int ov = 0;
+  RSG_CUDA("ccd", rsg::copy_async(&ov, c->scratch.p + 6, sizeof(int), cudaMemcpyDeviceToHost, s));
+  RSG_CUDA("ccd", cudaStreamSynchronize(s));
+  if (ov) fail(RS_INTERNAL, "Internal", "ccd", "box tree stack overflow");
+}
+
+void check_positions(const double *x, size_t n, const char *what) {
+  for (size_t i = 0; i < n; ++i)
+    if (!std::isfinite(x[i])) fail(RS_INVALID_OPTION, "InvalidOption", "ccd", std::string(what) + " must be finite");
+}
+
+// The candidate face pairs of the static hulls of `positions` (uploaded into c->start) and
+// their intersection flags (c->hit); returns the number of candidates.
+unsigned long long face_pairs(rs_ccd *c, const double *positions, cudaStream_t s) {
+  rs_ctx *ctx = c->ctx;
+  c->start.upload(reinterpret_cast<const double3 *>(positions), c->nv, s);
+  RSG_CUDA("ccd", cudaMemsetAsync(c->vel.p, 0, c->vel.bytes(), s));
+  RSG_CUDA("ccd", cudaMemsetAsync(c->scratch.p, 0, c->scratch.bytes(), s));
+  vbox_kernel<<<blocks(c->nv, 256), 256, 0, s>>>(c->nv, c->start.p, c->vel.p, 0.0, 0.0, c->vbox.p);
+  RSG_LAUNCHED(ctx, "ccd boxes");
+  double3 gl, gs;
+  morton_grid(positions, c->nv, 0.0, gl, gs);
+  build_tree(c, c->ft, 0, 0.0, gl, gs, s);
+  const Params P = make_params(c, 0.0, 0.0, 1, 0.0, 0.0, 0.0, nullptr);
+  const unsigned long long n = collect<2>(c, P, c->ft.view(), c->nf, 0, false, s);
+  if (n > c->hit.n) c->hit.alloc((size_t)(n * 5 / 4 + 1024));
+  if (n) {
+    isect_kernel<<<blocks((long long)n, 128), 128, 0, s>>>(P, c->pairs.p, n, c->hit.p);
+    RSG_LAUNCHED(ctx, "ccd intersection test");
+  }
+  check_overflow(c, s);
+  return n;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -477,16 +694,17 @@ int rs_ccd_create(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, rs_ccd **o
     c->faces.upload(faces, 3 * (size_t)nf, s);
     c->edges.upload(c->edges_h, s);
     c->start.alloc(nv), c->vel.alloc(nv), c->speed.alloc(nv), c->vbox.alloc(nv);
+    c->core.alloc(nv), c->band.alloc(nv);
     c->ft.init(nf, s), c->et.init(c->ne, s);
-    size_t t1 = 0, t2 = 0;
+    size_t t1 = 0, t2 = 0, t3 = 0;
     RSG_CUDA("ccd", cub::DeviceRadixSort::SortPairs(nullptr, t1, c->ft.key.p, c->ft.key_sorted.p, c->ft.idx.p,
                                                     c->ft.order.p, nf, 0, 30, s));
     RSG_CUDA("ccd", cub::DeviceRadixSort::SortPairs(nullptr, t2, c->et.key.p, c->et.key_sorted.p, c->et.idx.p,
                                                     c->et.order.p, c->ne, 0, 30, s));
-    c->count.alloc((size_t)nv + c->ne + 2);
-    c->offs.alloc((size_t)nv + c->ne + 2);
-    size_t t3 = 0;
-    RSG_CUDA("ccd", cub::DeviceScan::ExclusiveSum(nullptr, t3, c->count.p, c->offs.p, std::max(nv, c->ne) + 1, s));
+    const int nq = std::max(std::max(nv, c->ne), nf);
+    c->count.alloc((size_t)nq + 1);
+    c->offs.alloc((size_t)nq + 1);
+    RSG_CUDA("ccd", cub::DeviceScan::ExclusiveSum(nullptr, t3, c->count.p, c->offs.p, nq + 1, s));
     c->cub_tmp.alloc(std::max<size_t>(std::max(std::max(t1, t2), t3), 16));
     c->scratch.alloc(8);
     RSG_CUDA("ccd", cudaStreamSynchronize(s));
@@ -502,8 +720,66 @@ void rs_ccd_free(rs_ccd *c) {
   ctx_release(ctx);
 }
 
+int rs_ccd_intersecting_pairs(rs_ccd *c, const double *positions, int64_t cap, uint32_t *out, int64_t *n) {
+  return guard([&] {
+    check_positions(positions, 3 * (size_t)c->nv, "positions");
+    rs_ctx *ctx = c->ctx;
+    ctx->use();
+    cudaStream_t s = ctx->stream;
+    const unsigned long long m = face_pairs(c, positions, s);
+    std::vector<uint2> pr(m);
+    std::vector<uint8_t> hit(m);
+    if (m) {
+      c->pairs.download(pr.data(), m, s);
+      c->hit.download(hit.data(), m, s);
+    }
+    RSG_CUDA("ccd", cudaStreamSynchronize(s));
+    std::vector<std::pair<uint32_t, uint32_t>> res;
+    for (size_t i = 0; i < m; ++i)
+      if (hit[i]) res.push_back({pr[i].x, pr[i].y});
+    std::sort(res.begin(), res.end());
+    *n = (int64_t)res.size();
+    for (size_t i = 0; i < res.size() && (int64_t)i < cap; ++i) out[2 * i] = res[i].first, out[2 * i + 1] = res[i].second;
+  });
+}
+
+int rs_ccd_set_band(rs_ccd *c, const double *positions, int64_t *n_pairs, int64_t *n_vertices) {
+  return guard([&] {
+    c->has_band = false;
+    if (!positions) {
+      if (n_pairs) *n_pairs = 0;
+      if (n_vertices) *n_vertices = 0;
+      return;
+    }
+    check_positions(positions, 3 * (size_t)c->nv, "positions");
+    rs_ctx *ctx = c->ctx;
+    ctx->use();
+    cudaStream_t s = ctx->stream;
+    const unsigned long long m = face_pairs(c, positions, s);
+    RSG_CUDA("ccd", cudaMemsetAsync(c->core.p, 0, c->core.bytes(), s));
+    RSG_CUDA("ccd", cudaMemsetAsync(c->scratch.p, 0, c->scratch.bytes(), s));
+    unsigned long long *hits = c->scratch.p + 7, *count = c->scratch.p + 5;
+    const Params P = make_params(c, 0.0, 0.0, 1, 0.0, 0.0, 0.0, nullptr);
+    if (m) {
+      core_kernel<<<blocks((long long)m, 128), 128, 0, s>>>(P, c->pairs.p, c->hit.p, m, c->core.p, hits);
+      RSG_LAUNCHED(ctx, "ccd band");
+    }
+    RSG_CUDA("ccd", cudaMemcpyAsync(c->band.p, c->core.p, c->core.bytes(), cudaMemcpyDeviceToDevice, s));
+    ring_kernel<<<blocks(c->ne, 256), 256, 0, s>>>(P, c->core.p, c->band.p);
+    RSG_LAUNCHED(ctx, "ccd band");
+    count_flags_kernel<<<blocks(c->nv, 256), 256, 0, s>>>(c->nv, c->band.p, count);
+    RSG_LAUNCHED(ctx, "ccd band");
+    unsigned long long res[8];
+    c->scratch.download(res, 8, s);
+    RSG_CUDA("ccd", cudaStreamSynchronize(s));
+    c->has_band = res[5] > 0;  // an empty band is no band (ccd.rs:790-792)
+    if (n_pairs) *n_pairs = (int64_t)res[7];
+    if (n_vertices) *n_vertices = (int64_t)res[5];
+  });
+}
+
 int rs_ccd_first_contact(rs_ccd *c, const double *start, const double *velocity, double tau_end,
-                         const rs_ccd_options *opts, double *tau_max, int64_t *report6) {
+                         const rs_ccd_options *opts, double *tau_max, int64_t *report7) {
   return guard([&] {
     auto t_begin = std::chrono::steady_clock::now();
     const rs_ccd_options o = opts ? *opts : rs_ccd_options_default();
@@ -519,16 +795,15 @@ int rs_ccd_first_contact(rs_ccd *c, const double *start, const double *velocity,
     if (!(std::isfinite(tau_end) && tau_end >= 0.0))
       fail(RS_INVALID_OPTION, "InvalidOption", "ccd", "tau_end must be finite and non-negative");
     const int nv = c->nv;
-    for (size_t i = 0; i < 3 * (size_t)nv; ++i) {
-      if (!std::isfinite(start[i])) fail(RS_INVALID_OPTION, "InvalidOption", "ccd", "positions must be finite");
+    check_positions(start, 3 * (size_t)nv, "positions");
+    for (size_t i = 0; i < 3 * (size_t)nv; ++i)
       if (!std::isfinite(velocity[i]))
         fail(RS_INVALID_OPTION, "InvalidOption", "ccd", "velocity must have finite components");
-    }
     rs_ctx *ctx = c->ctx;
     ctx->use();
     cudaStream_t s = ctx->stream;
-    // host scalars, in the reference's order: the mean edge length over the sorted edges,
-    // the largest speed, the box bounds of the sweep (these only place the Morton grid)
+    // host scalars, in the reference's order: the mean edge length over the sorted edges and
+    // the largest speed
     double sum = 0.0;
     for (int i = 0; i < c->ne; ++i) {
       const double *x = start + 3 * (size_t)c->edges_h[2 * i], *y = start + 3 * (size_t)c->edges_h[2 * i + 1];
@@ -539,11 +814,9 @@ int rs_ccd_first_contact(rs_ccd *c, const double *start, const double *velocity,
     const double ell = o.reference_length > 0.0 ? o.reference_length : mel;
     const double gap_abs = o.gap * ell;
     double vmax = 0.0;
-    double blo[3] = {INFINITY, INFINITY, INFINITY}, bhi[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (int v = 0; v < nv; ++v) {
-      const double *u = velocity + 3 * (size_t)v, *p = start + 3 * (size_t)v;
+      const double *u = velocity + 3 * (size_t)v;
       vmax = std::fmax(vmax, std::sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]));
-      for (int k = 0; k < 3; ++k) blo[k] = std::fmin(blo[k], p[k]), bhi[k] = std::fmax(bhi[k], p[k]);
     }
     const double t1 = vmax > 0.0 ? mel / vmax : INFINITY;
     c->start.upload(reinterpret_cast<const double3 *>(start), nv, s);
@@ -551,84 +824,26 @@ int rs_ccd_first_contact(rs_ccd *c, const double *start, const double *velocity,
     speed_kernel<<<blocks(nv, 256), 256, 0, s>>>(nv, c->vel.p, c->speed.p);
     RSG_LAUNCHED(ctx, "ccd speed");
     const double h = 0.5 * gap_abs * (1.0 + 1e-6);
-    unsigned long long *best = c->scratch.p, *tally = c->scratch.p + 1;
-    int *overflow = reinterpret_cast<int *>(c->scratch.p + 5);
-    RSG_CUDA("ccd", cudaMemsetAsync(c->scratch.p, 0, 8 * sizeof(unsigned long long), s));
-    unsigned long long tally_h[4] = {0, 0, 0, 0};
-    int64_t windows = 0, pairs_total = 0, close = 0, touching = 0, evals = 0, contact = 0;
+    RSG_CUDA("ccd", cudaMemsetAsync(c->scratch.p, 0, c->scratch.bytes(), s));
+    const uint8_t *band = c->has_band ? c->band.p : nullptr;
+    int64_t windows = 0, pairs_total = 0, close = 0, touching = 0, exempt = 0, evals = 0, contact = 0;
     double tau = tau_end, lo = 0.0, hi = std::fmin(t1, tau_end);
     const unsigned long long kInf = 0x7FF0000000000000ull;
     for (;;) {
       if (vmax == 0.0) hi = 0.0;
       windows += 1;
-      reset_kernel<<<1, 32, 0, s>>>(best, tally);
+      const Params P = make_params(c, gap_abs, o.close_factor, o.max_iterations, h, lo, hi, band);
+      reset_kernel<<<1, 32, 0, s>>>(P.best, P.tally);
       RSG_LAUNCHED(ctx, "ccd reset");
       vbox_kernel<<<blocks(nv, 256), 256, 0, s>>>(nv, c->start.p, c->vel.p, lo, hi, c->vbox.p);
       RSG_LAUNCHED(ctx, "ccd boxes");
-      // the Morton grid spans the sweep of the window (any grid gives the same pairs)
       double3 gl, gs;
-      {
-        const double ext = vmax * hi + h;
-        double l3[3], s3[3];
-        for (int k = 0; k < 3; ++k) {
-          l3[k] = blo[k] - ext;
-          const double w = (bhi[k] + ext) - l3[k];
-          s3[k] = w > 0.0 ? 1023.0 / w : 0.0;
-        }
-        gl = make_double3(l3[0], l3[1], l3[2]);
-        gs = make_double3(s3[0], s3[1], s3[2]);
-      }
-      for (int kind = 0; kind < 2; ++kind) {
-        TreeBufs &T = kind == 0 ? c->ft : c->et;
-        const int n = T.n;
-        if (kind == 0)
-          prim_box_kernel<3><<<blocks(n, 256), 256, 0, s>>>(n, c->faces.p, c->vbox.p, h, gl, gs, T.box.p, T.key.p,
-                                                            T.idx.p);
-        else
-          prim_box_kernel<2><<<blocks(n, 256), 256, 0, s>>>(n, c->edges.p, c->vbox.p, h, gl, gs, T.box.p, T.key.p,
-                                                            T.idx.p);
-        RSG_LAUNCHED(ctx, "ccd primitive boxes");
-        size_t tb = c->cub_tmp.n;
-        RSG_CUDA("ccd", cub::DeviceRadixSort::SortPairs(c->cub_tmp.p, tb, T.key.p, T.key_sorted.p, T.idx.p,
-                                                        T.order.p, n, 0, 30, s));
-        ctx->launches++;
-        gather_boxes_kernel<<<blocks(n, 256), 256, 0, s>>>(n, T.order.p, T.box.p, T.sbox.p);
-        RSG_LAUNCHED(ctx, "ccd gather");
-        level0_kernel<<<blocks(T.len[0], 128), 128, 0, s>>>(T.len[0], T.sbox.p, n, T.levels.p);
-        RSG_LAUNCHED(ctx, "ccd tree level");
-        for (size_t k = 1; k < T.off.size(); ++k) {
-          level_kernel<<<blocks(T.len[k], 128), 128, 0, s>>>(T.len[k], T.levels.p + T.off[k - 1], T.len[k - 1],
-                                                               T.levels.p + T.off[k]);
-          RSG_LAUNCHED(ctx, "ccd tree level");
-        }
-      }
-      Params P{c->start.p, c->vel.p, c->speed.p, c->faces.p, c->edges.p, c->vbox.p, c->et.box.p,
-               nv, c->ne, o.max_iterations, gap_abs, o.close_factor, h, lo, hi, best, tally, overflow};
-      // broad phase: count the candidates of every query, offsets by an exclusive sum
-      unsigned long long *cnt_vt = c->count.p, *cnt_ee = c->count.p + nv + 1;
-      unsigned long long *off_vt = c->offs.p, *off_ee = c->offs.p + nv + 1;
-      RSG_CUDA("ccd", cudaMemsetAsync(c->count.p, 0, c->count.bytes(), s));
-      walk_kernel<0, false><<<blocks(nv, 128), 128, 0, s>>>(P, c->ft.view(), cnt_vt, nullptr, nullptr);
-      RSG_LAUNCHED(ctx, "ccd walk");
-      walk_kernel<1, false><<<blocks(c->ne, 128), 128, 0, s>>>(P, c->et.view(), cnt_ee, nullptr, nullptr);
-      RSG_LAUNCHED(ctx, "ccd walk");
-      for (int kind = 0; kind < 2; ++kind) {
-        size_t tb = c->cub_tmp.n;
-        const int nq = kind == 0 ? nv : c->ne;
-        RSG_CUDA("ccd", cub::DeviceScan::ExclusiveSum(c->cub_tmp.p, tb, kind == 0 ? cnt_vt : cnt_ee,
-                                                      kind == 0 ? off_vt : off_ee, nq + 1, s));
-        ctx->launches++;
-      }
-      unsigned long long tot[2];
-      RSG_CUDA("ccd", rsg::copy_async(&tot[0], off_vt + nv, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-      RSG_CUDA("ccd", rsg::copy_async(&tot[1], off_ee + c->ne, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-      RSG_CUDA("ccd", cudaStreamSynchronize(s));
-      const unsigned long long n_vt = tot[0], n_ee = tot[1];
-      if (n_vt + n_ee > c->pairs.n) c->pairs.alloc((size_t)((n_vt + n_ee) * 5 / 4 + 1024));
-      walk_kernel<0, true><<<blocks(nv, 128), 128, 0, s>>>(P, c->ft.view(), nullptr, off_vt, c->pairs.p);
-      RSG_LAUNCHED(ctx, "ccd walk");
-      walk_kernel<1, true><<<blocks(c->ne, 128), 128, 0, s>>>(P, c->et.view(), nullptr, off_ee, c->pairs.p + n_vt);
-      RSG_LAUNCHED(ctx, "ccd walk");
+      morton_grid(start, nv, vmax * hi + h, gl, gs);
+      build_tree(c, c->ft, 0, h, gl, gs, s);
+      build_tree(c, c->et, 1, h, gl, gs, s);
+      // broad phase: the candidate pairs of both kinds, vertex-face first
+      const unsigned long long n_vt = collect<0>(c, P, c->ft.view(), nv, 0, false, s);
+      const unsigned long long n_ee = collect<1>(c, P, c->et.view(), c->ne, n_vt, true, s);
       // narrow phase, one thread per candidate pair
       if (n_vt) {
         narrow_kernel<0><<<blocks((long long)n_vt, 128), 128, 0, s>>>(P, c->pairs.p, n_vt);
@@ -641,11 +856,10 @@ int rs_ccd_first_contact(rs_ccd *c, const double *start, const double *velocity,
       unsigned long long res[8];
       c->scratch.download(res, 8, s);
       RSG_CUDA("ccd", cudaStreamSynchronize(s));
-      if (reinterpret_cast<int *>(res + 5)[0]) fail(RS_INTERNAL, "Internal", "ccd", "box tree stack overflow");
-      for (int k = 0; k < 4; ++k) tally_h[k] = res[1 + k];
-      pairs_total += (int64_t)tally_h[0];
-      evals += (int64_t)tally_h[3];
-      if (lo == 0.0) close = (int64_t)tally_h[1], touching = (int64_t)tally_h[2];
+      if (reinterpret_cast<int *>(res + 6)[0]) fail(RS_INTERNAL, "Internal", "ccd", "box tree stack overflow");
+      pairs_total += (int64_t)res[1];
+      evals += (int64_t)res[4];
+      if (lo == 0.0) close = (int64_t)res[2], touching = (int64_t)res[3], exempt = (int64_t)res[5];
       if (res[0] != kInf) {
         double b;
         std::memcpy(&b, &res[0], sizeof(b));
@@ -659,9 +873,9 @@ int rs_ccd_first_contact(rs_ccd *c, const double *start, const double *velocity,
       if (hi <= lo) break;
     }
     *tau_max = tau;
-    if (report6) {
-      report6[0] = contact, report6[1] = windows, report6[2] = pairs_total;
-      report6[3] = close, report6[4] = touching, report6[5] = evals;
+    if (report7) {
+      report7[0] = contact, report7[1] = windows, report7[2] = pairs_total, report7[3] = close;
+      report7[4] = touching, report7[5] = exempt, report7[6] = evals;
     }
     c->last_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_begin).count();
   });

@@ -420,7 +420,10 @@ int rs_flow_step(rs_flow *F, double *report) {
       co.gap = F->o.ccd_gap, co.reference_length = F->l0;
       co.max_iterations = F->o.ccd_max_iterations, co.close_factor = F->o.ccd_close_factor;
       double tmax = 0.0;
-      int64_t cr[6] = {0, 0, 0, 0, 0, 0};
+      int64_t cr[7] = {0, 0, 0, 0, 0, 0, 0}, band_pairs = 0, band_vertices = 0;
+      // the faces that intersect at the start of the step exempt their neighbourhood
+      // (IntersectionBand, session.rs:917-928); empty for an embedded mesh
+      check(rs_ccd_set_band(F->ccd, F->pos.data(), &band_pairs, &band_vertices), "flow (ccd)");
       check(rs_ccd_first_contact(F->ccd, F->pos.data(), vel.data(), tau, &co, &tmax, cr), "flow (ccd)");
       if (cr[0]) tau = std::min(tau, 2.0 / 3.0 * tmax);
       rep[27] = tmax;

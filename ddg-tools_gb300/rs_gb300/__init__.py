@@ -90,6 +90,8 @@ def load_library(path: str | os.PathLike | None = None):
         "rs_ccd_create": [_vp, C.c_int, C.c_int, _u32p, C.POINTER(_vp)],
         "rs_ccd_first_contact": [_vp, _f64p, _f64p, C.c_double, C.POINTER(CcdOptions), _dp, _i64p],
         "rs_ccd_last_seconds": [_vp, _dp],
+        "rs_ccd_set_band": [_vp, C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
+        "rs_ccd_intersecting_pairs": [_vp, _f64p, C.c_int64, _u32p, C.POINTER(C.c_int64)],
         "rs_device_info": [C.c_int, C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                            C.POINTER(C.c_uint64)],
         "rs_ctx_create": [C.c_int, C.POINTER(_vp)],
@@ -752,7 +754,8 @@ class CcdSurface:
     RS/src/ccd.rs:762-884, without obstacles and without the exempt band): the topology lives
     on the device, each ``first_contact`` call sweeps one linear motion."""
 
-    REPORT_KEYS = ["contact", "windows", "pairs_tested", "close_pairs", "touching_pairs", "evaluations"]
+    REPORT_KEYS = ["contact", "windows", "pairs_tested", "close_pairs", "touching_pairs", "exempt_pairs",
+                   "evaluations"]
 
     def __init__(self, faces, n_vertices: int, ctx: Context | None = None):
         self.ctx = ctx or default_context()
@@ -774,10 +777,36 @@ class CcdSurface:
             raise RsError(1, "InvalidOption", "ccd", "start and velocity need one vector per vertex")
         o = options or ccd_options()
         tau = C.c_double()
-        rep = np.zeros(6, np.int64)
+        rep = np.zeros(7, np.int64)
         _check(_lib.rs_ccd_first_contact(self._h, start.ravel(), vel.ravel(), float(tau_end), C.byref(o),
                                          C.byref(tau), rep))
         return {"tau_max": tau.value, **{k: int(v) for k, v in zip(self.REPORT_KEYS, rep)}}
+
+    def set_band(self, positions) -> tuple[int, int]:
+        """The exempt band of `positions` for the following calls (IntersectionBand::new,
+        RS/src/ccd.rs:1292-1319); None clears it. Returns (intersecting pairs, band vertices)."""
+        npairs, nverts = C.c_int64(), C.c_int64()
+        if positions is None:
+            _check(_lib.rs_ccd_set_band(self._h, None, C.byref(npairs), C.byref(nverts)))
+        else:
+            p = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+            if len(p) != self.n_vertices:
+                raise RsError(1, "InvalidOption", "ccd", "positions need one vector per vertex")
+            _check(_lib.rs_ccd_set_band(self._h, p.ctypes.data_as(C.c_void_p), C.byref(npairs), C.byref(nverts)))
+        return npairs.value, nverts.value
+
+    def intersecting_pairs(self, positions) -> np.ndarray:
+        """The intersecting face pairs (f < g), sorted (intersecting_pairs, RS/src/ccd.rs:1229-1279)."""
+        p = np.ascontiguousarray(positions, dtype=np.float64).reshape(-1, 3)
+        if len(p) != self.n_vertices:
+            raise RsError(1, "InvalidOption", "ccd", "positions need one vector per vertex")
+        n = C.c_int64()
+        out = np.zeros(2 * 1024, np.uint32)
+        _check(_lib.rs_ccd_intersecting_pairs(self._h, p.ravel(), len(out) // 2, out, C.byref(n)))
+        if n.value > len(out) // 2:
+            out = np.zeros(2 * n.value, np.uint32)
+            _check(_lib.rs_ccd_intersecting_pairs(self._h, p.ravel(), n.value, out, C.byref(n)))
+        return out[: 2 * n.value].reshape(-1, 2)
 
     def last_seconds(self) -> float:
         t = C.c_double()

@@ -379,12 +379,21 @@ void rs_ccd_free(rs_ccd *c);
  * V x 3) on [0, tau_end], against itself: the largest tau_max <= tau_end that keeps every
  * vertex-triangle pair (vertex not in the triangle) and every edge-edge pair without a common
  * vertex at distance >= gap (pairs closer at t = 0: >= close_factor times their distance;
- * touching pairs unconstrained). No obstacles and no exempt band of self-intersecting inputs.
- * tau_max is bitwise the crate's. report6 (may be NULL): contact found (0/1), windows,
- * candidate pairs tested, close pairs, touching pairs, distance evaluations (the last
- * depends on the order pairs are met and is not the crate's count). */
+ * touching pairs unconstrained). With a band set (rs_ccd_set_band) a pair whose two elements
+ * both have a vertex in the band is exempt (first_contact_with_band, ccd.rs:781-884). No
+ * obstacles. tau_max is bitwise the crate's. report7 (may be NULL): contact found (0/1),
+ * windows, candidate pairs tested, close pairs, touching pairs, exempt pairs, distance
+ * evaluations (the last depends on the order pairs are met and is not the crate's count). */
 int rs_ccd_first_contact(rs_ccd *c, const double *start, const double *velocity, double tau_end,
-                         const rs_ccd_options *o, double *tau_max, int64_t *report6);
+                         const rs_ccd_options *o, double *tau_max, int64_t *report7);
+/* IntersectionBand::new (ccd.rs:1292-1319) of `positions` (V x 3, host), kept for the following
+ * rs_ccd_first_contact calls: the vertices of the intersecting faces widened by one ring. NULL
+ * positions clear it. n_pairs: intersecting face pairs; n_vertices: band vertices (0: the mesh
+ * is embedded and nothing is exempt). */
+int rs_ccd_set_band(rs_ccd *c, const double *positions, int64_t *n_pairs, int64_t *n_vertices);
+/* intersecting_pairs (ccd.rs:1229-1279): the face pairs (f, g), f < g, that intersect, sorted;
+ * up to cap pairs are written to out (2 per pair), *n is their number. */
+int rs_ccd_intersecting_pairs(rs_ccd *c, const double *positions, int64_t cap, uint32_t *out, int64_t *n);
 /* Wall seconds of the last rs_ccd_first_contact. No counterpart in the crate. */
 int rs_ccd_last_seconds(rs_ccd *c, double *seconds);
 
@@ -407,8 +416,8 @@ int rs_ccd_last_seconds(rs_ccd *c, double *seconds);
  *     solve/schur.rs:450-461), 26 energy at the accepted trial, before the projection,
  *  27 tau_max of the collision detection (NaN when it is off), 28 its seconds.
  * With ccd on, the first trial is min(tau0, 2/3 tau_max) when the motion x -> x - t d meets a
- * contact before tau0 (session.rs:927-955; reference length the initial mean edge length).
- * The exempt band of a self-intersecting start and the projection guard are not applied. */
+ * contact before tau0 (session.rs:927-955; reference length the initial mean edge length),
+ * with the exempt band of the step's start positions. The projection guard is not applied. */
 int rs_flow_step(rs_flow *f, double *report);
 /* The current positions (V x 3). */
 int rs_flow_positions(rs_flow *f, double *positions_host);

@@ -126,12 +126,18 @@ int rso_vfrac_stats(const rso_vfrac *h, int64_t *out5);
 int rso_vfrac_apply(const rso_vfrac *h, int nb, const double *xs, double *ys);
 
 /* first_contact of a mesh moving against itself, start + t velocity on [0, tau_end]
- * (RS/src/ccd.rs:762-884; no obstacles, no exempt band). gap, max_iterations and close_factor
- * are CcdOptions (ccd.rs:86-111); reference_length 0 takes the mean edge length of start.
- * out5: contact found (0/1), windows, candidate pairs tested, close pairs, touching pairs. */
+ * (RS/src/ccd.rs:762-884; no obstacles), with the exempt band of the start positions when
+ * use_band (first_contact_with_band, ccd.rs:781-884). gap, max_iterations and close_factor are
+ * CcdOptions (ccd.rs:86-111); reference_length 0 takes the mean edge length of start.
+ * out7: contact found (0/1), windows, candidate pairs tested, close pairs, touching pairs,
+ * exempt pairs, band vertices. */
 int rso_ccd_first_contact(int nv, const double *start, int nf, const uint32_t *faces,
                           const double *velocity, double tau_end, double gap, double reference_length,
-                          int max_iterations, double close_factor, double *tau_max, int64_t *out5);
+                          int max_iterations, double close_factor, int use_band, double *tau_max,
+                          int64_t *out7);
+/* intersecting_pairs (ccd.rs:1229-1279): sorted (f, g) pairs, up to cap written to out. */
+int rso_ccd_intersecting_pairs(int nv, const double *pos, int nf, const uint32_t *faces, int64_t cap,
+                               uint32_t *out, int64_t *n);
 const char *rso_ccd_last_error(void);
 /* The smallest vertex-triangle / edge-edge distance over the pairs CCD constrains. */
 int rso_ccd_min_distance(int nv, const double *pos, int nf, const uint32_t *faces, double *out);

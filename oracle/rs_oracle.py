@@ -296,24 +296,25 @@ class VertexFractionalTree:
 
 
 def ccd_first_contact(faces, start, velocity, tau_end, gap=0.05, reference_length=0.0, max_iterations=100,
-                      close_factor=0.5) -> dict:
+                      close_factor=0.5, band=False) -> dict:
     """first_contact of the mesh moving as start + t velocity on [0, tau_end], against itself
-    (RS/src/ccd.rs:762-884; no obstacles, no exempt band). reference_length 0: the mean edge
-    length of start."""
+    (RS/src/ccd.rs:762-884; no obstacles); with band, the exempt band of the start positions
+    (first_contact_with_band). reference_length 0: the mean edge length of start."""
     start, faces = _mesh(start, faces)
     vel = np.ascontiguousarray(velocity, dtype=np.float64).reshape(-1, 3)
     L = lib()
     L.rso_ccd_first_contact.argtypes = [C.c_int, _f64p, C.c_int, _u32p, _f64p, C.c_double, C.c_double,
-                                        C.c_double, C.c_int, C.c_double, C.POINTER(C.c_double), _i64p]
+                                        C.c_double, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_double), _i64p]
     L.rso_ccd_last_error.restype = C.c_char_p
     tau = C.c_double()
-    out = np.zeros(5, np.int64)
+    out = np.zeros(7, np.int64)
     code = L.rso_ccd_first_contact(len(start), start.ravel(), len(faces), faces.ravel(), vel.ravel(),
                                    float(tau_end), float(gap), float(reference_length), int(max_iterations),
-                                   float(close_factor), C.byref(tau), out)
+                                   float(close_factor), int(bool(band)), C.byref(tau), out)
     if code != 0:
         raise OracleError(code, L.rso_ccd_last_error().decode())
-    keys = ["contact", "windows", "pairs_tested", "close_pairs", "touching_pairs"]
+    keys = ["contact", "windows", "pairs_tested", "close_pairs", "touching_pairs", "exempt_pairs",
+            "band_vertices"]
     return {"tau_max": tau.value, **{k: int(v) for k, v in zip(keys, out)}}
 
 
@@ -327,3 +328,21 @@ def ccd_min_distance(pos, faces) -> float:
     if code != 0:
         raise OracleError(code, L.rso_ccd_last_error().decode())
     return d.value
+
+
+def ccd_intersecting_pairs(pos, faces) -> np.ndarray:
+    """The intersecting face pairs (f < g), sorted (intersecting_pairs, RS/src/ccd.rs:1229-1279)."""
+    pos, faces = _mesh(pos, faces)
+    L = lib()
+    L.rso_ccd_intersecting_pairs.argtypes = [C.c_int, _f64p, C.c_int, _u32p, C.c_int64, _u32p,
+                                             C.POINTER(C.c_int64)]
+    n = C.c_int64()
+    out = np.zeros(2 * max(len(faces), 16), np.uint32)
+    code = L.rso_ccd_intersecting_pairs(len(pos), pos.ravel(), len(faces), faces.ravel(), len(out) // 2, out,
+                                        C.byref(n))
+    if code != 0:
+        raise OracleError(code, L.rso_ccd_last_error().decode())
+    if n.value > len(out) // 2:
+        out = np.zeros(2 * n.value, np.uint32)
+        L.rso_ccd_intersecting_pairs(len(pos), pos.ravel(), len(faces), faces.ravel(), n.value, out, C.byref(n))
+    return out[: 2 * n.value].reshape(-1, 2)

@@ -104,7 +104,7 @@ double lipschitz(const std::vector<v3> &ua, const std::vector<v3> &ub) {
 constexpr double kMargin = 1.0 + 1e-12;  // ccd.rs:498-499
 
 struct Tally {
-  int64_t pairs = 0, close = 0, touching = 0;
+  int64_t pairs = 0, close = 0, touching = 0, exempt = 0;
 };
 
 // Conservative advancement of one pair on [lo, hi] (ccd.rs:529-592); NaN for "none".
@@ -173,7 +173,8 @@ struct Result {
 // All pairs of one window (ccd.rs:887-1045 without obstacles and band).
 Result window(const std::vector<tri> &faces, const std::vector<std::pair<uint32_t, uint32_t>> &edges,
               const std::vector<v3> &start, const std::vector<v3> &vel, const std::vector<double> &speed,
-              double gap_abs, int max_iterations, double close_factor, double lo, double hi) {
+              double gap_abs, int max_iterations, double close_factor, double lo, double hi,
+              const uint8_t *band) {
   const size_t nv = start.size(), nf = faces.size(), ne = edges.size();
   const double h = 0.5 * gap_abs * (1.0 + 1e-6);
   std::vector<Box> vbox(nv), fbox(nf), ebox(ne);
@@ -202,6 +203,10 @@ Result window(const std::vector<tri> &faces, const std::vector<std::pair<uint32_
       if (!overlaps(fbox[f], q)) continue;
       const tri &t = faces[f];
       if (t[0] == v || t[1] == v || t[2] == v) continue;
+      if (band && band[v] && (band[t[0]] || band[t[1]] || band[t[2]])) {  // ccd.rs:947-950
+        out.tally.exempt += 1;
+        continue;
+      }
       const v3 p = start[v], u = vel[v];
       const v3 tp[3] = {at(start[t[0]], vel[t[0]], 0.0), at(start[t[1]], vel[t[1]], 0.0),
                         at(start[t[2]], vel[t[2]], 0.0)};
@@ -224,6 +229,10 @@ Result window(const std::vector<tri> &faces, const std::vector<std::pair<uint32_
       if (!overlaps(ebox[e2], q)) continue;
       const uint32_t c = edges[e2].first, d = edges[e2].second;
       if (c == a || c == b || d == a || d == b) continue;
+      if (band && (band[a] || band[b]) && (band[c] || band[d])) {  // ccd.rs:1001-1004
+        out.tally.exempt += 1;
+        continue;
+      }
       const v3 pp[2] = {start[a], start[b]}, uu[2] = {vel[a], vel[b]};
       const v3 qq[2] = {start[c], start[d]}, ww[2] = {vel[c], vel[d]};
       const double lc = (fmax_(speed[a], speed[b]) + fmax_(speed[c], speed[d])) * kMargin;
@@ -236,6 +245,90 @@ Result window(const std::vector<tri> &faces, const std::vector<std::pair<uint32_
     }
   }
   return out;
+}
+
+// ---- static queries (ccd.rs:1153-1215) ----
+
+double orient(v3 a, v3 b, v3 c, v3 d) { return dot(cross(sub(b, a), sub(c, a)), sub(d, a)); }
+
+bool segment_meets_triangle(v3 p, v3 q, const v3 (&t)[3]) {  // ccd.rs:1158-1186
+  const v3 a = t[0], b = t[1], c = t[2];
+  const double d1 = orient(a, b, c, p), d2 = orient(a, b, c, q);
+  if ((d1 > 0.0 && d2 > 0.0) || (d1 < 0.0 && d2 < 0.0)) return false;
+  const double n = norm(cross(sub(b, a), sub(c, a)));
+  const double len = fmax_(fmax_(fmax_(norm(sub(q, p)), norm(sub(b, a))), norm(sub(c, a))), norm(sub(c, b)));
+  const double flat = 1e-12 * n * len;
+  if (std::fabs(d1) <= flat && std::fabs(d2) <= flat) {
+    const double eps = 1e-14 * (norm(sub(b, a)) + norm(sub(c, a)));
+    return point_triangle_distance(p, a, b, c) <= eps || point_triangle_distance(q, a, b, c) <= eps ||
+           segment_segment_distance(p, q, a, b) <= eps || segment_segment_distance(p, q, b, c) <= eps ||
+           segment_segment_distance(p, q, c, a) <= eps;
+  }
+  const double s1 = orient(p, q, a, b), s2 = orient(p, q, b, c), s3 = orient(p, q, c, a);
+  return (s1 >= 0.0 && s2 >= 0.0 && s3 >= 0.0) || (s1 <= 0.0 && s2 <= 0.0 && s3 <= 0.0);
+}
+
+bool triangles_intersect(const v3 (&t1)[3], const v3 (&t2)[3]) {  // ccd.rs:1188-1191
+  for (int k = 0; k < 3; ++k)
+    if (segment_meets_triangle(t1[k], t1[(k + 1) % 3], t2)) return true;
+  for (int k = 0; k < 3; ++k)
+    if (segment_meets_triangle(t2[k], t2[(k + 1) % 3], t1)) return true;
+  return false;
+}
+
+// intersecting_pairs (ccd.rs:1229-1279): pairs f < g whose corner hulls overlap and that
+// intersect (no common vertex), or whose one common vertex's opposite edge meets the other
+// face; sorted. The candidate set is that of the reference's box tree (every element box is
+// tested), enumerated by brute force.
+std::vector<std::pair<uint32_t, uint32_t>> intersecting_pairs(const std::vector<tri> &faces,
+                                                              const std::vector<v3> &p) {
+  const size_t nf = faces.size();
+  std::vector<Box> box(nf);
+  for (size_t f = 0; f < nf; ++f) {
+    Box b{{INFINITY, INFINITY, INFINITY}, {-INFINITY, -INFINITY, -INFINITY}};
+    for (int c = 0; c < 3; ++c)
+      for (int k = 0; k < 3; ++k)
+        b.lo[k] = fmin_(b.lo[k], p[faces[f][c]][k]), b.hi[k] = fmax_(b.hi[k], p[faces[f][c]][k]);
+    box[f] = b;
+  }
+  std::vector<std::pair<uint32_t, uint32_t>> out;
+  for (uint32_t f = 0; f < nf; ++f)
+    for (uint32_t g = f + 1; g < nf; ++g) {
+      if (!overlaps(box[g], box[f])) continue;
+      const tri &a = faces[f], &b = faces[g];
+      int common[3], n_common = 0;
+      for (int i = 0; i < 3; ++i)
+        if (b[0] == a[i] || b[1] == a[i] || b[2] == a[i]) common[n_common++] = i;
+      const v3 tf[3] = {p[a[0]], p[a[1]], p[a[2]]}, tg[3] = {p[b[0]], p[b[1]], p[b[2]]};
+      bool hit = false;
+      if (n_common == 0) {
+        hit = triangles_intersect(tf, tg);
+      } else if (n_common == 1) {
+        const int i = common[0];
+        int j = 0;
+        while (b[j] != a[i]) ++j;
+        hit = segment_meets_triangle(p[a[(i + 1) % 3]], p[a[(i + 2) % 3]], tg) ||
+              segment_meets_triangle(p[b[(j + 1) % 3]], p[b[(j + 2) % 3]], tf);
+      }
+      if (hit) out.push_back({f, g});
+    }
+  return out;
+}
+
+// IntersectionBand::new (ccd.rs:1292-1319): the vertices of the intersecting faces, widened by
+// one ring over the edges.
+std::vector<uint8_t> intersection_band(const std::vector<tri> &faces,
+                                       const std::vector<std::pair<uint32_t, uint32_t>> &edges,
+                                       const std::vector<std::pair<uint32_t, uint32_t>> &pairs, size_t nv) {
+  std::vector<uint8_t> core(nv, 0);
+  for (auto [f, g] : pairs)
+    for (uint32_t fid : {f, g})
+      for (int c = 0; c < 3; ++c) core[faces[fid][c]] = 1;
+  std::vector<uint8_t> band = core;
+  if (!pairs.empty())
+    for (auto [a, b] : edges)
+      if (core[a] || core[b]) band[a] = band[b] = 1;
+  return band;
 }
 
 }  // namespace
@@ -252,9 +345,13 @@ static int rso_fail(int code, const char *message) {
 
 extern "C" const char *rso_ccd_last_error(void) { return g_ccd_err.c_str(); }
 
+// first_contact_with_band (ccd.rs:781-884) when use_band: the band of the start positions
+// (IntersectionBand::new; empty for an embedded mesh, which changes nothing).
+// out7: contact, windows, pairs tested, close pairs, touching pairs, exempt pairs, band vertices.
 extern "C" int rso_ccd_first_contact(int nv, const double *start, int nf, const uint32_t *faces,
                                      const double *velocity, double tau_end, double gap, double reference_length,
-                                     int max_iterations, double close_factor, double *tau_max, int64_t *out5) {
+                                     int max_iterations, double close_factor, int use_band, double *tau_max,
+                                     int64_t *out7) {
   // CcdOptions::validate (ccd.rs:126-153) and first_contact's own checks (ccd.rs:820-835)
   if (!(std::isfinite(gap) && gap > 0.0)) return rso_fail(1, "ccd.gap must be finite and positive");
   if (!(std::isfinite(reference_length) && reference_length >= 0.0))
@@ -284,6 +381,13 @@ extern "C" int rso_ccd_first_contact(int nv, const double *start, int nf, const 
   std::sort(edges.begin(), edges.end());
   edges.erase(std::unique(edges.begin(), edges.end()), edges.end());
   if (edges.empty()) return rso_fail(1, "a surface has edges");
+  std::vector<uint8_t> band;
+  int64_t band_vertices = 0;
+  if (use_band) {
+    band = intersection_band(F, edges, intersecting_pairs(F, p), (size_t)nv);
+    for (uint8_t b : band) band_vertices += b;
+    if (band_vertices == 0) band.clear();  // an empty band is no band (ccd.rs:790-792)
+  }
   const double mel = mean_edge_length(edges, p);
   const double ell = reference_length > 0.0 ? reference_length : mel;
   const double gap_abs = gap * ell;
@@ -291,15 +395,16 @@ extern "C" int rso_ccd_first_contact(int nv, const double *start, int nf, const 
   for (int v = 0; v < nv; ++v) vmax = fmax_(vmax, norm(u[v]));
   const double t1 = vmax > 0.0 ? mel / vmax : INFINITY;
   double lo = 0.0, hi = fmin_(t1, tau_end);
-  int64_t windows = 0, pairs = 0, close = 0, touching = 0;
+  int64_t windows = 0, pairs = 0, close = 0, touching = 0, exempt = 0;
   double tau = tau_end;
   int64_t contact = 0;
   for (;;) {
     if (vmax == 0.0) hi = 0.0;
     windows += 1;
-    const Result r = window(F, edges, p, u, speed, gap_abs, max_iterations, close_factor, lo, hi);
+    const Result r = window(F, edges, p, u, speed, gap_abs, max_iterations, close_factor, lo, hi,
+                            band.empty() ? nullptr : band.data());
     pairs += r.tally.pairs;
-    if (lo == 0.0) close = r.tally.close, touching = r.tally.touching;
+    if (lo == 0.0) close = r.tally.close, touching = r.tally.touching, exempt = r.tally.exempt;
     if (!std::isnan(r.tau)) {
       tau = r.tau;
       contact = 1;
@@ -311,7 +416,25 @@ extern "C" int rso_ccd_first_contact(int nv, const double *start, int nf, const 
     if (hi <= lo) break;
   }
   *tau_max = tau;
-  out5[0] = contact, out5[1] = windows, out5[2] = pairs, out5[3] = close, out5[4] = touching;
+  out7[0] = contact, out7[1] = windows, out7[2] = pairs, out7[3] = close, out7[4] = touching;
+  out7[5] = exempt, out7[6] = band_vertices;
+  return 0;
+}
+
+// intersecting_pairs (ccd.rs:1229-1279) of the positions, sorted; out holds up to cap pairs.
+extern "C" int rso_ccd_intersecting_pairs(int nv, const double *pos, int nf, const uint32_t *faces, int64_t cap,
+                                          uint32_t *out, int64_t *n) {
+  std::vector<v3> p(nv);
+  for (int v = 0; v < nv; ++v) p[v] = {pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]};
+  std::vector<tri> F(nf);
+  for (int f = 0; f < nf; ++f) {
+    F[f] = {faces[3 * f], faces[3 * f + 1], faces[3 * f + 2]};
+    for (int k = 0; k < 3; ++k)
+      if (F[f][k] >= (uint32_t)nv) return rso_fail(1, "face index out of range");
+  }
+  const auto pairs = intersecting_pairs(F, p);
+  *n = (int64_t)pairs.size();
+  for (size_t i = 0; i < pairs.size() && (int64_t)i < cap; ++i) out[2 * i] = pairs[i].first, out[2 * i + 1] = pairs[i].second;
   return 0;
 }
 

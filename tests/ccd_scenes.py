@@ -101,3 +101,54 @@ def torus_sweep(nu=24, nv=12, reach=3.0, seed=5):
     mel = _mean_edge_length(faces, pos)
     vel *= reach * mel / np.linalg.norm(vel, axis=1).max()
     return faces, pos, vel, 1.0, 0.0
+
+
+def _sphere(level, center, radius):
+    from rs_gb300 import generators as gen
+
+    p, f = gen.icosphere(level)
+    return np.asarray(f, np.uint32), np.asarray(center) + radius * np.asarray(p, np.float64)
+
+
+def union(*meshes):
+    faces, pos, n = [], [], 0
+    for f, p in meshes:
+        faces.append(f + n)
+        pos.append(p)
+        n += len(p)
+    return np.concatenate(faces).astype(np.uint32), np.concatenate(pos)
+
+
+def embedded_spheres():
+    """Two level-2 spheres 4 apart moving towards each other (tests/ccd.rs:641-662)."""
+    f, p = union(_sphere(2, [0.0, 0.0, 0.0], 1.0), _sphere(2, [4.0, 0.0, 0.0], 1.0))
+    n = len(p) // 2
+    vel = np.zeros_like(p)
+    vel[:n] = [1.0, 0.0, 0.0]
+    vel[n:] = [-1.0, 0.0, 0.0]
+    return f, p, vel, 3.0, _mean_edge_length(f, p)
+
+
+def overlapping_and_apart():
+    """Overlapping spheres A, B (an intersecting input) and C, D far from them
+    (tests/ccd.rs:664-672); returns faces, positions and the vertex ranges of A, B, C, D."""
+    parts = [_sphere(2, c, 1.0) for c in ([0.0, 0.0, 0.0], [1.2, 0.0, 0.0], [0.0, 0.0, 6.0], [0.0, 0.0, 9.0])]
+    f, p = union(*parts)
+    n = len(parts[0][1])
+    return f, p, [range(k * n, (k + 1) * n) for k in range(4)]
+
+
+def flat_grid(n, seed):
+    """An n x n grid of squares split into triangles, placed in a random plane."""
+    rng = np.random.default_rng(seed)
+    i, j = np.meshgrid(np.arange(n + 1), np.arange(n + 1), indexing="ij")
+    uv = np.stack([i.ravel(), j.ravel()], 1) / n
+    u, w = rng.uniform(-0.5, 0.5, 3), rng.uniform(-0.5, 0.5, 3)
+    pos = 0.3 + uv[:, :1] * u + uv[:, 1:] * w
+    idx = lambda a, b: a * (n + 1) + b
+    faces = []
+    for a in range(n):
+        for b in range(n):
+            faces.append([idx(a, b), idx(a + 1, b), idx(a + 1, b + 1)])
+            faces.append([idx(a, b), idx(a + 1, b + 1), idx(a, b + 1)])
+    return np.asarray(faces, np.uint32), pos

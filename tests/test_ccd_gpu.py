@@ -83,3 +83,45 @@ def test_errors_are_invalid_option():
         c.first_contact(p, bad, 1.0)
     with pytest.raises(R.RsError):
         c.first_contact(p, v, -1.0)
+
+
+def test_intersecting_pairs_and_band_bitwise():
+    f, p, r = S.overlapping_and_apart()
+    ell = S._mean_edge_length(f, p)
+    c = R.CcdSurface(f, len(p))
+    assert c.intersecting_pairs(p).tolist() == O.ccd_intersecting_pairs(p, f).tolist()
+    npairs, nverts = c.set_band(p)
+    assert npairs == len(O.ccd_intersecting_pairs(p, f)) and nverts > 0
+    for k, vz in ((1, 0.4), (2, 1.0)):
+        v = np.zeros_like(p)
+        v[r[k].start:r[k].stop] = [0.0, 0.0, vz]
+        o = O.ccd_first_contact(f, p, v, 3.0, reference_length=ell, band=True)
+        g = c.first_contact(p, v, 3.0, R.ccd_options(reference_length=ell))
+        _same(o, g)
+        assert g["exempt_pairs"] == o["exempt_pairs"] and o["band_vertices"] == nverts
+    c.set_band(None)
+    v = np.zeros_like(p)
+    v[r[1].start:r[1].stop] = [0.0, 0.0, 0.4]
+    _same(O.ccd_first_contact(f, p, v, 1.0, reference_length=ell), c.first_contact(p, v, 1.0, R.ccd_options(reference_length=ell)))
+
+
+def test_band_of_an_embedded_mesh_is_empty():
+    f, p, v, tau_end, ell = S.embedded_spheres()
+    c = R.CcdSurface(f, len(p))
+    assert c.set_band(p) == (0, 0)
+    assert len(c.intersecting_pairs(p)) == 0
+    _same(O.ccd_first_contact(f, p, v, tau_end, reference_length=ell), c.first_contact(p, v, tau_end,
+                                                                                    R.ccd_options(reference_length=ell)))
+
+
+def test_coplanar_and_random_intersections_bitwise():
+    for seed in range(4):
+        f, p = S.flat_grid(12, seed)
+        assert len(R.CcdSurface(f, len(p)).intersecting_pairs(p)) == 0
+    for seed in range(20):
+        f, p, v, tau_end, ell = S.random_soup(2000 + seed, k=12)
+        c = R.CcdSurface(f, len(p))
+        assert c.intersecting_pairs(p).tolist() == O.ccd_intersecting_pairs(p, f).tolist()
+        c.set_band(p)
+        _same(O.ccd_first_contact(f, p, v, tau_end, reference_length=ell, band=True),
+              c.first_contact(p, v, tau_end, R.ccd_options(reference_length=ell)))

@@ -77,3 +77,46 @@ def test_torus_sweep_is_safe_and_uses_windows():
     mel = S._mean_edge_length(f, p)
     assert min(O.ccd_min_distance(p + t * v, f) for t in ts) >= 0.05 * mel * (1 - 1e-6)
     assert r["windows"] >= 1 and r["pairs_tested"] > 0
+
+
+def test_band_of_an_embedded_mesh_changes_nothing():
+    f, p, v, tau_end, ell = S.embedded_spheres()
+    assert len(O.ccd_intersecting_pairs(p, f)) == 0
+    a = O.ccd_first_contact(f, p, v, tau_end, reference_length=ell)
+    b = O.ccd_first_contact(f, p, v, tau_end, reference_length=ell, band=True)
+    assert a["contact"] == 1 and b["band_vertices"] == 0 and b["exempt_pairs"] == 0
+    assert {k: a[k] for k in a if k != "band_vertices"} == {k: b[k] for k in b if k != "band_vertices"}
+
+
+def test_exemption_frees_the_intersection_curve_but_not_other_regions():
+    f, p, r = S.overlapping_and_apart()
+    ell = S._mean_edge_length(f, p)
+    pairs = O.ccd_intersecting_pairs(p, f)
+    assert len(pairs) > 0
+    nf_sphere = len(f) // 4
+    assert (pairs < 2 * nf_sphere).all()  # only faces of A and B intersect
+    # B slides along A: the plain CCD stops it at once, the band frees it
+    v = np.zeros_like(p)
+    v[r[1].start:r[1].stop] = [0.0, 0.0, 0.4]
+    plain = O.ccd_first_contact(f, p, v, 1.0, reference_length=ell)
+    banded = O.ccd_first_contact(f, p, v, 1.0, reference_length=ell, band=True)
+    assert banded["exempt_pairs"] > 0 and banded["band_vertices"] > 0
+    assert banded["tau_max"] > plain["tau_max"]
+    # C moves into D: the contact is that of C and D alone
+    v = np.zeros_like(p)
+    v[r[2].start:r[2].stop] = [0.0, 0.0, 1.0]
+    banded = O.ccd_first_contact(f, p, v, 3.0, reference_length=ell, band=True)
+    fc, pc = S.union(S._sphere(2, [0.0, 0.0, 6.0], 1.0), S._sphere(2, [0.0, 0.0, 9.0], 1.0))
+    vc = np.zeros_like(pc)
+    vc[: len(pc) // 2] = [0.0, 0.0, 1.0]
+    alone = O.ccd_first_contact(fc, pc, vc, 3.0, reference_length=ell)
+    assert alone["contact"] == 1 and banded["contact"] == 1
+    assert abs(banded["tau_max"] - alone["tau_max"]) < 1e-6 * alone["tau_max"]
+
+
+def test_coplanar_neighbours_do_not_intersect():
+    hits = sum(len(O.ccd_intersecting_pairs(*reversed(S.flat_grid(12, seed)))) for seed in range(10))
+    assert hits == 0
+    f, p = S.soup([[[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0]],
+                   [[0.2, 0.2, 0.0], [1.2, 0.2, 0.0], [0.2, 1.2, 0.0]]])
+    assert O.ccd_intersecting_pairs(p, f).tolist() == [[0, 1]]

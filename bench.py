@@ -379,6 +379,21 @@ def bench_flow(args, rank, world, local):
                                   "GMRES capped at 100 iterations before the plain fallback"}
     except R.RsError as e:
         learned = {"error": str(e)}
+    # one step with the collision cap of the line search (rs_flow_options.ccd, the crate's
+    # default line search) on the current surface: its cost inside a step
+    with_ccd = None
+    try:
+        o = flow_options(R)
+        o.ccd = 1
+        fc = R.Flow(F, Q, o, ctx)
+        rc = fc.step()
+        with_ccd = {"seconds_step": rc["seconds"], "seconds_ccd": rc["seconds_ccd"],
+                    "tau_ccd": rc["tau_ccd"], "tau0": rc["tau0"], "accepted": rc["accepted"],
+                    "note": "one step after the timed region; band of the start, then first contact "
+                            "of x - t d on [0, tau0]"}
+        del fc
+    except R.RsError as e:
+        with_ccd = {"error": str(e)}
     # phases of one step's solve (three right-hand sides) on the current surface
     solve_phases = None
     try:
@@ -453,6 +468,7 @@ def bench_flow(args, rank, world, local):
                         "frac": (FLOP_PER_INTERACTION * n_int / (t_pair * 1e-3) / 1e12 / peak) if t_pair else None},
         "solve_phases_ms": solve_phases,
         "learned_preconditioner": learned,
+        "step_with_ccd": with_ccd,
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }

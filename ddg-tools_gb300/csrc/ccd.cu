@@ -345,10 +345,16 @@ __device__ void flush_tally(const Params &P, const Tally &t) {
 // KIND 2 (the band): a face against the face tree of the static hulls, partners g > f
 // (intersecting_pairs, ccd.rs:1229-1279); the intersection test runs per pair afterwards.
 // A pair whose two elements both have a vertex in the band is exempt (ccd.rs:947-950,
-// 1001-1004): it is not a candidate, and the count pass tallies it.
-template <int KIND, bool FILL>
-__global__ void __launch_bounds__(128) walk_kernel(Params P, Tree t, unsigned long long *count,
-                                                   const unsigned long long *off, uint2 *pairs) {
+// 1001-1004): it is not a candidate, and it is counted in `counters[1]`.
+// Candidates are appended as (query, element) to `pairs`: each thread buffers up to 16 and
+// reserves room for them with one atomic add on `counters[0]`; pairs beyond `cap` are not
+// written (the caller grows the list and walks again). The order of the list depends on the
+// atomics; nothing computed from it does (a minimum, and sums of counts).
+constexpr int kAppend = 16;
+
+template <int KIND>
+__global__ void __launch_bounds__(128) walk_kernel(Params P, Tree t, unsigned long long *counters, uint2 *pairs,
+                                                   unsigned long long cap) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   const int nq = KIND == 0 ? P.nv : (KIND == 1 ? P.ne : P.nf);
   if (q >= nq) return;
@@ -356,8 +362,15 @@ __global__ void __launch_bounds__(128) walk_kernel(Params P, Tree t, unsigned lo
   uint32_t a = 0, b = 0;
   if (KIND == 1) a = P.edges[2 * q], b = P.edges[2 * q + 1];
   const bool qband = P.band && (KIND == 0 ? P.band[q] : (KIND == 1 ? (P.band[a] || P.band[b]) : false));
-  unsigned long long w = FILL ? off[q] : 0;
-  uint32_t n = 0, exempt = 0;
+  uint32_t buf[kAppend];
+  int nb = 0;
+  uint32_t exempt = 0;
+  auto flush = [&]() {
+    const unsigned long long base = atomicAdd(counters, (unsigned long long)nb);
+    for (int i = 0; i < nb; ++i)
+      if (base + i < cap) pairs[base + i] = make_uint2((uint32_t)q, buf[i]);
+    nb = 0;
+  };
   const bool ok = query(t, qb, [&](uint32_t el) {
     if (KIND == 0) {
       const uint32_t fa = P.faces[3 * el], fb = P.faces[3 * el + 1], fc = P.faces[3 * el + 2];
@@ -377,14 +390,12 @@ __global__ void __launch_bounds__(128) walk_kernel(Params P, Tree t, unsigned lo
     } else {
       if (el <= (uint32_t)q) return;
     }
-    if (FILL) pairs[w++] = make_uint2((uint32_t)q, el);
-    ++n;
+    buf[nb++] = el;
+    if (nb == kAppend) flush();
   });
+  if (nb) flush();
   if (!ok) atomicExch(P.overflow, 1);
-  if (!FILL) {
-    count[q] = n;
-    if (exempt) atomicAdd(P.tally + 4, (unsigned long long)exempt);
-  }
+  if (exempt) atomicAdd(counters + 1, (unsigned long long)exempt);
 }
 
 // The intersection test of one candidate face pair (f, g), f < g (ccd.rs:1247-1270): faces
@@ -529,8 +540,7 @@ struct rs_ccd {
   DevBuf<double> speed;
   DevBuf<DBox> vbox;
   TreeBufs ft, et;
-  DevBuf<unsigned long long> count;   // candidates per query
-  DevBuf<unsigned long long> offs;    // their exclusive sums
+  DevBuf<unsigned long long> counters;  // appended candidates, exempt pairs (one walk)
   DevBuf<uint2> pairs;                // candidate pairs of a window (or of the band's walk)
   DevBuf<uint8_t> hit, core, band;    // the band: intersection flags per candidate, per vertex
   bool has_band = false;
@@ -580,32 +590,30 @@ void morton_grid(const double *start, int nv, double ext, double3 &gl, double3 &
   gs = make_double3(s3[0], s3[1], s3[2]);
 }
 
-// Candidate pairs of one kind: count, exclusive sum, fill at c->pairs + base. Returns their
-// number (the caller has synchronised nothing; this reads the total back).
+// Candidate pairs of one kind, appended at c->pairs + base by one walk (walked again into a
+// larger list when they did not fit). Returns their number; adds the exempt pairs to *exempt.
 template <int KIND>
 unsigned long long collect(rs_ccd *c, const Params &P, const Tree &t, int nq, unsigned long long base,
-                           bool grow_keep, cudaStream_t s) {
+                           bool grow_keep, cudaStream_t s, int64_t *exempt = nullptr) {
   rs_ctx *ctx = c->ctx;
-  RSG_CUDA("ccd", cudaMemsetAsync(c->count.p, 0, ((size_t)nq + 1) * sizeof(unsigned long long), s));
-  walk_kernel<KIND, false><<<blocks(nq, 128), 128, 0, s>>>(P, t, c->count.p, nullptr, nullptr);
-  RSG_LAUNCHED(ctx, "ccd walk");
-  size_t tb = c->cub_tmp.n;
-  RSG_CUDA("ccd", cub::DeviceScan::ExclusiveSum(c->cub_tmp.p, tb, c->count.p, c->offs.p, nq + 1, s));
-  ctx->launches++;
-  unsigned long long tot = 0;
-  RSG_CUDA("ccd", rsg::copy_async(&tot, c->offs.p + nq, sizeof(tot), cudaMemcpyDeviceToHost, s));
-  RSG_CUDA("ccd", cudaStreamSynchronize(s));
-  if (base + tot > c->pairs.n) {
-    DevBuf<uint2> bigger((size_t)((base + tot) * 5 / 4 + 1024));
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    const unsigned long long cap = c->pairs.n > base ? c->pairs.n - base : 0;
+    RSG_CUDA("ccd", cudaMemsetAsync(c->counters.p, 0, c->counters.bytes(), s));
+    walk_kernel<KIND><<<blocks(nq, 128), 128, 0, s>>>(P, t, c->counters.p, cap ? c->pairs.p + base : nullptr, cap);
+    RSG_LAUNCHED(ctx, "ccd walk");
+    unsigned long long got[2] = {0, 0};
+    RSG_CUDA("ccd", rsg::copy_async(got, c->counters.p, sizeof(got), cudaMemcpyDeviceToHost, s));
+    RSG_CUDA("ccd", cudaStreamSynchronize(s));
+    if (got[0] <= cap) {
+      if (exempt) *exempt += (int64_t)got[1];
+      return got[0];
+    }
+    DevBuf<uint2> bigger((size_t)((base + got[0]) * 5 / 4 + 1024));
     if (grow_keep && base)
       RSG_CUDA("ccd", cudaMemcpyAsync(bigger.p, c->pairs.p, base * sizeof(uint2), cudaMemcpyDeviceToDevice, s));
     c->pairs = std::move(bigger);
   }
-  if (tot) {
-    walk_kernel<KIND, true><<<blocks(nq, 128), 128, 0, s>>>(P, t, nullptr, c->offs.p, c->pairs.p + base);
-    RSG_LAUNCHED(ctx, "ccd walk");
-  }
-  return tot;
+  fail(RS_INTERNAL, "Internal", "ccd", "candidate list did not fit after growing");
 }
 
 Params make_params(rs_ccd *c, double gap_abs, double close_factor, int max_iterations, double h, double lo,
@@ -701,10 +709,8 @@ int rs_ccd_create(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, rs_ccd **o
                                                     c->ft.order.p, nf, 0, 30, s));
     RSG_CUDA("ccd", cub::DeviceRadixSort::SortPairs(nullptr, t2, c->et.key.p, c->et.key_sorted.p, c->et.idx.p,
                                                     c->et.order.p, c->ne, 0, 30, s));
-    const int nq = std::max(std::max(nv, c->ne), nf);
-    c->count.alloc((size_t)nq + 1);
-    c->offs.alloc((size_t)nq + 1);
-    RSG_CUDA("ccd", cub::DeviceScan::ExclusiveSum(nullptr, t3, c->count.p, c->offs.p, nq + 1, s));
+    c->counters.alloc(2);
+    c->pairs.alloc((size_t)8 * (nv + c->ne));  // grown on demand
     c->cub_tmp.alloc(std::max<size_t>(std::max(std::max(t1, t2), t3), 16));
     c->scratch.alloc(8);
     RSG_CUDA("ccd", cudaStreamSynchronize(s));
@@ -842,8 +848,9 @@ int rs_ccd_first_contact(rs_ccd *c, const double *start, const double *velocity,
       build_tree(c, c->ft, 0, h, gl, gs, s);
       build_tree(c, c->et, 1, h, gl, gs, s);
       // broad phase: the candidate pairs of both kinds, vertex-face first
-      const unsigned long long n_vt = collect<0>(c, P, c->ft.view(), nv, 0, false, s);
-      const unsigned long long n_ee = collect<1>(c, P, c->et.view(), c->ne, n_vt, true, s);
+      int64_t exempt_w = 0;
+      const unsigned long long n_vt = collect<0>(c, P, c->ft.view(), nv, 0, false, s, &exempt_w);
+      const unsigned long long n_ee = collect<1>(c, P, c->et.view(), c->ne, n_vt, true, s, &exempt_w);
       // narrow phase, one thread per candidate pair
       if (n_vt) {
         narrow_kernel<0><<<blocks((long long)n_vt, 128), 128, 0, s>>>(P, c->pairs.p, n_vt);
@@ -859,7 +866,7 @@ int rs_ccd_first_contact(rs_ccd *c, const double *start, const double *velocity,
       if (reinterpret_cast<int *>(res + 6)[0]) fail(RS_INTERNAL, "Internal", "ccd", "box tree stack overflow");
       pairs_total += (int64_t)res[1];
       evals += (int64_t)res[4];
-      if (lo == 0.0) close = (int64_t)res[2], touching = (int64_t)res[3], exempt = (int64_t)res[5];
+      if (lo == 0.0) close = (int64_t)res[2], touching = (int64_t)res[3], exempt = exempt_w;
       if (res[0] != kInf) {
         double b;
         std::memcpy(&b, &res[0], sizeof(b));

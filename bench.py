@@ -47,7 +47,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "ddg-tools_gb300"))
 
-FLOP_PER_INTERACTION = 61  # energy + gradient, SURVEY's count (FMA = 2, Kahan not counted)
+FLOP_PER_INTERACTION = 61  # energy + gradient per interaction (FMA = 2; the compensation is not counted)
 
 
 def replica_rate(units, seconds, world, device=None):

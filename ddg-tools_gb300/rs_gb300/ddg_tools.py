@@ -216,6 +216,10 @@ class _Options:
             raise _bad("backend", f"'dense' {_OFF_PATH}: 'hierarchical' or 'auto' run the hierarchical solver")
         if o["device"] == "cpu":
             raise _bad("device", "'cpu' is not served: this library runs on the GPU only; use 'cuda' or 'auto'")
+        if o["gpu_determinism"] == "match_cpu":
+            raise _bad("gpu_determinism", "'match_cpu' is outside this library's GPU path: its results are "
+                                          "run-to-run deterministic ('run_to_run') but computed in compensated "
+                                          "FP32, not bitwise the reference's FP64 CPU path")
         if o["barycenter_mode"] == "per_component":
             raise _bad("barycenter_mode", f"'per_component' {_OFF_PATH}: the global barycenter is held")
         if o["barycenter"] is False:

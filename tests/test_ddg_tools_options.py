@@ -116,6 +116,7 @@ def test_bad_values_are_named(kw, name):
     ({"penalties": [{"type": "area"}]}, "penalties"),
     ({"barycenter": False}, "barycenter"),
     ({"barycenter_mode": "per_component"}, "barycenter_mode"),
+    ({"gpu_determinism": "match_cpu"}, "gpu_determinism"),
     ({"constraints": [{"type": "volume"}]}, "constraints"),
     ({"constraints": [{"type": "barycenter"}, {"type": "area", "target": 3.0}]}, "constraints[1].target"),
     ({"constraints": [{"type": "barycenter"}, {"type": "volume", "factor": 1.1, "steps": 3}]},

@@ -648,10 +648,28 @@ def bench_ccd(args, rank, world, local):
         "gpu_launches": launches,
         "clocks": clk.summary(),
     }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = ccd_cpu(P, F, V)
     if world > 1:
         torch.distributed.destroy_process_group()
     print(json.dumps(line), flush=True)
     return 0
+
+
+def ccd_cpu(P, F, V, calls=1):
+    """The oracle's first_contact of the same motion on all host cores (x-sweep broad phase)."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import rs_oracle as O
+
+    O.build()
+    n = os.cpu_count() or 1
+    O.set_threads(n)
+    t0 = time.perf_counter()
+    for _ in range(calls):
+        r = O.ccd_first_contact(F, P, V, 1.0)
+    dt = (time.perf_counter() - t0) / calls
+    return {"value": 1.0 / dt, "unit": "calls/s", "cores": n, "kind": "port", "tau_max": r["tau_max"],
+            "sample": f"{calls} call(s) of the FP64 C++ restatement on {n} threads ({dt:.2f} s each)"}
 
 
 METRIC = "pair GFLOP/s, Barnes-Hut energy+differential (61 FLOP/interaction)"
@@ -674,9 +692,19 @@ def main() -> int:
     if args.impl == "reference":
         if args.workload == "ccd":
             if rank == 0:
-                print(json.dumps({"impl": "reference", "unavailable": (
-                    "the CCD oracle enumerates pairs by brute force (quadratic in the faces): "
-                    "no timed CPU arm at 204,800 faces")}), flush=True)
+                P, F, _, desc = workload("flow")
+                V = ccd_motion(P, F)
+                cb = ccd_cpu(P, F, V, calls=max(1, min(args.steps, 3)))
+                print(json.dumps({
+                    "impl": "reference", "metric": "CCD first_contact calls/s @204,800 faces (self contacts, gap "
+                    "0.05 of the mean edge)", "value": cb["value"], "unit": "calls/s", "n_gpus": 1,
+                    "steps": max(1, min(args.steps, 3)), "warmup": 0, "ms_per_step": 1e3 / cb["value"],
+                    "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                    "data": "synthetic (seeded mesh generator and motion)",
+                    "config": {"workload": f"ccd: {desc}; smooth seeded velocity, fastest vertex 2 mean edges by t = 1",
+                               "tau_end": 1.0},
+                    "cpu_baseline": cb, "e2e": {"value": cb["value"], "unit": "calls/s", "h2d_bytes_per_step": 0,
+                                                "d2h_bytes_per_step": 0}}), flush=True)
             return 0
         if args.workload.startswith("flow"):
             return run_reference_flow(args, rank)

@@ -4,9 +4,10 @@
 // (ccd.rs:529-592), the Lipschitz bound (ccd.rs:480-496) and the distances of
 // RC/src/ccd.rs:237-319, operation for operation (built with -ffp-contract=off).
 //
-// The broad phase here enumerates every pair whose inflated swept boxes overlap, by brute
-// force. The reference reaches the same set through its box trees: the tree query tests every
-// element box against the query box (ccd.rs:359-389), so the tree only prunes.
+// The broad phase here finds every pair whose inflated swept boxes overlap by an x sweep with
+// the exact overlap test. The reference reaches the same set through its box trees: the tree
+// query tests every element box against the query box (ccd.rs:359-389), so the tree only
+// prunes.
 //
 // The reference also passes each pair a horizon, the earliest contact its query has found so
 // far. A pair's result does not depend on it: the advancement reaches its contact time through
@@ -17,6 +18,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <mutex>
 #include <string>
 #include <utility>
 #include <vector>
@@ -192,58 +194,106 @@ Result window(const std::vector<tri> &faces, const std::vector<std::pair<uint32_
     fbox[f] = inflate(unite(unite(vbox[faces[f][0]], vbox[faces[f][1]]), vbox[faces[f][2]]), h);
   for (size_t e = 0; e < ne; ++e) ebox[e] = inflate(unite(vbox[edges[e].first], vbox[edges[e].second]), h);
 
+  // Broad phase by an x sweep: the element boxes sorted by lo.x; a query scans the elements
+  // with lo.x in [q.lo.x - W, q.hi.x], W the widest element box in x (padded against rounding),
+  // which every box overlapping q satisfies; the exact overlap test then decides, so the
+  // candidates are those of an enumeration of all pairs. Queries run on the oracle's threads;
+  // their results combine by a minimum and integer sums, which do not depend on the order.
+  struct Sweep {
+    std::vector<uint32_t> ord;
+    std::vector<double> key;
+    double w = 0.0;
+  };
+  auto make_sweep = [](const std::vector<Box> &b) {
+    Sweep sw;
+    sw.ord.resize(b.size());
+    for (size_t i = 0; i < b.size(); ++i) sw.ord[i] = (uint32_t)i, sw.w = fmax_(sw.w, b[i].hi[0] - b[i].lo[0]);
+    std::sort(sw.ord.begin(), sw.ord.end(), [&](uint32_t x, uint32_t y) {
+      return b[x].lo[0] < b[y].lo[0] || (b[x].lo[0] == b[y].lo[0] && x < y);
+    });
+    sw.key.resize(b.size());
+    for (size_t i = 0; i < b.size(); ++i) sw.key[i] = b[sw.ord[i]].lo[0];
+    sw.w = sw.w * 1.000001 + 1e-300;
+    return sw;
+  };
+  const Sweep fs = make_sweep(fbox), es = make_sweep(ebox);
+  auto range = [](const Sweep &sw, const Box &q) {
+    const double from = q.lo[0] - sw.w - std::fabs(q.lo[0]) * 1e-12;
+    const size_t b = std::lower_bound(sw.key.begin(), sw.key.end(), from) - sw.key.begin();
+    const size_t e = std::upper_bound(sw.key.begin(), sw.key.end(), q.hi[0]) - sw.key.begin();
+    return std::make_pair(b, e);
+  };
   Result out;
-  auto offer = [&](double t) {
-    if (!std::isnan(t) && (std::isnan(out.tau) || t < out.tau)) out.tau = t;
+  std::mutex mu;
+  auto merge = [&](const Result &r) {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!std::isnan(r.tau) && (std::isnan(out.tau) || r.tau < out.tau)) out.tau = r.tau;
+    out.tally.pairs += r.tally.pairs, out.tally.close += r.tally.close;
+    out.tally.touching += r.tally.touching, out.tally.exempt += r.tally.exempt;
+  };
+  auto offer = [](Result &r, double t) {
+    if (!std::isnan(t) && (std::isnan(r.tau) || t < r.tau)) r.tau = t;
   };
   // vertex against triangle
-  for (uint32_t v = 0; v < nv; ++v) {
-    const Box q = inflate(vbox[v], h);
-    for (uint32_t f = 0; f < nf; ++f) {
-      if (!overlaps(fbox[f], q)) continue;
-      const tri &t = faces[f];
-      if (t[0] == v || t[1] == v || t[2] == v) continue;
-      if (band && band[v] && (band[t[0]] || band[t[1]] || band[t[2]])) {  // ccd.rs:947-950
-        out.tally.exempt += 1;
-        continue;
+  parallel_for((int64_t)nv, [&](int64_t v0, int64_t v1) {
+    Result loc;
+    for (uint32_t v = (uint32_t)v0; v < (uint32_t)v1; ++v) {
+      const Box q = inflate(vbox[v], h);
+      const auto [rb, re] = range(fs, q);
+      for (size_t k = rb; k < re; ++k) {
+        const uint32_t f = fs.ord[k];
+        if (!overlaps(fbox[f], q)) continue;
+        const tri &t = faces[f];
+        if (t[0] == v || t[1] == v || t[2] == v) continue;
+        if (band && band[v] && (band[t[0]] || band[t[1]] || band[t[2]])) {  // ccd.rs:947-950
+          loc.tally.exempt += 1;
+          continue;
+        }
+        const v3 p = start[v], u = vel[v];
+        const v3 tp[3] = {at(start[t[0]], vel[t[0]], 0.0), at(start[t[1]], vel[t[1]], 0.0),
+                          at(start[t[2]], vel[t[2]], 0.0)};
+        const v3 tu[3] = {vel[t[0]], vel[t[1]], vel[t[2]]};
+        const double tri_speed = fmax_(fmax_(speed[t[0]], speed[t[1]]), speed[t[2]]);
+        const double lc = (speed[v] + tri_speed) * kMargin;
+        auto dist = [&](double tt) {
+          return point_triangle_distance(at(p, u, tt), at(tp[0], tu[0], tt), at(tp[1], tu[1], tt),
+                                         at(tp[2], tu[2], tt));
+        };
+        auto lref = [&] { return lipschitz({u}, {tu[0], tu[1], tu[2]}); };
+        offer(loc, advance(dist, lc, lref, gap_abs, max_iterations, close_factor, lo, hi, loc.tally));
       }
-      const v3 p = start[v], u = vel[v];
-      const v3 tp[3] = {at(start[t[0]], vel[t[0]], 0.0), at(start[t[1]], vel[t[1]], 0.0),
-                        at(start[t[2]], vel[t[2]], 0.0)};
-      const v3 tu[3] = {vel[t[0]], vel[t[1]], vel[t[2]]};
-      const double tri_speed = fmax_(fmax_(speed[t[0]], speed[t[1]]), speed[t[2]]);
-      const double lc = (speed[v] + tri_speed) * kMargin;
-      auto dist = [&](double tt) {
-        return point_triangle_distance(at(p, u, tt), at(tp[0], tu[0], tt), at(tp[1], tu[1], tt),
-                                       at(tp[2], tu[2], tt));
-      };
-      auto lref = [&] { return lipschitz({u}, {tu[0], tu[1], tu[2]}); };
-      offer(advance(dist, lc, lref, gap_abs, max_iterations, close_factor, lo, hi, out.tally));
     }
-  }
+    merge(loc);
+  });
   // edge against edge, e2 > e, no common vertex
-  for (uint32_t e = 0; e < ne; ++e) {
-    const Box q = ebox[e];
-    const uint32_t a = edges[e].first, b = edges[e].second;
-    for (uint32_t e2 = e + 1; e2 < ne; ++e2) {
-      if (!overlaps(ebox[e2], q)) continue;
-      const uint32_t c = edges[e2].first, d = edges[e2].second;
-      if (c == a || c == b || d == a || d == b) continue;
-      if (band && (band[a] || band[b]) && (band[c] || band[d])) {  // ccd.rs:1001-1004
-        out.tally.exempt += 1;
-        continue;
+  parallel_for((int64_t)ne, [&](int64_t e0, int64_t e1) {
+    Result loc;
+    for (uint32_t e = (uint32_t)e0; e < (uint32_t)e1; ++e) {
+      const Box q = ebox[e];
+      const uint32_t a = edges[e].first, b = edges[e].second;
+      const auto [rb, re] = range(es, q);
+      for (size_t k = rb; k < re; ++k) {
+        const uint32_t e2 = es.ord[k];
+        if (e2 <= e || !overlaps(ebox[e2], q)) continue;
+        const uint32_t c = edges[e2].first, d = edges[e2].second;
+        if (c == a || c == b || d == a || d == b) continue;
+        if (band && (band[a] || band[b]) && (band[c] || band[d])) {  // ccd.rs:1001-1004
+          loc.tally.exempt += 1;
+          continue;
+        }
+        const v3 pp[2] = {start[a], start[b]}, uu[2] = {vel[a], vel[b]};
+        const v3 qq[2] = {start[c], start[d]}, ww[2] = {vel[c], vel[d]};
+        const double lc = (fmax_(speed[a], speed[b]) + fmax_(speed[c], speed[d])) * kMargin;
+        auto dist = [&](double tt) {
+          return segment_segment_distance(at(pp[0], uu[0], tt), at(pp[1], uu[1], tt), at(qq[0], ww[0], tt),
+                                          at(qq[1], ww[1], tt));
+        };
+        auto lref = [&] { return lipschitz({uu[0], uu[1]}, {ww[0], ww[1]}); };
+        offer(loc, advance(dist, lc, lref, gap_abs, max_iterations, close_factor, lo, hi, loc.tally));
       }
-      const v3 pp[2] = {start[a], start[b]}, uu[2] = {vel[a], vel[b]};
-      const v3 qq[2] = {start[c], start[d]}, ww[2] = {vel[c], vel[d]};
-      const double lc = (fmax_(speed[a], speed[b]) + fmax_(speed[c], speed[d])) * kMargin;
-      auto dist = [&](double tt) {
-        return segment_segment_distance(at(pp[0], uu[0], tt), at(pp[1], uu[1], tt), at(qq[0], ww[0], tt),
-                                        at(qq[1], ww[1], tt));
-      };
-      auto lref = [&] { return lipschitz({uu[0], uu[1]}, {ww[0], ww[1]}); };
-      offer(advance(dist, lc, lref, gap_abs, max_iterations, close_factor, lo, hi, out.tally));
     }
-  }
+    merge(loc);
+  });
   return out;
 }
 

@@ -125,3 +125,16 @@ def test_coplanar_and_random_intersections_bitwise():
         c.set_band(p)
         _same(O.ccd_first_contact(f, p, v, tau_end, reference_length=ell, band=True),
               c.first_contact(p, v, tau_end, R.ccd_options(reference_length=ell)))
+
+
+def test_full_size_torus_bitwise():
+    """The bench's workload: the 204,800-face torus along a smooth motion (tau_max and every
+    exact count equal to the oracle's at full size)."""
+    import bench
+
+    P, F, _, _ = bench.workload("flow")
+    V = bench.ccd_motion(P, F)
+    g = R.CcdSurface(F, len(P)).first_contact(P, V, 1.0)
+    o = O.ccd_first_contact(F, P, V, 1.0)
+    _same(o, g)
+    assert g["pairs_tested"] > 1_000_000

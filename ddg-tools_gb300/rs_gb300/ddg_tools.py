@@ -220,6 +220,11 @@ class _Options:
             raise _bad("gpu_determinism", "'match_cpu' is outside this library's GPU path: its results are "
                                           "run-to-run deterministic ('run_to_run') but computed in compensated "
                                           "FP32, not bitwise the reference's FP64 CPU path")
+        if o["barycenter_mode"] == "auto" and not o["low_order"]:
+            # resolved_barycenter_mode (RS/src/step/options.rs:580-588): "auto" is per component
+            # unless the metric is the Sobolev metric with its low-order term
+            raise _bad("barycenter_mode", "'auto' with low_order=False resolves to per-component barycenters, "
+                                          "which are outside this library's GPU path; give barycenter_mode='global'")
         if o["barycenter_mode"] == "per_component":
             raise _bad("barycenter_mode", f"'per_component' {_OFF_PATH}: the global barycenter is held")
         if o["barycenter"] is False:

@@ -58,7 +58,7 @@ def test_passing_the_defaults_back_changes_nothing():
 def test_options_map_onto_the_flow():
     o = D._Options(dict(alpha=4.0, beta=9.0, theta=0.3, leaf_size=6, chi=0.25, cluster_leaf_size=12,
                         gmres_restart=30, gmres_tolerance=1e-6, gmres_max_iterations=77, tp_weight=2.0,
-                        low_order=False, armijo_c=0.1, max_halvings=9, newton_max=3,
+                        low_order=False, barycenter_mode="global", armijo_c=0.1, max_halvings=9, newton_max=3,
                         constraints=[{"type": "barycenter"}, {"type": "area"}, {"type": "volume"}]))
     f = o.flow_options()
     assert (f.alpha, f.beta, f.theta, f.leaf_size) == (4.0, 9.0, 0.3, 6)
@@ -67,6 +67,8 @@ def test_options_map_onto_the_flow():
     assert (s.chi, s.leaf_size, s.restart, s.tolerance, s.max_iterations) == (0.25, 12, 30, 1e-6, 77)
     assert (s.tp_weight, s.low_order) == (2.0, 0)
     assert (f.ccd, f.ccd_gap, f.ccd_max_iterations, f.ccd_close_factor) == (1, 0.05, 100, 0.5)
+    f = D._Options(dict(low_order=False, barycenter_mode="global")).flow_options()
+    assert f.solver.low_order == 0
     f = D._Options(dict(ccd=False)).flow_options()
     assert f.ccd == 0
     f = D._Options(dict(ccd_gap=0.1, ccd_max_iterations=7, ccd_close_factor=0.25)).flow_options()
@@ -117,6 +119,7 @@ def test_bad_values_are_named(kw, name):
     ({"barycenter": False}, "barycenter"),
     ({"barycenter_mode": "per_component"}, "barycenter_mode"),
     ({"gpu_determinism": "match_cpu"}, "gpu_determinism"),
+    ({"low_order": False}, "barycenter_mode"),
     ({"constraints": [{"type": "volume"}]}, "constraints"),
     ({"constraints": [{"type": "barycenter"}, {"type": "area", "target": 3.0}]}, "constraints[1].target"),
     ({"constraints": [{"type": "barycenter"}, {"type": "volume", "factor": 1.1, "steps": 3}]},

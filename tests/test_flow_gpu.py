@@ -49,3 +49,32 @@ def test_flow_steps(hold):
     b1 = (m1[:, None] * Q).sum(0) / m1.sum()
     assert np.abs(b1 - b0).max() < 1e-10
     assert energies == sorted(energies, reverse=True)
+
+
+def test_two_linked_tori_at_full_size():
+    """One step on the geometry of the two-torus configuration: two 400 x 400 tori (640,000
+    faces) linked as a Hopf pair, here with N(0, 0.0005) noise (the specified 0.01 is 2.5 minor
+    edge lengths and crumples the surface). The global barycenter, total area and volume are
+    held; the step is accepted and lowers the energy."""
+    P, F = gen.torus(400, 400, 1.0, 0.25)
+    Q = np.stack([P[:, 0] + 1.0, -P[:, 2], P[:, 1]], axis=1)
+    P2 = np.vstack([P, Q])
+    F2 = np.vstack([F, F + len(P)]).astype(np.uint32)
+    P2 = P2 + 0.0005 * np.random.default_rng(5).standard_normal(P2.shape)
+    assert len(F2) == 640_000
+    A0, V0 = _area_volume(P2, F2)
+    flow = R.Flow(F2, P2, R.flow_options(theta=0.25, hold_area=1, hold_volume=1))
+    rep = flow.step()
+    print(rep)
+    assert rep["accepted"] == 1.0 and rep["energy_after"] < rep["energy_before"]
+    Q2 = flow.positions()
+    A1, V1 = _area_volume(Q2, F2)
+    assert abs(A1 - A0) / A0 < 1e-8 and abs(V1 - V0) / abs(V0) < 1e-8
+    a0, _, _ = O.face_geometry(P2, F2)
+    a1, _, _ = O.face_geometry(Q2, F2)
+    m0, m1 = np.zeros(len(P2)), np.zeros(len(P2))
+    np.add.at(m0, F2.ravel().astype(np.int64), np.repeat(a0 / 3.0, 3))
+    np.add.at(m1, F2.ravel().astype(np.int64), np.repeat(a1 / 3.0, 3))
+    b0 = (m0[:, None] * P2).sum(0) / m0.sum()
+    b1 = (m1[:, None] * Q2).sum(0) / m1.sum()
+    assert np.abs(b1 - b0).max() < 1e-10

@@ -8,7 +8,8 @@ Same names, keyword options, array conventions and report dicts as the reference
 * ``RepulsiveSurfaceSession(positions, faces, **options)`` with ``step``, ``run``,
   ``snapshot``, ``cancel``, ``reset`` and the getters;
 * ``repulsive_surface_flow(positions, faces, steps=None, progress=None, **options)``;
-* ``repulsive_surface_defaults()`` and ``gpu_info()``.
+* ``repulsive_surface_defaults()``, ``gpu_info()`` and ``repulsive_surface_scene(path)`` (the
+  statements of a scene file that are on this path).
 
 Positions are any buffer or (nested) sequence of 3 reals per vertex, faces 3 indices per face;
 results are ``array('d')`` / ``array('i')``. Every option name of the reference is known. The
@@ -649,3 +650,104 @@ def repulsive_surface_flow(positions, faces, steps=None, progress=None, **option
               "steps": [dict(r, session_status=status) for r in out],
               "pinned": snap["pinned"], "face_origin": snap["face_origin"]}
     return snap["positions"], snap["faces"], report
+
+
+# ----------------------------------------------------------------------------------------------
+# Scene files
+# ----------------------------------------------------------------------------------------------
+
+_SCENE_OFF_PATH = {"minimize", "obstacle", "point_cloud_obstacle", "implicit", "allow_barycenter_shift",
+                   "autotarget_volume"}
+_SCENE_METHODS = {"hs", "aqp", "bqn", "h1", "h1-lbfgs", "h2", "willmore", "l2"}
+
+
+def repulsive_surface_scene(path):
+    """A scene file of the reference program as ``(positions, faces, options)``
+    (repulsive_surface_scene, crates/ddg-py/src/python/repulsive_surfaces.rs:693-710; the format
+    of RS/src/scene.rs:466-700 and its options, RS/src/step/scene_run.rs:34-104).
+
+    The statements on this library's path are read: ``repel_mesh <obj> <alpha> <beta>`` (the
+    OBJ path relative to the scene's directory), ``constrain barycenter|area|volume`` without a
+    growth schedule, ``iteration_limit``, ``time_limit`` (milliseconds), ``method hs``,
+    ``disable_near_field`` and ``log`` (ignored). The options are this library's defaults with
+    the scene's exponents, constraints and limits (no remeshing, as everywhere here). Any other
+    statement or value, such as a potential, an obstacle, an implicit surface, a growth
+    schedule, vertex pins or another method, raises ``RepulsiveSurfaceInputError`` naming it
+    and its line."""
+    from pathlib import Path
+
+    from . import obj
+
+    path = Path(path)
+    try:
+        text = path.read_text()
+    except OSError as e:
+        raise _bad("path", f"{path}: {e}") from None
+    mesh, alpha, beta, constraints, seen = None, None, None, [], {}
+    limits, low_order = {}, True
+
+    def err(line, msg):
+        return RepulsiveSurfaceInputError(f"{path}:{line}: {msg}")
+
+    for i, raw in enumerate(text.splitlines(), 1):
+        t = raw.strip()
+        if not t or t.startswith("#"):
+            continue
+        words = t.split()
+        kw, rest = words[0], words[1:]
+        if kw in ("repel_mesh", "iteration_limit", "time_limit", "method", "log"):
+            if kw in seen:
+                raise err(i, f"`{kw}` is given twice (first on line {seen[kw]})")
+            seen[kw] = i
+        if kw == "repel_mesh":
+            if len(rest) != 3:
+                raise err(i, "`repel_mesh` needs an OBJ path and the exponents `alpha beta`")
+            mesh = rest[0]
+            try:
+                alpha, beta = float(rest[1]), float(rest[2])
+            except ValueError:
+                raise err(i, "the exponents must be numbers") from None
+        elif kw == "constrain":
+            if not rest:
+                raise err(i, "`constrain` needs a constraint type")
+            kind = rest[0]
+            if kind not in ("barycenter", "area", "volume"):
+                raise err(i, f"`constrain {kind}` {_OFF_PATH}")
+            if len(rest) > 1:
+                raise err(i, f"a growth schedule (`constrain {kind} {' '.join(rest[1:])}`) {_OFF_PATH}")
+            constraints.append({"type": kind})
+        elif kw in ("iteration_limit", "time_limit"):
+            if len(rest) != 1 or not rest[0].isdigit():
+                raise err(i, f"`{kw}` needs one non-negative integer")
+            n = int(rest[0])
+            if n > 0:
+                limits[kw] = n
+        elif kw == "method":
+            if len(rest) != 1 or rest[0] not in _SCENE_METHODS:
+                raise err(i, f"unknown method `{' '.join(rest)}`")
+            if rest[0] != "hs":
+                raise err(i, f"method `{rest[0]}` {_OFF_PATH}")
+        elif kw == "disable_near_field":
+            low_order = False
+        elif kw == "log":
+            pass
+        elif kw in _SCENE_OFF_PATH:
+            raise err(i, f"`{kw}` {_OFF_PATH}")
+        else:
+            raise err(i, f"unknown keyword `{kw}`")
+    if mesh is None:
+        raise err(0, "the scene has no `repel_mesh` statement")
+    try:
+        P, F = obj.read_obj(path.parent / mesh)
+    except RsError as e:
+        raise _lib_err(e) from None
+    options = repulsive_surface_defaults()
+    options.update(alpha=alpha, beta=beta, constraints=constraints, low_order=low_order)
+    if not low_order:
+        options["barycenter_mode"] = "global"
+    if "iteration_limit" in limits:
+        options["max_iterations"] = limits["iteration_limit"]
+    if "time_limit" in limits:
+        options["time_limit"] = limits["time_limit"] / 1000.0
+    _Options(options)  # the same checks as a session (exponents, constraints)
+    return _flat_points(P), _flat_faces(F), options

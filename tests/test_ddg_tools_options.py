@@ -166,3 +166,43 @@ def test_error_kinds_map_as_the_reference():
     assert isinstance(D._lib_err(RsError(5, "NonFiniteEnergy", "flow", "x")), D.SolveError)
     assert isinstance(D._lib_err(RsError(3, "SolverDiverged", "solve", "x")), D.SolveError)
     assert isinstance(D._lib_err(RsError(2, "DegenerateFace", "surface", "x")), D.RepulsiveSurfaceInputError)
+
+
+def _scene(tmp_path, body):
+    from rs_gb300 import generators as gen
+    from rs_gb300 import obj
+
+    P, F = gen.icosphere(1)
+    obj.write_obj(tmp_path / "s.obj", P, F)
+    (tmp_path / "a.scene").write_text(body)
+    return tmp_path / "a.scene", P, F
+
+
+def test_scene_files_on_the_path(tmp_path):
+    path, P, F = _scene(tmp_path, "# a scene\nrepel_mesh s.obj 6 12\nconstrain barycenter\n"
+                                  "constrain volume\niteration_limit 50\ntime_limit 2500\nmethod hs\nlog out.csv\n")
+    p, f, o = D.repulsive_surface_scene(path)
+    assert np.frombuffer(p, np.float64).tobytes() == np.ascontiguousarray(P, np.float64).tobytes()
+    assert np.frombuffer(f, np.int32).tolist() == np.asarray(F).ravel().tolist()
+    assert o["constraints"] == [{"type": "barycenter"}, {"type": "volume"}]
+    assert (o["alpha"], o["beta"], o["max_iterations"], o["time_limit"]) == (6.0, 12.0, 50, 2.5)
+    D._Options(o)
+
+
+@pytest.mark.parametrize("body, what", [
+    ("repel_mesh s.obj 6 12\nminimize area 1\n", "minimize"),
+    ("repel_mesh s.obj 6 12\nobstacle o.obj 1\n", "obstacle"),
+    ("repel_mesh s.obj 6 12\nconstrain area 2 100\n", "growth"),
+    ("repel_mesh s.obj 6 12\nconstrain vertices 1 2\n", "constrain vertices"),
+    ("repel_mesh s.obj 6 12\nmethod aqp\n", "aqp"),
+    ("repel_mesh s.obj 6 12\nbogus\n", "unknown keyword"),
+    ("constrain barycenter\n", "repel_mesh"),
+    ("repel_mesh s.obj 6 12\nrepel_mesh s.obj 6 12\n", "twice"),
+    ("repel_mesh s.obj 1 3\nconstrain barycenter\n", "alpha"),
+    ("repel_mesh s.obj 6 12\nconstrain volume\n", "constraints"),
+])
+def test_scene_statements_off_the_path_are_named(tmp_path, body, what):
+    path, _, _ = _scene(tmp_path, body)
+    with pytest.raises(D.RepulsiveSurfaceInputError) as e:
+        D.repulsive_surface_scene(path)
+    assert what in str(e.value)

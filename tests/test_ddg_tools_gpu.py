@@ -215,3 +215,21 @@ def test_collision_cap_in_the_flow():
         else:
             assert b["tau0"] == min(t0, 2.0 / 3.0 * b["tau_ccd"])
         assert b["energy_after"] < b["energy_before"]
+
+
+def test_a_scene_file_runs(tmp_path):
+    """A scene of the reference program's format runs through the session
+    (crates/ddg-py/python-tests/test_repulsive_surfaces.py:739-772 does the same)."""
+    from rs_gb300 import obj
+
+    P, F = _torus()
+    obj.write_obj(tmp_path / "t.obj", P, F)
+    (tmp_path / "t.scene").write_text("repel_mesh t.obj 6 12\nconstrain barycenter\nconstrain volume\n"
+                                      "iteration_limit 3\n")
+    p, f, o = D.repulsive_surface_scene(tmp_path / "t.scene")
+    s = D.RepulsiveSurfaceSession(p, f, **o)
+    end = s.run()
+    assert (end["end"], end["status"], end["steps_taken"]) == ("final", "max_iterations", 3)
+    Q = np.frombuffer(s.positions, np.float64).reshape(-1, 3)
+    assert abs(_volume(Q, F) - _volume(P, F)) <= 1e-6 * abs(_volume(P, F))
+    assert end["energy_after"] < end["energy_before"]

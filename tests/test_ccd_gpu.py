@@ -138,3 +138,24 @@ def test_full_size_torus_bitwise():
     o = O.ccd_first_contact(F, P, V, 1.0)
     _same(o, g)
     assert g["pairs_tested"] > 1_000_000
+
+
+def test_edge_cases_bitwise():
+    # tau_end = 0, no motion, one triangle, a degenerate (zero-area) triangle, many windows
+    f, p, v, tau_end, ell = S.random_soup(3000, k=6)
+    _same(*_both(f, p, v, 0.0, ell))
+    _same(*_both(f, p, np.zeros_like(v), 2.0, ell))
+    one_f = np.array([[0, 1, 2]], np.uint32)
+    one_p = np.array([[0.0, 0, 0], [1, 0, 0], [0, 1, 0]])
+    o, g = _both(one_f, one_p, np.ones((3, 3)), 1.0, 1.0)
+    _same(o, g)
+    assert g["pairs_tested"] == 0 and g["tau_max"] == 1.0
+    deg_f, deg_p = S.soup([[[0.0, 0, 0], [1, 0, 0], [0, 1, 0]], [[0.3, 0.3, 1.0], [0.3, 0.3, 1.0], [0.6, 0.6, 1.0]]])
+    deg_v = np.zeros((6, 3))
+    deg_v[3:] = [0.0, 0.0, -1.0]
+    _same(*_both(deg_f, deg_p, deg_v, 2.0, 1.0))
+    # a long sweep: the window doubles several times before the contact near t = 9.95
+    f, p, v = S.two_triangles([[0.2, 0.2, 10.0], [1.0, 1.0, 10.5], [-0.5, 1.2, 10.5]], [0.0, 0.0, -1.0])
+    o, g = _both(f, p, v, 20.0, 1.0)
+    _same(o, g)
+    assert g["windows"] >= 4 and 9.9 < g["tau_max"] <= 9.95 + 1e-9

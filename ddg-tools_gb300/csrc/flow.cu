@@ -15,6 +15,7 @@
 //      at most 5), then the barycenter translated back to its target.
 // Host-side vectors (positions, constraint rows) are FP64 and O(V); the rest is on the device.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -151,6 +152,7 @@ struct rs_flow {
   int l_cheap = 2, l_cap = 0;
   int iteration = 0;
   rs_ccd *ccd = nullptr;  // the surface's topology for the collision cap (ccd on)
+  std::atomic<int> cancel{0};  // set by rs_flow_cancel from any thread
   ~rs_flow() { rs_ccd_free(ccd); }
 };
 
@@ -214,6 +216,10 @@ int rs_flow_set_learned(rs_flow *F, rs_learned *model, int cheap_steps, int max_
   });
 }
 
+int rs_flow_cancel(rs_flow *F, int cancel) {
+  return guard([&] { F->cancel.store(cancel ? 1 : 0); });
+}
+
 int rs_flow_positions(rs_flow *F, double *positions_host) {
   return guard([&] { std::memcpy(positions_host, F->pos.data(), F->pos.size() * sizeof(double)); });
 }
@@ -221,6 +227,7 @@ int rs_flow_positions(rs_flow *F, double *positions_host) {
 int rs_flow_step(rs_flow *F, double *report) {
   return guard([&] {
     TrustedTopology trusted;  // validated by rs_flow_create; the face list never changes
+    if (F->cancel.load()) fail(RS_CANCELLED, "Cancelled", "flow", "the step was cancelled");
     auto t_step = clk::now();
     rs_ctx *ctx = F->ctx;
     ctx->use();
@@ -437,6 +444,7 @@ int rs_flow_step(rs_flow *F, double *report) {
     bool accepted = false;
     int halvings = 0;
     while (halvings <= F->o.max_halvings && tau >= tau_min) {
+      if (F->cancel.load()) fail(RS_CANCELLED, "Cancelled", "flow", "the step was cancelled");
       for (size_t r = 0; r < nd; ++r) trial[r] = F->pos[r] - tau * x[r];
       bool ok = true;
       for (double v : trial) ok = ok && std::isfinite(v);

@@ -165,6 +165,7 @@ def load_library(path: str | os.PathLike | None = None):
         "rs_flow_create": [_vp, C.c_int, C.c_int, _u32p, _f64p, C.c_void_p, C.POINTER(_vp)],
         "rs_flow_step": [_vp, _f64p],
         "rs_flow_positions": [_vp, _f64p],
+        "rs_flow_cancel": [_vp, C.c_int],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -739,6 +740,11 @@ class Flow:
         out = np.empty((self.n_vertices, 3))
         _check(_lib.rs_flow_positions(self._h, out.ravel()))
         return out
+
+    def cancel(self, on: bool = True) -> None:
+        """Stops the running step between line-search trials, and later steps, with RsError
+        kind "Cancelled"; the positions stay those of the last completed step."""
+        _check(_lib.rs_flow_cancel(self._h, int(bool(on))))
 
 
 def ccd_options(**kw) -> CcdOptions:

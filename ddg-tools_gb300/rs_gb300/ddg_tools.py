@@ -410,7 +410,8 @@ class RepulsiveSurfaceSession:
     line search is capped at two thirds of the first contact time of the motion
     (RS/src/ccd.rs:762-884, on the GPU). ``step`` and ``run`` release the GIL inside the
     library; ``snapshot`` and the getters never wait for a running step; ``cancel`` is safe from
-    any thread and takes effect before the next step (a step in progress completes). There is
+    any thread and stops a running step between line-search trials (the mesh stays that of the
+    last completed step). There is
     no remeshing: the faces, ``face_origin`` (the identity) and ``pinned`` (empty) never change.
     """
 
@@ -479,8 +480,13 @@ class RepulsiveSurfaceSession:
 
     # ---- control -----------------------------------------------------------------------------
     def cancel(self) -> None:
-        """Stops the session before its next step; the snapshot reads "cancelled" at once."""
+        """Stops a running step between line-search trials, and every later step; the snapshot
+        reads "cancelled" at once (Engine::cancel, crates/ddg-py/src/repulsive_surfaces.rs:1688-1695)."""
         self._cancel = True
+        try:
+            self._flow.cancel(True)
+        except RsError:
+            pass
         with self._snap_lock:
             self._snap["status"] = "cancelled"
 
@@ -507,6 +513,10 @@ class RepulsiveSurfaceSession:
             try:
                 r = self._flow.step()
             except RsError as e:
+                if e.kind == "Cancelled":  # the step stopped between trials: nothing moved
+                    with self._snap_lock:
+                        self._snap["status"] = "cancelled"
+                        return self._cancelled_report()
                 with self._snap_lock:
                     self._snap["status"], self._snap["error"] = "error", str(e)
                 raise _lib_err(e) from None

@@ -44,6 +44,7 @@ enum rs_status {
   RS_SOLVER_DIVERGED = 8,    /* RsError::SolverDiverged (:174) */
   RS_SINGULAR = 9,           /* RsError::SingularSaddle (:169) */
   RS_GPU = 10,               /* RsError::Gpu (:218) */
+  RS_CANCELLED = 11,         /* RsError::Cancelled: a step stopped by rs_flow_cancel */
   RS_INTERNAL = 99
 };
 
@@ -424,6 +425,10 @@ int rs_flow_positions(rs_flow *f, double *positions_host);
 /* Uses (model != NULL) or stops using a learned preconditioner in the following steps (see
  * rs_solver_set_learned); the model must outlive its use. No counterpart in the crate. */
 int rs_flow_set_learned(rs_flow *f, rs_learned *model, int cheap_steps, int max_iterations);
+/* Asks the running step (between line-search trials) and every later step to stop with
+ * RS_CANCELLED; the positions stay those of the last completed step (Session's cancel flag,
+ * session.rs:989-998). Safe from any thread; never waits. rs_flow_cancel(f, 0) clears it. */
+int rs_flow_cancel(rs_flow *f, int cancel);
 
 #ifdef __cplusplus
 }

@@ -45,6 +45,9 @@ class FakeFlow:
     def positions(self):
         return self.pos.copy()
 
+    def cancel(self, on=True):
+        self.cancelled = on
+
 
 class FakeTree:
     @classmethod
@@ -155,3 +158,15 @@ def test_step_report_keys_follow_the_reference():
     assert r["tau_ccd"] is None and r["remesh"] is None
     assert set(r["seconds"]) == {"bvh", "energy", "factor", "solve", "line_search", "ccd", "projection",
                                  "remesh", "total"}
+
+
+def test_a_step_stopped_between_trials_is_a_cancelled_step():
+    FakeFlow.script = [_report(e1=9.0), RsError(11, "Cancelled", "flow", "the step was cancelled")]
+    s = D.RepulsiveSurfaceSession(P, F)
+    s.step()
+    before = s.positions.tobytes()
+    r = s.step()
+    assert r["status"] == "cancelled" and s.status == "cancelled" and s.iteration == 1
+    assert s.positions.tobytes() == before and s.energy == 9.0
+    s.cancel()
+    assert s._flow.cancelled and s.run()["end"] == "cancelled"

@@ -78,3 +78,17 @@ def test_two_linked_tori_at_full_size():
     b0 = (m0[:, None] * P2).sum(0) / m0.sum()
     b1 = (m1[:, None] * Q2).sum(0) / m1.sum()
     assert np.abs(b1 - b0).max() < 1e-10
+
+
+def test_cancel_flag():
+    P, F = gen.noisy_torus(32, 16, 1.0, 0.3, 0.003, 2)
+    flow = R.Flow(F, P, R.flow_options(theta=0.5))
+    flow.step()
+    Q = flow.positions()
+    flow.cancel(True)
+    with pytest.raises(R.RsError) as e:
+        flow.step()
+    assert e.value.kind == "Cancelled"
+    assert flow.positions().tobytes() == Q.tobytes()
+    flow.cancel(False)
+    assert flow.step()["accepted"] == 1.0

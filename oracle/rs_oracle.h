@@ -142,6 +142,114 @@ const char *rso_ccd_last_error(void);
 /* The smallest vertex-triangle / edge-edge distance over the pairs CCD constrains. */
 int rso_ccd_min_distance(int nv, const double *pos, int nf, const uint32_t *faces, double *out);
 
+/* ---- constraints, saddle, preconditioner, GMRES and the step (rs_oracle_solve.cpp) ---- */
+
+/* A list of constraints (RS/src/constraints/mod.rs:36-110): kind 0 barycenter, 1 pins, 2 area,
+ * 3 volume; comp = component or -1 (barycenter: every component separately when per_component,
+ * else one global group; area/volume: the whole mesh). n_target[i] doubles of `target` (in
+ * order) give the targets (0: the current value); n_pin[i] vertices of `pin` are pinned. */
+typedef struct rso_constraints {
+  int n;
+  const int *kind;
+  const int *comp;
+  const int *n_target;
+  const double *target;
+  const int *n_pin;
+  const uint32_t *pin;
+  int per_component;
+} rso_constraints;
+
+/* Options of the hierarchical saddle solver (HierarchicalOptions, RS/src/solve/iterative.rs:348-395;
+ * PreconditionerOptions, RS/src/solve/precond.rs:466-583; GmresOptions, gmres.rs:135-190). */
+typedef struct rso_solver_options {
+  double chi;
+  int leaf_size, leaf_pairs;
+  double tp_weight;
+  int low_order;
+  double eps_rel, eps_multi_rel;
+  int preconditioner; /* 1 the augmented vertex-pair preconditioner, 0 none */
+  int coarse;         /* the coarse correction for components without own positional rows */
+  int restart, max_iterations;
+  double tolerance;
+} rso_solver_options;
+rso_solver_options rso_solver_options_default(void);
+
+/* Options of one step (FlowOptions, RS/src/step/options.rs:290-382). energy_theta < 0: the
+ * exact energy, else Barnes-Hut lists at that opening angle. backend 0: dense saddle (LU),
+ * 1: hierarchical (the solver options). start_rule 0 absolute start_value, 1 start_value mean
+ * edge lengths for the farthest vertex, 2 reference 2/|x|, 3 grow previous_tau by start_value
+ * (without one: first_rule with first_value). max_halvings < 0: unbounded. l0 = 0: the mean edge
+ * length of the positions. */
+typedef struct rso_step_options {
+  double energy_theta;
+  int leaf_size;
+  int backend;
+  rso_solver_options solver;
+  int start_rule;
+  double start_value;
+  int first_rule;
+  double first_value;
+  double previous_tau;
+  double armijo_c;
+  int max_halvings;
+  double tau_min_rel;
+  int newton_fixed, newton_max;
+  int guard_projection;
+  double l0;
+} rso_step_options;
+rso_step_options rso_step_options_default(void);
+
+const char *rso_solve_last_error(void);
+
+/* ConstraintSet::new / values / jacobian (constraints/mod.rs:191-604): rows in order, their
+ * kind (0..3), whether positional, Phi, the dense Jacobian (n_rows x 3V, may be NULL), the
+ * component of every vertex and the number of components. */
+int rso_constraint_rows(int nv, const double *pos, int nf, const uint32_t *faces, const rso_constraints *c,
+                        int max_rows, int *n_rows, int *kind, int *positional, double *phi, double *jac,
+                        uint32_t *vcomp, int *n_comp);
+
+/* The dense nested saddle (RS/src/solve/dense.rs, schur.rs:101-356) with A = w_TP (B + c_lo B0)
+ * and the exact energy gradient g: the direction x, S = -C_N Z (kn x kn), Phi_N, the Newton
+ * correction h and <g, x>. */
+int rso_dense_saddle(int nv, const double *pos, int nf, const uint32_t *faces, double alpha, double beta,
+                     double tp_weight, int low_order, const rso_constraints *c, int max_rows, int *kq, int *kn,
+                     double *g, double *x, double *S, double *phin, double *h, double *gx);
+
+/* The dense face-pair preconditioner (RS/src/solve/dense.rs:527-600): eps, L_{2-s} (V x V),
+ * L' ((3V+kQ)^2) and z = P^-1 [r; 0] (3V). */
+int rso_dense_precond(int nv, const double *pos, int nf, const uint32_t *faces, double alpha, double beta,
+                      double eps_rel, const rso_constraints *c, const double *r, double *eps, double *lfr, double *lp,
+                      double *z, int *kq);
+
+#define RSO_STEP_REPORT_LEN 28
+/* One step (Session::step_inner, RS/src/step/session.rs:749-1100). report: 0 F0, 1 F after the
+ * projection, 2 F at the accepted trial, 3 tau (0 stuck), 4 tau0, 5 accepted, 6 halvings,
+ * 7 slope <g,x>, 8 |x|_2, 9 |x|_inf, 10 l0, 11 Newton rounds, 12 projection status (0 converged,
+ * 1 max rounds, 2 not improving, 3 blocked), 13 |g|_2, 14 rows, 15 blocked projections,
+ * 16..22 seconds (objective build, energy, solver build, solves, line search, projection, total),
+ * 23 operator products, 24 GMRES iterations, 25 worst true relative residual, 26 solves,
+ * 27 preconditioner applications. trials: (tau, energy, outcome) with outcome 0 accepted,
+ * 1 armijo-failed, 2 non-finite, 3 projection blocked. */
+int rso_step(int nv, const double *pos, int nf, const uint32_t *faces, double alpha, double beta,
+             const rso_constraints *c, const rso_step_options *o, double *pos_out, double *x_out, double *g_out,
+             double *report, double *trials, int max_trials, int *n_trials, double *phi_before, double *phi_after,
+             int max_rows);
+
+/* The hierarchical saddle solver alone (hierarchical_saddle_with, iterative.rs:487-575): A' and
+ * P^-1 on vectors [x (3V); l (k_Q)], GMRES solves (report 5 per rhs: iterations, true relative
+ * residual, converged, seconds, cycles). info: eps, multi (0/1), fractional scale, coarse
+ * dimension, build seconds (metric, fractional tree, Laplacian factor, coarse space). */
+typedef struct rso_hsolver rso_hsolver;
+int rso_hsolver_build(int nv, const double *pos, int nf, const uint32_t *faces, double alpha, double beta,
+                      const rso_solver_options *o, const rso_constraints *c, rso_hsolver **out);
+void rso_hsolver_free(rso_hsolver *h);
+int rso_hsolver_dims(rso_hsolver *h, int64_t *n_dofs, int64_t *n_constraints);
+int rso_hsolver_set_gmres(rso_hsolver *h, int restart, int max_iterations, double tolerance);
+int rso_hsolver_apply(rso_hsolver *h, int nb, const double *xs, double *ys);
+int rso_hsolver_precondition(rso_hsolver *h, int nb, const double *rs, double *zs);
+int rso_hsolver_solve(rso_hsolver *h, int nb, const double *rhs, double *sol, double *report5);
+int rso_hsolver_info(rso_hsolver *h, double *out8);
+
 #ifdef __cplusplus
 }
 #endif

@@ -346,3 +346,263 @@ def ccd_intersecting_pairs(pos, faces) -> np.ndarray:
         out = np.zeros(2 * n.value, np.uint32)
         L.rso_ccd_intersecting_pairs(len(pos), pos.ravel(), len(faces), faces.ravel(), n.value, out, C.byref(n))
     return out[: 2 * n.value].reshape(-1, 2)
+
+
+# ---------------------------------------------------------------- constraints, solves, the step
+
+
+class _RsoConstraints(C.Structure):
+    _fields_ = [("n", C.c_int), ("kind", C.c_void_p), ("comp", C.c_void_p), ("n_target", C.c_void_p),
+                ("target", C.c_void_p), ("n_pin", C.c_void_p), ("pin", C.c_void_p), ("per_component", C.c_int)]
+
+
+class SolverOptions(C.Structure):
+    """rso_solver_options (HierarchicalOptions / PreconditionerOptions / GmresOptions)."""
+    _fields_ = [("chi", C.c_double), ("leaf_size", C.c_int), ("leaf_pairs", C.c_int), ("tp_weight", C.c_double),
+                ("low_order", C.c_int), ("eps_rel", C.c_double), ("eps_multi_rel", C.c_double),
+                ("preconditioner", C.c_int), ("coarse", C.c_int), ("restart", C.c_int),
+                ("max_iterations", C.c_int), ("tolerance", C.c_double)]
+
+
+class StepOptions(C.Structure):
+    """rso_step_options (FlowOptions of one step)."""
+    _fields_ = [("energy_theta", C.c_double), ("leaf_size", C.c_int), ("backend", C.c_int),
+                ("solver", SolverOptions), ("start_rule", C.c_int), ("start_value", C.c_double),
+                ("first_rule", C.c_int), ("first_value", C.c_double), ("previous_tau", C.c_double),
+                ("armijo_c", C.c_double), ("max_halvings", C.c_int), ("tau_min_rel", C.c_double),
+                ("newton_fixed", C.c_int), ("newton_max", C.c_int), ("guard_projection", C.c_int),
+                ("l0", C.c_double)]
+
+
+def _solve_lib():
+    L = lib()
+    if not getattr(L, "_solve_ready", False):
+        L.rso_solve_last_error.restype = C.c_char_p
+        L.rso_solver_options_default.restype = SolverOptions
+        L.rso_step_options_default.restype = StepOptions
+        cp = C.POINTER(_RsoConstraints)
+        L.rso_constraint_rows.argtypes = [C.c_int, _f64p, C.c_int, _u32p, cp, C.c_int, C.POINTER(C.c_int),
+                                          C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                          C.POINTER(C.c_int)]
+        L.rso_dense_saddle.argtypes = [C.c_int, _f64p, C.c_int, _u32p, C.c_double, C.c_double, C.c_double,
+                                       C.c_int, cp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), _f64p,
+                                       _f64p, _f64p, _f64p, _f64p, C.POINTER(C.c_double)]
+        L.rso_dense_precond.argtypes = [C.c_int, _f64p, C.c_int, _u32p, C.c_double, C.c_double, C.c_double,
+                                        cp, _f64p, C.POINTER(C.c_double), _f64p, _f64p, _f64p,
+                                        C.POINTER(C.c_int)]
+        L.rso_step.argtypes = [C.c_int, _f64p, C.c_int, _u32p, C.c_double, C.c_double, cp,
+                               C.POINTER(StepOptions), _f64p, _f64p, _f64p, _f64p, _f64p, C.c_int,
+                               C.POINTER(C.c_int), _f64p, _f64p, C.c_int]
+        L.rso_hsolver_build.argtypes = [C.c_int, _f64p, C.c_int, _u32p, C.c_double, C.c_double,
+                                        C.POINTER(SolverOptions), cp, C.POINTER(C.c_void_p)]
+        L.rso_hsolver_free.argtypes = [C.c_void_p]
+        L.rso_hsolver_dims.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        L.rso_hsolver_set_gmres.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double]
+        for f in ("rso_hsolver_apply", "rso_hsolver_precondition"):
+            getattr(L, f).argtypes = [C.c_void_p, C.c_int, _f64p, _f64p]
+        L.rso_hsolver_solve.argtypes = [C.c_void_p, C.c_int, _f64p, _f64p, _f64p]
+        L.rso_hsolver_info.argtypes = [C.c_void_p, _f64p]
+        L._solve_ready = True
+    return L
+
+
+def _scheck(code: int) -> None:
+    if code != 0:
+        raise OracleError(code, _solve_lib().rso_solve_last_error().decode())
+
+
+KINDS = {"barycenter": 0, "pins": 1, "area": 2, "volume": 3}
+
+
+class Constraints:
+    """A constraint list (Constraint, RS/src/constraints/mod.rs:36-110), in order.
+
+    ``barycenter(comp=None)`` with ``per_component`` holds every component's barycenter
+    separately (BarycenterMode::PerComponent), else one global group."""
+
+    def __init__(self, per_component: bool = False):
+        self.items: list[tuple[int, int, list[float], list[int]]] = []
+        self.per_component = per_component
+
+    def barycenter(self, comp=None, target=None):
+        self.items.append((0, -1 if comp is None else comp, [] if target is None else list(target), []))
+        return self
+
+    def pins(self, vertices, targets=None):
+        t = [] if targets is None else list(np.asarray(targets, dtype=np.float64).ravel())
+        self.items.append((1, -1, t, [int(v) for v in vertices]))
+        return self
+
+    def area(self, comp=None, target=None):
+        self.items.append((2, -1 if comp is None else comp, [] if target is None else [float(target)], []))
+        return self
+
+    def volume(self, comp=None, target=None):
+        self.items.append((3, -1 if comp is None else comp, [] if target is None else [float(target)], []))
+        return self
+
+    def _c(self):
+        n = len(self.items)
+        self._kind = np.array([i[0] for i in self.items] or [0], np.int32)
+        self._comp = np.array([i[1] for i in self.items] or [0], np.int32)
+        self._nt = np.array([len(i[2]) for i in self.items] or [0], np.int32)
+        self._t = np.array([x for i in self.items for x in i[2]] or [0.0], np.float64)
+        self._npin = np.array([len(i[3]) for i in self.items] or [0], np.int32)
+        self._pin = np.array([x for i in self.items for x in i[3]] or [0], np.uint32)
+        s = _RsoConstraints(n, self._kind.ctypes.data, self._comp.ctypes.data, self._nt.ctypes.data,
+                            self._t.ctypes.data, self._npin.ctypes.data, self._pin.ctypes.data,
+                            int(self.per_component))
+        self._s = s
+        return C.byref(s)
+
+
+def solver_options(**kw) -> SolverOptions:
+    o = _solve_lib().rso_solver_options_default()
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+def step_options(**kw) -> StepOptions:
+    o = _solve_lib().rso_step_options_default()
+    for k, v in kw.items():
+        if k == "solver":
+            for kk, vv in v.items():
+                setattr(o.solver, kk, vv)
+        else:
+            setattr(o, k, v)
+    return o
+
+
+def constraint_rows(pos, faces, cons: Constraints) -> dict:
+    """Rows of the constraint set: kind, positional flag, Phi, dense Jacobian, components."""
+    pos, faces = _mesh(pos, faces)
+    L = _solve_lib()
+    nv = len(pos)
+    cap = 3 * nv + 64
+    nr, ncomp = C.c_int(), C.c_int()
+    kind, posi = np.zeros(cap, np.int32), np.zeros(cap, np.int32)
+    phi, jac = np.zeros(cap), np.zeros(cap * 3 * nv)
+    vcomp = np.zeros(nv, np.uint32)
+    _scheck(L.rso_constraint_rows(nv, pos.ravel(), len(faces), faces.ravel(), cons._c(), cap, C.byref(nr),
+                                  _ptr(kind), _ptr(posi), _ptr(phi), _ptr(jac), _ptr(vcomp), C.byref(ncomp)))
+    n = nr.value
+    return dict(kind=kind[:n], positional=posi[:n].astype(bool), phi=phi[:n], jac=jac[: n * 3 * nv].reshape(n, 3 * nv),
+                vcomp=vcomp, n_components=ncomp.value)
+
+
+def dense_saddle(pos, faces, cons: Constraints, alpha=6.0, beta=12.0, tp_weight=1.0, low_order=True) -> dict:
+    """The dense nested saddle at the exact energy gradient: g, x, S, Phi_N, h, <g, x>."""
+    pos, faces = _mesh(pos, faces)
+    L = _solve_lib()
+    nv = len(pos)
+    kq, kn, gx = C.c_int(), C.c_int(), C.c_double()
+    g, x, h = np.zeros(3 * nv), np.zeros(3 * nv), np.zeros(3 * nv)
+    S, phin = np.zeros(64 * 64), np.zeros(64)
+    _scheck(L.rso_dense_saddle(nv, pos.ravel(), len(faces), faces.ravel(), alpha, beta, tp_weight, int(low_order),
+                               cons._c(), 64, C.byref(kq), C.byref(kn), g, x, S, phin, h, C.byref(gx)))
+    k = kn.value
+    return dict(kq=kq.value, kn=k, g=g.reshape(-1, 3), x=x.reshape(-1, 3), S=S[: k * k].reshape(k, k),
+                phin=phin[:k], h=h.reshape(-1, 3), gx=gx.value)
+
+
+def dense_precond(pos, faces, cons: Constraints, r, alpha=6.0, beta=12.0, eps_rel=1e-10) -> dict:
+    """The dense face-pair preconditioner: eps, L_{2-s}, L', z = P^-1 [r; 0]."""
+    pos, faces = _mesh(pos, faces)
+    L = _solve_lib()
+    nv = len(pos)
+    cap = 3 * nv + 3 * nv
+    eps, kq = C.c_double(), C.c_int()
+    lfr, lp, z = np.zeros(nv * nv), np.zeros(cap * cap), np.zeros(3 * nv)
+    r = np.ascontiguousarray(r, dtype=np.float64).ravel()
+    _scheck(L.rso_dense_precond(nv, pos.ravel(), len(faces), faces.ravel(), alpha, beta, eps_rel, cons._c(), r,
+                                C.byref(eps), lfr, lp, z, C.byref(kq)))
+    n = 3 * nv + kq.value
+    return dict(eps=eps.value, Lfr=lfr.reshape(nv, nv), Lp=lp[: n * n].reshape(n, n), z=z.reshape(-1, 3),
+                kq=kq.value)
+
+
+STEP_KEYS = ["energy_before", "energy_after", "energy_trial", "tau", "tau0", "accepted", "halvings", "slope",
+             "xnorm", "xinf", "l0", "newton_rounds", "projection_status", "gradient_norm", "rows",
+             "projection_blocked", "s_objective", "s_energy", "s_solver_build", "s_solve", "s_line_search",
+             "s_projection", "s_total", "operator_products", "gmres_iterations", "worst_residual", "solves",
+             "preconditioner_applications"]
+OUTCOMES = ["accepted", "armijo-failed", "non-finite", "projection-blocked"]
+
+
+def step(pos, faces, cons: Constraints, options: StepOptions | None = None, alpha=6.0, beta=12.0) -> dict:
+    """One descent step (Session::step_inner): report, trials, positions, direction, gradient,
+    Phi of every row after the line search and at the end."""
+    pos, faces = _mesh(pos, faces)
+    L = _solve_lib()
+    nv = len(pos)
+    o = options if options is not None else L.rso_step_options_default()
+    rep = np.zeros(28)
+    trials = np.zeros(3 * 256)
+    nt = C.c_int()
+    cap = 3 * nv + 64
+    pb, pa = np.zeros(cap), np.zeros(cap)
+    P, x, g = np.zeros(3 * nv), np.zeros(3 * nv), np.zeros(3 * nv)
+    _scheck(L.rso_step(nv, pos.ravel(), len(faces), faces.ravel(), alpha, beta, cons._c(), C.byref(o), P, x, g,
+                       rep, trials, 256, C.byref(nt), pb, pa, cap))
+    out = dict(zip(STEP_KEYS, rep.tolist()))
+    nr = int(out["rows"])
+    out.update(positions=P.reshape(-1, 3), direction=x.reshape(-1, 3), gradient=g.reshape(-1, 3),
+               trials=[(trials[3 * i], trials[3 * i + 1], OUTCOMES[int(trials[3 * i + 2])])
+                       for i in range(min(nt.value, 256))],
+               phi_before=pb[:nr], phi_after=pa[:nr])
+    return out
+
+
+class HSolver:
+    """The hierarchical saddle solver (A', the augmented preconditioner, GMRES) of the oracle."""
+
+    def __init__(self, pos, faces, cons: Constraints, options: SolverOptions | None = None, alpha=6.0, beta=12.0):
+        pos, faces = _mesh(pos, faces)
+        L = _solve_lib()
+        h = C.c_void_p()
+        o = options if options is not None else L.rso_solver_options_default()
+        _scheck(L.rso_hsolver_build(len(pos), pos.ravel(), len(faces), faces.ravel(), alpha, beta, C.byref(o),
+                                    cons._c(), C.byref(h)))
+        self._h = h
+        nd, nq = C.c_int64(), C.c_int64()
+        L.rso_hsolver_dims(h, C.byref(nd), C.byref(nq))
+        self.n_dofs, self.n_constraints = nd.value, nq.value
+        self.n = self.n_dofs + self.n_constraints
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.rso_hsolver_free(self._h)
+            self._h = None
+
+    def info(self) -> dict:
+        o = np.zeros(8)
+        _solve_lib().rso_hsolver_info(self._h, o)
+        return dict(zip(["eps", "multi", "fractional_scale", "coarse_dim", "s_metric", "s_fractional",
+                         "s_laplacian", "s_coarse"], o.tolist()))
+
+    def set_gmres(self, restart=30, max_iterations=200, tolerance=1e-6):
+        _solve_lib().rso_hsolver_set_gmres(self._h, restart, max_iterations, tolerance)
+
+    def _batch(self, fn, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        xs = x.reshape(-1, self.n)
+        ys = np.empty_like(xs)
+        _scheck(fn(self._h, len(xs), xs.ravel(), ys.ravel()))
+        return ys.reshape(x.shape)
+
+    def apply(self, x):
+        return self._batch(_solve_lib().rso_hsolver_apply, x)
+
+    def precondition(self, r):
+        return self._batch(_solve_lib().rso_hsolver_precondition, r)
+
+    def solve(self, rhs):
+        rhs = np.ascontiguousarray(rhs, dtype=np.float64)
+        rs = rhs.reshape(-1, self.n)
+        sol = np.empty_like(rs)
+        rep = np.zeros(5 * len(rs))
+        _scheck(_solve_lib().rso_hsolver_solve(self._h, len(rs), rs.ravel(), sol.ravel(), rep))
+        reps = [dict(iterations=int(rep[5 * q]), relative_residual=rep[5 * q + 1], converged=bool(rep[5 * q + 2]),
+                     seconds=rep[5 * q + 3], cycles=int(rep[5 * q + 4])) for q in range(len(rs))]
+        return sol.reshape(rhs.shape), reps

@@ -47,8 +47,13 @@ struct KernelIface {
   std::function<void(size_t, size_t, double *)> near;
 };
 
-struct BlockTree {  // block_tree.rs:61-91 (near values evaluated on demand; same values)
+struct BlockTree {  // block_tree.rs:61-91
   int N = 1;
+  // The near-field values, stored once per build as the crate stores its dense near blocks
+  // (block_tree.rs:372-415), in the order the product visits them: per leaf, per block of its
+  // chain, row-major over (row, column), N values each; near_off[li] starts leaf li.
+  std::vector<double> near_val;
+  std::vector<size_t> near_off;
   std::vector<uint32_t> start, end, right, order, position, leaves, chain_ptr, chain;
   std::vector<size_t> far_ptr, near_ptr;
   std::vector<uint32_t> far_col, near_col;
@@ -130,6 +135,42 @@ struct BlockTree {  // block_tree.rs:61-91 (near values evaluated on demand; sam
       }
   }
 
+  // Evaluates every near entry once (the kernels at (min, max) index, so the values equal the
+  // on-demand ones bit for bit).
+  void store_near() {
+    const size_t nl = leaves.size();
+    near_off.assign(nl + 1, 0);
+    for (size_t li = 0; li < nl; ++li) {
+      uint32_t l = leaves[li];
+      size_t rows = end[l] - start[l], cnt = 0;
+      for (size_t ci = chain_ptr[li]; ci < chain_ptr[li + 1]; ++ci) {
+        uint32_t a = chain[ci];
+        for (size_t q = near_ptr[a]; q < near_ptr[a + 1]; ++q) cnt += rows * (end[near_col[q]] - start[near_col[q]]);
+      }
+      near_off[li + 1] = near_off[li] + cnt * N;
+    }
+    near_val.assign(near_off[nl], 0.0);
+    parallel_for((int64_t)nl, [&](int64_t lb, int64_t le) {
+      for (int64_t li = lb; li < le; ++li) {
+        uint32_t l = leaves[li];
+        uint32_t s = start[l];
+        size_t rows = end[l] - s;
+        double *o = &near_val[near_off[li]];
+        for (size_t ci = chain_ptr[li]; ci < chain_ptr[li + 1]; ++ci) {
+          uint32_t a = chain[ci];
+          size_t r0 = s - start[a];
+          for (size_t q = near_ptr[a]; q < near_ptr[a + 1]; ++q) {
+            uint32_t b = near_col[q];
+            uint32_t sb = start[b], cb = end[b] - start[b];
+            for (size_t r = 0; r < rows; ++r)
+              for (uint32_t cc = 0; cc < cb; ++cc, o += N)
+                if (!(a == b && cc == r0 + r)) k->near(order[s + r], order[sb + cc], o);
+          }
+        }
+      }
+    });
+  }
+
   // multiply_core (block_tree.rs:536-613) with channel c on kernel kmap[c]; psi/out in BVH
   // order, C channels per element.
   void multiply_core(const std::vector<int> &kmap, const std::vector<double> &psi,
@@ -167,6 +208,7 @@ struct BlockTree {  // block_tree.rs:61-91 (near values evaluated on demand; sam
         size_t rows = end[l] - s;
         for (size_t r = 0; r < rows; ++r)
           for (size_t c = 0; c < C; ++c) out[(s + r) * C + c] = 1.0 * acc[l * C + c];
+        const double *stored = near_val.empty() ? nullptr : &near_val[near_off[li]];
         for (size_t ci = chain_ptr[li]; ci < chain_ptr[li + 1]; ++ci) {
           uint32_t a = chain[ci];
           size_t r0 = s - start[a];
@@ -177,11 +219,15 @@ struct BlockTree {  // block_tree.rs:61-91 (near values evaluated on demand; sam
               size_t i = order[s + r];
               double *o = &out[(s + r) * C];
               for (uint32_t cc = 0; cc < cb; ++cc) {
+                const double *kv = stored;
+                if (stored) stored += N;
                 if (a == b && cc == r0 + r) continue;  // the element itself
-                size_t j = order[sb + cc];
-                k->near(i, j, kvv.data());
+                if (!kv) {
+                  k->near(i, order[sb + cc], kvv.data());
+                  kv = kvv.data();
+                }
                 const double *x = &psi[(sb + cc) * C];
-                for (size_t c = 0; c < C; ++c) o[c] += kvv[kmap[c]] * x[c];
+                for (size_t c = 0; c < C; ++c) o[c] += kv[kmap[c]] * x[c];
               }
             }
           }
@@ -272,6 +318,7 @@ int rso_metric_build(int nv, const double *pos, int nf, const uint32_t *faces, d
       hi_lo(d, ns * ns, nt * nt, o);
     };
     h->bct.build(h->tree.bvh, h->kern, (size_t)leaf_pairs);
+    h->bct.store_near();
     std::vector<double> psi(2 * (size_t)nf);
     for (int f = 0; f < nf; ++f) psi[2 * f] = psi[2 * f + 1] = h->g.areas[f];
     std::vector<double> ha = h->bct.multiply({0, 1}, psi);
@@ -445,6 +492,7 @@ int rso_vfrac_build(int nv, const double *pos, const double *mass, double tau, d
       o[0] = std::pow(dot(d, d), H->expo);
     };
     h->bct.build(h->bvh, h->kern, (size_t)leaf_pairs);
+    h->bct.store_near();
     h->ha = h->bct.multiply({0}, h->mass);
     for (int v = 0; v < nv; ++v)
       if (!std::isfinite(h->ha[v])) throw Error(RSO_INVALID_OPTION, "coincident vertices");

@@ -5,13 +5,14 @@ JSON written here, never the reference tree).
 Sources (data, not code):
 
 * ``lean/oracle/fixtures/rs/*.in|*.out`` -- the Lean Float oracle's answers (bit-exact hex
-  doubles) for the tasks ``energy``, ``df``, ``metric``, ``precond`` and ``saddle``,
-  replayed by the reference's ``RS/tests/oracle.rs``;
+  doubles) for the tasks ``energy``, ``df``, ``metric``, ``constraints``, ``saddle``,
+  ``precond`` and ``step``, replayed by the reference's ``RS/tests/oracle.rs``;
 * ``crates/ddg-repulsive-surfaces/tests/fixtures/reference/{torus192,torus504,tube_regular}.*``
   -- dumps of the authors' C++ program (all-pairs and Barnes-Hut energies and differentials),
   replayed by ``RS/tests/reference_fixtures.rs``.
 
-Usage: ``python tests/golden/make_golden.py [REFERENCE_ROOT]``.
+Usage: ``python tests/golden/make_golden.py REFERENCE_ROOT`` (the root of the reference
+project's checkout).
 """
 from __future__ import annotations
 
@@ -19,7 +20,7 @@ import json
 import sys
 from pathlib import Path
 
-TASKS = {"energy", "df", "metric", "precond", "saddle"}
+TASKS = {"energy", "df", "metric", "constraints", "precond", "saddle", "step"}
 REF_MESHES = ["torus192", "torus504", "tube_regular"]
 
 
@@ -46,4 +47,6 @@ def main(root: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py REFERENCE_ROOT")
+    main(Path(sys.argv[1]))

@@ -72,6 +72,29 @@ class LeanCase:
         return np.array([[hexf(x) for x in r[1:]] for r in rows])
 
 
+    def constraint_items(self) -> list[tuple[str, int | None, list[float], list[int]]]:
+        """The ``c`` lines in order as (kind, component or None, targets, pinned vertices).
+
+        ``c barycenter all`` holds every component's barycenter separately (the Lean oracle's
+        reading, the crate's ``BarycenterMode::PerComponent``)."""
+        out = []
+        for t in self.inputs.get("c", []):
+            kind = t[0]
+            if kind == "pins":
+                n = int(t[1])
+                verts = [int(x) for x in t[2:2 + n]]
+                targets = [hexf(x) for x in t[2 + n:]]
+                out.append((kind, None, targets, verts))
+            else:
+                comp = None if t[1] == "all" else int(t[1])
+                out.append((kind, comp, [hexf(x) for x in t[2:]], []))
+        return out
+
+    def line(self, key: str) -> list[str] | None:
+        v = self.inputs.get(key)
+        return v[0] if v else None
+
+
 def lean_names(task: str, status: str | None = "ok") -> list[str]:
     out = []
     for name, c in sorted(lean_cases().items()):

@@ -171,10 +171,13 @@ std::vector<double> dense_inverse(std::vector<double> a, int n) {
 
 }  // namespace
 
-AmgHost amg_setup(const Csr &A0, int coarse_max, int max_levels) {
+AmgHost amg_setup(const Csr &A0, int coarse_max, int max_levels, const std::vector<uint32_t> *groups) {
   AmgHost H;
   H.A.push_back(A0);
   std::vector<double> z(A0.n, 1.0);  // near-null vector (constants)
+  // the group of every node (aggregates never join unconnected rows, so an aggregate lies in
+  // one group when the groups are connected components)
+  std::vector<uint32_t> gid = groups ? *groups : std::vector<uint32_t>(A0.n, 0u);
   while ((int)H.A.size() < max_levels && H.A.back().n > coarse_max) {
     const Csr &A = H.A.back();
     std::vector<double> d = diag(A);
@@ -238,10 +241,15 @@ AmgHost amg_setup(const Csr &A0, int coarse_max, int max_levels) {
     H.dinv.push_back(dinv);
     H.P.push_back(P);
     H.R.push_back(R);
+    // (A refers into H.A: read it before the push_back below)
+    std::vector<uint32_t> gc(na, 0u);
+    for (int i = 0; i < A.n; ++i) gc[agg[i]] = gid[i];
+    gid.swap(gc);
     H.A.push_back(Ac);
     z = zn;
   }
-  // coarsest level: dense inverse of A_L + (tr A_L / n) zhat zhat^T
+  // coarsest level: dense inverse of A_L + (tr A_L / n) sum_g zhat_g zhat_g^T, the constant of
+  // every group g regularised (one group: the global constant)
   const Csr &Ac = H.A.back();
   int n = Ac.n;
   {
@@ -258,11 +266,13 @@ AmgHost amg_setup(const Csr &A0, int coarse_max, int max_levels) {
       dense[(size_t)i * n + Ac.col[p]] += Ac.val[p];
       if (Ac.col[p] == i) tr += Ac.val[p];
     }
-  double zz = 0.0;
-  for (double v : z) zz += v * v;
-  double sc = (tr / std::max(n, 1)) / std::max(zz, 1e-300);
+  uint32_t ng = 0;
+  for (uint32_t g : gid) ng = std::max(ng, g + 1);
+  std::vector<double> zz(ng, 0.0);
+  for (int i = 0; i < n; ++i) zz[gid[i]] += z[i] * z[i];
   for (int i = 0; i < n; ++i)
-    for (int j = 0; j < n; ++j) dense[(size_t)i * n + j] += sc * z[i] * z[j];
+    for (int j = 0; j < n; ++j)
+      if (gid[i] == gid[j]) dense[(size_t)i * n + j] += (tr / std::max(n, 1)) / std::max(zz[gid[i]], 1e-300) * z[i] * z[j];
   H.coarse_inv = dense_inverse(dense, n);
   return H;
 }

@@ -30,7 +30,11 @@ struct AmgHost {
   std::vector<std::vector<double>> dinv;  // damped inverse diagonals of A[l]
   std::vector<double> coarse_inv;         // dense n_L x n_L
 };
-AmgHost amg_setup(const Csr &A, int coarse_max = 300, int max_levels = 12);
+// groups (optional, one label per row): rows that form separate near-null blocks (the
+// components of a surface whose barycenters are held one by one); the coarsest level is then
+// regularised along the constant of every group instead of the global constant only.
+AmgHost amg_setup(const Csr &A, int coarse_max = 300, int max_levels = 12,
+                  const std::vector<uint32_t> *groups = nullptr);
 
 // The hierarchy on the device and its V-cycle for C interleaved columns per row
 // (x[row * C + c]): pre- and post-smoothing by `sweeps` damped Jacobi steps, dense coarse solve.

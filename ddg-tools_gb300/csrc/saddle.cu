@@ -551,7 +551,7 @@ int rs_solver_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const do
       Csr K = laplacian_block(nv, nf, faces, positions_host, S->vmass, multi ? o->eps_multi_rel : o->eps_rel,
                               o->clamp_laplacian != 0, eps);
       auto t1 = clk::now();
-      AmgHost h = amg_setup(K);
+      AmgHost h = amg_setup(K, 300, 12, per_comp && ncomp > 1 ? &comp : nullptr);
       t_lap = secs(t0, t1), t_amg = secs(t1, clk::now());
       return h;
     });

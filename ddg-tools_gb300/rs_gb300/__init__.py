@@ -51,7 +51,15 @@ class FlowOptions(C.Structure):
                 ("leaf_size", C.c_int), ("solver", SolverOptions), ("hold_area", C.c_int),
                 ("hold_volume", C.c_int), ("armijo_c", C.c_double), ("max_halvings", C.c_int),
                 ("newton_max", C.c_int), ("ccd", C.c_int), ("ccd_gap", C.c_double),
-                ("ccd_max_iterations", C.c_int), ("ccd_close_factor", C.c_double)]
+                ("ccd_max_iterations", C.c_int), ("ccd_close_factor", C.c_double),
+                ("start_rule", C.c_int), ("start_value", C.c_double), ("first_rule", C.c_int),
+                ("first_value", C.c_double), ("tau_min_rel", C.c_double), ("newton_fixed", C.c_int),
+                ("newton_tolerance", C.c_double), ("area_target", C.c_double),
+                ("volume_target", C.c_double), ("guard_projection", C.c_int)]
+
+
+# StartRule codes of rs_flow_options.start_rule / first_rule
+START_ABSOLUTE, START_MAX_DISPLACEMENT, START_REFERENCE, START_GROW_PREVIOUS = 0, 1, 2, 3
 
 
 class CcdOptions(C.Structure):
@@ -164,6 +172,9 @@ def load_library(path: str | os.PathLike | None = None):
                               C.POINTER(C.c_int)],
         "rs_flow_create": [_vp, C.c_int, C.c_int, _u32p, _f64p, C.c_void_p, C.POINTER(_vp)],
         "rs_flow_step": [_vp, _f64p],
+        "rs_flow_direction": [_vp, _f64p],
+        "rs_flow_last_direction": [_vp, _f64p, _f64p],
+        "rs_flow_last_trials": [_vp, _f64p, C.c_int, C.POINTER(C.c_int)],
         "rs_flow_positions": [_vp, _f64p],
         "rs_flow_cancel": [_vp, C.c_int],
     }
@@ -705,7 +716,9 @@ FLOW_REPORT_KEYS = ["energy_before", "energy_after", "tau", "halvings", "gmres_a
                     "seconds_solver_build", "seconds_solve", "seconds_line_search", "seconds_projection",
                     "accepted", "slope", "constraint_residual", "fallbacks", "learned_solves",
                     "learned_fallbacks", "gradient_norm", "tau0", "direction_max", "newton_steps",
-                    "projection_max_rounds", "energy_trial", "tau_ccd", "seconds_ccd"]
+                    "projection_status", "energy_trial", "tau_ccd", "seconds_ccd", "projection_blocked"]
+PROJECTION_STATUS = ["converged", "maxrounds", "notimproving", "blocked"]
+TRIAL_OUTCOMES = ["accepted", "armijo-failed", "non-finite", "projection-blocked"]
 
 
 class Flow:
@@ -731,6 +744,27 @@ class Flow:
         rep = np.zeros(len(FLOW_REPORT_KEYS))
         _check(_lib.rs_flow_step(self._h, rep))
         return dict(zip(FLOW_REPORT_KEYS, rep.tolist()))
+
+    def direction(self) -> dict:
+        """Energy, differential and constrained direction at the current positions without a
+        line search (the report's solve entries); ``last_direction()`` returns x and g."""
+        rep = np.zeros(len(FLOW_REPORT_KEYS))
+        _check(_lib.rs_flow_direction(self._h, rep))
+        return dict(zip(FLOW_REPORT_KEYS, rep.tolist()))
+
+    def last_direction(self) -> tuple[np.ndarray, np.ndarray]:
+        """(x, g), V x 3 each, of the last step or direction: the step moves f <- f - tau x."""
+        x, g = np.empty((self.n_vertices, 3)), np.empty((self.n_vertices, 3))
+        _check(_lib.rs_flow_last_direction(self._h, x.ravel(), g.ravel()))
+        return x, g
+
+    def last_trials(self) -> list[tuple[float, float, str]]:
+        """(tau, energy, outcome) of every line-search trial of the last step."""
+        n = C.c_int()
+        _check(_lib.rs_flow_last_trials(self._h, np.zeros(3), 0, C.byref(n)))
+        out = np.zeros(3 * max(n.value, 1))
+        _check(_lib.rs_flow_last_trials(self._h, out, n.value, C.byref(n)))
+        return [(out[3 * i], out[3 * i + 1], TRIAL_OUTCOMES[int(out[3 * i + 2])]) for i in range(n.value)]
 
     def set_learned(self, model: "LearnedModel | None", cheap_steps: int = 2, max_iterations: int = 0) -> None:
         self._learned = model

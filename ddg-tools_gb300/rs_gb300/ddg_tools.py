@@ -33,8 +33,8 @@ from collections import deque
 
 import numpy as np
 
-from . import (BhOptions, BhTree, Context, Exponents, Flow, RsError, device_count, device_info,
-               flow_options, load_library)
+from . import (PROJECTION_STATUS, BhOptions, BhTree, Context, Exponents, Flow, RsError, device_count,
+               device_info, flow_options, load_library)
 
 
 class DdgError(Exception):
@@ -565,7 +565,7 @@ class RepulsiveSurfaceSession:
             "gradient_norm": r["gradient_norm"], "sobolev_norm_sq": slope,
             "tau": r["tau"], "tau0": r["tau0"], "tau_ccd": None if math.isnan(r["tau_ccd"]) else r["tau_ccd"],
             "halvings": int(r["halvings"]), "newton_steps": int(r["newton_steps"]),
-            "projection": "maxrounds" if r["projection_max_rounds"] > 0 else "converged",
+            "projection": PROJECTION_STATUS[int(r["projection_status"])],
             "max_violation": r["constraint_residual"], "dropped_rows": [],
             "linear": {"solver": "gmres", "dimension": 3 * self.n_vertices + 3, "solves": holds + 1,
                        "iterations": iters, "relative_residual": r["relative_residual"]},

@@ -4,7 +4,7 @@
  *
  * A plain C ABI: opaque handles, plain pointers and sizes, int status codes. It is the
  * boundary a host in any language binds (the reference's Rust crate would bind it with
- * `extern "C"` declarations; see INTEGRATION.md). Each entry point names the reference
+ * `extern "C"` declarations). Each entry point names the reference
  * interface it replaces (paths relative to the reference project; RS/ =
  * crates/ddg-repulsive-surfaces/).
  *
@@ -313,6 +313,21 @@ typedef struct rs_flow_options {
   double ccd_gap;            /* CcdOptions: gap relative to the initial mean edge length (0.05), */
   int ccd_max_iterations;    /* advances per pair and window (100), */
   double ccd_close_factor;   /* closing fraction of pairs closer than the gap (0.5) */
+  /* StartRule (RS/src/step/options.rs:60-107; session.rs:1604-1615): 3 GrowPrevious (the last
+   * accepted tau times start_value; the first step uses first_rule with first_value), 0 Absolute
+   * (tau = start_value), 1 MaxDisplacement (the farthest vertex moves start_value initial mean
+   * edge lengths), 2 Reference (tau = 2 / |x|). Default: 3, 2.0, first 1, 1.0. */
+  int start_rule;
+  double start_value;
+  int first_rule;
+  double first_value;
+  double tau_min_rel;        /* the search stops below tau_min_rel l0 / |x|_inf (1e-12) */
+  int newton_fixed;          /* 1: NewtonSteps::Fixed(newton_max), 0: UntilTolerance (0) */
+  double newton_tolerance;   /* a held row is met within newton_tolerance |target| (1e-8,
+                                NONLINEAR_TOLERANCE, RS/src/constraints/mod.rs:147) */
+  double area_target;        /* NaN: the initial total area */
+  double volume_target;      /* NaN: the initial volume */
+  int guard_projection;      /* keep an Armijo trial only if its projection is admissible (1) */
 } rs_flow_options;
 
 rs_flow_options rs_flow_options_default(void);
@@ -398,7 +413,7 @@ int rs_ccd_intersecting_pairs(rs_ccd *c, const double *positions, int64_t cap, u
 /* Wall seconds of the last rs_ccd_first_contact. No counterpart in the crate. */
 int rs_ccd_last_seconds(rs_ccd *c, double *seconds);
 
-#define RS_FLOW_REPORT_LEN 29
+#define RS_FLOW_REPORT_LEN 30
 /* Session::step (session.rs:724-747): one step. report[RS_FLOW_REPORT_LEN]:
  *  0 energy before, 1 energy after the projection (on the step's lists; the energy before
  *  when refused), 2 accepted tau (0: refused), 3 halvings,
@@ -422,6 +437,18 @@ int rs_ccd_last_seconds(rs_ccd *c, double *seconds);
 int rs_flow_step(rs_flow *f, double *report);
 /* The current positions (V x 3). */
 int rs_flow_positions(rs_flow *f, double *positions_host);
+/* The energy, differential and constrained direction at the current positions, without a line
+ * search (Objective::evaluate and SchurComplement::with_direction, RS/src/step/objective.rs:
+ * 151-249, RS/src/solve/schur.rs:101-126, as step_inner computes them, session.rs:771-860).
+ * report as rs_flow_step's entries 0, 4..12, 16, 18, 21, 23; the positions do not change. */
+int rs_flow_direction(rs_flow *f, double *report);
+/* The direction x (f <- f - tau x) and the differential g (V x 3 each) of the last
+ * rs_flow_step or rs_flow_direction (StepReport's direction and gradient, session.rs:1255-1262). */
+int rs_flow_last_direction(rs_flow *f, double *x_host, double *g_host);
+/* The line-search trials of the last step (StepReport::trials, session.rs:1262): up to
+ * max_trials triples (tau, energy, outcome: 0 accepted, 1 Armijo failed, 2 non-finite,
+ * 3 projection blocked); *n_trials is their number. */
+int rs_flow_last_trials(rs_flow *f, double *out3, int max_trials, int *n_trials);
 /* Uses (model != NULL) or stops using a learned preconditioner in the following steps (see
  * rs_solver_set_learned); the model must outlive its use. No counterpart in the crate. */
 int rs_flow_set_learned(rs_flow *f, rs_learned *model, int cheap_steps, int max_iterations);

@@ -44,8 +44,9 @@ def test_defaults_are_the_references_on_the_path():
 
 
 def _fields(st):
-    """A ctypes structure as nested tuples of its fields (its padding bytes are unset)."""
-    return tuple(_fields(v) if hasattr(v, "_fields_") else v
+    """A ctypes structure as nested tuples of its fields (its padding bytes are unset); NaN
+    fields (unset targets) as a string so that equal structures compare equal."""
+    return tuple(_fields(v) if hasattr(v, "_fields_") else ("nan" if v != v else v)
                  for v in (getattr(st, n) for n, _ in st._fields_))
 
 

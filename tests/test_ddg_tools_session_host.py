@@ -20,7 +20,7 @@ def _report(accepted=True, e0=10.0, e1=9.0, slope=1.0):
              seconds_energy=0.0, seconds_solver_build=0.0, seconds_solve=0.0, seconds_line_search=0.0,
              seconds_projection=0.0, accepted=1.0 if accepted else 0.0, slope=slope, constraint_residual=0.0,
              fallbacks=0.0, learned_solves=0.0, learned_fallbacks=0.0, gradient_norm=1.0, tau0=0.1,
-             direction_max=1.0, newton_steps=0.0, projection_max_rounds=0.0, energy_trial=e1,
+             direction_max=1.0, newton_steps=0.0, projection_status=0.0, energy_trial=e1,
              tau_ccd=math.nan, seconds_ccd=0.0)
 
 

@@ -1,9 +1,17 @@
 """The no-allocation variant of the metric product, rs_metric_apply_device_noalloc, called
-through the C ABI: two calls in a row give the product of the regular device entry point
-rs_metric_apply_device on the same input (the same kernels in the same order, so the tolerance
-below is loose for what is expected to be equal bit for bit), and a product whose scratch would
-exceed the fixed 64 MiB is refused with InvalidOption. Collected last on purpose; it also
-passes alone in a fresh process, where its first call does the scratch set-up."""
+through the C ABI. It exists for callers that cannot allocate device memory while a product
+runs (a host whose device memory is held by its own pool after set-up, or a latency-critical
+stream, since cudaMalloc and cudaFree can synchronize the device).
+
+* On a freshly built metric, before any regular product has reserved that metric's buffers,
+  two no-alloc calls in a row leave the device's free memory unchanged (cudaMemGetInfo), and
+  both give the product of the regular device entry point rs_metric_apply_device on the same
+  input (the same kernels in the same order, so the tolerance below is loose for what is
+  expected to be equal bit for bit).
+* A product whose scratch would exceed the fixed 64 MiB is refused with InvalidOption.
+
+Collected last on purpose; it also passes alone in a fresh process, where its first call does
+the scratch set-up."""
 import ctypes as C
 
 import numpy as np
@@ -32,15 +40,23 @@ def test_noalloc_product_matches_the_device_entry_point(nb):
     torch = pytest.importorskip("torch")
     ctx = R.Context(0)
     P, F = gen.config_c2(level=4)
-    m = R.FaceMetricTree(F, P, R.Exponents(), R.ClusterTreeOptions(), ctx)
     x = torch.from_numpy(np.random.default_rng(11).standard_normal((nb, 3 * len(P)))).cuda()
     y_ref = torch.zeros_like(x)
     y1 = torch.full_like(x, float("nan"))
     y2 = torch.full_like(x, float("nan"))
+    # the kernels of the product loaded once (lazy module loading may place their code on first
+    # use), on another metric of the same mesh
+    warm = R.FaceMetricTree(F, P, R.Exponents(), R.ClusterTreeOptions(), ctx)
+    _noalloc(warm, x, y1, nb, 1.0, 0.7)
+    m = R.FaceMetricTree(F, P, R.Exponents(), R.ClusterTreeOptions(), ctx)
+    ctx.synchronize()
     torch.cuda.synchronize()
-    m.apply_device(x.data_ptr(), y_ref.data_ptr(), nb, 1.0, 0.7)
+    free0 = torch.cuda.mem_get_info()[0]
     _noalloc(m, x, y1, nb, 1.0, 0.7)
     _noalloc(m, x, y2, nb, 1.0, 0.7)
+    ctx.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free0  # nothing allocated by the two calls
+    m.apply_device(x.data_ptr(), y_ref.data_ptr(), nb, 1.0, 0.7)
     ctx.synchronize()
     ref = y_ref.cpu().numpy()
     assert np.all(np.isfinite(ref))

@@ -45,6 +45,7 @@ def check(ctx, P, F, theta, alpha=6.0, beta=12.0, leaf=8, lists_equal=True):
         assert s["pairs_exact"] == so["pairs_exact"]
     E, dE = t.energy_and_differential(ex)
     Eo, dEo = o.energy_and_differential(alpha, beta)
+    print(f"energy {rel(E, Eo):.2e} differential {G.normwise(dE, dEo):.2e}")
     assert rel(E, Eo) <= E_TOL, (E, Eo)
     assert G.normwise(dE, dEo) <= D_TOL
     return t, o, E, dE
@@ -189,6 +190,16 @@ def test_full_size_c2_against_oracle(ctx):
     """Config c2 at its full size (81,920 faces, theta 0.25) against the FP64 oracle."""
     P, F = gen.config_c2()
     check(ctx, P, F, 0.25)
+
+
+@pytest.mark.parametrize("sigma", [0.01, 0.001])
+def test_full_size_c3_against_oracle(ctx, sigma):
+    """The 204,800-face torus of the step configuration at its full size (theta 0.25), as
+    specified (noise 0.01, crumpled) and as the flow bench runs it (0.001): trees and lists equal
+    to the oracle's, energy within 1e-6 and differential within 1e-5 of the FP64 oracle."""
+    P, F = gen.config_c3(sigma=sigma)
+    _, _, E, dE = check(ctx, P, F, 0.25)
+    print(f"c3 sigma {sigma}: E {E:.6e}")
 
 
 def test_full_size_c3_identities(ctx):

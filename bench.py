@@ -19,11 +19,11 @@ is N(0, 0.001) per coordinate: the specified N(0, 0.01) exceeds the torus' minor
   against the measured HBM copy bandwidth, with its FP32 view (``compute``: counted FLOP
   against the measured FP32 FMA peak; the compensated arithmetic keeps it at the FP32 issue
   limit, far below HBM); the pair kernel is reported beside it.
-* ``cpu_baseline`` / ``--impl reference``: the FP64 C++ restatement of the reference (the
-  oracle; the Rust crate cannot be built here) on the host cores: one BH energy + differential
-  and one metric product of the same mesh, combined with the step's measured GMRES iteration
-  counts into a CPU step time (preconditioner and set-up not counted: an upper bound on the
-  CPU's steps/s).
+* ``cpu_baseline`` / ``--impl reference``: complete FP64 steps of the C++ restatement of the
+  reference (the oracle; the Rust crate cannot be built here) on the host cores, from the
+  workload's start surface with the same settings: Barnes-Hut objective, hierarchical saddle
+  solver with a sparse LDL^T of L' and the augmented preconditioner, three GMRES solves to
+  1e-6, Armijo search and projection (about a minute on 16 host cores).
 
 ``--workload c2`` / ``c3``: the Barnes-Hut pair kernel alone (GFLOP/s, 61 FLOP per pair
 interaction) on the 81,920-face icosphere or the specified torus.
@@ -257,58 +257,80 @@ def near_roofline(near_entries, n_faces, t_rows_ms, fp32_peak, traffic, kernel_m
                         "frac": (tflops / fp32_peak) if tflops else None,
                         "peak_source": "measured FP32 FMA throughput (rs_fp32_peak)",
                         "work": f"{NEAR_FLOP_PER_ENTRY} FLOP x {near_entries} near entries per launch"}}
-# Operator applications per step assumed by the CPU reference arm (which has no preconditioned
-# solver of its own): the GPU arm's mean on this workload, GMRES iterations of the three
-# right-hand sides.
-REFERENCE_ITERATIONS_PER_STEP = 188
-
-
 def flow_options(R):
     return R.flow_options(theta=0.25, hold_area=1, hold_volume=1, solver_chi=0.5, solver_restart=30,
                           solver_tolerance=1e-6, solver_max_iterations=300)
 
 
-def cpu_flow_step(P, F, theta, iterations, threads=None):
-    """The FP64 oracle on the host cores: one BH energy + differential and one metric product
-    of the mesh, combined into a step of `iterations` operator applications."""
+def cpu_flow_step(P, F, theta, threads=None, l0=0.0):
+    """One complete FP64 step of the oracle on the host cores, with the GPU arm's settings: the
+    Barnes-Hut objective (lists frozen for the step), the hierarchical saddle solver (metric tree
+    chi 0.5, vertex fractional tree, sparse LDL^T of L', the augmented preconditioner), three
+    GMRES solves (restart 30, true relative residual 1e-6), the Armijo search and the projection
+    (Session::step_inner without remeshing and collision detection). Returns (steps/s, report,
+    threads)."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import rs_oracle as O
 
     O.build()
     n = threads or os.cpu_count() or 1
     O.set_threads(n)
-    bh = O.BhTree(P, F, theta=theta)
+    cons = O.Constraints().barycenter().area().volume()
+    o = O.step_options(backend=1, energy_theta=theta, max_halvings=30, start_rule=3, start_value=2.0,
+                       first_rule=1, first_value=1.0, l0=l0,
+                       solver={"chi": 0.5, "restart": 30, "tolerance": 1e-6, "max_iterations": 300})
     t0 = time.perf_counter()
-    bh.energy_and_differential()
-    t_bh = time.perf_counter() - t0
-    m = O.FaceMetricTree(P, F, chi=0.5)
-    x = np.random.default_rng(0).standard_normal(3 * len(P))
-    t0 = time.perf_counter()
-    m.apply(x)
-    t_prod = time.perf_counter() - t0
-    t_step = t_bh + iterations * t_prod
-    return 1.0 / t_step, t_bh, t_prod, n
+    rep = O.step(P, F, cons, o)
+    dt = time.perf_counter() - t0
+    return 1.0 / dt, rep, n
+
+
+def _cpu_step_summary(rep, n, dt_label=""):
+    return (f"one complete FP64 step of the workload's start surface (BH energy and differential, "
+            f"solver build with a sparse LDL^T of L', 3 GMRES solves of {int(rep['gmres_iterations'])} "
+            f"iterations in total, Armijo search, projection) by the C++ restatement of the reference "
+            f"on {n} threads in {rep['s_total']:.1f} s{dt_label}: objective build {rep['s_objective']:.1f} s, "
+            f"energy {rep['s_energy']:.1f} s, solver build {rep['s_solver_build']:.1f} s, solves "
+            f"{rep['s_solve']:.1f} s, line search {rep['s_line_search']:.1f} s, projection "
+            f"{rep['s_projection']:.1f} s; the reference crate (Rust) cannot be built here")
 
 
 def run_reference_flow(args, rank):
+    """The reference arm of the flow workloads: complete FP64 steps of the oracle, as many as
+    fit in about two minutes after the first (at least one), from the workload's start surface."""
     if rank != 0:
         return 0
     P, F, theta, desc = workload(args.workload)
-    v, t_bh, t_prod, n = cpu_flow_step(P, F, theta, REFERENCE_ITERATIONS_PER_STEP)
-    sample = (f"one BH energy+differential ({t_bh:.2f} s) and one metric product ({t_prod:.2f} s) of the "
-              f"workload by the FP64 C++ restatement on {n} threads, combined as a step of "
-              f"{REFERENCE_ITERATIONS_PER_STEP} operator applications (preconditioner and set-up not "
-              "counted); the reference crate (Rust) cannot be built here")
+    t_all = time.perf_counter()
+    v, rep, n = cpu_flow_step(P, F, theta)
+    times = [1.0 / v]
+    while time.perf_counter() - t_all + times[-1] < 120.0 and len(times) < args.steps:
+        v2, _, _ = cpu_flow_step(P, F, theta)
+        times.append(1.0 / v2)
+    value = len(times) / sum(times)
     line = {
-        "impl": "reference", "metric": FLOW_METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus,
-        "steps": 1, "warmup": 0, "ms_per_step": 1e3 / v, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"{args.workload}: {desc}", "theta": theta, "chi": 0.5, "alpha": 6, "beta": 12},
-        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": n, "kind": "port", "sample": sample},
-        "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "impl": "reference", "metric": FLOW_METRIC, "value": value, "unit": "steps/s", "n_gpus": args.gpus,
+        "steps": len(times), "warmup": 0, "ms_per_step": 1e3 / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": flow_config(args.workload, desc, theta, 1),
+        "cpu_baseline": {"value": value, "unit": "steps/s", "cores": n, "kind": "port",
+                         "sample": _cpu_step_summary(rep, n) + f"; {len(times)} step(s) timed, the same step "
+                                   "from the same start each time (no warm-up: no JIT or cache to warm)"},
+        "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "step_report": {k: rep[k] for k in ("energy_before", "energy_after", "tau", "accepted", "gmres_iterations",
+                                            "worst_residual", "newton_rounds")},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def flow_config(workload_name, desc, theta, world):
+    return {"workload": f"{workload_name}: {desc}", "theta": theta, "chi": 0.5, "alpha": 6, "beta": 12,
+            "leaf_size": 8, "constraints": "barycenter + area + volume (3 right-hand sides per step)",
+            "gmres": "restart 30, true relative residual 1e-6, at most 300 iterations",
+            "line_search": "Armijo c 1e-2, start: farthest vertex one mean edge, then twice the last tau",
+            "l2": "not flushed: every step moves several GB (trees, lists, solver rebuilt)",
+            "parallelism": "replicas" if world > 1 else "single GPU"}
 
 
 def bench_flow(args, rank, world, local):
@@ -327,7 +349,10 @@ def bench_flow(args, rank, world, local):
     dev = torch.device(f"cuda:{local}")
     stream = torch.cuda.ExternalStream(ctx.stream, device=dev)
     flow = R.Flow(F, P, flow_options(R), ctx)
-    for _ in range(warmup):
+    t0 = time.perf_counter()
+    first = flow.step()  # the first step from the start surface (the CPU arm's step)
+    first_wall = time.perf_counter() - t0
+    for _ in range(warmup - 1):
         flow.step()
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
            for _ in range(args.steps)]
@@ -442,12 +467,9 @@ def bench_flow(args, rank, world, local):
         "warmup": warmup, "ms_per_step": t_total / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded mesh generator of the configuration)",
-        "config": {"workload": f"{args.workload}: {desc}", "theta": theta, "chi": 0.5, "alpha": 6, "beta": 12,
-                   "leaf_size": 8, "constraints": "barycenter + area + volume (3 right-hand sides per step)",
-                   "gmres": "restart 30, true relative residual 1e-6, FP64 Arnoldi (CGS2)",
-                   "preconditioner": "fractional (plain); L' by 6 multigrid-preconditioned CG steps",
-                   "l2": "not flushed: every step moves several GB (trees, lists, solver rebuilt)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "config": flow_config(args.workload, desc, theta, world),
+        "implementation": {"gmres": "FP64 Arnoldi (CGS2) on the device",
+                           "preconditioner": "fractional (plain); L' by 6 multigrid-preconditioned CG steps"},
         "steps_report": {
             "gmres_iterations_per_step": float(np.mean(its)),
             "gmres_iterations": [[int(r["gmres_area"]), int(r["gmres_volume"]), int(r["gmres_direction"])]
@@ -466,6 +488,11 @@ def bench_flow(args, rank, world, local):
         "pair_kernel": {"gflops": FLOP_PER_INTERACTION * n_int / (t_pair * 1e-3) / 1e9 if t_pair else None,
                         "interactions": n_int, "ms": t_pair,
                         "frac": (FLOP_PER_INTERACTION * n_int / (t_pair * 1e-3) / 1e12 / peak) if t_pair else None},
+        "first_step": {"wall_s": first_wall, "gmres_iterations": int(first["gmres_area"] + first["gmres_volume"]
+                                                                   + first["gmres_direction"]),
+                       "energy": [first["energy_before"], first["energy_after"]],
+                       "note": "the first (warm-up) step from the start surface, the step the CPU arm "
+                               "times; host wall clock including the library's first-use set-up"},
         "solve_phases_ms": solve_phases,
         "learned_preconditioner": learned,
         "step_with_ccd": with_ccd,
@@ -473,14 +500,9 @@ def bench_flow(args, rank, world, local):
         "clocks": clk.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        its_mean = float(np.mean(its))
-        v, t_bh, t_prod, n = cpu_flow_step(F=F, P=Q, theta=theta, iterations=its_mean)
-        line["cpu_baseline"] = {
-            "value": v, "unit": "steps/s", "cores": n, "kind": "port",
-            "sample": f"one BH energy+differential ({t_bh:.2f} s) and one metric product ({t_prod:.2f} s) "
-                      f"of the current surface by the FP64 C++ restatement on {n} threads, combined as a "
-                      f"step of {its_mean:.0f} operator applications (the measured GMRES iterations; "
-                      "preconditioner and set-up not counted)"}
+        v, crep, n = cpu_flow_step(P, F, theta)
+        line["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": n, "kind": "port",
+                                "sample": _cpu_step_summary(crep, n)}
     if world > 1:
         torch.distributed.destroy_process_group()
     print(json.dumps(line), flush=True)

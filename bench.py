@@ -359,6 +359,7 @@ def bench_flow(args, rank, world, local):
     reps = []
     if world > 1:
         torch.distributed.barrier()
+    Q0 = flow.positions()  # the start of the timed steps, for the e2e run over the same steps
     torch.cuda.synchronize(dev)
     l0 = ctx.launch_count()
     with Clocks(local) as clk:
@@ -371,15 +372,17 @@ def bench_flow(args, rank, world, local):
     ms = [a.elapsed_time(b) for a, b in evs]
     value, t_total = replica_rate(args.steps, sum(ms) / 1e3, world, dev)
 
-    # e2e: the public call with host positions read back after every step, wall clock
+    # e2e: the public call with host positions read back after every step, wall clock, over the
+    # same steps: a flow created from the positions where the timed steps started
     if world > 1:
         torch.distributed.barrier()
+    flow_e = R.Flow(F, Q0, flow_options(R), ctx)
     c0 = R.copy_counters()
     t0 = time.perf_counter()
     e2e_reps = []
     for _ in range(args.steps):
-        e2e_reps.append(flow.step())
-        Q = flow.positions()
+        e2e_reps.append(flow_e.step())
+        Q = flow_e.positions()
     c1 = R.copy_counters()
     e2e, t_e2e = replica_rate(args.steps, time.perf_counter() - t0, world, dev)
 
@@ -404,6 +407,35 @@ def bench_flow(args, rank, world, local):
                                   "GMRES capped at 100 iterations before the plain fallback"}
     except R.RsError as e:
         learned = {"error": str(e)}
+    # the step configuration's own noise, N(0, 0.01) (1.7 minor edge lengths: a crumpled torus):
+    # one step from it with the same settings, the residual GMRES reaches there, and the
+    # operator's linearity defect |A(x (1 + 2^-20)) / (1 + 2^-20) - A x| / |A x| on the
+    # direction's solution, which shows that conditioning, not rounding, limits the solve
+    flow_spec = None
+    if args.workload == "flow":
+        try:
+            Ps, Fs = workload("flow-spec")[:2]
+            fs = R.Flow(Fs, Ps, flow_options(R), ctx)
+            t0 = time.perf_counter()
+            rs = fs.step()
+            t_fs = time.perf_counter() - t0
+            Ss = R.SaddleSolver(Fs, Ps, R.Exponents(), R.solver_options(chi=0.5, restart=30, tolerance=1e-6,
+                                                                        max_iterations=300), ctx)
+            xs, gs = fs.last_direction()
+            v = np.zeros((1, Ss.n))
+            v[0, :Ss.n_dofs] = xs.ravel()
+            a1 = Ss.apply(v)[0]
+            a2 = Ss.apply(v * (1.0 + 2.0 ** -20))[0] / (1.0 + 2.0 ** -20)
+            flow_spec = {"noise": 0.01, "seconds_step": t_fs, "relative_residual": rs["relative_residual"],
+                         "gmres_iterations": [int(rs["gmres_area"]), int(rs["gmres_volume"]),
+                                              int(rs["gmres_direction"])],
+                         "energy": [rs["energy_before"], rs["energy_after"]], "accepted": rs["accepted"],
+                         "operator_linearity_defect": float(np.linalg.norm(a2 - a1) / np.linalg.norm(a1)),
+                         "note": "one step of the specified N(0, 0.01) torus with the headline settings "
+                                 "(tolerance 1e-6, 300 iterations): the residual GMRES reaches there"}
+            del fs, Ss
+        except R.RsError as e:
+            flow_spec = {"error": str(e)}
     # one step with the collision cap of the line search (rs_flow_options.ccd, the crate's
     # default line search) on the current surface: its cost inside a step
     with_ccd = None
@@ -494,6 +526,7 @@ def bench_flow(args, rank, world, local):
                        "note": "the first (warm-up) step from the start surface, the step the CPU arm "
                                "times; host wall clock including the library's first-use set-up"},
         "solve_phases_ms": solve_phases,
+        "flow_spec": flow_spec,
         "learned_preconditioner": learned,
         "step_with_ccd": with_ccd,
         "gpu_launches": launches,

@@ -138,6 +138,9 @@ struct rs_flow {
   std::vector<uint32_t> group;   // group of every vertex
   std::vector<double> bary0;     // target barycenter of every group (3 per group)
   std::vector<double> last_x, last_g, trials;  // the last direction, differential, trials
+  std::vector<double> last_sol;  // the last step's saddle solutions: Z columns, then y (n each)
+  int last_k = 0;
+  int64_t last_n = 0;
   rs_learned *lmodel = nullptr;
   int l_cheap = 2, l_cap = 0;
   int iteration = 0;
@@ -534,6 +537,7 @@ void flow_step(rs_flow *F, double *report, bool direction_only) {
   rep[23] = xinf;
   rep[0] = E0;
   F->last_x = x, F->last_g = g;
+  F->last_sol = hs, F->last_k = k, F->last_n = (int64_t)n;
   if (direction_only) {
     rep[1] = E0, rep[26] = E0;
     rep[8] = since(t_step);
@@ -752,6 +756,15 @@ int rs_flow_last_direction(rs_flow *F, double *x_host, double *g_host) {
     if (F->last_x.empty()) fail(RS_INVALID_OPTION, "InvalidOption", "flow", "no step or direction computed yet");
     if (x_host) std::memcpy(x_host, F->last_x.data(), F->last_x.size() * sizeof(double));
     if (g_host) std::memcpy(g_host, F->last_g.data(), F->last_g.size() * sizeof(double));
+  });
+}
+
+int rs_flow_last_solutions(rs_flow *F, double *sol_host, int *n_held, int64_t *n) {
+  return guard([&] {
+    if (F->last_sol.empty()) fail(RS_INVALID_OPTION, "InvalidOption", "flow", "no step or direction computed yet");
+    if (n_held) *n_held = F->last_k;
+    if (n) *n = F->last_n;
+    if (sol_host) std::memcpy(sol_host, F->last_sol.data(), F->last_sol.size() * sizeof(double));
   });
 }
 

@@ -165,6 +165,128 @@ __global__ void shift_kernel(const double *__restrict__ cy, const double *__rest
   shift[t] = r[q * ld + nd + i] - cy[t];
 }
 
+// ---- the coarse space (CoarseSpace, RS/src/solve/coarse.rs:101-327): columns 3 k + a are the
+// translations of free component slot k along axis a, scaled by 1/sqrt(|members|); the last
+// n_rows columns are the multipliers of the positional rows that touch a free component.
+
+// t[q][j] = (Z^T x_q)_j from the slot sums gs[q][3 k + a] (slot n_free collects the vertices
+// of fixed components) and the multiplier entries of x.
+__global__ void coarse_zt_kernel(const double *__restrict__ gs, int gstride, const double *__restrict__ x,
+                                 size_t ld, size_t nd, int nb, int nfree, const double *__restrict__ scale,
+                                 const int *__restrict__ rows, int nrows, double *__restrict__ t) {
+  const int cm = 3 * nfree + nrows;
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nb * cm) return;
+  int q = i / cm, j = i % cm;
+  t[i] = j < 3 * nfree ? scale[j / 3] * gs[(size_t)q * gstride + j] : x[q * ld + nd + rows[j - 3 * nfree]];
+}
+
+// out[q][i] = sum_j E+[i][j] t[q][j]; with sub, out = sub - that
+__global__ void coarse_esolve_kernel(const double *__restrict__ epinv, const double *__restrict__ t, int nb, int cm,
+                                     const double *__restrict__ sub, double *__restrict__ out) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nb * cm) return;
+  int q = k / cm, i = k % cm;
+  double s = 0.0;
+  for (int j = 0; j < cm; ++j) s += epinv[i * cm + j] * t[q * cm + j];
+  out[k] = sub ? sub[k] - s : s;
+}
+
+// rp_q = r_q - (A'Z) yc_q
+__global__ void coarse_sub_kernel(const double *__restrict__ r, double *__restrict__ rp, size_t ld, size_t n, int nb,
+                                  const double *__restrict__ az, const double *__restrict__ yc, int cm) {
+  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= (size_t)nb * n) return;
+  int q = (int)(t / n);
+  size_t i = t % n;
+  double s = r[q * ld + i];
+  for (int j = 0; j < cm; ++j) s -= az[(size_t)j * n + i] * yc[q * cm + j];
+  rp[q * ld + i] = s;
+}
+
+// part[b][q][j] = the chunk b partial of (A'Z)_j . z_q (fixed chunks, fixed order in a chunk)
+constexpr int kCoarseChunks = 128;
+__global__ void coarse_azt_partial(const double *__restrict__ az, const double *__restrict__ z, size_t ld, size_t n,
+                                   int nb, int cm, double *__restrict__ part) {
+  const int b = blockIdx.x, qj = blockIdx.y, q = qj / cm, j = qj % cm;
+  const size_t chunk = (n + kCoarseChunks - 1) / kCoarseChunks, i0 = b * chunk, i1 = min(n, i0 + chunk);
+  double s = 0.0;
+  for (size_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) s += az[(size_t)j * n + i] * z[q * ld + i];
+  __shared__ double ws[8];
+  for (int m = 16; m >= 1; m >>= 1) s += __shfl_xor_sync(0xffffffffu, s, m);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += ws[w];
+    part[(size_t)b * nb * cm + qj] = t;
+  }
+}
+__global__ void coarse_azt_finish(const double *__restrict__ part, int nbcm, double *__restrict__ out) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nbcm) return;
+  double s = 0.0;
+  for (int b = 0; b < kCoarseChunks; ++b) s += part[(size_t)b * nbcm + k];
+  out[k] = s;
+}
+
+// z_q += Z c_q
+__global__ void coarse_addz_kernel(double *__restrict__ z, size_t ld, size_t nd, size_t n, int nb,
+                                   const uint32_t *__restrict__ slot_of_vertex, int nfree,
+                                   const double *__restrict__ scale, const int *__restrict__ rowcol,
+                                   const double *__restrict__ c, int cm) {
+  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (t >= (size_t)nb * n) return;
+  int q = (int)(t / n);
+  size_t i = t % n;
+  if (i < nd) {
+    const uint32_t k = slot_of_vertex[i / 3];
+    if ((int)k < nfree) z[q * ld + i] += scale[k] * c[q * cm + 3 * k + (int)(i % 3)];
+  } else {
+    const int j = rowcol[i - nd];
+    if (j >= 0) z[q * ld + i] += c[q * cm + j];
+  }
+}
+
+// Symmetric eigendecomposition (m x m, row-major) by cyclic Jacobi rotations: the coarse matrix
+// has 3 columns per free component and one per multiplier row.
+void jacobi_eigen(int m, std::vector<double> a, std::vector<double> &lam, std::vector<double> &u) {
+  u.assign((size_t)m * m, 0.0);
+  for (int i = 0; i < m; ++i) u[(size_t)i * m + i] = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j) {
+        const double x = a[(size_t)i * m + j] * a[(size_t)i * m + j];
+        tot += x;
+        if (i != j) off += x;
+      }
+    if (!(off > 1e-30 * tot)) break;
+    for (int p = 0; p < m; ++p)
+      for (int q = p + 1; q < m; ++q) {
+        const double apq = a[(size_t)p * m + q];
+        if (apq == 0.0) continue;
+        const double th = 0.5 * (a[(size_t)q * m + q] - a[(size_t)p * m + p]) / apq;
+        const double t = (th >= 0.0 ? 1.0 : -1.0) / (std::fabs(th) + std::sqrt(th * th + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < m; ++k) {
+          const double akp = a[(size_t)k * m + p], akq = a[(size_t)k * m + q];
+          a[(size_t)k * m + p] = c * akp - sn * akq, a[(size_t)k * m + q] = sn * akp + c * akq;
+        }
+        for (int k = 0; k < m; ++k) {
+          const double apk = a[(size_t)p * m + k], aqk = a[(size_t)q * m + k];
+          a[(size_t)p * m + k] = c * apk - sn * aqk, a[(size_t)q * m + k] = sn * apk + c * aqk;
+        }
+        for (int k = 0; k < m; ++k) {
+          const double ukp = u[(size_t)k * m + p], ukq = u[(size_t)k * m + q];
+          u[(size_t)k * m + p] = c * ukp - sn * ukq, u[(size_t)k * m + q] = sn * ukp + c * ukq;
+        }
+      }
+  }
+  lam.resize(m);
+  for (int i = 0; i < m; ++i) lam[i] = a[(size_t)i * m + i];
+}
+
 // Planar symbol ratio 4 I(sigma) I(2 - s) of W^-1 L_{2-s} W^-1 B, I(t) = pi Gamma(1-t) /
 // (t 4^t Gamma(1+t)) (fractional_symbol_ratio, RS/src/solve/precond.rs:548-568).
 double symbol_ratio(double s) {
@@ -207,16 +329,61 @@ struct rs_solver {
   DevBuf<mgreal> mg_in, mg_out;  // right-hand sides and solutions on the multigrid layout
   std::vector<GmresReport> last;
   Operator op, prec;
+  // the coarse space (coarse.rs): cm columns, 0 when every component is fixed by rows of its own
+  int cm = 0, c_nfree = 0;
+  std::vector<int> c_rows_h;                // multiplier rows touching a free component
+  DevBuf<uint32_t> c_slot;                  // per vertex: free slot of its component, n_free if fixed
+  DevBuf<double> c_scale, c_az, c_epinv;    // per slot 1/sqrt(|members|); A'Z (n x cm); E+ (cm x cm)
+  DevBuf<int> c_rows, c_rowcol;             // the rows; per multiplier row its column or -1
+  DevBuf<double> c_t, c_yc, c_t2, c_part, c_rp;
+  double c_conditioning = 0.0;
+  int c_dropped = 0;
 
   cudaStream_t st() const { return ctx->stream; }
 
   // group sums (weighted by c or not) of nb vectors into out [nb][3G]
   void group_sums(const double *x, size_t ld, int nb, const double *wgt, double *out) {
-    int K = 3 * G * nb;
+    group_sums_by(x, ld, nb, wgt, group.p, G, out);
+  }
+  void group_sums_by(const double *x, size_t ld, int nb, const double *wgt, const uint32_t *grp, int ng,
+                     double *out) {
+    int K = 3 * ng * nb;
     if (part.n < (size_t)GB * K) part.alloc((size_t)GB * K);
-    group_sums_partial<<<GB, 256, (size_t)K * sizeof(double), st()>>>(x, ld, nb, nv, group.p, wgt, G, part.p,
+    group_sums_partial<<<GB, 256, (size_t)K * sizeof(double), st()>>>(x, ld, nb, nv, grp, wgt, ng, part.p,
                                                                       gs_ticket.p, out);
     RSG_LAUNCHED(ctx, "group_sums");
+  }
+
+  // t = Z^T x for nb vectors (ld n) into t [nb][cm]
+  void coarse_zt(int nb, const double *x, double *t) {
+    const int ng = c_nfree + 1;
+    group_sums_by(x, n, nb, nullptr, c_slot.p, ng, c_part.p);
+    coarse_zt_kernel<<<nblk((size_t)nb * cm, 128), 128, 0, st()>>>(c_part.p, 3 * ng, x, n, nd, nb, c_nfree,
+                                                                  c_scale.p, c_rows.p, (int)c_rows_h.size(), t);
+    RSG_LAUNCHED(ctx, "coarse_zt");
+  }
+
+  // the balancing preconditioner around the fine one (CoarseSpace::apply_many, coarse.rs:296-327):
+  // yc = E+ Z^T r, z = P^-1 (r - A'Z yc), z += Z (yc - E+ (A'Z)^T z)
+  void apply_prec_coarse(int nb, const double *r, double *z, int steps) {
+    const size_t nbcm = (size_t)nb * cm;
+    if (c_t.n < nbcm) c_t.alloc(nbcm), c_yc.alloc(nbcm), c_t2.alloc(nbcm);
+    if (c_rp.n < (size_t)nb * n) c_rp.alloc((size_t)nb * n);
+    coarse_zt(nb, r, c_t.p);
+    coarse_esolve_kernel<<<nblk(nbcm, 128), 128, 0, st()>>>(c_epinv.p, c_t.p, nb, cm, nullptr, c_yc.p);
+    RSG_LAUNCHED(ctx, "coarse_esolve");
+    coarse_sub_kernel<<<nblk((size_t)nb * n, 256), 256, 0, st()>>>(r, c_rp.p, n, n, nb, c_az.p, c_yc.p, cm);
+    RSG_LAUNCHED(ctx, "coarse_sub");
+    apply_prec_fine(nb, c_rp.p, z, steps);
+    coarse_azt_partial<<<dim3(kCoarseChunks, (unsigned)nbcm), 256, 0, st()>>>(c_az.p, z, n, n, nb, cm, c_part.p);
+    RSG_LAUNCHED(ctx, "coarse_azt");
+    coarse_azt_finish<<<nblk(nbcm, 128), 128, 0, st()>>>(c_part.p, (int)nbcm, c_t.p);
+    RSG_LAUNCHED(ctx, "coarse_azt_finish");
+    coarse_esolve_kernel<<<nblk(nbcm, 128), 128, 0, st()>>>(c_epinv.p, c_t.p, nb, cm, c_yc.p, c_t2.p);
+    RSG_LAUNCHED(ctx, "coarse_esolve");
+    coarse_addz_kernel<<<nblk((size_t)nb * n, 256), 256, 0, st()>>>(z, n, nd, n, nb, c_slot.p, c_nfree, c_scale.p,
+                                                                    c_rowcol.p, c_t2.p, cm);
+    RSG_LAUNCHED(ctx, "coarse_addz");
   }
 
   void reserve(int nb) {
@@ -272,6 +439,10 @@ struct rs_solver {
   // outgrows the order -2s main term at high frequencies (the iteration count then grows
   // with the mesh), while the second form only perturbs the main term by (I - E) factors.
   void apply_prec(int nb, const double *r, double *z, int steps = 0) {
+    if (cm > 0) apply_prec_coarse(nb, r, z, steps);
+    else apply_prec_fine(nb, r, z, steps);
+  }
+  void apply_prec_fine(int nb, const double *r, double *z, int steps = 0) {
     reserve(nb);
     prof.begin(st(), "precondition");
     double *y = tmp.p, *v = tmp2.p;
@@ -606,6 +777,75 @@ int rs_solver_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const do
     S->prec.apply = [P](int nb, const double *x, double *y) { P->apply_prec(nb, x, y); };
     S->lprec.n = S->n;
     S->lprec.apply = [P](int nb, const double *x, double *y) { P->apply_learned(nb, x, y); };
+    // the coarse space (CoarseSpace::free_components and build, RS/src/solve/coarse.rs:63-247):
+    // with one global barycenter group on several components no component is fixed by rows of
+    // its own, so every component is free and the group's three rows touch them; columns are
+    // the scaled translations of every component and the three multipliers
+    // the operator's products below need the metric (still owned by m and vf here)
+    S->metric = m.get(), S->vfrac = vf.get();
+    const int nfree = ncomp, cmm = 3 * ncomp + 3;
+    if (o->coarse && S->use_prec && !per_comp && ncomp > 1 && (double)S->n * cmm <= (double)(1 << 25)) {
+      const size_t n = S->n;
+      S->c_nfree = nfree;
+      S->c_rows_h = {0, 1, 2};
+      std::vector<double> members(nfree, 0.0), scale(nfree);
+      for (int v = 0; v < nv; ++v) members[comp[v]] += 1.0;
+      for (int k = 0; k < nfree; ++k) scale[k] = 1.0 / std::sqrt(members[k]);
+      S->c_slot.upload(comp, s);
+      S->c_scale.upload(scale, s);
+      S->c_rows.upload(S->c_rows_h, s);
+      std::vector<int> rowcol = {3 * nfree, 3 * nfree + 1, 3 * nfree + 2};
+      S->c_rowcol.upload(rowcol, s);
+      S->c_az.alloc(n * cmm);
+      // A'Z of the translation columns, four per product
+      std::vector<double> zc(n * 3 * nfree, 0.0);
+      for (int v = 0; v < nv; ++v)
+        for (int a = 0; a < 3; ++a) zc[(size_t)(3 * comp[v] + a) * n + 3 * v + a] = scale[comp[v]];
+      DevBuf<double> zd;
+      zd.upload(zc, s);
+      for (int j0 = 0; j0 < 3 * nfree; j0 += 4)
+        S->apply_op(std::min(4, 3 * nfree - j0), zd.p + (size_t)j0 * n, S->c_az.p + (size_t)j0 * n);
+      // A' e_(nd + r) = [C_Q^T e_r; 0]: c_v on axis r
+      std::vector<double> mc(n * 3, 0.0);
+      for (int r = 0; r < 3; ++r)
+        for (int v = 0; v < nv; ++v) mc[(size_t)r * n + 3 * v + r] = ch[v];
+      RSG_CUDA("solver", rsg::copy_async(S->c_az.p + (size_t)3 * nfree * n, mc.data(), mc.size() * sizeof(double),
+                                         cudaMemcpyHostToDevice, s));
+      S->c_part.alloc(std::max<size_t>((size_t)kCoarseChunks * 4 * cmm, (size_t)3 * (nfree + 1) * std::max(4, cmm)));
+      S->c_t.alloc((size_t)4 * cmm), S->c_yc.alloc((size_t)4 * cmm), S->c_t2.alloc((size_t)4 * cmm);
+      S->c_rp.alloc((size_t)4 * n);
+      // E = Z^T A'Z, symmetrized, and its pseudo-inverse (eigenvalues at or below 1e-12 of the
+      // largest dropped)
+      S->cm = cmm;
+      DevBuf<double> et((size_t)cmm * cmm);
+      S->coarse_zt(cmm, S->c_az.p, et.p);
+      std::vector<double> e((size_t)cmm * cmm);
+      et.download(e.data(), e.size(), s);
+      RSG_CUDA("solver", cudaStreamSynchronize(s));
+      for (int i = 0; i < cmm; ++i)
+        for (int j = 0; j < i; ++j) {
+          const double v = 0.5 * (e[(size_t)i * cmm + j] + e[(size_t)j * cmm + i]);
+          e[(size_t)i * cmm + j] = e[(size_t)j * cmm + i] = v;
+        }
+      std::vector<double> lam, u;
+      jacobi_eigen(cmm, e, lam, u);
+      double lmax = 0.0;
+      for (double l : lam) lmax = std::max(lmax, std::fabs(l));
+      std::vector<double> pinv((size_t)cmm * cmm, 0.0);
+      double lmin = INFINITY;
+      for (int k = 0; k < cmm; ++k) {
+        const double l = lam[k];
+        if (std::isnan(l) || std::fabs(l) <= 1e-12 * lmax) {
+          ++S->c_dropped;
+          continue;
+        }
+        lmin = std::min(lmin, std::fabs(l));
+        for (int i = 0; i < cmm; ++i)
+          for (int j = 0; j < cmm; ++j) pinv[(size_t)i * cmm + j] += u[(size_t)i * cmm + k] / l * u[(size_t)j * cmm + k];
+      }
+      S->c_conditioning = lmax > 0.0 ? lmin / lmax : 0.0;
+      S->c_epinv.upload(pinv, s);
+    }
     RSG_CUDA("solver", cudaStreamSynchronize(s));
     lap(S->build_times[4]);
     S->build_times[5] = std::chrono::duration<double>(clk::now() - t_all).count();
@@ -798,6 +1038,7 @@ rs_solver_options rs_solver_options_default(void) {
   o.vcycles = 6;
   o.preconditioner = 1;
   o.clamp_laplacian = 0;
+  o.coarse = 1;
   return o;
 }
 

@@ -41,7 +41,7 @@ class SolverOptions(C.Structure):
                 ("tp_weight", C.c_double), ("low_order", C.c_int), ("eps_rel", C.c_double),
                 ("eps_multi_rel", C.c_double), ("barycenter_per_component", C.c_int),
                 ("vcycles", C.c_int), ("preconditioner", C.c_int),
-                ("clamp_laplacian", C.c_int)]
+                ("clamp_laplacian", C.c_int), ("coarse", C.c_int)]
 
 
 class FlowOptions(C.Structure):
@@ -175,6 +175,7 @@ def load_library(path: str | os.PathLike | None = None):
         "rs_flow_direction": [_vp, _f64p],
         "rs_flow_last_direction": [_vp, _f64p, _f64p],
         "rs_flow_last_trials": [_vp, _f64p, C.c_int, C.POINTER(C.c_int)],
+        "rs_flow_last_solutions": [_vp, C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int64)],
         "rs_flow_positions": [_vp, _f64p],
         "rs_flow_cancel": [_vp, C.c_int],
     }
@@ -757,6 +758,15 @@ class Flow:
         x, g = np.empty((self.n_vertices, 3)), np.empty((self.n_vertices, 3))
         _check(_lib.rs_flow_last_direction(self._h, x.ravel(), g.ravel()))
         return x, g
+
+    def last_solutions(self) -> np.ndarray:
+        """The last step's saddle solutions, (k + 1) x n: the Schur columns of the held rows
+        (area, then volume), then y = A'^-1 [g; 0]."""
+        k, n = C.c_int(), C.c_int64()
+        _check(_lib.rs_flow_last_solutions(self._h, None, C.byref(k), C.byref(n)))
+        out = np.empty((k.value + 1, n.value))
+        _check(_lib.rs_flow_last_solutions(self._h, out.ctypes.data_as(C.c_void_p), C.byref(k), C.byref(n)))
+        return out
 
     def last_trials(self) -> list[tuple[float, float, str]]:
         """(tau, energy, outcome) of every line-search trial of the last step."""

@@ -182,14 +182,17 @@ def config_c3s(n: int = 320):
     return config_c3(n, 0.001)
 
 
-def config_c5(n: int = 400):
+def config_c5(n: int = 400, sigma: float = 0.01):
+    """Two interlinked tori (R = 1, r = 0.25, n x n grids; 640,000 faces at n = 400): the
+    second rotated 90 degrees about x and moved +1 along x (a Hopf link), N(0, sigma) per
+    coordinate, seed 5. sigma = 0.01 is the configuration as specified (2.5 minor-circle edges
+    at n = 400: a crumpled surface)."""
     P, F = torus(n, n, 1.0, 0.25)
-    # second torus: rotated 90 degrees about x, moved +1 along x (a Hopf link)
     Q = np.stack([P[:, 0] + 1.0, -P[:, 2], P[:, 1]], axis=1)
     PP = np.vstack([P, Q])
     FF = np.vstack([F, F + len(P)]).astype(np.uint32)
     z = SplitMix64(5).normals(PP.size).reshape(PP.shape)
-    return PP + 0.01 * z, FF
+    return PP + sigma * z, FF
 
 
 CONFIGS = {"c1": config_c1, "c2": config_c2, "c3": config_c3, "c3s": config_c3s, "c5": config_c5}

@@ -245,6 +245,10 @@ typedef struct rs_solver_options {
   int preconditioner;    /* 1: the fractional preconditioner, 0: none */
   int clamp_laplacian;   /* 1: edges with negative cotan weight dropped from the
                             preconditioner's Laplacian (an M-matrix for multigrid), 0: cotan */
+  int coarse;            /* the coarse (deflation) correction on the translations of components
+                            that no positional row of their own fixes: a global barycenter on
+                            several components (PreconditionerOptions::coarse, CoarseSpace,
+                            RS/src/solve/coarse.rs; 1) */
 } rs_solver_options;
 
 rs_solver_options rs_solver_options_default(void);
@@ -445,6 +449,12 @@ int rs_flow_direction(rs_flow *f, double *report);
 /* The direction x (f <- f - tau x) and the differential g (V x 3 each) of the last
  * rs_flow_step or rs_flow_direction (StepReport's direction and gradient, session.rs:1255-1262). */
 int rs_flow_last_direction(rs_flow *f, double *x_host, double *g_host);
+/* The saddle solutions of the last rs_flow_step or rs_flow_direction: the k Schur columns
+ * Z_r = A'^-1 [C_N^T e_r; 0] of the held rows (area first, then volume), then
+ * y = A'^-1 [g; 0], each n = 3V + k_Q entries [x; multipliers] (SchurComplement::z and the
+ * direction's solve, RS/src/solve/schur.rs:101-126). sol_host NULL: only *n_held and *n. No
+ * counterpart call in the crate (a diagnostic, for checking the solves against an FP64 operator). */
+int rs_flow_last_solutions(rs_flow *f, double *sol_host, int *n_held, int64_t *n);
 /* The line-search trials of the last step (StepReport::trials, session.rs:1262): up to
  * max_trials triples (tau, energy, outcome: 0 accepted, 1 Armijo failed, 2 non-finite,
  * 3 projection blocked); *n_trials is their number. */

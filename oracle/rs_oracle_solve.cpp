@@ -1046,6 +1046,7 @@ struct HSaddle : Saddle {
     auto t0 = clk::now();
     check_c(rso_metric_build(nv, pos, nf, faces, alpha, beta, o.chi, o.leaf_size, o.leaf_pairs, &metric), "metric");
     seconds_build[0] = since(t0);
+    if (!o.preconditioner) return;  // the operator alone
     t0 = clk::now();
     std::vector<double> fa, va;
     areas_of(*t, P, fa, va);

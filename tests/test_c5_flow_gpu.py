@@ -1,0 +1,77 @@
+"""Config c5: the Hs flow on two interlinked 400 x 400 tori (R = 1, r = 0.25, 640,000 faces,
+one global barycenter, total area and volume held; Barnes-Hut theta 0.25, metric chi 0.5,
+GMRES restart 30 to a true relative residual of 1e-6, the fractional preconditioner with the
+coarse correction of the two free components).
+
+Every 10 steps, at the positions the step starts from, the FP64 oracle checks the step on the
+same face tree and lists:
+
+* the energy within 1e-6 and the differential within 1e-5 (normwise) of the oracle's Barnes-Hut;
+* each of the step's three saddle solutions (the area and volume Schur columns and y = A'^-1 g)
+  solves the oracle's FP64 operator A' to a relative residual below 1e-5;
+* the direction recomputed in FP64 from those solutions (x = y - Z N^-1 C_N y with the oracle's
+  constraint Jacobian) equals the GPU's within 1e-5 (normwise).
+
+The noise is N(0, 0.0005), an eighth of the minor-circle edge: the specified N(0, 0.01) is 2.5
+edges and crumples the surface so that no solve reaches 1e-6 (as for the single torus). The
+test runs RS_C5_STEPS steps (20 by default, checks at steps 0 and 10; 100 gives the
+configuration's full flow with ten checks)."""
+import os
+
+import numpy as np
+import pytest
+
+import golden_io as G
+import rs_oracle as O
+import rs_gb300 as R
+from rs_gb300 import generators as gen
+
+pytestmark = pytest.mark.gpu
+
+STEPS = int(os.environ.get("RS_C5_STEPS", "20"))
+
+
+def oracle_check(P, F, flow, rep):
+    x, g = flow.last_direction()
+    sols = flow.last_solutions()
+    nd = 3 * len(P)
+    bh = O.BhTree(P, F, theta=0.25)
+    Eo, go = bh.energy_and_differential()
+    del bh
+    out = {"energy": abs(rep["energy_before"] - Eo) / abs(Eo), "differential": G.normwise(g, go)}
+    rows = O.constraint_rows(P, F, O.Constraints().barycenter().area().volume())
+    cn = rows["jac"][3:5]
+    H = O.HSolver(P, F, O.Constraints().barycenter(), O.solver_options(preconditioner=0, coarse=0))
+    rhs = np.zeros((3, H.n))
+    rhs[0, :nd], rhs[1, :nd], rhs[2, :nd] = cn[0], cn[1], go.ravel()
+    res = [np.linalg.norm(H.apply(sols[i]) - rhs[i]) / np.linalg.norm(rhs[i]) for i in range(3)]
+    del H
+    Z, y = sols[:2, :nd], sols[2, :nd]
+    N = cn @ Z.T
+    x64 = y - Z.T @ np.linalg.solve(0.5 * (N + N.T), cn @ y)
+    out.update(residuals=res, direction=G.normwise(x.ravel(), x64))
+    return out
+
+
+def test_linked_tori_flow_with_oracle_checks():
+    P, F = gen.config_c5(n=400, sigma=0.0005)
+    assert len(F) == 640_000
+    o = R.flow_options(theta=0.25, hold_area=1, hold_volume=1, solver_chi=0.5, solver_restart=30,
+                       solver_tolerance=1e-6, solver_max_iterations=600)
+    flow = R.Flow(F, P, o)
+    energies, checks = [], []
+    for step in range(STEPS):
+        Q = flow.positions()
+        rep = flow.step()
+        assert rep["accepted"] == 1.0 and rep["relative_residual"] <= 1e-6, rep
+        energies.append(rep["energy_after"])
+        if step % 10 == 0:
+            c = oracle_check(Q, F, flow, rep)
+            checks.append(c)
+            print(f"step {step}: E {rep['energy_before']:.6e} -> {rep['energy_after']:.6e}, "
+                  f"{rep['seconds']:.2f} s, GMRES {rep['gmres_area']:.0f}/{rep['gmres_volume']:.0f}/"
+                  f"{rep['gmres_direction']:.0f}; oracle: energy {c['energy']:.1e} differential "
+                  f"{c['differential']:.1e} residuals {max(c['residuals']):.1e} direction {c['direction']:.1e}")
+            assert c["energy"] <= 1e-6 and c["differential"] <= 1e-5
+            assert max(c["residuals"]) <= 1e-5 and c["direction"] <= 1e-5
+    assert all(b < a for a, b in zip(energies, energies[1:]))

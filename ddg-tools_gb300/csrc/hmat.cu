@@ -1388,7 +1388,11 @@ int rs_vfrac_stats(rs_vfrac *V, int64_t *o) {
 //
 // Limits: the scratch is kNoAllocScratchBytes per device, shared by every call in the process,
 // so calls that overlap in time (two host threads, or two streams in flight) race on it and
-// must be serialized by the caller. The first call on a device looks up the array's address
+// must be serialized by the caller; a call also uses the metric's own arrival counters (the
+// upward pass), so it must not overlap any other product on the same rs_metric either. The
+// array is resident on every device where this file's kernels are loaded (from the first
+// metric build or product there, with lazy module loading), whether or not this entry point
+// is ever called. The first call on a device looks up the array's address
 // (cudaGetSymbolAddress, with that device current); when that call is made inside a stream
 // capture the lookup should have been done before it, by one earlier call.
 

@@ -357,9 +357,8 @@ void gmres_batch(rs_ctx *ctx, const Operator &A, const Operator *P, int nb, cons
   }
   double secs = std::chrono::duration<double>(clk::now() - t0).count();
   reports.assign(nb, GmresReport());
+  for (int q = 0; q < nb; ++q) R[q].rep.seconds = secs, reports[q] = R[q].rep;
   for (int q = 0; q < nb; ++q) {
-    R[q].rep.seconds = secs;
-    reports[q] = R[q].rep;
     if (!R[q].rep.converged && !(R[q].rep.relative_residual <= 0.1))
       fail(RS_SOLVER_DIVERGED, "SolverDiverged", "gmres",
            "true relative residual " + std::to_string(R[q].rep.relative_residual));

@@ -196,8 +196,13 @@ int rs_metric_apply_device(rs_metric *m, double w_hi, double w_lo, int nb, const
  * vectors on 80,000 faces) lives in one file-scope device array, so it serves callers that
  * must not allocate while the product runs (a host whose device memory is held by its own
  * pool after set-up; a latency-critical stream, as cudaMalloc/cudaFree can synchronize the
- * device). Calls that overlap in time race on the shared scratch: serialize them. The first
- * call on a device looks up the scratch address; make that call outside any stream capture. */
+ * device). The 64 MiB are a file-scope device array: they stay resident on every device
+ * where the library's metric kernels are loaded, whether or not this call is ever made (with
+ * CUDA_MODULE_LOADING=LAZY, the CUDA default, from the first metric build or product on that
+ * device). Calls that overlap in time race on the shared scratch, and a call also shares the
+ * metric's arrival counters with the other products of the same rs_metric: serialize them
+ * with each other and with every product on that metric. The first call on a device looks up
+ * the scratch address; make that call outside any stream capture. */
 int rs_metric_apply_device_noalloc(rs_metric *m, double w_hi, double w_lo, int nb,
                                    const double *xs_dev, double *ys_dev);
 /* BctStats (far blocks, near blocks, near entries, depth, nodes). */

@@ -125,3 +125,15 @@ def test_cancel_from_another_thread_during_a_step():
         time.sleep(0.01)
     print(outcomes)
     assert flow.step()["accepted"] == 1.0
+
+
+def test_recovery_repeats_a_diverged_solve():
+    """The recovery of RobustHierarchical (RS/src/step/direction.rs:269-379): a step whose solves
+    end above the divergence threshold (here: one iteration allowed) is solved again with
+    restart 60 and at least 800 iterations, counted in the report, and the step proceeds."""
+    P, F = gen.noisy_torus(32, 16, 1.0, 0.3, 0.003, 2)
+    flow = R.Flow(F, P, R.flow_options(theta=0.5, hold_volume=1, solver_max_iterations=1, solver_tolerance=1e-6))
+    rep = flow.step()
+    print(rep)
+    assert rep["fallbacks"] == 1.0
+    assert rep["accepted"] == 1.0 and rep["relative_residual"] <= 1e-6

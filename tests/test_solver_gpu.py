@@ -86,3 +86,18 @@ def test_gmres_without_preconditioner_needs_more_iterations(ctx):
         assert r["iterations"] > with_p["iterations"]
     except R.RsError as e:  # diverging without a preconditioner is the expected failure mode
         assert e.kind == "SolverDiverged"
+
+
+@pytest.mark.parametrize("mesh", ["c1", "torus48x24"])
+def test_preconditioner_matches_oracle_with_converged_lprime(ctx, mesh):
+    """The fractional preconditioner (a20) and its L' solve (a19) against the oracle's restatement
+    of the crate's (the augmented form with an exact sparse LDL^T of L', pinned to the Lean
+    precond fixtures): with enough conjugate-gradient steps the multigrid L'^-1 converges, and
+    the GPU's X (s L + C) X equals the crate's X + X (s L - K) X (identical for an exact X)."""
+    P, F = {"c1": gen.config_c1, "torus48x24": lambda: gen.noisy_torus(48, 24, 1.0, 0.3, 0.003, 7)}[mesh]()
+    S = R.SaddleSolver(F, P, R.Exponents(), R.solver_options(chi=0.5, vcycles=100), ctx)
+    H = O.HSolver(P, F, O.Constraints().barycenter(), O.solver_options(chi=0.5, coarse=0))
+    r = np.random.default_rng(12).standard_normal((2, S.n))
+    err = G.normwise(S.precondition(r), H.precondition(r))
+    print(f"{mesh}: preconditioner against the oracle's {err:.2e}")
+    assert err <= 1e-4

@@ -255,7 +255,7 @@ def near_roofline(near_entries, n_faces, t_rows_ms, fp32_peak, traffic, kernel_m
             "traffic": traffic, "kernel_ms": kernel_ms,
             "compute": {"bound": "fp32", "achieved": tflops, "peak": fp32_peak, "unit": "TFLOP/s",
                         "frac": (tflops / fp32_peak) if tflops else None,
-                        "peak_source": "measured FP32 FMA throughput (rs_fp32_peak)",
+                        "peak_source": "measured FP32 FMA throughput (rsp_fp32_peak, librsprobe.so)",
                         "work": f"{NEAR_FLOP_PER_ENTRY} FLOP x {near_entries} near entries per launch"}}
 def flow_options(R):
     return R.flow_options(theta=0.25, hold_area=1, hold_volume=1, solver_chi=0.5, solver_restart=30,
@@ -885,7 +885,7 @@ def main() -> int:
         "roofline": {"bound": "fp32", "kernel": "bh_pair_grad", "achieved": achieved,
                      "peak": peak, "unit": "TFLOP/s",
                      "frac": (achieved / peak) if achieved else None,
-                     "peak_source": "measured FP32 FMA throughput (rs_fp32_peak); "
+                     "peak_source": "measured FP32 FMA throughput (rsp_fp32_peak, librsprobe.so); "
                                     "MEASURED_PEAKS.json has no FP32 figure",
                      "traffic": traffic_from_profiles("bh_pair", args.workload),
                      "kernel_ms": prof},

@@ -3,6 +3,8 @@
 //
 // Layer l: h_l[v] = act(W_l,self h_{l-1}[v] + W_l,nb mean_{u in N(v)} h_{l-1}[u] + b_l), with
 // act = SiLU for the two hidden layers and the identity for the output layer (3 channels).
+// The layers' products (forward, input gradient, weight gradient) run on the tensor cores
+// (mma.sync, BF16 operands, FP32 accumulation).
 // Features h_0[v] (13): position (centred, divided by the RMS radius), unit vertex normal,
 // dual area / mean, r_v / rms(r), y_v / rms(y). Every reduction is a fixed-order two-stage
 // sum, so training and inference are deterministic.
@@ -106,29 +108,223 @@ __global__ void ring_mean_bwd(int nv, int W, const uint32_t *__restrict__ off, c
   dh[t] += s;
 }
 
-// One layer: thread (v, o) of VPB vertices per block; weights (BF16 -> float) in shared memory.
+// ---- the three products of a layer on the tensor cores: mma.sync m16n8k16 with BF16 operands
+// and FP32 accumulation. The BF16 weights enter exactly; FP32 activations and gradients are split
+// into BF16 parts whose products with a BF16 factor are exact in FP32: three parts (h + m + l)
+// carry all 24 significand bits of an FP32 value (the remainders x - h and x - h - m are exact
+// FP32 numbers of at most 16 and 8 significant bits). So the forward layer and the input
+// gradient equal the FP32 products up to the order of the FP32 additions; the weight gradient
+// (two FP32 factors) keeps the three leading products of two-part splits (relative 2^-16).
+
+__device__ __forceinline__ uint32_t bf16x2(float e0, float e1) {
+  __nv_bfloat162 t = __floats2bfloat162_rn(e0, e1);  // e0 in the low half
+  return *reinterpret_cast<uint32_t *>(&t);
+}
+__device__ __forceinline__ float bf16_round(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+__device__ __forceinline__ void split3(float x, float &h, float &m, float &l) {
+  h = bf16_round(x);
+  const float r = x - h;
+  m = bf16_round(r);
+  l = r - m;
+}
+__device__ __forceinline__ void split2(float x, float &h, float &l) {
+  h = bf16_round(x);
+  l = x - h;
+}
+
+// d += a b for one m16n8k16 tile: a (16 x 16, row-major fragment), b (16 x 8, column-major)
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// The A fragment of a 16 x 16 tile whose element (row, col) is at(row, col): lane (g, t) holds
+// rows g and g + 8, columns 2t, 2t + 1, 2t + 8, 2t + 9.
+template <class F>
+__device__ __forceinline__ void load_a(F at, int g, int t, float (&e)[8]) {
+  e[0] = at(g, 2 * t), e[1] = at(g, 2 * t + 1), e[2] = at(g + 8, 2 * t), e[3] = at(g + 8, 2 * t + 1);
+  e[4] = at(g, 2 * t + 8), e[5] = at(g, 2 * t + 9), e[6] = at(g + 8, 2 * t + 8), e[7] = at(g + 8, 2 * t + 9);
+}
+__device__ __forceinline__ void pack_a(const float (&e)[8], uint32_t (&a)[4]) {
+  a[0] = bf16x2(e[0], e[1]), a[1] = bf16x2(e[2], e[3]), a[2] = bf16x2(e[4], e[5]), a[3] = bf16x2(e[6], e[7]);
+}
+
+// One layer, out[v][o] = act(b[o] + sum_i Ws[o][i] xs[v][i] + sum_i Wn[o][i] xn[v][i]): a warp
+// per 16 vertices, all outputs; the weights (zero-padded to K = 16k, N = 8k) in shared memory.
 template <int IN, int OUT, bool ACT>
-__global__ void dense_fwd(int nv, const __nv_bfloat16 *__restrict__ ws, const __nv_bfloat16 *__restrict__ wn,
-                          const __nv_bfloat16 *__restrict__ bias, const float *__restrict__ xs,
-                          const float *__restrict__ xn, float *__restrict__ pre, float *__restrict__ out) {
-  __shared__ float sw[2 * OUT * IN + OUT];
-  for (int i = threadIdx.x; i < OUT * IN; i += blockDim.x) {
-    sw[i] = __bfloat162float(ws[i]);
-    sw[OUT * IN + i] = __bfloat162float(wn[i]);
+__global__ void __launch_bounds__(128) dense_fwd(int nv, const __nv_bfloat16 *__restrict__ ws,
+                                                 const __nv_bfloat16 *__restrict__ wn,
+                                                 const __nv_bfloat16 *__restrict__ bias, const float *__restrict__ xs,
+                                                 const float *__restrict__ xn, float *__restrict__ pre,
+                                                 float *__restrict__ out) {
+  constexpr int KP = (IN + 15) / 16 * 16, NP = (OUT + 7) / 8 * 8, NT = NP / 8, KS = KP + 8;
+  __shared__ __align__(16) __nv_bfloat16 sw[2][NP][KS];
+  __shared__ float sb[NP];
+  for (int q = threadIdx.x; q < 2 * NP * KS; q += blockDim.x) {
+    const int part = q / (NP * KS), n = (q / KS) % NP, k = q % KS;
+    sw[part][n][k] = (n < OUT && k < IN) ? (part ? wn : ws)[n * IN + k] : __float2bfloat16(0.f);
   }
-  for (int i = threadIdx.x; i < OUT; i += blockDim.x) sw[2 * OUT * IN + i] = __bfloat162float(bias[i]);
+  for (int q = threadIdx.x; q < NP; q += blockDim.x) sb[q] = q < OUT ? __bfloat162float(bias[q]) : 0.f;
   __syncthreads();
-  constexpr int VPB = 256 / OUT;
-  const int o = threadIdx.x % OUT, vl = threadIdx.x / OUT;
-  const int v = blockIdx.x * VPB + vl;
-  if (vl >= VPB || v >= nv) return;
-  const float *a = xs + (size_t)v * IN, *b = xn + (size_t)v * IN;
-  const float *wa = sw + o * IN, *wb = sw + OUT * IN + o * IN;
-  float acc = sw[2 * OUT * IN + o];
-#pragma unroll 8
-  for (int i = 0; i < IN; ++i) acc = fmaf(wa[i], a[i], fmaf(wb[i], b[i], acc));
-  if (pre) pre[(size_t)v * OUT + o] = acc;
-  out[(size_t)v * OUT + o] = ACT ? silu(acc) : acc;
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const int v0 = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 16;
+  if (v0 >= nv) return;
+  float acc[NT][4];
+#pragma unroll
+  for (int nt = 0; nt < NT; ++nt) {
+    const int n0 = nt * 8 + 2 * t;
+    acc[nt][0] = sb[n0], acc[nt][1] = sb[n0 + 1], acc[nt][2] = sb[n0], acc[nt][3] = sb[n0 + 1];
+  }
+#pragma unroll
+  for (int part = 0; part < 2; ++part) {
+    const float *X = part ? xn : xs;
+#pragma unroll
+    for (int k0 = 0; k0 < KP; k0 += 16) {
+      float e[8], h[8], m[8], l[8];
+      load_a([&](int r, int c) { return (v0 + r < nv && k0 + c < IN) ? X[(size_t)(v0 + r) * IN + k0 + c] : 0.f; }, g,
+             t, e);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) split3(e[i], h[i], m[i], l[i]);
+      uint32_t ah[4], am[4], al[4];
+      pack_a(h, ah), pack_a(m, am), pack_a(l, al);
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt) {
+        const __nv_bfloat16 *wr = &sw[part][nt * 8 + g][k0 + 2 * t];
+        const uint32_t b0 = *reinterpret_cast<const uint32_t *>(wr), b1 = *reinterpret_cast<const uint32_t *>(wr + 8);
+        mma_bf16(acc[nt], ah, b0, b1);
+        mma_bf16(acc[nt], am, b0, b1);
+        mma_bf16(acc[nt], al, b0, b1);
+      }
+    }
+  }
+#pragma unroll
+  for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int v = v0 + g + (i >= 2 ? 8 : 0), n = nt * 8 + 2 * t + (i & 1);
+      if (v < nv && n < OUT) {
+        if (pre) pre[(size_t)v * OUT + n] = acc[nt][i];
+        out[(size_t)v * OUT + n] = ACT ? silu(acc[nt][i]) : acc[nt][i];
+      }
+    }
+}
+
+// Input gradients din_self[v][i] = sum_o Ws[o][i] dpre[v][o] and din_nb likewise with Wn: a
+// warp per 16 vertices; K = OUT, N = IN, the transposed weights in shared memory.
+template <int IN, int OUT>
+__global__ void __launch_bounds__(128) dense_bwd_in(int nv, const __nv_bfloat16 *__restrict__ ws,
+                                                    const __nv_bfloat16 *__restrict__ wn,
+                                                    const float *__restrict__ dpre, float *__restrict__ dself,
+                                                    float *__restrict__ dnb) {
+  constexpr int KP = (OUT + 15) / 16 * 16, NP = (IN + 7) / 8 * 8, NT = NP / 8, KS = KP + 8;
+  __shared__ __align__(16) __nv_bfloat16 sw[2][NP][KS];  // sw[part][i][o] = W[o][i]
+  for (int q = threadIdx.x; q < 2 * NP * KS; q += blockDim.x) {
+    const int part = q / (NP * KS), i = (q / KS) % NP, o = q % KS;
+    sw[part][i][o] = (i < IN && o < OUT) ? (part ? wn : ws)[o * IN + i] : __float2bfloat16(0.f);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const int v0 = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 16;
+  if (v0 >= nv) return;
+  float acc[2][NT][4];
+#pragma unroll
+  for (int part = 0; part < 2; ++part)
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) acc[part][nt][0] = acc[part][nt][1] = acc[part][nt][2] = acc[part][nt][3] = 0.f;
+#pragma unroll
+  for (int k0 = 0; k0 < KP; k0 += 16) {
+    float e[8], h[8], m[8], l[8];
+    load_a([&](int r, int c) { return (v0 + r < nv && k0 + c < OUT) ? dpre[(size_t)(v0 + r) * OUT + k0 + c] : 0.f; },
+           g, t, e);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) split3(e[i], h[i], m[i], l[i]);
+    uint32_t ah[4], am[4], al[4];
+    pack_a(h, ah), pack_a(m, am), pack_a(l, al);
+#pragma unroll
+    for (int part = 0; part < 2; ++part)
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt) {
+        const __nv_bfloat16 *wr = &sw[part][nt * 8 + g][k0 + 2 * t];
+        const uint32_t b0 = *reinterpret_cast<const uint32_t *>(wr), b1 = *reinterpret_cast<const uint32_t *>(wr + 8);
+        mma_bf16(acc[part][nt], ah, b0, b1);
+        mma_bf16(acc[part][nt], am, b0, b1);
+        mma_bf16(acc[part][nt], al, b0, b1);
+      }
+  }
+#pragma unroll
+  for (int part = 0; part < 2; ++part)
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int v = v0 + g + (i >= 2 ? 8 : 0), n = nt * 8 + 2 * t + (i & 1);
+        if (v < nv && n < IN) (part ? dnb : dself)[(size_t)v * IN + n] = acc[part][nt][i];
+      }
+}
+
+// Weight and bias gradients of one layer per vertex chunk c (fixed split, grid = chunks):
+// partial[c] = dpre^T [xs | 1 | xn] over the chunk's vertices, K = vertices. Warp w takes the
+// output rows 16 (w mod MT) .. and the self (with the bias column at index IN) or the
+// neighbour part. Layout of partial[c]: self [o][i], neighbour [o][i], bias [o].
+template <int IN, int OUT>
+__global__ void dense_bwd_w(int nv, const float *__restrict__ xs, const float *__restrict__ xn,
+                            const float *__restrict__ dpre, float *__restrict__ partial) {
+  constexpr int MT = (OUT + 15) / 16, NS = (IN + 1 + 7) / 8, NN = (IN + 7) / 8;
+  constexpr int NTM = NS > NN ? NS : NN;
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3, warp = threadIdx.x >> 5;
+  const int mt = warp % MT, part = warp / MT;
+  const int NT = part ? NN : NS;
+  const float *X = part ? xn : xs;
+  const int chunk = (nv + gridDim.x - 1) / gridDim.x;
+  const int c0 = blockIdx.x * chunk, c1 = min(nv, c0 + chunk);
+  const int o0 = mt * 16 + g, o1 = o0 + 8;
+  float acc[NTM][4];
+#pragma unroll
+  for (int nt = 0; nt < NTM; ++nt) acc[nt][0] = acc[nt][1] = acc[nt][2] = acc[nt][3] = 0.f;
+  for (int k0 = c0; k0 < c1; k0 += 16) {
+    float e[8], h[8], l[8];
+    load_a([&](int r, int c) { return (mt * 16 + r < OUT && k0 + c < c1) ? dpre[(size_t)(k0 + c) * OUT + mt * 16 + r] : 0.f; },
+           g, t, e);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) split2(e[i], h[i], l[i]);
+    uint32_t ah[4], al[4];
+    pack_a(h, ah), pack_a(l, al);
+    auto bx = [&](int v, int i) -> float {
+      if (v >= c1) return 0.f;
+      if (i < IN) return X[(size_t)v * IN + i];
+      return (part == 0 && i == IN) ? 1.f : 0.f;
+    };
+#pragma unroll
+    for (int nt = 0; nt < NTM; ++nt) {
+      if (nt >= NT) break;
+      const int n = nt * 8 + g;
+      float f[4] = {bx(k0 + 2 * t, n), bx(k0 + 2 * t + 1, n), bx(k0 + 2 * t + 8, n), bx(k0 + 2 * t + 9, n)};
+      float fh[4], fl[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) split2(f[i], fh[i], fl[i]);
+      const uint32_t bh0 = bf16x2(fh[0], fh[1]), bh1 = bf16x2(fh[2], fh[3]);
+      const uint32_t bl0 = bf16x2(fl[0], fl[1]), bl1 = bf16x2(fl[2], fl[3]);
+      mma_bf16(acc[nt], ah, bh0, bh1);
+      mma_bf16(acc[nt], ah, bl0, bl1);
+      mma_bf16(acc[nt], al, bh0, bh1);
+    }
+  }
+  const size_t P = 2 * (size_t)OUT * IN + OUT;
+  float *pc = partial + (size_t)blockIdx.x * P;
+#pragma unroll
+  for (int nt = 0; nt < NTM; ++nt) {
+    if (nt >= NT) break;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int o = i >= 2 ? o1 : o0, n = nt * 8 + 2 * t + (i & 1);
+      if (o >= OUT) continue;
+      if (n < IN) pc[(part ? (size_t)OUT * IN : 0) + (size_t)o * IN + n] = acc[nt][i];
+      else if (part == 0 && n == IN) pc[2 * (size_t)OUT * IN + o] = acc[nt][i];
+    }
+  }
 }
 
 // z = y + rms(y) o on the position rows; rows >= 3V of the vector are copied from y
@@ -173,30 +369,6 @@ __global__ void dpre_kernel(size_t n, const float *__restrict__ dout, const floa
   dpre[t] = ACT ? dout[t] * silu_grad(pre[t]) : dout[t];
 }
 
-// Weight gradients of one layer, per vertex chunk: grid (kChunks, OUT), block 2 IN threads;
-// partial[c][o][i] (self, then nb at OUT IN + ...), bias at 2 OUT IN + o.
-template <int IN, int OUT>
-__global__ void dense_bwd_w(int nv, const float *__restrict__ xs, const float *__restrict__ xn,
-                            const float *__restrict__ dpre, float *__restrict__ partial) {
-  const int c = blockIdx.x, o = blockIdx.y, i = threadIdx.x;
-  const int chunk = (nv + gridDim.x - 1) / gridDim.x;
-  const int v0 = c * chunk, v1 = min(nv, v0 + chunk);
-  const bool self = i < IN;
-  const int ii = self ? i : i - IN;
-  if (ii >= IN) return;
-  const float *x = self ? xs : xn;
-  float acc = 0.f, accb = 0.f;
-  for (int v = v0; v < v1; ++v) {
-    const float d = dpre[(size_t)v * OUT + o];
-    acc = fmaf(d, x[(size_t)v * IN + ii], acc);
-    accb += d;
-  }
-  const size_t P = 2 * (size_t)OUT * IN + OUT;
-  float *pc = partial + (size_t)c * P;
-  pc[(self ? 0 : (size_t)OUT * IN) + (size_t)o * IN + ii] = acc;
-  if (i == 0) pc[2 * (size_t)OUT * IN + o] = accb;
-}
-
 // grad[k] += sum over chunks of partial[c][k] (fixed order)
 __global__ void grad_reduce(int nchunks, size_t P, const float *__restrict__ partial, float *__restrict__ grad) {
   size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
@@ -204,29 +376,6 @@ __global__ void grad_reduce(int nchunks, size_t P, const float *__restrict__ par
   float s = 0.f;
   for (int c = 0; c < nchunks; ++c) s += partial[(size_t)c * P + k];
   grad[k] += s;
-}
-
-// din_self[v][i] = sum_o Ws[o][i] dpre[v][o]; din_nb likewise with Wn
-template <int IN, int OUT>
-__global__ void dense_bwd_in(int nv, const __nv_bfloat16 *__restrict__ ws, const __nv_bfloat16 *__restrict__ wn,
-                             const float *__restrict__ dpre, float *__restrict__ dself, float *__restrict__ dnb) {
-  __shared__ float sw[2 * OUT * IN];
-  for (int i = threadIdx.x; i < OUT * IN; i += blockDim.x) {
-    sw[i] = __bfloat162float(ws[i]);
-    sw[OUT * IN + i] = __bfloat162float(wn[i]);
-  }
-  __syncthreads();
-  size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  if (t >= (size_t)nv * IN) return;
-  const int v = (int)(t / IN), i = (int)(t % IN);
-  const float *d = dpre + (size_t)v * OUT;
-  float a = 0.f, b = 0.f;
-  for (int o = 0; o < OUT; ++o) {
-    a = fmaf(sw[o * IN + i], d[o], a);
-    b = fmaf(sw[OUT * IN + o * IN + i], d[o], b);
-  }
-  dself[t] = a;
-  dnb[t] = b;
 }
 
 __global__ void adam_kernel(size_t P, float *__restrict__ w, float *__restrict__ g, float *__restrict__ m,
@@ -314,15 +463,15 @@ void forward(rs_learned *M, rs_lgraph *G, const double *r, const double *y, bool
     RSG_LAUNCHED(ctx, "learned_mean");
   };
   mean(kIn, M->X.p, M->nX.p);
-  dense_fwd<kIn, 64, true><<<nblk(nv, 256 / 64), 256, 0, s>>>(nv, wb + M->o1s, wb + M->o1n, wb + M->o1b, M->X.p,
+  dense_fwd<kIn, 64, true><<<nblk(nv, 64), 128, 0, s>>>(nv, wb + M->o1s, wb + M->o1n, wb + M->o1b, M->X.p,
                                                                M->nX.p, keep ? M->pre1.p : nullptr, M->h1.p);
   RSG_LAUNCHED(ctx, "learned_dense");
   mean(H, M->h1.p, M->nh1.p);
-  dense_fwd<64, 64, true><<<nblk(nv, 256 / 64), 256, 0, s>>>(nv, wb + M->o2s, wb + M->o2n, wb + M->o2b, M->h1.p,
+  dense_fwd<64, 64, true><<<nblk(nv, 64), 128, 0, s>>>(nv, wb + M->o2s, wb + M->o2n, wb + M->o2b, M->h1.p,
                                                               M->nh1.p, keep ? M->pre2.p : nullptr, M->h2.p);
   RSG_LAUNCHED(ctx, "learned_dense");
   mean(H, M->h2.p, M->nh2.p);
-  dense_fwd<64, kOut, false><<<nblk(nv, 256 / kOut), 256, 0, s>>>(nv, wb + M->o3s, wb + M->o3n, wb + M->o3b,
+  dense_fwd<64, kOut, false><<<nblk(nv, 64), 128, 0, s>>>(nv, wb + M->o3s, wb + M->o3n, wb + M->o3b,
                                                                    M->h2.p, M->nh2.p, nullptr, M->o.p);
   RSG_LAUNCHED(ctx, "learned_dense");
 }
@@ -334,7 +483,7 @@ void layer_grad(rs_learned *M, int nv, const float *xs, const float *xn, size_t 
   const int nch = std::max(1, std::min(kChunks, (nv + 255) / 256));
   const size_t P = 2 * (size_t)OUT * IN + OUT;
   if (M->partial.n < (size_t)kChunks * P) M->partial.alloc((size_t)kChunks * P);
-  dense_bwd_w<IN, OUT><<<dim3(nch, OUT), 2 * IN, 0, s>>>(nv, xs, xn, M->dpre.p, M->partial.p);
+  dense_bwd_w<IN, OUT><<<nch, 64 * ((OUT + 15) / 16), 0, s>>>(nv, xs, xn, M->dpre.p, M->partial.p);
   RSG_LAUNCHED(ctx, "learned_bwd_w");
   // the layer's parameters are contiguous: self, nb, bias
   grad_reduce<<<nblk(P, 256), 256, 0, s>>>(nch, P, M->partial.p, M->g.p + ows);
@@ -534,7 +683,7 @@ int rs_learned_loss_and_gradient_device(rs_learned *M, rs_lgraph *G, const doubl
     RSG_CUDA("product", cudaMemcpyAsync(M->dpre.p, M->dO.p, n3 * sizeof(float), cudaMemcpyDeviceToDevice, s));
     layer_grad<64, kOut>(M, nv, M->h2.p, M->nh2.p, M->o3s);
     const __nv_bfloat16 *wb = M->wb.p;
-    dense_bwd_in<64, kOut><<<nblk((size_t)nv * H, 256), 256, 0, s>>>(nv, wb + M->o3s, wb + M->o3n, M->dpre.p,
+    dense_bwd_in<64, kOut><<<nblk(nv, 64), 128, 0, s>>>(nv, wb + M->o3s, wb + M->o3n, M->dpre.p,
                                                                       M->dself.p, M->dnb.p);
     RSG_LAUNCHED(ctx, "learned_bwd_in");
     // dh2 = dself + mean^T(dnb)
@@ -545,7 +694,7 @@ int rs_learned_loss_and_gradient_device(rs_learned *M, rs_lgraph *G, const doubl
     dpre_kernel<true><<<nblk((size_t)nv * H, 256), 256, 0, s>>>((size_t)nv * H, M->dh.p, M->pre2.p, M->dpre.p);
     RSG_LAUNCHED(ctx, "learned_dpre");
     layer_grad<64, 64>(M, nv, M->h1.p, M->nh1.p, M->o2s);
-    dense_bwd_in<64, 64><<<nblk((size_t)nv * H, 256), 256, 0, s>>>(nv, wb + M->o2s, wb + M->o2n, M->dpre.p,
+    dense_bwd_in<64, 64><<<nblk(nv, 64), 128, 0, s>>>(nv, wb + M->o2s, wb + M->o2n, M->dpre.p,
                                                                     M->dself.p, M->dnb.p);
     RSG_LAUNCHED(ctx, "learned_bwd_in");
     RSG_CUDA("product", cudaMemcpyAsync(M->dh.p, M->dself.p, (size_t)nv * H * sizeof(float), cudaMemcpyDeviceToDevice, s));

@@ -108,7 +108,6 @@ def load_library(path: str | os.PathLike | None = None):
         "rs_ctx_info": [_vp, C.c_char_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                         C.POINTER(C.c_int)],
         "rs_ctx_launch_count": [_vp, C.POINTER(C.c_int64)],
-        "rs_fp32_peak": [_vp, C.POINTER(C.c_double)],
         "rs_surface_validate": [C.c_int, C.c_int, _u32p, _f64p],
         "rs_face_tree_build": [C.c_int, C.c_int, _u32p, _f64p, C.c_int, C.c_int, _u32p, _u32p,
                                _u32p, _u32p, _f64p, _f64p, C.POINTER(C.c_int)],
@@ -263,9 +262,15 @@ class Context:
         return {"name": name.value.decode(), "sm_count": sm.value, "cc": (ma.value, mi.value)}
 
     def fp32_peak_tflops(self) -> float:
-        """Measured FP32 FMA throughput of the device (TFLOP/s)."""
+        """Measured FP32 FMA throughput of the device (TFLOP/s), by the separate measurement
+        library librsprobe.so (rsp_fp32_peak)."""
+        probe = C.CDLL(str(Path(__file__).resolve().parent / "librsprobe.so"))
+        probe.rsp_fp32_peak.argtypes = [C.c_int, C.POINTER(C.c_double)]
+        probe.rsp_fp32_peak.restype = C.c_int
         t = C.c_double()
-        _check(_lib.rs_fp32_peak(self._h, C.byref(t)))
+        err = probe.rsp_fp32_peak(self.ordinal, C.byref(t))
+        if err:
+            raise RsError(f"rsp_fp32_peak: CUDA error {err}")
         return t.value
 
     def launch_count(self) -> int:

@@ -4,7 +4,9 @@ Every translation unit under ``ddg-tools_gb300/csrc`` is compiled in parallel: `
 ``nvcc -gencode arch=compute_103a,code=sm_103a`` (GB300 only), ``.cpp`` host files by the host
 compiler with ``-ffp-contract=off`` (the face tree must round like the reference). Objects go
 to ``ddg-tools_gb300/_build/``, the library to ``ddg-tools_gb300/rs_gb300/librsgpu.so``.
-Rebuilds only what changed (by modification time).
+The measurement aid under ``csrc/probe`` (the device's FP32 FMA throughput) becomes its own
+``librsprobe.so`` beside it, outside the product's C ABI. Rebuilds only what changed (by
+modification time).
 """
 from __future__ import annotations
 
@@ -20,6 +22,8 @@ CSRC = ROOT / "csrc"
 BUILD = ROOT / "_build"
 INCLUDE = ROOT.parent / "include"
 LIB = PKG / "librsgpu.so"
+PROBE_SRC = CSRC / "probe" / "fp32_peak.cu"
+PROBE_LIB = PKG / "librsprobe.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Device code that must round like the reference's FP64 host code, operation for operation:
 # no multiply-add contraction.
@@ -76,9 +80,11 @@ def build(verbose: bool = False, jobs: int | None = None) -> Path:
         if verbose and (r.stdout or r.stderr):
             print(r.stdout, r.stderr, flush=True)
 
+    if _stale(PROBE_LIB, [PROBE_SRC, Path(__file__)]):
+        cmds.append([nvcc, *ARCH, "-O3", "-Xcompiler", "-fPIC", "-shared", str(PROBE_SRC), "-o", str(PROBE_LIB)])
     with ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 1)) as ex:
         list(ex.map(run, cmds))
-    if cmds or _stale(LIB, objs):
+    if _stale(LIB, objs):
         link = [nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-lcudart"]
         run(link)
     return LIB

@@ -36,20 +36,27 @@ def _constraint_gradients(P, F):
     return ga, gv
 
 
+# (major, minor) grid sizes of the training tori: 20,000 to 204,800 faces, up to the size of
+# the 320 x 320 evaluation torus, so that the network sees the global smooth error of the
+# largest surfaces it preconditions.
+TRAIN_TORI = [(100, 100), (160, 100), (200, 128), (240, 160), (256, 200), (288, 240), (320, 320)]
+
+
 def training_meshes(count: int = 8, seed: int = 100):
-    """Seeded noisy tori and icospheres of 20k-48k faces."""
+    """Seeded noisy tori (20,000-204,800 faces; noise 0.1-0.3 of the minor edge) and jittered
+    icospheres (level 5 or 6: 20,480 or 81,920 faces), one icosphere in four."""
     rng = np.random.default_rng(seed)
     out = []
     for i in range(count):
         s = int(rng.integers(1 << 30))
-        if i % 2 == 0:
-            nu = int(rng.choice([160, 200, 240]))
-            nv = int(rng.choice([64, 80, 100]))
-            r = float(rng.uniform(0.2, 0.4))
-            P, F = gen.noisy_torus(nu, nv, 1.0, r, float(rng.uniform(2e-4, 1.5e-3)), s)
-        else:
-            P, F = gen.icosphere(5)
+        if i % 4 == 3:
+            P, F = gen.icosphere(int(rng.choice([5, 6])))
             P = P * (1.0 + float(rng.uniform(0.005, 0.02)) * gen.SplitMix64(s).normals(len(P))[:, None])
+        else:
+            nu, nv = TRAIN_TORI[int(rng.integers(len(TRAIN_TORI)))]
+            r = float(rng.uniform(0.25, 0.4))
+            edge = 2.0 * np.pi * r / nv
+            P, F = gen.noisy_torus(nu, nv, 1.0, r, float(rng.uniform(0.1, 0.3)) * edge, s)
         out.append((P, F))
     return out
 
@@ -143,7 +150,7 @@ def load(model, path: Path = PARAMS_FILE) -> bool:
 
 def main(argv=None) -> int:
     """Generates the pairs, trains, evaluates on held-out pairs and writes PARAMS_FILE:
-    python -m rs_gb300.learned [--meshes 8] [--per-mesh 250] [--epochs 10]."""
+    python -m rs_gb300.learned [--meshes 8] [--per-mesh 250] [--epochs 20]."""
     import argparse
 
     import rs_gb300 as R
@@ -151,7 +158,7 @@ def main(argv=None) -> int:
     ap = argparse.ArgumentParser()
     ap.add_argument("--meshes", type=int, default=8)
     ap.add_argument("--per-mesh", type=int, default=250)
-    ap.add_argument("--epochs", type=int, default=10)
+    ap.add_argument("--epochs", type=int, default=20)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--cheap-steps", type=int, default=2)
     ap.add_argument("--out", default=str(PARAMS_FILE))

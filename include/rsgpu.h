@@ -87,10 +87,6 @@ int rs_ctx_launch_count(rs_ctx *ctx, int64_t *count);
  * (all contexts). No counterpart in the crate. */
 int rs_copy_counters(uint64_t *h2d_bytes, uint64_t *d2h_bytes);
 
-/* Measured FP32 (non-tensor) FMA throughput of the context's device in TFLOP/s: the
- * denominator of the pair kernel's roofline. No reference counterpart (a measurement aid). */
-int rs_fp32_peak(rs_ctx *ctx, double *tflops);
-
 /* ---------------------------------------------------------------- surface validation */
 
 /* Surface::new topology checks (RS/src/surface.rs:132-330) followed by

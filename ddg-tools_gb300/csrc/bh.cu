@@ -340,36 +340,6 @@ __global__ void offsets_from_sorted(const uint32_t *key, uint32_t n, uint32_t m,
 
 // ------------------------------------------------------------------ the pair kernel
 
-// Transposing reduce of a per-lane 8 x 4 array P over the 8 lanes of a lane group (lane bits
-// 0..2): afterwards lane s holds the group sum of row s. 28 shuffles, fixed order.
-__device__ __forceinline__ float4 group_transpose_reduce(float (&P)[32], int s) {
-  float Q[16];
-  const bool b2 = (s >> 2) & 1;
-#pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    float send = b2 ? P[i] : P[16 + i];
-    float keep = b2 ? P[16 + i] : P[i];
-    Q[i] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
-  }
-  float R[8];
-  const bool b1 = (s >> 1) & 1;
-#pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    float send = b1 ? Q[i] : Q[8 + i];
-    float keep = b1 ? Q[8 + i] : Q[i];
-    R[i] = keep + __shfl_xor_sync(0xffffffffu, send, 2);
-  }
-  float T[4];
-  const bool b0 = s & 1;
-#pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    float send = b0 ? R[i] : R[4 + i];
-    float keep = b0 ? R[4 + i] : R[i];
-    T[i] = keep + __shfl_xor_sync(0xffffffffu, send, 1);
-  }
-  return make_float4(T[0], T[1], T[2], T[3]);
-}
-
 // Error-free product and sum (Dekker/Knuth with FMA): a*b = p + e, a+b = s + t exactly.
 __device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
   p = a * b;
@@ -410,39 +380,58 @@ __device__ __forceinline__ void pair_diff(const float4 &ah, const float4 &al, co
   l[2] = t2 + (al.z - bl.z);
 }
 
+// Per-warp staging of the pair kernel in shared memory (one batch of up to kBatch sources).
+constexpr int kBatch = 64;
+struct PairStage {
+  // lumped: per node entry, X_L - X_C rounded to FP32 (xyz) and A_C (w);
+  // exact: per source face T, y_T = X_T - X_L as a float pair: hi (xyz) with a_T (w), lo (xyz)
+  // with T's slot in the target leaf when C = L, else -1 (w, integer bits)
+  float4 src_hi[kBatch], src_lo[kBatch];
+  uint32_t src_slot[kBatch];            // exact: partner slot of each staged face
+  float4 ent_h[32], ent_l[32];          // exact: X_L - X_C of each entry as a float pair
+  uint32_t ent_cs[32], ent_po[32], ent_first[32];
+  uint8_t fmap[256];                    // exact: entry of every face of the chunk
+  float4 red[264];                      // per (target slot s, source e): the terms summed over s;
+                                        // ns (8 G + 1) <= 264 for every leaf size ns <= 8
+};
+
 // The pair kernel. One warp per work item: a slice of one target leaf's lumped and exact
 // lists (leaf size <= 8; long lists are split so that no warp carries a whole-mesh leaf).
-// Lane = s + 8 j: s is the target face of the leaf, j one of four entry groups. Lumped entries
-// are taken in batches of 8 per group (the node terms b = sum_S a_S K, u = -sum_S a_S dK/dv
-// reduced over s by one transposing reduce), exact entries one leaf block per group (the
-// partner terms reduced the same way). Own partials and the energy go through Kahan
-// accumulators and are written per work item (leaf_with_gradient, barnes_hut.rs:627-689; value
-// only: leaf_energy, barnes_hut.rs:583-614).
+// Lanes are (group g, target face s) = g ns + s for the leaf's ns faces and G = min(8, 32/ns)
+// groups, so that 24-32 lanes work whatever the leaf size. Sources go through shared memory in
+// batches of 8 G: lumped nodes (one per entry) and the faces of exact leaves (flattened over
+// up to 32 entries at a time); group g takes sources g, g + G, ... The per-source terms
+// (node terms b = sum_S a_S K, u = -sum_S a_S dK/dv, and the exact partner terms) are summed
+// over s from shared memory in fixed order; own partials and the energy go through Kahan
+// accumulators and are written per work item (leaf_with_gradient, barnes_hut.rs:627-689;
+// value only: leaf_energy, barnes_hut.rs:583-614).
 //
-// nu = N_S . (X_S - X_T) is formed from float pairs with compensated dot products: on a
-// smooth surface nu is ~|v|^2 kappa, far below |v|, plain FP32 loses it, and the differential
-// (a sum of large terms that cancel around every vertex) inherits the loss. Lumped entries:
-// nu = alpha_S + N_S.(X_L - X_C); exact entries: nu = [alpha_S + N_S.(X_L - X_C)] - N_S.(X_T - X_C)
-// with the bracket kept as a float pair per entry, and v = X_S - X_T summed with its rounding
-// error (leaf offsets can be large next to |v| in a stretched leaf). alpha_S = N_S.(X_S - X_L)
-// is a float pair from the FP64 refit.
+// Lumped nodes are admissible, so |v| is at least the node's size over theta and
+// nu = alpha_S + N_S.(X_L - X_C) keeps FP32 relative precision in plain arithmetic. Exact
+// pairs are near: on a smooth surface nu is ~|v|^2 kappa, far below |v|, plain FP32 loses it,
+// and the differential (large terms that cancel around every vertex) inherits the loss. So
+// nu = alpha_S - N_S.y_T with y_T = X_T - X_L held as a float pair and a compensated dot
+// product, and v = X_S - X_T is summed with its rounding error (leaf offsets can be large next
+// to |v| in a stretched leaf). alpha_S = N_S.(X_S - X_L) is a float pair from the FP64 refit.
 template <bool GRAD, bool FAST>
-__global__ void __launch_bounds__(128, 5) bh_pair_kernel(BhDev d, Pow pw) {
+__global__ void __launch_bounds__(128, 6) bh_pair_kernel(BhDev d, Pow pw) {
+  __shared__ PairStage stage[4];
+  PairStage &st = stage[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
-  const int s = lane & 7;
-  const int j = lane >> 3;
   for (;;) {
     unsigned int w = 0;
     if (lane == 0) w = atomicAdd(d.ticket, 1u);
     w = __shfl_sync(0xffffffffu, w, 0);
     if (w >= (unsigned)d.n_items) return;
     const uint32_t item = d.schedule[w];
-    const uint4 it = d.items[item];  // (leaf ordinal, lumped begin, exact begin, packed ends)
+    const uint4 it = d.items[item];  // lumped [x, y), exact [z, w) entry ranges
     const uint32_t k = d.item_leaf[item];
     const uint32_t leaf = d.leaves[k];
     const uint32_t s0 = d.node_start[leaf];
-    const uint32_t ns = d.node_end[leaf] - s0;
-    const bool act = (uint32_t)s < ns;
+    const int ns = (int)(d.node_end[leaf] - s0);
+    const int G = min(8, 32 / ns), B = 8 * G, RS = B + 1;
+    const int g = lane / ns, s = lane - g * ns;
+    const bool act = g < G;
     const float4 xs = act ? d.fxa[s0 + s] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 nS = act ? d.fnn[s0 + s] : make_float4(0.f, 0.f, 1.f, 0.f);
     const float4 nL = act ? d.fnl[s0 + s] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -451,47 +440,43 @@ __global__ void __launch_bounds__(128, 5) bh_pair_kernel(BhDev d, Pow pw) {
     const float a_s = xs.w;
     Kahan e_acc, da_acc, dx0, dx1, dx2, dn0, dn1, dn2;
 
-    // ---- lumped nodes, 8 per group per batch
+    // ---- lumped nodes
     const uint32_t llo = it.x, lhi = it.y;
-    for (uint32_t base = llo; base < lhi; base += 32) {
-      float P[32];
+    for (uint32_t base = llo; base < lhi; base += B) {
+      const int cnt = (int)min((uint32_t)B, lhi - base);
+      __syncwarp();
+      for (int e = lane; e < cnt; e += 32) {
+        const uint32_t c = d.lumped[base + e];
+        const float4 ch = d.nch[c], cl = d.ncl[c];
+        float h[3], l[3];
+        pair_diff(cLh, cLl, ch, cl, h, l);
+        st.src_hi[e] = make_float4(h[0] + l[0], h[1] + l[1], h[2] + l[2], ch.w);
+      }
+      __syncwarp();
       float bda = 0.f, be = 0.f, bx0 = 0.f, bx1 = 0.f, bx2 = 0.f, bn0 = 0.f, bn1 = 0.f, bn2 = 0.f;
-#pragma unroll
+#pragma unroll 2
       for (int i = 0; i < 8; ++i) {
-        const uint32_t q = base + 8 * j + i;
-        const bool ok = act && q < lhi;
-        float K = 0.f, cn = 0.f, g = 0.f;
-        float v0 = 0.f, v1 = 0.f, v2 = 0.f, Ac = 0.f;
-        if (q < lhi) {
-          const uint32_t c = d.lumped[q];
-          const float4 ch = d.nch[c], cl = d.ncl[c];
-          float h[3], l[3];
-          pair_diff(cLh, cLl, ch, cl, h, l);
-          v0 = (xs.x + h[0]) + l[0];
-          v1 = (xs.y + h[1]) + l[1];
-          v2 = (xs.z + h[2]) + l[2];
-          Ac = ch.w;
-          if (ok) {
-            float u, lo;
-            dot2(nS.x, nS.y, nS.z, nL.x, nL.y, nL.z, h[0], h[1], h[2], l[0], l[1], l[2], u, lo);
-            const float nu = nL.w + (u + (lo + xsl.w));
-            float r2 = v0 * v0 + v1 * v1 + v2 * v2;
-            float ir2 = __fdividef(1.f, r2);
-            kernel_k<FAST>(pw, nu, r2, ir2, K, cn);
-            g = pw.beta * K * ir2;
-          }
-        }
+        const int e = g + G * i;
+        if (!act || e >= cnt) continue;
+        const float4 nd = st.src_hi[e];
+        const float v0 = xs.x + nd.x, v1 = xs.y + nd.y, v2 = xs.z + nd.z;
+        const float u = fmaf(nS.z, nd.z, fmaf(nS.y, nd.y, nS.x * nd.x));
+        const float nu = nL.w + (u + xsl.w);
+        const float r2 = v0 * v0 + v1 * v1 + v2 * v2;
+        const float ir2 = __fdividef(1.f, r2);
+        float K, cn;
+        kernel_k<FAST>(pw, nu, r2, ir2, K, cn);
+        const float Ac = nd.w;
         be += a_s * K * Ac;
         if (GRAD) {
-          float dv0 = cn * nS.x - g * v0, dv1 = cn * nS.y - g * v1, dv2 = cn * nS.z - g * v2;
+          const float gg = pw.beta * K * ir2;
+          const float dv0 = cn * nS.x - gg * v0, dv1 = cn * nS.y - gg * v1, dv2 = cn * nS.z - gg * v2;
           bda += K * Ac;
-          float aa = a_s * Ac;
+          const float aa = a_s * Ac;
           bx0 += aa * dv0, bx1 += aa * dv1, bx2 += aa * dv2;
-          bn0 += aa * cn * v0, bn1 += aa * cn * v1, bn2 += aa * cn * v2;
-          P[4 * i + 0] = a_s * K;
-          P[4 * i + 1] = -a_s * dv0;
-          P[4 * i + 2] = -a_s * dv1;
-          P[4 * i + 3] = -a_s * dv2;
+          const float ac = aa * cn;
+          bn0 += ac * v0, bn1 += ac * v1, bn2 += ac * v2;
+          st.red[s * RS + e] = make_float4(a_s * K, -a_s * dv0, -a_s * dv1, -a_s * dv2);
         }
       }
       e_acc.add(be);
@@ -499,93 +484,140 @@ __global__ void __launch_bounds__(128, 5) bh_pair_kernel(BhDev d, Pow pw) {
         da_acc.add(bda);
         dx0.add(bx0), dx1.add(bx1), dx2.add(bx2);
         dn0.add(bn0), dn1.add(bn1), dn2.add(bn2);
-        float4 t = group_transpose_reduce(P, s);
-        const uint32_t q = base + 8 * j + s;
-        if (q < lhi) d.node_term[q] = t;
+        __syncwarp();
+        for (int e = lane; e < cnt; e += 32) {
+          float4 t = st.red[e];
+          for (int r = 1; r < ns; ++r) {
+            const float4 q = st.red[r * RS + e];
+            t.x += q.x, t.y += q.y, t.z += q.z, t.w += q.w;
+          }
+          d.node_term[base + e] = t;
+        }
       }
     }
 
-    // ---- exact leaves, one block per group
+    // ---- exact leaves, up to 32 entries at a time, their faces flattened
     const uint32_t elo = it.z, ehi = it.w;
-    for (uint32_t base = elo; base < ehi; base += 4) {
-      const uint32_t q = base + j;
-      const bool qok = q < ehi;
-      uint32_t c = 0, cs = 0, nc = 0;
-      float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f}, abh = 0.f, abl = 0.f;
-      if (qok) {
-        c = d.exact[q];
-        cs = d.node_start[c];
+    for (uint32_t cb = elo; cb < ehi; cb += 32) {
+      const int ncnt = (int)min(32u, ehi - cb);
+      __syncwarp();
+      uint32_t nc = 0;
+      if (lane < ncnt) {
+        const uint32_t q = cb + lane;
+        const uint32_t c = d.exact[q];
+        const uint32_t cs = d.node_start[c];
         nc = d.node_end[c] - cs;
-        const float4 ch = d.nch[c], cl = d.ncl[c];
-        pair_diff(cLh, cLl, ch, cl, h, l);  // X_L - X_C
-        // alpha_S + N_S . (X_L - X_C) as a float pair
-        float u, lo, t;
-        dot2(nS.x, nS.y, nS.z, nL.x, nL.y, nL.z, h[0], h[1], h[2], l[0], l[1], l[2], u, lo);
-        two_sum(nL.w, u, abh, t);
-        abl = (t + lo) + xsl.w;
+        float h[3], l[3];
+        pair_diff(cLh, cLl, d.nch[c], d.ncl[c], h, l);  // X_L - X_C
+        st.ent_h[lane] = make_float4(h[0], h[1], h[2], 0.f);
+        st.ent_l[lane] = make_float4(l[0], l[1], l[2], __int_as_float(c == leaf ? 1 : 0));
+        st.ent_cs[lane] = cs;
+        st.ent_po[lane] = d.partner_off[q];
       }
-      float P[32];
-      float row = 0.f, rx0 = 0.f, rx1 = 0.f, rx2 = 0.f, rn0 = 0.f, rn1 = 0.f, rn2 = 0.f;
+      uint32_t incl = nc;
 #pragma unroll
-      for (int t = 0; t < 8; ++t) {
-        float K = 0.f, cn = 0.f, g = 0.f, v0 = 0.f, v1 = 0.f, v2 = 0.f, a_t = 0.f;
-        if ((uint32_t)t < nc) {
-          const float4 xt = d.fxa[cs + t];
-          a_t = xt.w;
-          const bool self = (c == leaf) && (t == s);
-          if (act && !self) {
-            const float4 xl = d.fol[cs + t];  // offset lo part of T
-            float w0, e0, w1, e1, w2, e2;
-            two_sum(xs.x, -xt.x, w0, e0);
-            two_sum(xs.y, -xt.y, w1, e1);
-            two_sum(xs.z, -xt.z, w2, e2);
-            v0 = (w0 + h[0]) + ((e0 + l[0]) + (xsl.x - xl.x));
-            v1 = (w1 + h[1]) + ((e1 + l[1]) + (xsl.y - xl.y));
-            v2 = (w2 + h[2]) + ((e2 + l[2]) + (xsl.z - xl.z));
-            float r2 = v0 * v0 + v1 * v1 + v2 * v2;
-            float ir2 = __fdividef(1.f, r2);
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      const int FT = (int)__shfl_sync(0xffffffffu, incl, 31);
+      if (lane < ncnt) {
+        st.ent_first[lane] = incl - nc;
+        for (uint32_t t = 0; t < nc; ++t) st.fmap[incl - nc + t] = (uint8_t)lane;
+      }
+      for (int fb = 0; fb < FT; fb += B) {
+        const int cnt = min(B, FT - fb);
+        __syncwarp();
+        for (int f = lane; f < cnt; f += 32) {
+          const int i = st.fmap[fb + f];
+          const uint32_t t = (uint32_t)(fb + f) - st.ent_first[i];
+          const uint32_t p = st.ent_cs[i] + t;
+          const float4 xt = d.fxa[p], xl = d.fol[p];
+          const float4 hh = st.ent_h[i], ll = st.ent_l[i];
+          // y_T = x_T - (X_L - X_C) as a float pair
+          float y0, y1, y2, e0, e1, e2;
+          two_sum(xt.x, -hh.x, y0, e0);
+          two_sum(xt.y, -hh.y, y1, e1);
+          two_sum(xt.z, -hh.z, y2, e2);
+          st.src_hi[f] = make_float4(y0, y1, y2, xt.w);
+          st.src_lo[f] = make_float4(e0 + (xl.x - ll.x), e1 + (xl.y - ll.y), e2 + (xl.z - ll.z),
+                                     __int_as_float(__float_as_int(ll.w) ? (int)t : -1));
+          st.src_slot[f] = st.ent_po[i] + t;
+        }
+        __syncwarp();
+        float row = 0.f, rx0 = 0.f, rx1 = 0.f, rx2 = 0.f, rn0 = 0.f, rn1 = 0.f, rn2 = 0.f;
+#pragma unroll 2
+        for (int i = 0; i < 8; ++i) {
+          const int f = g + G * i;
+          if (!act || f >= cnt) continue;
+          const float4 yh = st.src_hi[f], yl = st.src_lo[f];
+          const float a_t = yh.w;
+          float K = 0.f, cn = 0.f, gg = 0.f, v0 = 0.f, v1 = 0.f, v2 = 0.f;
+          if (__float_as_int(yl.w) != s) {
+            float w0, w1, w2, e0, e1, e2;
+            two_sum(xs.x, -yh.x, w0, e0);
+            two_sum(xs.y, -yh.y, w1, e1);
+            two_sum(xs.z, -yh.z, w2, e2);
+            v0 = w0 + (e0 + (xsl.x - yl.x));
+            v1 = w1 + (e1 + (xsl.y - yl.y));
+            v2 = w2 + (e2 + (xsl.z - yl.z));
+            const float r2 = v0 * v0 + v1 * v1 + v2 * v2;
+            const float ir2 = __fdividef(1.f, r2);
             float ph, pl, sh, se;
-            dot2(nS.x, nS.y, nS.z, nL.x, nL.y, nL.z, xt.x, xt.y, xt.z, xl.x, xl.y, xl.z, ph, pl);
-            two_sum(abh, -ph, sh, se);
-            const float nu = sh + (se + (abl - pl));
+            dot2(nS.x, nS.y, nS.z, nL.x, nL.y, nL.z, yh.x, yh.y, yh.z, yl.x, yl.y, yl.z, ph, pl);
+            two_sum(nL.w, -ph, sh, se);
+            const float nu = sh + (se + (xsl.w - pl));
             kernel_k<FAST>(pw, nu, r2, ir2, K, cn);
-            g = pw.beta * K * ir2;
+            gg = pw.beta * K * ir2;
+          }
+          row += a_t * K;
+          if (GRAD) {
+            const float dv0 = cn * nS.x - gg * v0, dv1 = cn * nS.y - gg * v1, dv2 = cn * nS.z - gg * v2;
+            rx0 += a_t * dv0, rx1 += a_t * dv1, rx2 += a_t * dv2;
+            const float tc = a_t * cn;
+            rn0 += tc * v0, rn1 += tc * v1, rn2 += tc * v2;
+            const float aa = -a_s * a_t;
+            st.red[s * RS + f] = make_float4(a_s * K, aa * dv0, aa * dv1, aa * dv2);
           }
         }
-        row += a_t * K;
+        e_acc.add(a_s * row);
         if (GRAD) {
-          float dv0 = cn * nS.x - g * v0, dv1 = cn * nS.y - g * v1, dv2 = cn * nS.z - g * v2;
-          rx0 += a_t * dv0, rx1 += a_t * dv1, rx2 += a_t * dv2;
-          rn0 += a_t * cn * v0, rn1 += a_t * cn * v1, rn2 += a_t * cn * v2;
-          float aa = -a_s * a_t;
-          P[4 * t + 0] = a_s * K;
-          P[4 * t + 1] = aa * dv0;
-          P[4 * t + 2] = aa * dv1;
-          P[4 * t + 3] = aa * dv2;
+          da_acc.add(row);
+          dx0.add(a_s * rx0), dx1.add(a_s * rx1), dx2.add(a_s * rx2);
+          dn0.add(a_s * rn0), dn1.add(a_s * rn1), dn2.add(a_s * rn2);
+          __syncwarp();
+          for (int f = lane; f < cnt; f += 32) {
+            float4 t = st.red[f];
+            for (int r = 1; r < ns; ++r) {
+              const float4 q = st.red[r * RS + f];
+              t.x += q.x, t.y += q.y, t.z += q.z, t.w += q.w;
+            }
+            d.partner[st.src_slot[f]] = t;
+          }
         }
-      }
-      e_acc.add(a_s * row);
-      if (GRAD) {
-        da_acc.add(row);
-        dx0.add(a_s * rx0), dx1.add(a_s * rx1), dx2.add(a_s * rx2);
-        dn0.add(a_s * rn0), dn1.add(a_s * rn1), dn2.add(a_s * rn2);
-        float4 t4 = group_transpose_reduce(P, s);
-        if (qok && (uint32_t)s < nc) d.partner[d.partner_off[q] + s] = t4;
       }
     }
 
-    // ---- reduce over the four groups; lanes 0..7 write the item's own partials
+    // ---- own partials summed over the groups in order; lanes 0..7 write the item's slots
     if (GRAD) {
-      float o[7] = {da_acc.value(), dx0.value(), dx1.value(), dx2.value(),
-                    dn0.value(),    dn1.value(), dn2.value()};
-#pragma unroll
-      for (int i = 0; i < 7; ++i) {
-        o[i] += __shfl_xor_sync(0xffffffffu, o[i], 8);
-        o[i] += __shfl_xor_sync(0xffffffffu, o[i], 16);
+      __syncwarp();
+      if (act) {
+        st.red[2 * (g * 8 + s)] = make_float4(da_acc.value(), dx0.value(), dx1.value(), dx2.value());
+        st.red[2 * (g * 8 + s) + 1] = make_float4(dn0.value(), dn1.value(), dn2.value(), 0.f);
       }
-      if (j == 0) {
-        d.own[16 * (size_t)item + 2 * s] = make_float4(o[0], o[1], o[2], o[3]);
-        d.own[16 * (size_t)item + 2 * s + 1] = make_float4(o[4], o[5], o[6], 0.f);
+      __syncwarp();
+      if (lane < 8) {
+        float4 o0 = make_float4(0.f, 0.f, 0.f, 0.f), o1 = o0;
+        if (lane < ns) {
+          o0 = st.red[2 * lane], o1 = st.red[2 * lane + 1];
+          for (int r = 1; r < G; ++r) {
+            const float4 p0 = st.red[2 * (r * 8 + lane)], p1 = st.red[2 * (r * 8 + lane) + 1];
+            o0.x += p0.x, o0.y += p0.y, o0.z += p0.z, o0.w += p0.w;
+            o1.x += p1.x, o1.y += p1.y, o1.z += p1.z;
+          }
+        }
+        d.own[16 * (size_t)item + 2 * lane] = o0;
+        d.own[16 * (size_t)item + 2 * lane + 1] = o1;
       }
     }
     double e = (double)e_acc.s - (double)e_acc.c;

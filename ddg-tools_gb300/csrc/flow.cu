@@ -183,6 +183,8 @@ rs_flow_options rs_flow_options_default(void) {
   o.area_target = NAN;
   o.volume_target = NAN;
   o.guard_projection = 1;
+  o.retry_max_iterations = 0;
+  o.dense_fallback = 1;
   return o;
 }
 
@@ -487,11 +489,17 @@ void flow_step(rs_flow *F, double *report, bool direction_only) {
   int code = rs_solver_solve_many_device(sv.p, nb, rhs.p, sol.p, srep);
   if (code == RS_SOLVER_DIVERGED) {
     // the crate's recovery (RobustHierarchical::escalate, direction.rs:269-379): repeat the
-    // solves with restart 60 and at least four times the iteration cap (800 or more)
+    // solves with restart 60 and at least four times the iteration cap (800 or more), then by
+    // the dense LU of the exact metric for at most 6000 vertices
     const rs_solver_options &so = o.solver;
-    check(rs_solver_set_gmres(sv.p, 60, std::max(4 * so.max_iterations, 800), so.tolerance), "flow (solve)");
+    const int it = o.retry_max_iterations > 0 ? o.retry_max_iterations : std::max(4 * so.max_iterations, 800);
+    check(rs_solver_set_gmres(sv.p, 60, it, so.tolerance), "flow (solve)");
     rep[18] += 1.0;
     code = rs_solver_solve_many_device(sv.p, nb, rhs.p, sol.p, srep);
+    if (code == RS_SOLVER_DIVERGED && o.dense_fallback && nv <= RS_DENSE_FALLBACK_MAX_VERTICES) {
+      rep[18] += 1.0;
+      code = rs_solver_dense_solve_many_device(sv.p, nb, rhs.p, sol.p, srep);
+    }
   }
   check(code, "flow (solve)");
   rep[12] = since(t);

@@ -29,6 +29,7 @@
 #include "host_tree.hpp"
 #include "krylov.hpp"
 #include "learned.hpp"
+#include "dense.hpp"
 #include "profile.hpp"
 
 namespace rsg {
@@ -338,6 +339,13 @@ struct rs_solver {
   DevBuf<double> c_t, c_yc, c_t2, c_part, c_rp;
   double c_conditioning = 0.0;
   int c_dropped = 0;
+  // the dense last resort (at most kDenseMaxVertices vertices): the surface kept on the host for
+  // the exact metric, and the factor once built
+  std::vector<uint32_t> faces_h;
+  std::vector<double> pos_h;
+  double alpha = 6.0, beta = 12.0;
+  int leaf_size = 8, leaf_pairs = 64;
+  std::unique_ptr<DenseSaddleDev> dense;
 
   cudaStream_t st() const { return ctx->stream; }
 
@@ -693,6 +701,11 @@ int rs_solver_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const do
     S->ctx = ctx;
     S->nv = nv, S->nf = nf, S->nd = 3 * (size_t)nv;
     S->geom = face_geometry(nf, faces, positions_host);
+    S->alpha = alpha, S->beta = beta, S->leaf_size = o->leaf_size, S->leaf_pairs = o->leaf_pairs;
+    if (nv <= kDenseMaxVertices) {
+      S->faces_h.assign(faces, faces + 3 * (size_t)nf);
+      S->pos_h.assign(positions_host, positions_host + 3 * (size_t)nv);
+    }
     S->vmass.assign(nv, 0.0);
     for (int f = 0; f < nf; ++f)
       for (int c = 0; c < 3; ++c) S->vmass[faces[3 * f + c]] += S->geom.area[f] / 3.0;
@@ -945,6 +958,52 @@ int rs_solver_precondition_device(rs_solver *S, int nb, const double *r_dev, dou
     S->ctx->use();
     S->apply_prec(nb, r_dev, z_dev);
   });
+}
+
+int rs_solver_dense_solve_many_device(rs_solver *S, int nb, const double *rhs_dev, double *sol_dev,
+                                      double *report) {
+  return guard([&] {
+    S->ctx->use();
+    if (nb < 1 || nb > 4) fail(RS_INVALID_OPTION, "InvalidOption", "solver", "1 to 4 right-hand sides per batch");
+    if (S->nv > kDenseMaxVertices)
+      fail(RS_INVALID_OPTION, "InvalidOption", "solver",
+           "the dense last resort takes at most " + std::to_string(kDenseMaxVertices) + " vertices");
+    auto t0 = std::chrono::steady_clock::now();
+    if (!S->dense) {
+      // the exact metric: the block cluster tree at chi = 0 holds every pair in near blocks
+      rs_metric *m0 = nullptr;
+      int rc = rs_metric_build(S->ctx, S->nv, S->nf, S->faces_h.data(), S->pos_h.data(), S->alpha, S->beta, 0.0,
+                               S->leaf_size, S->leaf_pairs, &m0);
+      if (rc) fail(rc, "Gpu", "solver", std::string("dense metric: ") + rs_last_error());
+      std::unique_ptr<rs_metric, void (*)(rs_metric *)> own(m0, rs_metric_free);
+      auto D = std::make_unique<DenseSaddleDev>();
+      const double wh = S->w_hi, wl = S->w_lo;
+      const size_t nd = S->nd;
+      D->build(S->ctx, S->nv, S->G, S->group.p, S->c.p, [&](int k, const double *x, double *y) {
+        metric_apply_strided(m0, wh, wl, k, x, nd, y, nd);
+      });
+      S->dense = std::move(D);
+    }
+    std::vector<double> rel(nb);
+    S->dense->solve(nb, rhs_dev, sol_dev, rel.data());
+    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    S->last.assign(nb, GmresReport());
+    for (int q = 0; q < nb; ++q) {
+      S->last[q].iterations = 0, S->last[q].relative_residual = rel[q];
+      S->last[q].converged = true, S->last[q].seconds = secs / nb, S->last[q].cycles = 0;
+      if (report) {
+        report[5 * q + 0] = 0.0;
+        report[5 * q + 1] = rel[q];
+        report[5 * q + 2] = 1.0;
+        report[5 * q + 3] = secs / nb;
+        report[5 * q + 4] = 0.0;
+      }
+    }
+  });
+}
+
+int rs_solver_dense_pivot_ratio(rs_solver *S, double *ratio) {
+  return guard([&] { *ratio = S->dense ? S->dense->pivot_ratio : 0.0; });
 }
 
 int rs_solver_solve_many_device(rs_solver *S, int nb, const double *rhs_dev, double *sol_dev,

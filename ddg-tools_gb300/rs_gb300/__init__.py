@@ -55,7 +55,8 @@ class FlowOptions(C.Structure):
                 ("start_rule", C.c_int), ("start_value", C.c_double), ("first_rule", C.c_int),
                 ("first_value", C.c_double), ("tau_min_rel", C.c_double), ("newton_fixed", C.c_int),
                 ("newton_tolerance", C.c_double), ("area_target", C.c_double),
-                ("volume_target", C.c_double), ("guard_projection", C.c_int)]
+                ("volume_target", C.c_double), ("guard_projection", C.c_int),
+                ("retry_max_iterations", C.c_int), ("dense_fallback", C.c_int)]
 
 
 # StartRule codes of rs_flow_options.start_rule / first_rule
@@ -149,6 +150,8 @@ def load_library(path: str | os.PathLike | None = None):
         "rs_solver_precondition_device": [_vp, C.c_int, _vp, _vp],
         "rs_solver_solve_many": [_vp, C.c_int, _f64p, _f64p, _f64p],
         "rs_solver_solve_many_device": [_vp, C.c_int, _vp, _vp, _f64p],
+        "rs_solver_dense_solve_many_device": [_vp, C.c_int, _vp, _vp, _f64p],
+        "rs_solver_dense_pivot_ratio": [_vp, C.POINTER(C.c_double)],
         "rs_metric_apply_device_noalloc": [_vp, C.c_double, C.c_double, C.c_int, C.c_void_p, C.c_void_p],
         "rs_copy_counters": [C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)],
         "rs_solver_build_times": [_vp, _f64p],
@@ -659,6 +662,27 @@ class SaddleSolver:
             r["iterations"] = int(r["iterations"])
             r["converged"] = bool(r["converged"])
         return out, reports
+
+    def dense_solve_many(self, rhs):
+        """The dense last resort (rs_solver_dense_solve_many_device): A' with the exact metric
+        factored by LU on the device, one refinement step; returns (y, reports)."""
+        import torch
+
+        rhs = np.ascontiguousarray(rhs, dtype=np.float64).reshape(-1, self.n)
+        rd = torch.tensor(rhs, device=f"cuda:{self.ctx.ordinal}")
+        sd = torch.empty_like(rd)
+        rep = np.zeros(5 * len(rhs))
+        torch.cuda.synchronize(rd.device)
+        _check(_lib.rs_solver_dense_solve_many_device(self._h, len(rhs), _vp(rd.data_ptr()), _vp(sd.data_ptr()), rep))
+        self.ctx.synchronize()
+        keys = ["iterations", "relative_residual", "converged", "seconds", "cycles"]
+        reports = [dict(zip(keys, rep[5 * i: 5 * i + 5])) for i in range(len(rhs))]
+        return sd.cpu().numpy(), reports
+
+    def dense_pivot_ratio(self) -> float:
+        r = C.c_double()
+        _check(_lib.rs_solver_dense_pivot_ratio(self._h, C.byref(r)))
+        return r.value
 
     def profile(self, rhs) -> dict:
         """Milliseconds per phase of one solve of the stacked right-hand sides."""

@@ -299,6 +299,20 @@ int rs_solver_history(rs_solver *s, int q, double *estimates, int max_iter, int 
 int rs_solver_solve_many_device(rs_solver *s, int nb, const double *rhs_dev, double *sol_dev,
                                 double *report);
 
+/* The last stage of the recovery chain (RobustHierarchical::escalate, RS/src/step/
+ * direction.rs:238-300; DenseSaddle, RS/src/solve/dense.rs:282-470): A' with the exact metric
+ * (every face pair, chi = 0) assembled densely on the device, equilibrated and factored by LU
+ * with partial pivoting in FP64, per axis ((V + G) square with the barycenter rows); nb (1..4)
+ * right-hand sides solved with one step of iterative refinement. The factor is built on the
+ * first call and kept. Report as rs_solver_solve_many (iterations 0, relative residual on the
+ * dense operator, converged 1). InvalidOption above RS_DENSE_FALLBACK_MAX_VERTICES vertices;
+ * SingularSaddle when the equilibrated pivot ratio is at most 1e-13 (PIVOT_TOLERANCE). */
+#define RS_DENSE_FALLBACK_MAX_VERTICES 6000 /* DENSE_FALLBACK_MAX_VERTICES, direction.rs:238 */
+int rs_solver_dense_solve_many_device(rs_solver *s, int nb, const double *rhs_dev, double *sol_dev,
+                                      double *report);
+/* min |u_ii| / max |u_ii| of the equilibrated dense factor (0 before the first dense solve). */
+int rs_solver_dense_pivot_ratio(rs_solver *s, double *ratio);
+
 /* ---------------------------------------------------------------- one Hs step */
 
 typedef struct rs_flow rs_flow; /* Session (RS/src/step/session.rs:371-1369), step_inner's
@@ -333,6 +347,12 @@ typedef struct rs_flow_options {
   double area_target;        /* NaN: the initial total area */
   double volume_target;      /* NaN: the initial volume */
   int guard_projection;      /* keep an Armijo trial only if its projection is admissible (1) */
+  /* The recovery chain of a diverged solve (RobustHierarchical, direction.rs:269-379): the
+   * solves are repeated with restart 60 and retry_max_iterations GMRES iterations (0: the
+   * crate's max(4 solver.max_iterations, 800)), then, if dense_fallback is set and the mesh has
+   * at most RS_DENSE_FALLBACK_MAX_VERTICES vertices, by the dense LU (1). */
+  int retry_max_iterations;
+  int dense_fallback;
 } rs_flow_options;
 
 rs_flow_options rs_flow_options_default(void);

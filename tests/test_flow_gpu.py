@@ -137,3 +137,23 @@ def test_recovery_repeats_a_diverged_solve():
     print(rep)
     assert rep["fallbacks"] == 1.0
     assert rep["accepted"] == 1.0 and rep["relative_residual"] <= 1e-6
+
+
+def test_recovery_ends_with_the_dense_lu():
+    """The whole recovery chain (RobustHierarchical::escalate, direction.rs:269-379): when the
+    restart-60 retry diverges too (here one iteration each), a mesh of at most 6000 vertices
+    is solved by the dense LU of the exact metric; both escalations are counted and the step
+    proceeds with a direction that solves the dense system."""
+    P, F = gen.noisy_torus(32, 16, 1.0, 0.3, 0.003, 2)
+    flow = R.Flow(F, P, R.flow_options(theta=0.5, hold_volume=1, solver_max_iterations=1, solver_tolerance=1e-6,
+                                       retry_max_iterations=1))
+    rep = flow.step()
+    print(rep)
+    assert rep["fallbacks"] == 2.0
+    assert rep["accepted"] == 1.0 and rep["relative_residual"] <= 1e-10
+    # without the last stage the step fails with SolverDiverged
+    flow = R.Flow(F, P, R.flow_options(theta=0.5, hold_volume=1, solver_max_iterations=1, solver_tolerance=1e-6,
+                                       retry_max_iterations=1, dense_fallback=0))
+    with pytest.raises(R.RsError) as e:
+        flow.step()
+    assert e.value.kind == "SolverDiverged"

@@ -101,3 +101,35 @@ def test_preconditioner_matches_oracle_with_converged_lprime(ctx, mesh):
     err = G.normwise(S.precondition(r), H.precondition(r))
     print(f"{mesh}: preconditioner against the oracle's {err:.2e}")
     assert err <= 1e-4
+
+
+@pytest.mark.parametrize("mesh", ["c1", "torus48x24"])
+def test_dense_last_resort_solves_the_exact_saddle(ctx, mesh):
+    """The last stage of the recovery chain (DenseSaddle, RS/src/solve/dense.rs:282-470, for at
+    most 6000 vertices): A' with the exact metric assembled densely on the device and factored by
+    a pivoted FP64 LU with one refinement step. Its solution solves the oracle's FP64 operator
+    with the exact metric (chi = 0) to 1e-6 and equals GMRES on the library's chi = 0 operator
+    to 1e-6; the equilibrated pivot ratio is above PIVOT_TOLERANCE (1e-13)."""
+    P, F = {"c1": gen.config_c1, "torus48x24": lambda: gen.noisy_torus(48, 24, 1.0, 0.3, 0.003, 7)}[mesh]()
+    S = R.SaddleSolver(F, P, R.Exponents(), R.solver_options(), ctx)
+    rng = np.random.default_rng(21)
+    rhs = rng.standard_normal((2, S.n))
+    rhs[1, S.n_dofs:] = 0.0
+    y, reps = S.dense_solve_many(rhs)
+    ratio = S.dense_pivot_ratio()
+    print(mesh, reps, f"pivot ratio {ratio:.3e}")
+    assert ratio > 1e-13
+    A = oracle_operator(P, F, chi=0.0)
+    S0 = R.SaddleSolver(F, P, R.Exponents(), R.solver_options(chi=0.0, tolerance=1e-10, restart=60,
+                                                             max_iterations=2000), ctx)
+    y0, _ = S0.solve_many(rhs)
+    for i, r in enumerate(reps):
+        assert r["converged"] and r["relative_residual"] <= 1e-10
+        res = np.linalg.norm(A(y[i])[0] - rhs[i]) / np.linalg.norm(rhs[i])
+        print(f"{mesh}: dense solution, residual of the oracle operator {res:.2e}, "
+              f"against GMRES {G.normwise(y[i], y0[i]):.2e}")
+        assert res <= 1e-6
+        assert G.normwise(y[i], y0[i]) <= 1e-6
+    # the factor is kept: a second call solves with it again
+    y2, _ = S.dense_solve_many(rhs[:1])
+    assert G.normwise(y2[0], y[0]) <= 1e-12

@@ -15,11 +15,16 @@ same face tree and lists:
   the direction is recomputed in FP64 from the corrected solutions (x = y - Z N^-1 C_N y with
   the oracle's constraint Jacobian), and the GPU's direction, its slope g.x and the direction
   without each torus's mean translation (the weakest mode of A': the two tori's relative
-  translation) are compared with it.
+  translation) are compared with it: the direction within 1e-2 and the slope within 1e-3
+  (measured 2e-3 and 1e-5). The GPU metric's FP32 kernel values perturb A' by about 6e-7 of a
+  smooth product, and the direction's solve and its Schur combination amplify that by their
+  conditioning (the solve of y = A'^-1 g leaves 8e-6 on the oracle's operator, its solution
+  differs by 2e-4); on the smaller meshes of test_direction_gpu the same comparison holds
+  within 1e-5.
 
 The noise is N(0, 0.0005), an eighth of the minor-circle edge: the specified N(0, 0.01) is 2.5
 edges and crumples the surface so that no solve reaches 1e-6 (as for the single torus). The
-test runs RS_C5_STEPS steps (20 by default, checks at steps 0 and 10; 100 gives the
+test runs RS_C5_STEPS steps (11 by default, checks at steps 0 and 10; 100 gives the
 configuration's full flow with ten checks)."""
 import os
 
@@ -101,4 +106,5 @@ def test_linked_tori_flow_with_oracle_checks():
                   f"{c['direction_detrended']:.1e}, slope {c['slope']:.1e})")
             assert c["energy"] <= 1e-6 and c["differential"] <= 1e-5
             assert max(c["residuals"]) <= 1e-4
+            assert c["direction"] <= 1e-2 and c["slope"] <= 1e-3
     assert all(b < a for a, b in zip(energies, energies[1:]))

@@ -9,18 +9,25 @@
 #include <cstdint>
 #include <vector>
 
+#include "common.hpp"
 #include "host_tree.hpp"
 
 namespace rsg {
 
+// The blocks stay on the device, where the products use them; the host keeps their counts
+// and copies the lists only on request (download).
 struct Blocks {
-  std::vector<uint32_t> far_ptr, far_col;    // CSR by row node (stable: level order)
-  std::vector<uint32_t> near_ptr, near_col;  // CSR by row node
-  uint64_t near_entries = 0;                 // off-diagonal element pairs of the near blocks
-  uint64_t far_pairs = 0;                    // element pairs covered by far blocks
+  DevBuf<uint32_t> far_ptr, far_col;    // CSR by row node (stable: level order)
+  DevBuf<uint32_t> near_ptr, near_col;  // CSR by row node
+  size_t n_far = 0, n_near = 0;
+  uint64_t near_entries = 0;            // off-diagonal element pairs of the near blocks
+  uint64_t far_pairs = 0;               // element pairs covered by far blocks
   size_t depth = 0;
+  void download(std::vector<uint32_t> &fp, std::vector<uint32_t> &fc, std::vector<uint32_t> &np,
+                std::vector<uint32_t> &nc) const;
 };
 
+// Classifies on a stream of its own and returns when the blocks are on the device.
 Blocks classify_blocks_device(const Tree &T, double chi, size_t leaf_pairs);
 
 }  // namespace rsg

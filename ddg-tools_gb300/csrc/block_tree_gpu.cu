@@ -5,6 +5,7 @@
 // It runs on a stream of its own with stream-ordered allocations, so that it neither waits for
 // nor holds up other work on the context's stream.
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_reduce.cuh>
 #include <cub/device/device_scan.cuh>
 
 #include <algorithm>
@@ -154,31 +155,58 @@ struct StreamGuard {
   }
 };
 
-// the CSR (ptr, col) of `m` pairs grouped by row, level order kept
-void group_device(const AsyncBuf<uint2> &pairs, size_t m, uint32_t nn, cudaStream_t s, std::vector<uint32_t> &ptr,
-                  std::vector<uint32_t> &col) {
-  ptr.assign((size_t)nn + 1, 0);
-  col.resize(m);
-  if (m == 0) return;
-  AsyncBuf<uint32_t> r0(s), c0(s), r1(s), c1(s), p(s);
-  r0.alloc(m), c0.alloc(m), r1.alloc(m), c1.alloc(m), p.alloc((size_t)nn + 1);
+// the CSR (ptr, col) of `m` pairs grouped by row, level order kept, into device buffers
+void group_device(const AsyncBuf<uint2> &pairs, size_t m, uint32_t nn, cudaStream_t s, DevBuf<uint32_t> &ptr,
+                  DevBuf<uint32_t> &col) {
+  ptr.alloc((size_t)nn + 1);
+  col.alloc(std::max<size_t>(m, 1));
+  if (m == 0) {
+    RSG_CUDA("upload", cudaMemsetAsync(ptr.p, 0, ((size_t)nn + 1) * sizeof(uint32_t), s));
+    return;
+  }
+  AsyncBuf<uint32_t> r0(s), c0(s), r1(s);
+  r0.alloc(m), c0.alloc(m), r1.alloc(m);
   split_pairs_kernel<<<nblk(m, 256), 256, 0, s>>>(pairs.p, (uint32_t)m, r0.p, c0.p);
   RSG_CUDA("upload", cudaGetLastError());
   int bits = 1;
   while (bits < 32 && (1ull << bits) < nn) ++bits;
   size_t tmp_bytes = 0;
-  RSG_CUDA("upload", cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, r0.p, r1.p, c0.p, c1.p, (int)m, 0, bits, s));
+  RSG_CUDA("upload", cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, r0.p, r1.p, c0.p, col.p, (int)m, 0, bits, s));
   AsyncBuf<unsigned char> tmp(s);
   tmp.alloc(tmp_bytes);
-  RSG_CUDA("upload", cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, r0.p, r1.p, c0.p, c1.p, (int)m, 0, bits, s));
-  row_offsets_kernel<<<nblk(m + 1, 256), 256, 0, s>>>(r1.p, (uint32_t)m, nn, p.p);
+  RSG_CUDA("upload", cub::DeviceRadixSort::SortPairs(tmp.p, tmp_bytes, r0.p, r1.p, c0.p, col.p, (int)m, 0, bits, s));
+  row_offsets_kernel<<<nblk(m + 1, 256), 256, 0, s>>>(r1.p, (uint32_t)m, nn, ptr.p);
   RSG_CUDA("upload", cudaGetLastError());
-  RSG_CUDA("upload", copy_async(ptr.data(), p.p, ((size_t)nn + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-  RSG_CUDA("upload", copy_async(col.data(), c1.p, m * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-  RSG_CUDA("upload", cudaStreamSynchronize(s));
+}
+
+// element pairs of the blocks of row node a (integer sums): far |a||c|, near |a||c| (|a|(|a|-1)
+// on the diagonal)
+__global__ void block_pairs_kernel(uint32_t nn, const NodeRecD *__restrict__ rec, const uint32_t *far_ptr,
+                                   const uint32_t *far_col, const uint32_t *near_ptr, const uint32_t *near_col,
+                                   unsigned long long *fp, unsigned long long *ne) {
+  const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nn) return;
+  const unsigned long long la = rec[a].len;
+  unsigned long long f = 0, e = 0;
+  for (uint32_t q = far_ptr[a]; q < far_ptr[a + 1]; ++q) f += la * rec[far_col[q]].len;
+  for (uint32_t q = near_ptr[a]; q < near_ptr[a + 1]; ++q) {
+    const uint32_t c = near_col[q];
+    e += c == a ? la * (la - 1) : la * rec[c].len;
+  }
+  fp[a] = f, ne[a] = e;
 }
 
 }  // namespace
+
+void Blocks::download(std::vector<uint32_t> &fp, std::vector<uint32_t> &fc, std::vector<uint32_t> &np,
+                      std::vector<uint32_t> &nc) const {
+  fp.resize(far_ptr.n), fc.resize(n_far), np.resize(near_ptr.n), nc.resize(n_near);
+  RSG_CUDA("blocks", cudaMemcpy(fp.data(), far_ptr.p, far_ptr.n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  RSG_CUDA("blocks", cudaMemcpy(np.data(), near_ptr.p, near_ptr.n * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  if (n_far) RSG_CUDA("blocks", cudaMemcpy(fc.data(), far_col.p, n_far * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  if (n_near) RSG_CUDA("blocks", cudaMemcpy(nc.data(), near_col.p, n_near * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+  g_d2h_bytes += (fp.size() + fc.size() + np.size() + nc.size()) * sizeof(uint32_t);
+}
 
 Blocks classify_blocks_device(const Tree &T, double chi, size_t leaf_pairs) {
   const size_t nn = T.n_nodes();
@@ -237,19 +265,24 @@ Blocks classify_blocks_device(const Tree &T, double chi, size_t leaf_pairs) {
     fail(RS_INVALID_OPTION, "InvalidOption", "upload", "block lists exceed 2^32 entries");
   group_device(far_l, n_far, (uint32_t)nn, s, B.far_ptr, B.far_col);
   group_device(near_l, n_near, (uint32_t)nn, s, B.near_ptr, B.near_col);
+  B.n_far = n_far, B.n_near = n_near;
   // element pairs of the blocks (integer sums, any order)
-  auto len = [&](uint32_t a) { return (uint64_t)(T.end[a] - T.start[a]); };
-  std::vector<uint64_t> fp(nn, 0), ne(nn, 0);
-  parallel_for(nn, [&](size_t a0, size_t a1) {
-    for (size_t a = a0; a < a1; ++a) {
-      for (uint32_t q = B.far_ptr[a]; q < B.far_ptr[a + 1]; ++q) fp[a] += len((uint32_t)a) * len(B.far_col[q]);
-      for (uint32_t q = B.near_ptr[a]; q < B.near_ptr[a + 1]; ++q) {
-        const uint32_t c = B.near_col[q];
-        ne[a] += c == a ? len(c) * (len(c) - 1) : len((uint32_t)a) * len(c);
-      }
-    }
-  });
-  for (size_t a = 0; a < nn; ++a) B.far_pairs += fp[a], B.near_entries += ne[a];
+  {
+    AsyncBuf<unsigned long long> fp(s), ne(s), sums(s);
+    fp.alloc(nn), ne.alloc(nn), sums.alloc(2);
+    block_pairs_kernel<<<nblk(nn, 256), 256, 0, s>>>((uint32_t)nn, rec.p, B.far_ptr.p, B.far_col.p, B.near_ptr.p,
+                                                     B.near_col.p, fp.p, ne.p);
+    RSG_CUDA("upload", cudaGetLastError());
+    size_t bytes = 0;
+    RSG_CUDA("upload", cub::DeviceReduce::Sum(nullptr, bytes, fp.p, sums.p, (int)nn, s));
+    if (bytes > scan_tmp.n) scan_tmp.alloc(bytes);
+    RSG_CUDA("upload", cub::DeviceReduce::Sum(scan_tmp.p, bytes, fp.p, sums.p, (int)nn, s));
+    RSG_CUDA("upload", cub::DeviceReduce::Sum(scan_tmp.p, bytes, ne.p, sums.p + 1, (int)nn, s));
+    unsigned long long h[2] = {0, 0};
+    RSG_CUDA("upload", copy_async(h, sums.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+    RSG_CUDA("upload", cudaStreamSynchronize(s));
+    B.far_pairs = h[0], B.near_entries = h[1];
+  }
   return B;
 }
 

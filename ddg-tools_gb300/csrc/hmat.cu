@@ -29,6 +29,8 @@
 #include <type_traits>
 #include <vector>
 
+#include <cub/device/device_scan.cuh>
+
 #include "block_tree.hpp"
 #include "common.hpp"
 #include "host_tree.hpp"
@@ -428,7 +430,7 @@ __device__ __forceinline__ void cp_async_wait() {
 // quantities that cancel to a second-order result, and the output stage (M^T, a discrete
 // divergence) cancels once more, so plain FP32 sums of H~a m and H~(a m) would lose about
 // four digits.
-template <int KIND, int CC>
+template <int KIND, int CC, bool PLAIN>
 __global__ void __launch_bounds__(128, 5) hm_rows_kernel(HDev d, int c0) {
   static_assert(CC <= 12 && CC % 2 == 0, "at most twelve channels per pass");
   using WT = NearW<KIND>;
@@ -508,6 +510,13 @@ __global__ void __launch_bounds__(128, 5) hm_rows_kernel(HDev d, int c0) {
         for (int c2 = 0; c2 < CC / 2; ++c2) {
           const ulonglong2 v = *reinterpret_cast<const ulonglong2 *>(&tl.m[c2][k]);  // (hi pair, lo pair)
           const int wi = KIND == FACE ? (2 * c2 + 1 < 9 ? 0 : (2 * c2 >= 9 ? 2 : 1)) : 0;
+          if constexpr (PLAIN) {
+            // the inner operator: w (m_p - m_q) from the same exact differences, summed in plain
+            // FP32 (no error-free transformations)
+            const f32x2 t = f2_add(f2_sub(mh[c2], v.x), f2_sub(ml[c2], v.y));
+            ks[c2] = f2_fma(W[wi], t, ks[c2]);
+            continue;
+          }
           const f32x2 w = W[wi], wn = W[wi] ^ kF2Sign;
           // w (m_p - m_q) = pr + pe + w dl up to eps^2 terms: dh = mh_p - mh_q is exact (the
           // hi parts share a grid), dl = ml_p - ml_q, w dh = pr + pe (FMA), so no rounding that
@@ -728,6 +737,96 @@ __global__ void hm_pack_kernel(const double *pts, const double *wt, const double
                                 (float)nrm64[3 * (size_t)e + 2], 0.f);
 }
 
+// ---- the near columns and work items of every leaf, built on the device from the block lists
+
+// per leaf k: the length of its root-to-leaf chain, the near columns of the chain's blocks and
+// the number of work items (at most item_cols columns each, at least one)
+__global__ void near_count_kernel(uint32_t nl, const uint32_t *__restrict__ leaves, const uint32_t *__restrict__ parent,
+                                  const uint32_t *__restrict__ start, const uint32_t *__restrict__ end,
+                                  const uint32_t *__restrict__ near_ptr, const uint32_t *__restrict__ near_col,
+                                  uint32_t item_cols, uint32_t *depth, unsigned long long *cols, uint32_t *nitems) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nl) return;
+  uint32_t dep = 1;
+  unsigned long long c = 0;
+  for (uint32_t a = leaves[k];; a = parent[a]) {
+    for (uint32_t q = near_ptr[a]; q < near_ptr[a + 1]; ++q) {
+      const uint32_t b = near_col[q];
+      c += end[b] - start[b];
+    }
+    if (a == 0) break;
+    ++dep;
+  }
+  depth[k] = dep, cols[k] = c;
+  nitems[k] = (uint32_t)max(1ull, (c + item_cols - 1) / item_cols);
+}
+
+// per leaf k at its scanned offsets: the chain (root first), the near columns in chain, block and
+// element order, and the work items (leaf, column range [y, z), weight base filled later)
+__global__ void near_fill_kernel(uint32_t nl, const uint32_t *__restrict__ leaves, const uint32_t *__restrict__ parent,
+                                 const uint32_t *__restrict__ start, const uint32_t *__restrict__ end,
+                                 const uint32_t *__restrict__ near_ptr, const uint32_t *__restrict__ near_col,
+                                 uint32_t item_cols, const uint32_t *__restrict__ coff,
+                                 const unsigned long long *__restrict__ ncol, const uint32_t *__restrict__ ioff,
+                                 uint32_t *chain, uint32_t *cols, uint4 *items) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nl) return;
+  const uint32_t depth = coff[k + 1] - coff[k];
+  uint32_t *ch = chain + coff[k];
+  uint32_t a = leaves[k];
+  for (uint32_t i = depth; i-- > 0; a = parent[a]) ch[i] = a;
+  uint32_t x = (uint32_t)ncol[k];
+  for (uint32_t i = 0; i < depth; ++i) {
+    const uint32_t n = ch[i];
+    for (uint32_t q = near_ptr[n]; q < near_ptr[n + 1]; ++q) {
+      const uint32_t b = near_col[q];
+      for (uint32_t e = start[b]; e < end[b]; ++e) cols[x++] = e;
+    }
+  }
+  const uint32_t c_end = (uint32_t)ncol[k + 1];
+  uint32_t y0 = (uint32_t)ncol[k];
+  for (uint32_t it = ioff[k]; it < ioff[k + 1]; ++it) {
+    const uint32_t y1 = min(c_end, y0 + item_cols);
+    items[it] = make_uint4(k, y0, y1, 0u);
+    y0 = y1;
+  }
+}
+
+// the weight count of every work item: its rows times its columns padded to 32
+__global__ void item_weights_kernel(uint32_t n_items, const uint4 *__restrict__ items, const uint32_t *__restrict__ leaves,
+                                    const uint32_t *__restrict__ start, const uint32_t *__restrict__ end,
+                                    unsigned long long *w) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_items) return;
+  const uint4 it = items[i];
+  const uint32_t leaf = leaves[it.x];
+  w[i] = (unsigned long long)(end[leaf] - start[leaf]) * ((it.z - it.y + 31) & ~31u);
+}
+__global__ void item_base_kernel(uint32_t n_items, const unsigned long long *__restrict__ base, uint4 *items) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n_items) items[i].w = (uint32_t)base[i];
+}
+
+// far work items: node a's far blocks cut into runs of at most kFarChunk
+__global__ void far_count_kernel(uint32_t nn, const uint32_t *__restrict__ far_ptr, uint32_t *cnt) {
+  const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a < nn) cnt[a] = (far_ptr[a + 1] - far_ptr[a] + kFarChunk - 1) / kFarChunk;
+}
+__global__ void far_fill_kernel(uint32_t nn, const uint32_t *__restrict__ far_ptr, const uint32_t *__restrict__ off,
+                                uint4 *items) {
+  const uint32_t a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= nn) return;
+  const uint32_t q1 = far_ptr[a + 1];
+  uint32_t j = off[a];
+  for (uint32_t q0 = far_ptr[a]; q0 < q1; q0 += kFarChunk) items[j++] = make_uint4(a, q0, min(q0 + kFarChunk, q1), 0u);
+}
+
+// m = 1 in both channels of the paired layout: hi parts (1, 1), lo parts (0, 0)
+__global__ void ones_kernel(size_t n_el, float2 *m) {
+  const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n_el) m[2 * i] = make_float2(1.f, 1.f), m[2 * i + 1] = make_float2(0.f, 0.f);
+}
+
 }  // namespace rsg
 
 // ====================================================================== host side
@@ -753,7 +852,7 @@ struct HMat {
   size_t n_el = 0, n_items = 0;
   double neg_s = 0;
   DevBuf<uint32_t> start, end, right, parent, leaves, chain_off, chain, item_off;
-  DevBuf<uint32_t> far_ptr, far_col, count, far_item_off;
+  DevBuf<uint32_t> count, far_item_off;
   DevBuf<uint4> far_items;
   size_t n_far_items = 0;
   DevBuf<float2> fpart;
@@ -770,6 +869,7 @@ struct HMat {
   DevBuf<float2> part, m, z;
   DevBuf<unsigned long long> qmax;  // per channel: largest |m| (see split_q)
   int pw_mode = 0, pw_k = 0;
+  bool plain_rows = false;  // the near field of the next product in plain FP32 sums (inner operator)
   Profiler prof;
   double setup_times[3] = {0, 0, 0};  // seconds: work items, far coefficients, device part
 
@@ -777,7 +877,7 @@ struct HMat {
     HDev d;
     d.start = start.p, d.end = end.p, d.right = right.p, d.parent = parent.p, d.leaves = leaves.p;
     d.chain_off = chain_off.p, d.chain = chain.p;
-    d.far_ptr = far_ptr.p, d.far_col = far_col.p, d.far_coef = far_coef.p;
+    d.far_ptr = blocks.far_ptr.p, d.far_col = blocks.far_col.p, d.far_coef = far_coef.p;
     d.far_items = far_items.p, d.far_item_off = far_item_off.p, d.fpart = fpart.p;
     d.n_far_items = (int)n_far_items;
     d.xh = xh.p, d.xl = xl.p, d.nrm = nrm.p, d.leaf_farA = leaf_farA.p;
@@ -853,83 +953,83 @@ struct HMat {
     cudaStream_t s = st();
     const Tree &T = tree;
     size_t nn = T.n_nodes(), nl = T.leaves.size();
-    std::vector<uint32_t> parent_h(nn, 0), coff(nl + 1, 0), ioff(nl + 1, 0);
+    std::vector<uint32_t> parent_h(nn, 0);
     const uint32_t kItemCols = 512;
     for (size_t i = 0; i < nn; ++i)
       if (T.right[i]) parent_h[i + 1] = (uint32_t)i, parent_h[T.right[i]] = (uint32_t)i;
     for (size_t k = 0; k < nl; ++k)
       if (T.end[T.leaves[k]] - T.start[T.leaves[k]] > 8)
         fail(RS_INVALID_OPTION, "InvalidOption", "upload", "the GPU path needs leaf_size <= 8");
+    up_vec(start, T.start, s), up_vec(end, T.end, s), up_vec(right, T.right, s);
+    up_vec(parent, parent_h, s), up_vec(leaves, T.leaves, s);
     // per leaf: its root-to-leaf chain and the near columns of the chain (chain order, block
-    // order, element order), flattened and cut into items of at most kItemCols columns; two
-    // parallel passes (sizes, then fill at the prefix offsets)
-    std::vector<uint64_t> ncol(nl + 1, 0);
-    parallel_for(nl, [&](size_t k0, size_t k1) {
-      for (size_t k = k0; k < k1; ++k) {
-        uint32_t depth = 1;
-        uint64_t cols = 0;
-        for (uint32_t a = T.leaves[k];; a = parent_h[a]) {
-          for (uint32_t q = blocks.near_ptr[a]; q < blocks.near_ptr[a + 1]; ++q) {
-            uint32_t c = blocks.near_col[q];
-            cols += T.end[c] - T.start[c];
-          }
-          if (a == 0) break;
-          ++depth;
-        }
-        coff[k + 1] = depth;
-        ncol[k + 1] = cols;
-        ioff[k + 1] = (uint32_t)std::max<uint64_t>(1, (cols + kItemCols - 1) / kItemCols);
-      }
-    });
-    for (size_t k = 0; k < nl; ++k) coff[k + 1] += coff[k], ncol[k + 1] += ncol[k], ioff[k + 1] += ioff[k];
-    if (ncol[nl] > UINT32_MAX) fail(RS_INVALID_OPTION, "InvalidOption", "upload", "near field too large");
-    std::vector<uint32_t> chain_h(coff[nl]), cols_h(ncol[nl]);
-    std::vector<uint4> items_h(ioff[nl]);
-    parallel_for(nl, [&](size_t k0, size_t k1) {
-      for (size_t k = k0; k < k1; ++k) {
-        uint32_t *ch = chain_h.data() + coff[k];
-        uint32_t depth = coff[k + 1] - coff[k];
-        uint32_t a = T.leaves[k];
-        for (uint32_t i = depth; i-- > 0; a = parent_h[a]) ch[i] = a;
-        uint32_t x = (uint32_t)ncol[k];
-        for (uint32_t i = 0; i < depth; ++i)
-          for (uint32_t q = blocks.near_ptr[ch[i]]; q < blocks.near_ptr[ch[i] + 1]; ++q) {
-            uint32_t c = blocks.near_col[q];
-            for (uint32_t e = T.start[c]; e < T.end[c]; ++e) cols_h[x++] = e;
-          }
-        const uint32_t c_end = (uint32_t)ncol[k + 1];
-        uint32_t y0 = (uint32_t)ncol[k];
-        for (uint32_t it = ioff[k]; it < ioff[k + 1]; ++it) {
-          uint32_t y1 = std::min(c_end, y0 + kItemCols);
-          items_h[it] = make_uint4((uint32_t)k, y0, y1, 0);
-          y0 = y1;
-        }
-      }
-    });
-    n_items = items_h.size();
+    // order, element order), flattened and cut into items of at most kItemCols columns: counts,
+    // exclusive scans (one extra zero entry gives the totals), then the fill at the offsets
+    DevBuf<unsigned char> tmp;
+    auto scan = [&](auto *in, auto *out, size_t m) {
+      size_t bytes = 0;
+      RSG_CUDA("upload", cub::DeviceScan::ExclusiveSum(nullptr, bytes, in, out, (int)m, s));
+      if (bytes > tmp.n) tmp.alloc(bytes);
+      RSG_CUDA("upload", cub::DeviceScan::ExclusiveSum(tmp.p, bytes, in, out, (int)m, s));
+    };
+    {
+      DevBuf<uint32_t> dep(nl + 1), nit(nl + 1);
+      DevBuf<unsigned long long> cnt(nl + 1), ncol(nl + 1);
+      RSG_CUDA("upload", cudaMemsetAsync(dep.p + nl, 0, sizeof(uint32_t), s));
+      RSG_CUDA("upload", cudaMemsetAsync(nit.p + nl, 0, sizeof(uint32_t), s));
+      RSG_CUDA("upload", cudaMemsetAsync(cnt.p + nl, 0, sizeof(unsigned long long), s));
+      near_count_kernel<<<nblk(nl, 128), 128, 0, s>>>((uint32_t)nl, leaves.p, parent.p, start.p, end.p,
+                                                      blocks.near_ptr.p, blocks.near_col.p, kItemCols, dep.p, cnt.p,
+                                                      nit.p);
+      RSG_LAUNCHED(ctx, "hm_near_count");
+      chain_off.alloc(nl + 1), item_off.alloc(nl + 1);
+      scan(dep.p, chain_off.p, nl + 1), scan(cnt.p, ncol.p, nl + 1), scan(nit.p, item_off.p, nl + 1);
+      uint32_t n_chain = 0, n_it = 0;
+      unsigned long long n_col = 0;
+      RSG_CUDA("upload", copy_async(&n_chain, chain_off.p + nl, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+      RSG_CUDA("upload", copy_async(&n_col, ncol.p + nl, sizeof(n_col), cudaMemcpyDeviceToHost, s));
+      RSG_CUDA("upload", copy_async(&n_it, item_off.p + nl, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+      RSG_CUDA("upload", cudaStreamSynchronize(s));
+      if (n_col > UINT32_MAX) fail(RS_INVALID_OPTION, "InvalidOption", "upload", "near field too large");
+      chain.alloc(std::max<uint32_t>(n_chain, 1)), colidx.alloc(std::max<size_t>(n_col, 1)), items.alloc(n_it);
+      near_fill_kernel<<<nblk(nl, 128), 128, 0, s>>>((uint32_t)nl, leaves.p, parent.p, start.p, end.p,
+                                                     blocks.near_ptr.p, blocks.near_col.p, kItemCols, chain_off.p,
+                                                     ncol.p, item_off.p, chain.p, colidx.p, items.p);
+      RSG_LAUNCHED(ctx, "hm_near_fill");
+      n_items = n_it;
+    }
     lap(setup_times[0]);
     // weight base of every item: its rows times its columns padded to 32
-    n_wts = 0;
-    for (uint4 &it : items_h) {
-      const uint32_t leaf = T.leaves[it.x];
-      it.w = (uint32_t)n_wts;
-      n_wts += (size_t)(T.end[leaf] - T.start[leaf]) * ((it.z - it.y + 31) & ~31u);
-      if (n_wts > UINT32_MAX) fail(RS_INVALID_OPTION, "InvalidOption", "upload", "near field too large");
-    }
-    up_vec(start, T.start, s), up_vec(end, T.end, s), up_vec(right, T.right, s);
-    up_vec(parent, parent_h, s), up_vec(leaves, T.leaves, s), up_vec(chain_off, coff, s);
-    up_vec(chain, chain_h, s), up_vec(colidx, cols_h, s), up_vec(items, items_h, s), up_vec(item_off, ioff, s);
-    up_vec(far_ptr, blocks.far_ptr, s), up_vec(far_col, blocks.far_col, s);
     {
-      std::vector<uint4> fi;
-      std::vector<uint32_t> fo(nn + 1, 0);
-      for (size_t a = 0; a < nn; ++a) {
-        for (uint32_t q0 = blocks.far_ptr[a]; q0 < blocks.far_ptr[a + 1]; q0 += kFarChunk)
-          fi.push_back(make_uint4((uint32_t)a, q0, std::min(q0 + kFarChunk, blocks.far_ptr[a + 1]), 0));
-        fo[a + 1] = (uint32_t)fi.size();
-      }
-      n_far_items = fi.size();
-      up_vec(far_items, fi, s), up_vec(far_item_off, fo, s);
+      DevBuf<unsigned long long> w(n_items + 1), base(n_items + 1);
+      RSG_CUDA("upload", cudaMemsetAsync(w.p + n_items, 0, sizeof(unsigned long long), s));
+      item_weights_kernel<<<nblk(n_items, 256), 256, 0, s>>>((uint32_t)n_items, items.p, leaves.p, start.p, end.p,
+                                                              w.p);
+      RSG_LAUNCHED(ctx, "hm_item_weights");
+      scan(w.p, base.p, n_items + 1);
+      unsigned long long tot = 0;
+      RSG_CUDA("upload", copy_async(&tot, base.p + n_items, sizeof(tot), cudaMemcpyDeviceToHost, s));
+      RSG_CUDA("upload", cudaStreamSynchronize(s));
+      if (tot > UINT32_MAX) fail(RS_INVALID_OPTION, "InvalidOption", "upload", "near field too large");
+      n_wts = tot;
+      item_base_kernel<<<nblk(n_items, 256), 256, 0, s>>>((uint32_t)n_items, base.p, items.p);
+      RSG_LAUNCHED(ctx, "hm_item_weights");
+    }
+    // far work items
+    {
+      DevBuf<uint32_t> cnt(nn + 1);
+      RSG_CUDA("upload", cudaMemsetAsync(cnt.p + nn, 0, sizeof(uint32_t), s));
+      far_count_kernel<<<nblk(nn, 256), 256, 0, s>>>((uint32_t)nn, blocks.far_ptr.p, cnt.p);
+      RSG_LAUNCHED(ctx, "hm_far_items");
+      far_item_off.alloc(nn + 1);
+      scan(cnt.p, far_item_off.p, nn + 1);
+      uint32_t nfi = 0;
+      RSG_CUDA("upload", copy_async(&nfi, far_item_off.p + nn, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+      RSG_CUDA("upload", cudaStreamSynchronize(s));
+      n_far_items = nfi;
+      far_items.alloc(std::max<size_t>(n_far_items, 1));
+      far_fill_kernel<<<nblk(nn, 256), 256, 0, s>>>((uint32_t)nn, blocks.far_ptr.p, far_item_off.p, far_items.p);
+      RSG_LAUNCHED(ctx, "hm_far_items");
     }
     count.alloc(nn);
     RSG_CUDA("upload", cudaMemsetAsync(count.p, 0, nn * sizeof(uint32_t), s));
@@ -939,10 +1039,10 @@ struct HMat {
       DevBuf<double> cen, pj;
       cen.upload(T.centroid.data(), 3 * nn, s);
       if (kind == FACE) pj.upload(proj6, 6 * nn, s);
-      far_coef.alloc(std::max<size_t>(blocks.far_col.size(), 1));
+      far_coef.alloc(std::max<size_t>(blocks.n_far, 1));
       if (n_far_items > 0) {
         hm_far_coef_kernel<<<nblk(n_far_items * 32, 256), 256, 0, s>>>(
-            far_items.p, (int)n_far_items, far_col.p, cen.p, kind == FACE ? pj.p : nullptr, neg_s, far_coef.p);
+            far_items.p, (int)n_far_items, blocks.far_col.p, cen.p, kind == FACE ? pj.p : nullptr, neg_s, far_coef.p);
         RSG_LAUNCHED(ctx, "hm_far_coef");
       }
       RSG_CUDA("upload", cudaStreamSynchronize(s));  // before the staging buffers go
@@ -972,10 +1072,9 @@ struct HMat {
     // far part of H~a: upward over psi = a (m = 1, 2 channels) and far sums per node
     reserve(4);
     // m = 1 in both channels: hi parts (1, 1), lo parts (0, 0) in the paired layout
-    std::vector<float2> ones(2 * n_el);
-    for (size_t i = 0; i < n_el; ++i) ones[2 * i] = make_float2(1.f, 1.f), ones[2 * i + 1] = make_float2(0.f, 0.f);
-    DevBuf<float2> mm;
-    mm.upload(ones.data(), ones.size(), s);
+    DevBuf<float2> mm(2 * n_el);
+    ones_kernel<<<nblk(n_el, 256), 256, 0, s>>>(n_el, mm.p);
+    RSG_LAUNCHED(ctx, "hm_ones");
     HDev d = dev(2);
     d.m = mm.p;
     upward_far<ONES, 2>(d);
@@ -996,11 +1095,13 @@ struct HMat {
     prof.begin(s, K == FACE ? "metric_rows" : "vfrac_rows");
     if constexpr (K == FACE) {
       for (int q = 0; q < nb; ++q) {  // one vector (12 channels) per pass
-        hm_rows_kernel<K, 12><<<nblk(n_items * 32, 128), 128, 0, s>>>(d, 12 * q);
+        if (plain_rows) hm_rows_kernel<K, 12, true><<<nblk(n_items * 32, 128), 128, 0, s>>>(d, 12 * q);
+        else hm_rows_kernel<K, 12, false><<<nblk(n_items * 32, 128), 128, 0, s>>>(d, 12 * q);
         RSG_LAUNCHED(ctx, "hm_rows");
       }
     } else {
-      hm_rows_kernel<K, CC><<<nblk(n_items * 32, 128), 128, 0, s>>>(d, 0);
+      if (plain_rows) hm_rows_kernel<K, CC, true><<<nblk(n_items * 32, 128), 128, 0, s>>>(d, 0);
+      else hm_rows_kernel<K, CC, false><<<nblk(n_items * 32, 128), 128, 0, s>>>(d, 0);
       RSG_LAUNCHED(ctx, "hm_rows");
     }
     prof.end(s);
@@ -1166,10 +1267,11 @@ void metric_setup(rs_metric *M, rs_ctx *ctx, int nv, int nf, const uint32_t *fac
 // FaceMetricTree::apply_batch (hierarchical.rs:540-622) on device vectors with leading
 // dimensions ldx, ldy (>= 3V): groups of <= 3 vectors per tree pass.
 void rsg::metric_apply_strided(rs_metric *M, double w_hi, double w_lo, int nb, const double *xs,
-                               size_t ldx, double *ys, size_t ldy) {
+                               size_t ldx, double *ys, size_t ldy, bool plain) {
   if (!(std::isfinite(w_hi) && std::isfinite(w_lo)))
     fail(RS_INVALID_OPTION, "InvalidOption", "product", "finite weights");
   cudaStream_t s = M->h.st();
+  M->h.plain_rows = plain;
   for (int q0 = 0; q0 < nb; q0 += 3) {
     int k = std::min(3, nb - q0);
     int CC = 12 * k;
@@ -1193,8 +1295,9 @@ void rsg::metric_apply_strided(rs_metric *M, double w_hi, double w_lo, int nb, c
 
 // VertexFractionalTree::apply_batch (hierarchical.rs:1274-1345) scaled by `scale`.
 void rsg::vfrac_apply_strided(rs_vfrac *V, double scale, int nb, const double *xs, size_t ldx,
-                              double *ys, size_t ldy) {
+                              double *ys, size_t ldy, bool plain) {
   cudaStream_t s = V->h.st();
+  V->h.plain_rows = plain;
   for (int q0 = 0; q0 < nb; q0 += 3) {
     int k = std::min(3, nb - q0);
     int CC = 4 * k;  // 3 k channels padded to a multiple of 4
@@ -1278,8 +1381,8 @@ int rs_metric_build_times(rs_metric *M, double *out8) {
 
 int rs_metric_stats(rs_metric *M, int64_t *o) {
   return guard([&] {
-    o[0] = (int64_t)M->h.blocks.far_col.size();
-    o[1] = (int64_t)M->h.blocks.near_col.size();
+    o[0] = (int64_t)M->h.blocks.n_far;
+    o[1] = (int64_t)M->h.blocks.n_near;
     o[2] = (int64_t)M->h.blocks.near_entries;
     o[3] = (int64_t)M->h.blocks.depth;
     o[4] = (int64_t)M->h.tree.n_nodes();
@@ -1289,11 +1392,12 @@ int rs_metric_stats(rs_metric *M, int64_t *o) {
 int rs_metric_blocks(rs_metric *M, uint32_t *far_ptr, uint32_t *far_col, uint32_t *near_ptr,
                      uint32_t *near_col) {
   return guard([&] {
-    const Blocks &B = M->h.blocks;
-    std::copy(B.far_ptr.begin(), B.far_ptr.end(), far_ptr);
-    std::copy(B.far_col.begin(), B.far_col.end(), far_col);
-    std::copy(B.near_ptr.begin(), B.near_ptr.end(), near_ptr);
-    std::copy(B.near_col.begin(), B.near_col.end(), near_col);
+    std::vector<uint32_t> fp, fc, np, nc;
+    M->h.blocks.download(fp, fc, np, nc);
+    std::copy(fp.begin(), fp.end(), far_ptr);
+    std::copy(fc.begin(), fc.end(), far_col);
+    std::copy(np.begin(), np.end(), near_ptr);
+    std::copy(nc.begin(), nc.end(), near_col);
   });
 }
 
@@ -1367,8 +1471,8 @@ int rs_vfrac_apply_device(rs_vfrac *V, int nb, const double *xs_dev, double *ys_
 
 int rs_vfrac_stats(rs_vfrac *V, int64_t *o) {
   return guard([&] {
-    o[0] = (int64_t)V->h.blocks.far_col.size();
-    o[1] = (int64_t)V->h.blocks.near_col.size();
+    o[0] = (int64_t)V->h.blocks.n_far;
+    o[1] = (int64_t)V->h.blocks.n_near;
     o[2] = (int64_t)V->h.blocks.near_entries;
     o[3] = (int64_t)V->h.blocks.depth;
     o[4] = (int64_t)V->h.tree.n_nodes();
@@ -1467,7 +1571,7 @@ void noalloc_face_group(rs_metric *M, const HDev &d, unsigned long long *qmax, i
   }
   h.upward_far<FACE_CH, CC>(d);
   for (int q = 0; q < k; ++q) {
-    hm_rows_kernel<FACE, 12><<<nblk(h.n_items * 32, 128), 128, 0, s>>>(d, 12 * q);
+    hm_rows_kernel<FACE, 12, false><<<nblk(h.n_items * 32, 128), 128, 0, s>>>(d, 12 * q);
     RSG_LAUNCHED(h.ctx, "hm_rows");
   }
   h.epilogue<FACE_CH, CC>(d);

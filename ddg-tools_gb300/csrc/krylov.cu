@@ -135,7 +135,9 @@ struct Rhs {
 }  // namespace
 
 void gmres_batch(rs_ctx *ctx, const Operator &A, const Operator *P, int nb, const double *b,
-                 double *x, const GmresOptions &opt, std::vector<GmresReport> &reports) {
+                 double *x, const GmresOptions &opt, std::vector<GmresReport> &reports,
+                 const Operator *A_true) {
+  const Operator &At = A_true ? *A_true : A;
   using clk = std::chrono::steady_clock;
   auto t0 = clk::now();
   if (opt.restart < 1 || opt.restart > 63 || opt.max_iterations < 1 || !(opt.tolerance > 0.0 && opt.tolerance < 1.0))
@@ -190,7 +192,7 @@ void gmres_batch(rs_ctx *ctx, const Operator &A, const Operator *P, int nb, cons
       for (size_t i = 0; i < act.size(); ++i)
         RSG_CUDA("gmres", cudaMemcpyAsync(xbuf.p + i * n, x + (size_t)act[i] * n, n * sizeof(double),
                                           cudaMemcpyDeviceToDevice, s));
-      A.apply((int)act.size(), xbuf.p, ybuf.p);
+      At.apply((int)act.size(), xbuf.p, ybuf.p);
     }
     for (size_t i = 0; i < act.size(); ++i) {
       Rhs &Q = R[act[i]];

@@ -38,8 +38,13 @@ struct GmresReport {  // GmresReport (gmres.rs:200-225)
 // (flexible form), so a preconditioner that varies between applications is allowed.
 // b, x: nb*n device vectors. Throws RS_SOLVER_DIVERGED when a solve ends above a true relative
 // residual of 0.1 (DIVERGENCE_THRESHOLD, gmres.rs:196).
+// A_true (optional): the operator of the explicit residuals (every cycle start, and so the
+// convergence test), when the Arnoldi steps use a cheaper approximation A of it. Each cycle
+// then corrects the previous cycles' approximation error, as iterative refinement does, and the
+// reported residuals are those of A_true.
 void gmres_batch(rs_ctx *ctx, const Operator &A, const Operator *P, int nb, const double *b,
-                 double *x, const GmresOptions &opt, std::vector<GmresReport> &reports);
+                 double *x, const GmresOptions &opt, std::vector<GmresReport> &reports,
+                 const Operator *A_true = nullptr);
 
 // FP64 helpers (deterministic: fixed grid, fixed reduction trees).
 // out[i] = v_i . w for v_i = vs[i], or for the single vector v1 when given (nvec = 1); root:

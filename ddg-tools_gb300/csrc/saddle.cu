@@ -330,6 +330,10 @@ struct rs_solver {
   DevBuf<mgreal> mg_in, mg_out;  // right-hand sides and solutions on the multigrid layout
   std::vector<GmresReport> last;
   Operator op, prec;
+  // the Arnoldi steps on the inner operator (plain near-field sums, also in the preconditioner's
+  // vertex product), every cycle-start residual and the convergence test on op
+  bool inner_plain = true;
+  Operator op_inner;
   // the coarse space (coarse.rs): cm columns, 0 when every component is fixed by rows of its own
   int cm = 0, c_nfree = 0;
   std::vector<int> c_rows_h;                // multiplier rows touching a free component
@@ -403,10 +407,11 @@ struct rs_solver {
   }
 
   // A' x
-  void apply_op(int nb, const double *x, double *y) {
+  // plain: the inner operator of the Arnoldi steps (the near field in plain FP32 sums)
+  void apply_op(int nb, const double *x, double *y, bool plain = false) {
     reserve(nb);
     prof.begin(st(), "operator");
-    metric_apply_strided(metric, w_hi, w_lo, nb, x, n, y, n);
+    metric_apply_strided(metric, w_hi, w_lo, nb, x, n, y, n, plain);
     group_sums(x, n, nb, c.p, cy.p);
     size_t tot = (size_t)nb * n;
     cq_apply_kernel<<<nblk(tot, 256), 256, 0, st()>>>(x, y, n, nb, nv, group.p, c.p, G, cy.p);
@@ -456,7 +461,7 @@ struct rs_solver {
     double *y = tmp.p, *v = tmp2.p;
     lsolve(nb, r, y, nullptr, steps);
     prof.begin(st(), "precondition_fractional");
-    vfrac_apply_strided(vfrac, frac_scale, nb, y, n, v, n);
+    vfrac_apply_strided(vfrac, frac_scale, nb, y, n, v, n, inner_plain);
     prof.end(st());
     group_sums(y, n, nb, c.p, cy.p);
     size_t tot = (size_t)nb * n;
@@ -484,7 +489,7 @@ struct rs_solver {
       l_solves++;
       bool ok = true;
       try {
-        gmres_batch(ctx, op, &lprec, nb, b, x, ol, last);
+        gmres_batch(ctx, inner_plain ? op_inner : op, &lprec, nb, b, x, ol, last, inner_plain ? &op : nullptr);
         for (auto &r : last) ok = ok && r.converged;
       } catch (const Error &e) {
         if (e.code != RS_SOLVER_DIVERGED) throw;
@@ -493,7 +498,8 @@ struct rs_solver {
       if (ok) return;
       l_fallbacks++;
     }
-    gmres_batch(ctx, op, use_prec ? &prec : nullptr, nb, b, x, o, last);
+    gmres_batch(ctx, inner_plain ? op_inner : op, use_prec ? &prec : nullptr, nb, b, x, o, last,
+                inner_plain ? &op : nullptr);
   }
 };
 
@@ -786,6 +792,9 @@ int rs_solver_build(rs_ctx *ctx, int nv, int nf, const uint32_t *faces, const do
     rs_solver *P = S.get();
     S->op.n = S->n;
     S->op.apply = [P](int nb, const double *x, double *y) { P->apply_op(nb, x, y); };
+    S->op_inner.n = S->n;
+    S->op_inner.apply = [P](int nb, const double *x, double *y) { P->apply_op(nb, x, y, true); };
+    S->inner_plain = o->inner_plain != 0;
     S->prec.n = S->n;
     S->prec.apply = [P](int nb, const double *x, double *y) { P->apply_prec(nb, x, y); };
     S->lprec.n = S->n;
@@ -1098,6 +1107,7 @@ rs_solver_options rs_solver_options_default(void) {
   o.preconditioner = 1;
   o.clamp_laplacian = 0;
   o.coarse = 1;
+  o.inner_plain = 1;
   return o;
 }
 

@@ -41,7 +41,7 @@ class SolverOptions(C.Structure):
                 ("tp_weight", C.c_double), ("low_order", C.c_int), ("eps_rel", C.c_double),
                 ("eps_multi_rel", C.c_double), ("barycenter_per_component", C.c_int),
                 ("vcycles", C.c_int), ("preconditioner", C.c_int),
-                ("clamp_laplacian", C.c_int), ("coarse", C.c_int)]
+                ("clamp_laplacian", C.c_int), ("coarse", C.c_int), ("inner_plain", C.c_int)]
 
 
 class FlowOptions(C.Structure):

@@ -250,6 +250,11 @@ typedef struct rs_solver_options {
                             that no positional row of their own fixes: a global barycenter on
                             several components (PreconditionerOptions::coarse, CoarseSpace,
                             RS/src/solve/coarse.rs; 1) */
+  int inner_plain;       /* 1: the Arnoldi steps apply an inner operator whose near fields (of the
+                            metric, and of the preconditioner's vertex product) are summed in plain
+                            FP32; every cycle-start residual, and so the convergence test and the
+                            reported residual, uses the full operator. 0: the full operator
+                            throughout. No counterpart in the crate (1) */
 } rs_solver_options;
 
 rs_solver_options rs_solver_options_default(void);

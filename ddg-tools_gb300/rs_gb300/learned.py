@@ -43,17 +43,22 @@ TRAIN_TORI = [(100, 100), (160, 100), (200, 128), (240, 160), (256, 200), (288, 
 
 
 def training_meshes(count: int = 8, seed: int = 100):
-    """Seeded noisy tori (20,000-204,800 faces; noise 0.1-0.3 of the minor edge) and jittered
-    icospheres (level 5 or 6: 20,480 or 81,920 faces), one icosphere in four."""
+    """Seeded noisy tori and jittered icospheres: mesh i is an icosphere when i % 4 == 3 (level 5
+    or 6: 20,480 or 81,920 faces), otherwise the torus of TRAIN_TORI taken in turn from the
+    largest (204,800 faces) down, so that eight meshes span 20,000-204,800 faces; torus noise
+    0.1-0.3 of the minor edge."""
     rng = np.random.default_rng(seed)
     out = []
+    tori = TRAIN_TORI[::-1]
+    t = 0
     for i in range(count):
         s = int(rng.integers(1 << 30))
         if i % 4 == 3:
-            P, F = gen.icosphere(int(rng.choice([5, 6])))
+            P, F = gen.icosphere(5 if (i // 4) % 2 else 6)
             P = P * (1.0 + float(rng.uniform(0.005, 0.02)) * gen.SplitMix64(s).normals(len(P))[:, None])
         else:
-            nu, nv = TRAIN_TORI[int(rng.integers(len(TRAIN_TORI)))]
+            nu, nv = tori[t % len(tori)]
+            t += 1
             r = float(rng.uniform(0.25, 0.4))
             edge = 2.0 * np.pi * r / nv
             P, F = gen.noisy_torus(nu, nv, 1.0, r, float(rng.uniform(0.1, 0.3)) * edge, s)
@@ -92,12 +97,15 @@ def make_dataset(R, ctx, meshes, per_mesh: int, cheap_steps: int = 2, seed: int 
         t0 = time.time()
         bh = R.BhTree.build(F, P, R.BhOptions(0.25), ctx)
         _, dE = bh.energy_and_differential()
-        S = R.SaddleSolver(F, P, R.Exponents(), R.solver_options(tolerance=1e-7, restart=60, max_iterations=400), ctx)
+        S = R.SaddleSolver(F, P, R.Exponents(), R.solver_options(tolerance=1e-7, restart=60, max_iterations=800), ctx)
         Sc = R.SaddleSolver(F, P, R.Exponents(), R.solver_options(vcycles=cheap_steps), ctx)
         g = R.SurfaceGraph(F, P, ctx)
-        rs = residuals(P, F, dE, per_mesh, rng)
-        for i0 in range(0, len(rs), 4):
-            batch = rs[i0:i0 + 4]
+        # batches of four right-hand sides until the mesh holds per_mesh pairs (a solve that misses
+        # the tolerance is dropped and replaced), at most three times the batches needed
+        kept, tries = 0, 0
+        while kept < per_mesh and tries < 3 * ((per_mesh + 3) // 4):
+            tries += 1
+            batch = residuals(P, F, dE, min(4, per_mesh - kept), rng)
             rhs = np.zeros((len(batch), S.n))
             for k, r in enumerate(batch):
                 rhs[k, :S.n_dofs] = r
@@ -109,6 +117,7 @@ def make_dataset(R, ctx, meshes, per_mesh: int, cheap_steps: int = 2, seed: int 
             for k, r in enumerate(batch):
                 if not reps[k]["converged"]:
                     continue
+                kept += 1
                 data.append((g, torch.tensor(r, device=dev), torch.tensor(y[k, :S.n_dofs].copy(), device=dev),
                              torch.tensor(z[k, :S.n_dofs].copy(), device=dev)))
         log(f"mesh {mi}: {len(F)} faces, {len(data)} pairs, {time.time() - t0:.1f} s")

@@ -1,6 +1,7 @@
 """CPU tests of the product library's host side: it loads, exports every symbol of
 include/rsgpu.h, validates surfaces with the crate's error kinds, and builds the face BVH
 bit for bit as the oracle (no device work)."""
+import ctypes as C
 import re
 from pathlib import Path
 
@@ -112,3 +113,31 @@ def test_generators_match_reference_recipes():
     r = gen.SplitMix64(1)
     seq = [r.next_u64() for _ in range(3)]
     assert np.array_equal(gen.SplitMix64(1).draws(3), np.array(seq, dtype=np.uint64))
+
+
+@pytest.mark.parametrize("py_name, c_name", [("SolverOptions", "rs_solver_options"),
+                                             ("FlowOptions", "rs_flow_options"),
+                                             ("CcdOptions", "rs_ccd_options")])
+def test_option_structs_match_the_header(tmp_path, py_name, c_name):
+    """The ctypes mirrors of the option structs have the C header's size and field offsets
+    (compiled against include/rsgpu.h with the host compiler)."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    py = getattr(R, py_name)
+    fields = [f[0] for f in py._fields_]
+    src = tmp_path / "layout.c"
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "rsgpu.h"', "int main(void) {",
+             f'  printf("%zu\\n", sizeof({c_name}));']
+    lines += [f'  printf("%zu\\n", offsetof({c_name}, {f}));' for f in fields]
+    lines += ["  return 0;", "}"]
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    inc = Path(__file__).resolve().parents[1] / "include"
+    subprocess.run([cc, f"-I{inc}", str(src), "-o", str(exe)], check=True, capture_output=True)
+    out = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    assert out[0] == C.sizeof(py)
+    assert out[1:] == [getattr(py, f).offset for f in fields]

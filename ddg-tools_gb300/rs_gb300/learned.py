@@ -2,7 +2,7 @@
 that the plain solver produces on seeded meshes.
 
 For every training mesh a plain solver (the fractional preconditioner, L'^-1 by multigrid CG)
-solves A' z = r to the flow's tolerance (1e-6) for residuals r drawn from the flow's own right-hand sides
+solves A' z = r to a tight tolerance for residuals r drawn from the flow's own right-hand sides
 (the energy differential, the area and volume gradients) mixed with seeded smooth fields and
 noise; the cheap plain preconditioner gives y = P_cheap^-1 r. The network learns
 z - y from (surface, r, y) with the relative squared error |z_pred - z|^2 / |z|^2, by the
@@ -97,7 +97,7 @@ def make_dataset(R, ctx, meshes, per_mesh: int, cheap_steps: int = 2, seed: int 
         t0 = time.time()
         bh = R.BhTree.build(F, P, R.BhOptions(0.25), ctx)
         _, dE = bh.energy_and_differential()
-        S = R.SaddleSolver(F, P, R.Exponents(), R.solver_options(tolerance=1e-6, restart=60, max_iterations=800), ctx)
+        S = R.SaddleSolver(F, P, R.Exponents(), R.solver_options(tolerance=1e-7, restart=60, max_iterations=800), ctx)
         Sc = R.SaddleSolver(F, P, R.Exponents(), R.solver_options(vcycles=cheap_steps), ctx)
         g = R.SurfaceGraph(F, P, ctx)
         # batches of four right-hand sides until the mesh holds per_mesh pairs (a solve that misses

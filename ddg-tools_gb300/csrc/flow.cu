@@ -1,6 +1,6 @@
 // One Hs descent step of the repulsive-surface flow on the GPU (Session::step_inner,
-// RS/src/step/session.rs:749-1200, without remeshing and collision detection), behind rs_flow_*
-// of include/rsgpu.h.
+// RS/src/step/session.rs:749-1200, without remeshing; with rs_flow_options.ccd the first trial is
+// capped by continuous collision detection), behind rs_flow_* of include/rsgpu.h.
 //
 //   1. Barnes-Hut energy F and differential g (rs_bh_*; objective.rs:151-249)
 //   2. the saddle solver of the step (rs_solver_*; direction.rs:426-484)

@@ -47,6 +47,25 @@ struct KernelIface {
   std::function<void(size_t, size_t, double *)> near;
 };
 
+// One row of one near block with stored kernel values: out_r += sum over the block's columns
+// of k[kmap[c]] psi[c], in column order (the element itself skipped), with the row's CC sums
+// held in registers; N <= 2 kernels per entry, km[c] = (kmap[c] != 0).
+template <int CC>
+static inline void near_run(const double *&stored, int N, const unsigned char *km, const double *xb, uint32_t cb,
+                            bool self, uint32_t self_col, double *o) {
+  double acc[CC];
+  for (int c = 0; c < CC; ++c) acc[c] = o[c];
+  for (uint32_t cc = 0; cc < cb; ++cc) {
+    const double *kv = stored;
+    stored += N;
+    if (self && cc == self_col) continue;
+    const double *x = xb + (size_t)cc * CC;
+    const double k0 = kv[0], k1 = N == 2 ? kv[1] : kv[0];
+    for (int c = 0; c < CC; ++c) acc[c] += (km[c] ? k1 : k0) * x[c];
+  }
+  for (int c = 0; c < CC; ++c) o[c] = acc[c];
+}
+
 struct BlockTree {  // block_tree.rs:61-91
   int N = 1;
   // The near-field values, stored once per build as the crate stores its dense near blocks
@@ -186,20 +205,25 @@ struct BlockTree {  // block_tree.rs:61-91
         for (size_t c = 0; c < C; ++c) u[c] = up[(a + 1) * C + c] + up[right[a] * C + c];
       }
     }
-    for (size_t a = 0; a < nn; ++a) {
-      double *f = &acc[a * C];
-      for (size_t p = far_ptr[a]; p < far_ptr[a + 1]; ++p) {
-        const double *kc = &far_coef[p * N];
-        const double *u = &up[far_col[p] * C];
-        for (size_t c = 0; c < C; ++c) f[c] += kc[kmap[c]] * u[c];
+    // far blocks per row node (independent rows: the same sums in the same order per node)
+    parallel_for((int64_t)nn, [&](int64_t ab, int64_t ae) {
+      for (int64_t a = ab; a < ae; ++a) {
+        double *f = &acc[a * C];
+        for (size_t p = far_ptr[a]; p < far_ptr[a + 1]; ++p) {
+          const double *kc = &far_coef[p * N];
+          const double *u = &up[far_col[p] * C];
+          for (size_t c = 0; c < C; ++c) f[c] += kc[kmap[c]] * u[c];
+        }
       }
-    }
+    });
     for (size_t a = 0; a < nn; ++a)
       if (right[a] != 0)
         for (size_t ch : {a + 1, (size_t)right[a]})
           for (size_t c = 0; c < C; ++c) acc[ch * C + c] += acc[a * C + c];
     out.assign(n * C, 0.0);
     std::vector<double> kv(N);
+    std::vector<unsigned char> km(C);
+    for (size_t c = 0; c < C; ++c) km[c] = kmap[c] != 0;
     parallel_for((int64_t)leaves.size(), [&](int64_t lb, int64_t le) {
       std::vector<double> kvv(N);
       for (int64_t li = lb; li < le; ++li) {
@@ -218,6 +242,15 @@ struct BlockTree {  // block_tree.rs:61-91
             for (size_t r = 0; r < rows; ++r) {
               size_t i = order[s + r];
               double *o = &out[(s + r) * C];
+              if (stored && N <= 2 && (C == 12 || C == 3 || C == 1)) {
+                const bool self = a == b;
+                const uint32_t sc = (uint32_t)(r0 + r);
+                const double *xb = &psi[(size_t)sb * C];
+                if (C == 12) near_run<12>(stored, N, km.data(), xb, cb, self, sc, o);
+                else if (C == 3) near_run<3>(stored, N, km.data(), xb, cb, self, sc, o);
+                else near_run<1>(stored, N, km.data(), xb, cb, self, sc, o);
+                continue;
+              }
               for (uint32_t cc = 0; cc < cb; ++cc) {
                 const double *kv = stored;
                 if (stored) stored += N;
@@ -227,7 +260,12 @@ struct BlockTree {  // block_tree.rs:61-91
                   kv = kvv.data();
                 }
                 const double *x = &psi[(sb + cc) * C];
-                for (size_t c = 0; c < C; ++c) o[c] += kv[kmap[c]] * x[c];
+                if (N == 2) {  // the selection written as a blend, so that the loop vectorises
+                  const double k0 = kv[0], k1 = kv[1];
+                  for (size_t c = 0; c < C; ++c) o[c] += (km[c] ? k1 : k0) * x[c];
+                } else {
+                  for (size_t c = 0; c < C; ++c) o[c] += kv[kmap[c]] * x[c];
+                }
               }
             }
           }
